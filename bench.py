@@ -1,0 +1,398 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 pseudospectral step (one JSON line on stdout).
+
+Workload (the headline 2048^2 configuration): 2-D incompressible Navier-Stokes,
+vorticity-streamfunction, doubly periodic [0, 2pi]^2, 2048 x 2048, FP32 bulk
+arithmetic, classical RK4 with 2/3 dealiasing, nu = 1e-5, ramp hyperviscosity
+with order 4 (nu_h k^4 form) scaled so the damping at 2/3 kmax is O(1) per
+step, white-in-time Philox forcing on shells 4 <= |k| <= 6 at injection rate
+1e-3, adaptive dt at CFL 0.5, seeded random-phase initial vorticity with
+E(k) ~ k^4 exp(-(k/8)^2) and E = 0.5.  Synthetic data, no files.
+
+  value   grid-pt*steps/s of the device-resident step (C-ABI ns_gpu_advance),
+          K steps timed with CUDA events on the library stream, a 256 MiB L2
+          flush between steps outside the timed events (the step's working set
+          is below the 129 MB L2).
+  e2e     the same metric through the reference-facing drop-in API with host
+          arrays: per step ns_spectral_compute_cfl_timestep + ns_spectral_advance_rk4
+          (the reference's own loop), every host<->device copy inside the timing.
+  roofline  the dominant kernel's algorithmic HBM bytes per launch over its mean
+          CUDA-event duration, against MEASURED_PEAKS.json hbm_gbs.
+  cpu_baseline  the CPU oracle (C restatement of the reference step, FP64,
+          OpenMP over all host cores) on a bounded sample of the same workload.
+
+--impl reference times that CPU implementation alone (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "navier-stokes-solvers_gb300"))
+
+N = 2048
+RE = 1.0e5
+K0 = 8.0
+E0 = 0.5
+CFL = 0.5
+F_KMIN, F_KMAX, F_EPS, F_SEED = 4.0, 6.0, 1.0e-3, 20251203
+IC_SEED = 1
+FLUSH_BYTES = 256 << 20
+METRIC = "grid-pt*steps/s at 2048^2 (1 GB300)"
+UNIT = "grid-pt*steps/s"
+
+
+def hv_coefficient(n: int) -> float:
+    """Reference HV form w = c (|k|/kmax)^4 (cutoff_ratio 0, order 4) equals nu_h |k|^4
+    with c = nu_h kmax^4; nu_h makes w(2/3 kmax) * dt_ref = 1 with dt_ref = CFL dx / 3."""
+    kmax = math.hypot(n / 2, n / 2)
+    dt_ref = CFL * (2 * math.pi / n) / 3.0
+    kd = 2.0 / 3.0 * kmax
+    nu_h = 1.0 / (kd ** 4 * dt_ref)
+    return nu_h * kmax ** 4
+
+
+def workload_config(n: int) -> dict:
+    return {
+        "workload": f"forced 2-D turbulence {n}^2, RK4 + 2/3 dealiasing, hyperviscosity p=2, "
+                    f"Philox forcing |k| in [4,6] eps=1e-3, adaptive CFL 0.5",
+        "nx": n, "ny": n, "Re": RE, "hv_order": 4, "hv_coefficient": hv_coefficient(n),
+        "forcing": {"kmin": F_KMIN, "kmax": F_KMAX, "epsilon": F_EPS},
+        "ic": {"spectrum": "k^4 exp(-(k/8)^2)", "energy": E0, "seed": IC_SEED},
+        "l2": "256 MiB flush between timed steps (step working set < L2)",
+    }
+
+
+def gpu_params(nsgb_mod, n: int, adaptive: int = 1) -> dict:
+    return dict(Re=RE, cfl_factor=CFL, adaptive_dt=adaptive, dt=1e-4, hv_enabled=1,
+                hv_coefficient=hv_coefficient(n), hv_order=4, hv_cutoff_ratio=0.0,
+                forcing_enabled=1, forcing_kmin=F_KMIN, forcing_kmax=F_KMAX, forcing_epsilon=F_EPS,
+                forcing_seed=F_SEED)
+
+
+# --------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int = 0):
+        self.gpu_index = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.gpu_index), "-f", self.path],
+                stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sms, maxes, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            with open(self.path) as f:
+                for line in f:
+                    parts = [p.strip() for p in line.split(",")]
+                    if len(parts) < 9:
+                        continue
+                    try:
+                        sms.append(float(parts[1]))
+                        maxes.append(float(parts[2]))
+                    except ValueError:
+                        continue
+                    for name, val in zip(names, parts[5:9]):
+                        if val.lower().startswith("active"):
+                            reasons.add(name)
+        except OSError:
+            pass
+        finally:
+            if self.path and os.path.exists(self.path):
+                os.unlink(self.path)
+        if not sms:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sms), "sm_max_mhz": max(maxes), "reasons": sorted(reasons),
+                "samples": len(sms)}
+
+
+# ----------------------------------------------------------------- peaks
+def hbm_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kind: str, n: int, prec: str):
+    """DRAM bytes per launch of a kernel from the committed ncu summary, if recorded."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    try:
+        with open(p) as f:
+            for line in f:
+                if line.startswith("#") or not line.strip():
+                    continue
+                kv = dict(tok.split("=", 1) for tok in line.split() if "=" in tok)
+                if kv.get("kernel") == kind and int(kv.get("n", 0)) == n and kv.get("prec") == prec:
+                    return float(kv["dram_bytes_per_launch"])
+    except (OSError, ValueError, KeyError):
+        pass
+    return None
+
+
+def model_bytes(n: int, elem: int):
+    """Algorithmic HBM bytes per launch: row kernel 5A, column kernel 5A + 11C/4
+    (A = Kx*ny, C = Kx*Ky complex values; 40A + 11C per RK4 step)."""
+    nkx = n // 2 + 1
+    kx = (2 * nkx) // 3 + 1
+    ky = 2 * ((2 * n) // 6) + 1
+    A, Cc = kx * n, kx * ky
+    return {"row": 5 * A * elem, "col": (5 * A + 11 * Cc / 4) * elem, "step": (40 * A + 11 * Cc) * elem}
+
+
+# ------------------------------------------------------------ CPU legs
+def cpu_sample(n: int, budget_s: float, max_steps: int):
+    """Time the oracle restatement (FP64, OpenMP) on the workload for up to budget_s."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build(ref=False)
+    lib = O.load("port")
+    s = O.Solver(lib, n, n, Re=RE).setup(ic=None)
+    lib.nso_ext_init_random_spectrum(s.ptr, IC_SEED, K0, E0)
+    s.set_hyperviscosity(enabled=1, coefficient=hv_coefficient(n), order=4, cutoff_ratio=0.0)
+    s.d.cfl_factor = CFL
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < max_steps:
+        lib.nso_ext_run(s.ptr, 1, 1, 1, F_KMIN, F_KMAX, F_EPS, F_SEED, steps)
+        steps += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    el = time.perf_counter() - t0
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": n * n * steps / el, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{steps} RK4 step(s) of the {n}^2 workload in FP64 on the oracle restatement "
+                      f"(project FFT shim, not FFTW), {el:.1f} s"}
+
+
+# ---------------------------------------------------------------- main
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def reduce_max(x: float, ws: int):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws: int):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return 0
+    budget = float(os.environ.get("NS_BENCH_REF_BUDGET_S", "90"))
+    cb = cpu_sample(N, budget, max(1, args.steps))
+    line = {
+        "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": N * N / cb["value"] * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(N), "impl": "reference",
+        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--kernels-only", action="store_true",
+                    help="only warmup + timed steps (a short launch sequence for ncu captures); prints no JSON")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    ws, rank, local = dist_env()
+    if ws > 1:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        rc = run_reference(args, ws, rank)
+        if ws > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+        return rc
+
+    import numpy as np
+    import nsgb
+
+    n = args.n
+    prec = nsgb.FP32 if args.precision == "fp32" else nsgb.FP64
+    g = nsgb.Gpu(n, n, precision=prec)
+    g.set_params(**gpu_params(nsgb, n))
+    g.random_spectrum(IC_SEED, K0, E0)
+    g.advance(args.warmup)
+    g.sync()
+    if args.kernels_only:
+        g.advance(args.steps)
+        g.sync()
+        d = g.diagnostics()
+        print(f"kernels-only: {n}^2 {args.precision} {args.steps} steps, E={d['energy']:.6e}", file=sys.stderr)
+        g.close()
+        return 0
+
+    barrier(ws)
+    launches0 = g.launches()
+    import ctypes as C
+
+    total = C.c_double()
+    with ClockSampler(0) as clk:
+        t_wall0 = time.perf_counter()
+        g.check(g.lib.ns_gpu_advance_timed(g.h, args.steps, C.c_size_t(FLUSH_BYTES), C.byref(total), None),
+                "advance_timed")
+        t_wall = time.perf_counter() - t_wall0
+    clocks = clk.summary()
+    launches = g.launches() - launches0
+    ms_total = reduce_max(total.value, ws)
+    barrier(ws)
+    diag = g.diagnostics()
+    value = n * n * args.steps * ws / (ms_total * 1e-3)
+
+    # per-kernel CUDA-event timing for the roofline (separate pass, same flush)
+    prof_steps = min(args.steps, 50)
+    kms = (C.c_double * 2)()
+    kcnt = (C.c_int * 2)()
+    g.check(g.lib.ns_gpu_profile_kernels(g.h, prof_steps, C.c_size_t(FLUSH_BYTES), kms, kcnt), "profile_kernels")
+    mb = model_bytes(n, 8)
+    row_ms, col_ms = kms[0] / max(kcnt[0], 1), kms[1] / max(kcnt[1], 1)
+    dom = "row" if kms[0] >= kms[1] else "col"
+    dom_ms = row_ms if dom == "row" else col_ms
+    peak, peak_src = hbm_peak()
+    achieved = mb[dom] / (dom_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": ncu_traffic(dom, n, "fp32"), "kernel": f"k_{dom} (FP32, {n}^2)",
+                "peak_source": peak_src,
+                "algorithmic_bytes_per_launch": mb[dom], "mean_launch_ms": dom_ms,
+                "kernels": {"row": {"mean_ms": row_ms, "launches": kcnt[0], "bytes": mb["row"],
+                                    "GBps": mb["row"] / (row_ms * 1e-3) / 1e9},
+                            "col": {"mean_ms": col_ms, "launches": kcnt[1], "bytes": mb["col"],
+                                    "GBps": mb["col"] / (col_ms * 1e-3) / 1e9}},
+                "step_model_bytes": mb["step"],
+                "step_GBps": mb["step"] / (ms_total / args.steps * 1e-3) / 1e9}
+
+    # FP32 bulk vs FP64 on the device, same IC and forcing, short horizon
+    cmp_steps = 20
+    g64 = nsgb.Gpu(n, n, precision=nsgb.FP64)
+    g32 = nsgb.Gpu(n, n, precision=nsgb.FP32)
+    for x in (g64, g32):
+        x.set_params(**gpu_params(nsgb, n))
+        x.random_spectrum(IC_SEED, K0, E0)
+        x.advance(cmp_steps)
+    a = g32.download(("omega_hat",))
+    b = g64.download(("omega_hat",))
+    d32, d64 = g32.diagnostics(), g64.diagnostics()
+    fp32_cmp = {"steps": cmp_steps,
+                "rel_l2_vorticity": float(np.linalg.norm(a["omega_hat"] - b["omega_hat"]) / np.linalg.norm(b["omega_hat"])),
+                "energy_rel_err": abs(d32["energy"] - d64["energy"]) / abs(d64["energy"]),
+                "enstrophy_rel_err": abs(d32["enstrophy"] - d64["enstrophy"]) / abs(d64["enstrophy"]),
+                "t_fp32": d32["t"], "t_fp64": d64["t"]}
+    g64.close()
+    g32.close()
+
+    # end to end through the drop-in reference API (host arrays, copies inside the timing)
+    e2e = None
+    if not args.no_e2e:
+        s = nsgb.Solver(n, n, Re=RE, precision=nsgb.FP32).setup(ic=None)
+        s.set_hyperviscosity(enabled=1, coefficient=hv_coefficient(n), order=4, cutoff_ratio=0.0)
+        s.set_forcing(F_KMIN, F_KMAX, F_EPS, F_SEED)
+        s.d.cfl_factor = CFL
+        s.random_spectrum(IC_SEED, K0, E0)
+        s.advance(2, adaptive=True)
+        e_steps = max(3, min(args.steps, 20))
+        t0 = time.perf_counter()
+        s.advance(e_steps, adaptive=True)
+        el = time.perf_counter() - t0
+        nr, nc = n * n * 8, (n // 2 + 1) * n * 16
+        e2e = {"value": n * n * e_steps / el, "unit": UNIT, "steps": e_steps,
+               "h2d_bytes_per_step": 2 * nr + 2 * nc, "d2h_bytes_per_step": 4 * nc + 3 * nr,
+               "path": "ns_spectral_compute_cfl_timestep + ns_spectral_advance_rk4 per step (FP32 instance)"}
+        s.close()
+
+    cpu = None
+    if not args.no_cpu and rank == 0 and ws == 1:
+        cpu = cpu_sample(n, float(os.environ.get("NS_BENCH_CPU_BUDGET_S", "15")), 20)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_total / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic", "config": workload_config(n),
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+        "gpu_launches": launches, "wall_s_timed_region": t_wall,
+        "fp32_vs_fp64": fp32_cmp,
+        "diagnostics": {"energy": diag["energy"], "enstrophy": diag["enstrophy"], "t": diag["t"], "dt": diag["dt"]},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    g.close()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,203 @@
+/*
+ * ns_gpu.h -- thin C-ABI over the sm_103a kernels of the pseudospectral step.
+ *
+ * Plain pointers and sizes only; no CUDA or framework types cross this
+ * boundary.  Host arrays use the reference solver's layouts
+ * (src/spectral/ns_spectral_solver.h:22-68 of DiogoRibeiro7/navier-stokes-solvers):
+ *   real fields      double[ny][nx]             (idx = j*nx + i)
+ *   spectral fields  double complex[nky][nkx]   (interleaved re,im; nkx = nx/2+1, nky = ny)
+ *
+ * Every function returns an ns_gpu_status (0 = success).  Errors are never
+ * silent: a failing call returns non-zero and records a message retrievable
+ * with ns_gpu_last_error().  There is no CPU fallback: without a CUDA device
+ * ns_gpu_create fails with NS_GPU_ERR_NO_DEVICE.
+ *
+ * Each entry point names the reference routine whose work it performs
+ * (file:line in the reference project).  The drop-in implementation of the
+ * reference header (include/ns_spectral_solver.h) is written on top of this
+ * layer; an FFI binding (ctypes, cgo, JNI) can bind either.
+ */
+#ifndef NS_GPU_H
+#define NS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ns_gpu ns_gpu;
+
+typedef enum {
+    NS_GPU_OK = 0,
+    NS_GPU_ERR_INVALID = 1,     /* bad argument (size, NULL pointer, range) */
+    NS_GPU_ERR_NO_DEVICE = 2,   /* no CUDA device / driver */
+    NS_GPU_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+    NS_GPU_ERR_ALLOC = 4,       /* device allocation failed */
+    NS_GPU_ERR_DIVERGED = 5     /* non-finite values detected in the state */
+} ns_gpu_status;
+
+enum { NS_GPU_FP64 = 0, NS_GPU_FP32 = 1 };
+
+/* Solver parameters.  Fields mirror NSSpectralData scalars and
+ * NSSpectralHyperviscosityConfig (src/spectral/ns_spectral_solver.h:8-29)
+ * plus the forcing extension. */
+typedef struct {
+    double Re;                 /* Reynolds number, nu = 1/Re */
+    double cfl_factor;         /* CFL safety factor (reference default 0.3) */
+    int adaptive_dt;           /* 1: dt from the reference CFL rule at every step, on the device */
+    double dt;                 /* fixed dt when adaptive_dt == 0 */
+    /* hyperviscosity and selective frequency damping (hyperviscosity.c:15-178) */
+    int hv_enabled;
+    double hv_coefficient;
+    int hv_order;
+    double hv_cutoff_ratio;
+    int sfd_enabled;
+    double sfd_strength;
+    double sfd_timescale;
+    /* white-in-time forcing on the shell kmin <= |k| <= kmax with energy
+     * injection rate epsilon (Philox4x64-10 counter RNG keyed by seed) */
+    int forcing_enabled;
+    double forcing_kmin;
+    double forcing_kmax;
+    double forcing_epsilon;
+    uint64_t forcing_seed;
+} ns_gpu_params;
+
+/* ----------------------------------------------------------- lifetime */
+
+/* Replaces the device side of ns_spectral_allocate / initialize_fft_plans
+ * (spectral_memory.c:6-68, spectral_initialization.c:57-69).  nx, ny must be
+ * powers of two in [8, 4096]; precision is NS_GPU_FP64 or NS_GPU_FP32. */
+int ns_gpu_create(int nx, int ny, double Lx, double Ly, int precision, ns_gpu **out);
+/* Per-instance teardown (spectral_memory.c:71-104 without the global fftw_cleanup). */
+void ns_gpu_destroy(ns_gpu *g);
+const char *ns_gpu_last_error(const ns_gpu *g);
+const char *ns_gpu_status_string(int status);
+/* kept (dealiased) mode counts: kx columns 0..kx_kept-1, ky rows |band| <= (ky_kept-1)/2 */
+int ns_gpu_dims(const ns_gpu *g, int *kx_kept, int *ky_kept);
+int ns_gpu_set_params(ns_gpu *g, const ns_gpu_params *p);
+int ns_gpu_synchronize(ns_gpu *g);
+/* number of kernels this library has launched on the instance's stream */
+uint64_t ns_gpu_launch_count(const ns_gpu *g);
+
+/* ------------------------------------------------ geometry and tables */
+
+/* Grid, wavenumbers, k^2 and the 2/3 mask computed on the device and copied
+ * to host arrays (spectral_initialization.c:10-50).  Any pointer may be NULL. */
+int ns_gpu_geometry(ns_gpu *g, double *x, double *y, double *kx, double *ky, double *k2, int *mask);
+/* Hyperviscosity weights (hyperviscosity.c:60-102): computes kmax over all
+ * modes on the device, derives the cutoff and inverse bandwidth exactly as the
+ * reference, stores the weight table on the device and copies it to
+ * weights_out ([nky][nkx], may be NULL).  Uses the hv_* fields of the params. */
+int ns_gpu_hv_weights(ns_gpu *g, double *kmax, double *cutoff_wavenumber, double *inv_bandwidth,
+                      double *weights_out);
+
+/* ------------------------------------- transforms over host arrays */
+
+/* physical -> spectral: r2c, scale 1/(nx*ny), dealias (spectral_transforms.c:9-22) */
+int ns_gpu_forward(ns_gpu *g, const double *field, double *field_hat);
+/* spectral -> physical: dealias then unnormalised c2r (spectral_transforms.c:25-32).
+ * masked_copy (may be NULL) receives the dealiased input, the reference's
+ * nonlinear_hat scratch contents after the call. */
+int ns_gpu_inverse(ns_gpu *g, const double *field_hat, double *field, double *masked_copy);
+/* zero every mode outside the 2/3 mask, in place (spectral_transforms.c:35-43) */
+int ns_gpu_dealias(ns_gpu *g, double *field_hat);
+/* psi = -omega/k^2, u_hat = i ky psi, v_hat = -i kx psi (spectral_core.c:8-34) */
+int ns_gpu_velocity(ns_gpu *g, const double *omega_hat, double *psi_hat, double *u_hat, double *v_hat);
+/* velocity_from_vorticity plus the three masked c2r of u, v, omega
+ * (spectral_core.c:37-43).  masked_copy receives the dealiased omega_hat. */
+int ns_gpu_derivatives(ns_gpu *g, const double *omega_hat, double *psi_hat, double *u_hat,
+                       double *v_hat, double *u, double *v, double *omega, double *masked_copy);
+/* N_hat = -mask(r2c(psi_x omega_y - psi_y omega_x))/(nx ny) from omega_hat and the
+ * stored psi_hat (spectral_core.c:46-112).  The five physical outputs (may be
+ * NULL) receive psi_x, psi_y, omega_x, omega_y and the Jacobian. */
+int ns_gpu_nonlinear(ns_gpu *g, const double *omega_hat, const double *psi_hat, double *nonlinear_hat,
+                     double *psi_x, double *psi_y, double *omega_x, double *omega_y, double *jacobian);
+/* rhs -= w state + s ramp (state - sfd) over all modes (hyperviscosity.c:104-150) */
+int ns_gpu_hv_apply(ns_gpu *g, double *rhs_hat, const double *state_hat, const double *sfd_hat);
+/* sfd <- (1-a) sfd + a state, a = clamp(dt/tau) (hyperviscosity.c:152-178) */
+int ns_gpu_hv_post_step(ns_gpu *g, const double *state_hat, double *sfd_hat, double dt);
+
+enum { NS_GPU_REDUCE_CFL = 0, NS_GPU_REDUCE_ENERGY = 1, NS_GPU_REDUCE_ENSTROPHY = 2 };
+/* Reductions over host real arrays with FP64 compensated accumulation:
+ * CFL dt from max|u| (spectral_time_integration.c:9-31), energy mean 0.5(u^2+v^2)
+ * (spectral_analysis.c:8-19), enstrophy mean 0.5 omega^2 (:22-33). */
+int ns_gpu_reduce(ns_gpu *g, int kind, const double *a, const double *b, double *out);
+/* Spectral statistics of host spectra: resolution fraction above 0.8 kmax
+ * (spectral_analysis.c:36-66), max|omega_hat| and high-mode error (:69-100),
+ * shell-binned energy sums and counts of 0.5(|u_hat|^2+|v_hat|^2) over
+ * nbins = min(nkx, nky/2) bins (:103-142).  Outputs may be NULL. */
+int ns_gpu_spectral_stats(ns_gpu *g, const double *omega_hat, const double *u_hat, const double *v_hat,
+                          double *resolution_fraction, double *max_abs, double *spectral_error,
+                          double *bin_energy, int *bin_count);
+/* Taylor-Green initial fields (spectral_initialization.c:72-95): u, v, omega, p */
+int ns_gpu_taylor_green(ns_gpu *g, double *u, double *v, double *omega, double *p);
+
+/* ------------------------------------------------------ stepping */
+
+/* Copy the caller's spectral state to the device.  psi_hat is the stream
+ * function used by the first stage (the reference reads the stored psi_hat
+ * there, spectral_core.c:51,66,76); NULL means -omega_hat/k^2.  sfd_hat may be
+ * NULL when SFD is off.  step0 seeds the forcing counter. */
+int ns_gpu_upload_state(ns_gpu *g, const double *omega_hat, const double *psi_hat, const double *sfd_hat,
+                        double t, double dt, uint64_t step0);
+/* Advance nsteps classical RK4 steps on the device (spectral_time_integration.c:34-106,
+ * plus the forcing extension), with device-side CFL dt when adaptive. */
+int ns_gpu_advance(ns_gpu *g, int nsteps);
+/* Copy the device state back in reference layouts; any pointer may be NULL.
+ * psi_hat/u_hat/v_hat are recomputed from omega_hat as compute_derivatives does;
+ * u, v, omega are the masked inverse transforms. */
+int ns_gpu_download_state(ns_gpu *g, double *omega_hat, double *psi_hat, double *u_hat, double *v_hat,
+                          double *sfd_hat, double *u, double *v, double *omega, double *t, double *dt);
+/* Advance nsteps, timing each step with CUDA events on the instance stream.
+ * When flush_bytes > 0 a device buffer of that size is overwritten between
+ * steps, outside the timed events, so no timed step starts with the previous
+ * step's data resident in L2.  total_ms receives the sum of the step times,
+ * step_ms (nsteps entries, may be NULL) each step's time. */
+int ns_gpu_advance_timed(ns_gpu *g, int nsteps, size_t flush_bytes, double *total_ms, double *step_ms);
+/* Same stepping with CUDA events around every kernel launch: kernel_ms[0] and
+ * counts[0] total the row (x-pass) kernels, kernel_ms[1] and counts[1] the
+ * column (y-pass) kernels. */
+int ns_gpu_profile_kernels(ns_gpu *g, int nsteps, size_t flush_bytes, double *kernel_ms, int *counts);
+/* Energy, enstrophy (Parseval over the dealiased state, FP64 compensated),
+ * and time of the device state. */
+int ns_gpu_diagnostics(ns_gpu *g, double *energy, double *enstrophy, double *t, double *dt);
+/* Seeded random-phase vorticity with E(k) ~ k^4 exp(-(k/k0)^2) rescaled to the
+ * given kinetic energy, written to the device state (no reference counterpart). */
+int ns_gpu_init_random_spectrum(ns_gpu *g, uint64_t seed, double k0, double energy);
+/* Same field, also copied to a host-layout array omega_hat[nky][nkx]. */
+int ns_gpu_random_spectrum_host(ns_gpu *g, uint64_t seed, double k0, double energy, double *omega_hat);
+
+/* ------------------------------------------------ reference forcing stream */
+
+/* ns_forcing_state_init's shell selection (forcing.c:53-103) on the device:
+ * weights[idx] = 1 where kmin <= sqrt(k2[idx]) <= kmax; returns the count. */
+int ns_gpu_forcing_weights(ns_gpu *g, const double *k2, int n, double kmin, double kmax,
+                           double *weights, int *active);
+/* ns_forcing_generate (forcing.c:117-184) on the device: reproduces the
+ * reference splitmix64 + Box-Muller stream counter-addressably (mode m of a call
+ * whose generator state is s uses draws s+(2m+1)G and s+(2m+2)G), OU update for
+ * colored noise, global rescale to energy_target.  rng_state is advanced by
+ * 2*active draws. */
+int ns_gpu_forcing_generate(ns_gpu *g, int n, const double *weights, int active, int colored,
+                            double dt, double correlation_time, double energy_target,
+                            uint64_t *rng_state, double *colored_state, double *forcing_out);
+
+/* ------------------------------------------- device-resident access */
+
+/* Zero-initialised page-locked host memory for arrays that are copied to and
+ * from the device every step (the drop-in allocates its host arrays here). */
+void *ns_gpu_host_alloc(size_t bytes);
+void ns_gpu_host_free(void *ptr);
+
+/* Raw device pointer to the kept-mode vorticity state (layout [kx_kept][ky_kept]
+ * complex of the instance precision) for callers that keep data on the GPU. */
+void *ns_gpu_state_device_ptr(ns_gpu *g);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NS_GPU_H */

@@ -1,0 +1,215 @@
+// Shared-memory Stockham FFT engine for sm_103a (FP32 and FP64).
+//
+// One CTA transforms B independent sequences of length L (a power of two)
+// held in shared memory.  Each transform is owned by TT = L / E threads; every
+// thread keeps E complex values in registers per pass and exchanges them
+// through shared memory between passes (load -> sync -> butterflies -> store ->
+// sync).  Passes use radix min(E, remaining) in {16, 8, 4, 2}, so a length-2048
+// transform with E = 16 takes three passes (16, 16, 8).
+//
+// Pass p with radix R over Ns = product of earlier radices (Stockham autosort,
+// output in natural order):
+//   butterfly j in [0, L/R):  a_r = X[j + r L/R]  (r < R)
+//                             a_r *= W_{Ns R}^{+-(j mod Ns) r}
+//                             a   = DFT_R(a)
+//                             Y[(j - j mod Ns) R + j mod Ns + r Ns] = a_r
+// Forward uses W = exp(-2 pi i / n), backward its conjugate; both unnormalised.
+// Twiddles come from a per-length table tw[t] = exp(-2 pi i t / L) generated in
+// FP64 on the device and rounded once to the working precision.
+//
+// Shared-memory addresses are padded by one element every 16 (spad) so the
+// strided butterfly stores of the early passes spread over the banks.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace nsg {
+
+template <typename T> struct CT;
+template <> struct CT<float> { typedef float2 C; };
+template <> struct CT<double> { typedef double2 C; };
+
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+    C r;
+    r.x = a.x * b.x - a.y * b.y;
+    r.y = a.x * b.y + a.y * b.x;
+    return r;
+}
+template <typename C, typename T> __device__ __forceinline__ C cscale(C a, T s) { C r; r.x = a.x * s; r.y = a.y * s; return r; }
+template <typename C> __device__ __forceinline__ C cconj(C a) { C r; r.x = a.x; r.y = -a.y; return r; }
+template <typename C> __device__ __forceinline__ C cmake(double x, double y) { C r; r.x = x; r.y = y; return r; }
+// multiply by -i (forward) or +i (backward)
+template <bool INV, typename C> __device__ __forceinline__ C cmul_mi(C a) {
+    C r;
+    if (INV) { r.x = -a.y; r.y = a.x; } else { r.x = a.y; r.y = -a.x; }
+    return r;
+}
+
+__device__ __forceinline__ int spad(int i) { return i + (i >> 4); }
+// padded shared-memory length of one transform of length L
+__host__ __device__ inline int spad_len(int L) { return L + (L >> 4) + 4; }
+
+// ---------------------------------------------------------------- DFTs
+template <bool INV, typename C> __device__ __forceinline__ void dft2(C* a) {
+    C t = a[0];
+    a[0] = cadd(t, a[1]);
+    a[1] = csub(t, a[1]);
+}
+
+template <bool INV, typename C> __device__ __forceinline__ void dft4(C* a) {
+    C t0 = cadd(a[0], a[2]);
+    C t1 = csub(a[0], a[2]);
+    C t2 = cadd(a[1], a[3]);
+    C t3 = cmul_mi<INV>(csub(a[1], a[3]));
+    a[0] = cadd(t0, t2);
+    a[2] = csub(t0, t2);
+    a[1] = cadd(t1, t3);
+    a[3] = csub(t1, t3);
+}
+
+// y_k = E_k + W8^k O_k, y_{k+4} = E_k - W8^k O_k with E, O the DFT4 of even/odd inputs
+template <bool INV, typename C> __device__ __forceinline__ void dft8(C* a) {
+    typedef decltype(a[0].x) T;
+    const T r = (T)0.70710678118654752440;
+    C e[4] = {a[0], a[2], a[4], a[6]};
+    C o[4] = {a[1], a[3], a[5], a[7]};
+    dft4<INV>(e);
+    dft4<INV>(o);
+    C w1, w2, w3;
+    if (!INV) {
+        w1.x = r * (o[1].x + o[1].y); w1.y = r * (o[1].y - o[1].x);
+        w3.x = r * (o[3].y - o[3].x); w3.y = -r * (o[3].x + o[3].y);
+    } else {
+        w1.x = r * (o[1].x - o[1].y); w1.y = r * (o[1].x + o[1].y);
+        w3.x = -r * (o[3].x + o[3].y); w3.y = r * (o[3].x - o[3].y);
+    }
+    w2 = cmul_mi<INV>(o[2]);
+    a[0] = cadd(e[0], o[0]); a[4] = csub(e[0], o[0]);
+    a[1] = cadd(e[1], w1);   a[5] = csub(e[1], w1);
+    a[2] = cadd(e[2], w2);   a[6] = csub(e[2], w2);
+    a[3] = cadd(e[3], w3);   a[7] = csub(e[3], w3);
+}
+
+// y_k = E_k + W16^k O_k, y_{k+8} = E_k - W16^k O_k
+template <bool INV, typename C> __device__ __forceinline__ void dft16(C* a) {
+    typedef decltype(a[0].x) T;
+    const T c1 = (T)0.92387953251128675613;  // cos(pi/8)
+    const T s1 = (T)0.38268343236508977173;  // sin(pi/8)
+    const T r = (T)0.70710678118654752440;
+    C e[8], o[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) { e[k] = a[2 * k]; o[k] = a[2 * k + 1]; }
+    dft8<INV>(e);
+    dft8<INV>(o);
+    const T sg = INV ? (T)1 : (T)-1;  // sign of the imaginary part of W16^k for k in (0,8)
+    C w[8];
+    w[0] = cmake<C>(1.0, 0.0);
+    w[1] = cmake<C>(c1, sg * s1);
+    w[2] = cmake<C>(r, sg * r);
+    w[3] = cmake<C>(s1, sg * c1);
+    w[4] = cmake<C>(0.0, sg);
+    w[5] = cmake<C>(-s1, sg * c1);
+    w[6] = cmake<C>(-r, sg * r);
+    w[7] = cmake<C>(-c1, sg * s1);
+    C ow[8];
+    ow[0] = o[0];
+    ow[4] = cmul_mi<INV>(o[4]);
+#pragma unroll
+    for (int k = 1; k < 8; ++k)
+        if (k != 4) ow[k] = cmul(o[k], w[k]);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        a[k] = cadd(e[k], ow[k]);
+        a[k + 8] = csub(e[k], ow[k]);
+    }
+}
+
+template <int R, bool INV, typename C> __device__ __forceinline__ void dftR(C* a) {
+    if (R == 2) dft2<INV>(a);
+    else if (R == 4) dft4<INV>(a);
+    else if (R == 8) dft8<INV>(a);
+    else dft16<INV>(a);
+}
+
+// ---------------------------------------------------------------- passes
+// Load this thread's butterflies of a radix-R pass: v[q R + r] = X[j_q + r L/R], j_q = t + q TT
+template <int E, int R, typename C>
+__device__ __forceinline__ void pass_load(C (&v)[E], const C* sb, int L, int t, int TT) {
+    const int LR = L / R;
+#pragma unroll
+    for (int q = 0; q < E / R; ++q) {
+        const int j = t + q * TT;
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[q * R + r] = sb[spad(j + r * LR)];
+    }
+}
+
+template <int E, int R, bool INV, typename C>
+__device__ __forceinline__ void pass_compute_store(C (&v)[E], C* sb, int L, int Ns, int t, int TT,
+                                                   const C* __restrict__ tw) {
+#pragma unroll
+    for (int q = 0; q < E / R; ++q) {
+        const int j = t + q * TT;
+        const int k = j & (Ns - 1);
+        C* a = &v[q * R];
+        if (Ns > 1) {
+            const int step = (L / (Ns * R)) * k;
+#pragma unroll
+            for (int r = 1; r < R; ++r) {
+                C w = __ldg(&tw[step * r]);
+                if (INV) w.y = -w.y;
+                a[r] = cmul(a[r], w);
+            }
+        }
+        dftR<R, INV>(a);
+        const int base = (j - k) * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) sb[spad(base + r * Ns)] = a[r];
+    }
+}
+
+template <int LOGE> struct ConstLog;
+
+// In-place FFT of the sequence at sb (padded, natural order in and out).
+// All threads of the CTA must call this (it synchronises); thread t < TT of
+// this transform, TT = L / E.
+template <int E, bool INV, typename C>
+__device__ void fft_smem(C* sb, int L, int logL, int t, int TT, const C* __restrict__ tw) {
+    C v[E];
+    const int logE = (E == 16) ? 4 : (E == 8) ? 3 : (E == 4) ? 2 : 1;
+    int Ns = 1;
+    int rem = logL;
+    while (rem > 0) {
+        const int lr = rem < logE ? rem : logE;
+        if (lr == 4) {
+            if constexpr (E >= 16) {
+                pass_load<E, 16>(v, sb, L, t, TT);
+                __syncthreads();
+                pass_compute_store<E, 16, INV>(v, sb, L, Ns, t, TT, tw);
+            }
+        } else if (lr == 3) {
+            if constexpr (E >= 8) {
+                pass_load<E, 8>(v, sb, L, t, TT);
+                __syncthreads();
+                pass_compute_store<E, 8, INV>(v, sb, L, Ns, t, TT, tw);
+            }
+        } else if (lr == 2) {
+            if constexpr (E >= 4) {
+                pass_load<E, 4>(v, sb, L, t, TT);
+                __syncthreads();
+                pass_compute_store<E, 4, INV>(v, sb, L, Ns, t, TT, tw);
+            }
+        } else {
+            pass_load<E, 2>(v, sb, L, t, TT);
+            __syncthreads();
+            pass_compute_store<E, 2, INV>(v, sb, L, Ns, t, TT, tw);
+        }
+        __syncthreads();
+        Ns <<= lr;
+        rem -= lr;
+    }
+}
+
+}  // namespace nsg

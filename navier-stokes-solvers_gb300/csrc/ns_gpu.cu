@@ -1,0 +1,1172 @@
+// Host engine and C-ABI (include/ns_gpu.h) for the sm_103a pseudospectral step.
+//
+// One ns_gpu instance owns one CUDA stream and every device buffer of one
+// solver (no global state, so many instances can live side by side; the
+// reference's global fftw_cleanup in spectral_memory.c:100-103 has no
+// counterpart).  All work is issued on the instance stream; the host-array
+// entry points synchronise that stream before returning.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ns_gpu.h"
+#include "ns_kernels.cuh"
+
+using namespace nsg;
+
+struct ns_gpu {
+    Geo g;
+    int prec;
+    int ER, EC;
+    int device;
+    cudaStream_t st;
+    std::string err;
+    unsigned long long launches;
+    ns_gpu_params p;
+    int params_set;
+    double hv_kmax, hv_cutoff, hv_inv_bw;
+    double f_sigma;
+    // device buffers (complex of the instance precision unless noted)
+    void* F[4];
+    void* G;
+    void *W0, *WS, *ACC, *PSI0, *SFD, *KS, *KP;
+    void *hvw, *sfdw, *kxv, *kyv, *twc, *twr, *twh;
+    double* hvw_full;   // FP64 [nky][nkx]
+    DevScalars* ds;
+    double2* part;      // reduction partials
+    int part_n;
+    double* dres;       // small FP64 results
+    int* dflag;
+    // host-layout FP64 staging (allocated on first use)
+    double2* spec[5];
+    double* real[5];
+    double2 *out, *outsfd;  // masked-out modes of the state (FP64)
+    int outside_active;
+    int fields_valid;   // F holds the stage-1 fields of the current state
+    int psi0_valid;     // PSI0 holds the caller's psi_hat for the next prologue
+    void* scratch;
+    size_t scratch_bytes;
+    void* flushbuf;     // L2 flush target of the timed entry points
+    size_t flush_bytes;
+    // kernel-level profiling: events around every launch while non-null
+    struct ProfRec { cudaEvent_t a, b; int kind; };
+    std::vector<ProfRec>* prof;
+};
+
+// record an event pair around one launch when kernel profiling is on
+struct ProfScope {
+    ns_gpu* g;
+    int kind;
+    cudaEvent_t a, b;
+    ProfScope(ns_gpu* g_, int kind_) : g(g_), kind(kind_), a(nullptr), b(nullptr) {
+        if (g->prof) {
+            cudaEventCreate(&a);
+            cudaEventCreate(&b);
+            cudaEventRecord(a, g->st);
+        }
+    }
+    ~ProfScope() {
+        if (g->prof) {
+            cudaEventRecord(b, g->st);
+            g->prof->push_back({a, b, kind});
+        }
+    }
+};
+
+#define NSG_FAIL(g, code, ...)                                             \
+    do {                                                                   \
+        char _b[512];                                                      \
+        snprintf(_b, sizeof(_b), __VA_ARGS__);                             \
+        if (g) (g)->err = _b;                                              \
+        return (code);                                                     \
+    } while (0)
+
+#define NSG_CUDA(g, call)                                                                    \
+    do {                                                                                     \
+        cudaError_t _e = (call);                                                             \
+        if (_e != cudaSuccess) NSG_FAIL(g, NS_GPU_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(_e)); \
+    } while (0)
+
+#define NSG_LAUNCHED(g)                                                                          \
+    do {                                                                                         \
+        (g)->launches++;                                                                         \
+        cudaError_t _e = cudaGetLastError();                                                     \
+        if (_e != cudaSuccess) NSG_FAIL(g, NS_GPU_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(_e)); \
+    } while (0)
+
+#define NSG_TRY(...)            \
+    do {                        \
+        int _s = (__VA_ARGS__); \
+        if (_s != NS_GPU_OK) return _s; \
+    } while (0)
+
+static int ilog2(int n) {
+    int l = 0;
+    while ((1 << l) < n) ++l;
+    return l;
+}
+static int is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+static int grid_for(long long n, int threads = 256, int cap = 2048) {
+    long long b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > cap) b = cap;
+    return (int)b;
+}
+
+template <typename T> using Cx = typename CT<T>::C;
+
+
+// ------------------------------------------------------------- launchers
+template <typename K> static int set_smem(ns_gpu* g, K kernel, size_t bytes) {
+    if (bytes > 48 * 1024) NSG_CUDA(g, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    return NS_GPU_OK;
+}
+
+template <typename T, int E, int MODE> static int row_launch_e(ns_gpu* g, const RowArgs<T>& a) {
+    const int NF = RowNF<MODE>::v;
+    const int TT = g->g.H / E;
+    const size_t smem = (size_t)NF * g->g.RPC * spad_len(g->g.H) * sizeof(Cx<T>);
+    NSG_TRY(set_smem(g, k_row<T, E, MODE>, smem));
+    k_row<T, E, MODE><<<g->g.ny / g->g.RPC, g->g.RPC * TT, smem, g->st>>>(g->g, a);
+    NSG_LAUNCHED(g);
+    return NS_GPU_OK;
+}
+template <typename T, int MODE> static int row_launch(ns_gpu* g, const RowArgs<T>& a) {
+    return g->ER == 16 ? row_launch_e<T, 16, MODE>(g, a) : row_launch_e<T, 4, MODE>(g, a);
+}
+
+template <typename T, int E, int MODE, int STAGE> static int col_launch_e(ns_gpu* g, const ColArgs<T>& a) {
+    const int TC = g->g.ny / E;
+    const size_t smem = (size_t)g->g.CW * spad_len(g->g.ny) * sizeof(Cx<T>);
+    NSG_TRY(set_smem(g, k_col<T, E, MODE, STAGE>, smem));
+    k_col<T, E, MODE, STAGE><<<g->g.Kxp / g->g.CW, g->g.CW * TC, smem, g->st>>>(g->g, a);
+    NSG_LAUNCHED(g);
+    return NS_GPU_OK;
+}
+template <typename T, int MODE, int STAGE> static int col_launch(ns_gpu* g, const ColArgs<T>& a) {
+    return g->EC == 16 ? col_launch_e<T, 16, MODE, STAGE>(g, a) : col_launch_e<T, 4, MODE, STAGE>(g, a);
+}
+
+template <typename T> static StepParams step_params(const ns_gpu* g) {
+    StepParams sp;
+    memset(&sp, 0, sizeof(sp));
+    sp.Re = g->p.Re;
+    sp.inv_re = 1.0 / g->p.Re;
+    sp.cfl = g->p.cfl_factor;
+    sp.dxmin = fmin(g->g.Lx / g->g.nx, g->g.Ly / g->g.ny);
+    sp.scale = 1.0 / ((double)g->g.nx * (double)g->g.ny);
+    sp.adaptive = g->p.adaptive_dt;
+    sp.hv = (g->p.hv_enabled && g->p.hv_coefficient > 0.0) ? 1 : 0;
+    sp.sfd = (g->p.sfd_enabled && g->p.sfd_strength > 0.0 && g->p.sfd_timescale > 0.0) ? 1 : 0;
+    sp.sfd_tau = g->p.sfd_timescale;
+    sp.forcing = (g->p.forcing_enabled && g->f_sigma > 0.0) ? 1 : 0;
+    sp.f_kmin = g->p.forcing_kmin;
+    sp.f_kmax = g->p.forcing_kmax;
+    sp.f_sigma = g->f_sigma;
+    sp.f_seed = g->p.forcing_seed;
+    return sp;
+}
+
+template <typename T> static RowArgs<T> row_args(ns_gpu* g) {
+    RowArgs<T> a;
+    memset(&a, 0, sizeof(a));
+    a.kxv = (const T*)g->kxv;
+    a.twr = (const Cx<T>*)g->twr;
+    a.twh = (const Cx<T>*)g->twh;
+    a.ds = g->ds;
+    a.G = (Cx<T>*)g->G;
+    return a;
+}
+
+template <typename T> static ColArgs<T> col_args(ns_gpu* g) {
+    ColArgs<T> a;
+    memset(&a, 0, sizeof(a));
+    a.G = (const Cx<T>*)g->G;
+    for (int f = 0; f < 4; ++f) a.F[f] = (Cx<T>*)g->F[f];
+    a.W0 = (Cx<T>*)g->W0;
+    a.WS = (Cx<T>*)g->WS;
+    a.ACC = (Cx<T>*)g->ACC;
+    a.PSI0 = (const Cx<T>*)g->PSI0;
+    a.SFD = (Cx<T>*)g->SFD;
+    a.hvw = (const T*)g->hvw;
+    a.sfdw = (const T*)g->sfdw;
+    a.kxv = (const T*)g->kxv;
+    a.kyv = (const T*)g->kyv;
+    a.twc = (const Cx<T>*)g->twc;
+    a.ds = g->ds;
+    a.sp = step_params<T>(g);
+    a.nfields = 4;
+    return a;
+}
+
+// F <- fields of (W, psi) : Psi, Psi_y, Omega[, Omega_y]
+template <typename T> static int prologue(ns_gpu* g, void* W, void* P, int psi_from_w, int nfields) {
+    ColArgs<T> a = col_args<T>(g);
+    a.W0 = (Cx<T>*)W;
+    a.PSI0 = (const Cx<T>*)P;
+    a.psi_from_w = psi_from_w;
+    a.nfields = nfields;
+    return col_launch<T, COL_PROLOGUE, 0>(g, a);
+}
+
+template <typename T> static int stage_row(ns_gpu* g, int stage) {
+    ProfScope ps(g, 0);
+    RowArgs<T> a = row_args<T>(g);
+    for (int f = 0; f < 4; ++f) a.F[f] = (const Cx<T>*)g->F[f];
+    a.dx[0] = 1; a.dx[1] = 0; a.dx[2] = 1; a.dx[3] = 0;  // psi_x, psi_y, omega_x, omega_y
+    a.cfl = (stage == 1 && g->p.adaptive_dt) ? 1 : 0;
+    a.marker = (stage == 1) ? 1 : (stage == 2 ? 2 : 0);
+    return row_launch<T, ROW_STAGE>(g, a);
+}
+
+template <typename T> static int advance_t(ns_gpu* g, int nsteps) {
+    if (!g->fields_valid) {
+        NSG_TRY(prologue<T>(g, g->W0, g->PSI0, g->psi0_valid ? 0 : 1, 4));
+        g->fields_valid = 1;
+        g->psi0_valid = 0;
+    }
+    ColArgs<T> a = col_args<T>(g);
+    for (int n = 0; n < nsteps; ++n) {
+        NSG_TRY(stage_row<T>(g, 1));
+        { ProfScope ps(g, 1); NSG_TRY((col_launch<T, COL_STAGE, 1>(g, a))); }
+        NSG_TRY(stage_row<T>(g, 2));
+        { ProfScope ps(g, 1); NSG_TRY((col_launch<T, COL_STAGE, 2>(g, a))); }
+        NSG_TRY(stage_row<T>(g, 3));
+        { ProfScope ps(g, 1); NSG_TRY((col_launch<T, COL_STAGE, 3>(g, a))); }
+        NSG_TRY(stage_row<T>(g, 4));
+        { ProfScope ps(g, 1); NSG_TRY((col_launch<T, COL_STAGE, 4>(g, a))); }
+        if (g->outside_active) {
+            const long long nn = (long long)g->g.nkx * g->g.nky;
+            k_outside<<<grid_for(nn), 256, 0, g->st>>>(g->g, a.sp, g->hvw_full, g->hv_cutoff, g->hv_inv_bw,
+                                                       g->p.hv_order > 0 ? g->p.hv_order : 1, g->p.sfd_strength, g->ds,
+                                                       g->out, g->outsfd);
+            NSG_LAUNCHED(g);
+        }
+    }
+    return NS_GPU_OK;
+}
+
+// ------------------------------------------------------------ allocation
+static int dalloc(ns_gpu* g, void** p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        NSG_FAIL(g, NS_GPU_ERR_ALLOC, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+    }
+    e = cudaMemsetAsync(*p, 0, bytes, g->st);
+    if (e != cudaSuccess) NSG_FAIL(g, NS_GPU_ERR_CUDA, "cudaMemset: %s", cudaGetErrorString(e));
+    return NS_GPU_OK;
+}
+
+static int ensure_staging(ns_gpu* g) {
+    if (g->spec[0]) return NS_GPU_OK;
+    const size_t ns = (size_t)g->g.nkx * g->g.nky * sizeof(double2);
+    const size_t nr = (size_t)g->g.nx * g->g.ny * sizeof(double);
+    for (int i = 0; i < 5; ++i) NSG_TRY(dalloc(g, (void**)&g->spec[i], ns));
+    for (int i = 0; i < 5; ++i) NSG_TRY(dalloc(g, (void**)&g->real[i], nr));
+    return NS_GPU_OK;
+}
+
+static int ensure_outside(ns_gpu* g) {
+    if (g->out) return NS_GPU_OK;
+    const size_t ns = (size_t)g->g.nkx * g->g.nky * sizeof(double2);
+    NSG_TRY(dalloc(g, (void**)&g->out, ns));
+    NSG_TRY(dalloc(g, (void**)&g->outsfd, ns));
+    return NS_GPU_OK;
+}
+
+static int ensure_scratch(ns_gpu* g, size_t bytes) {
+    if (g->scratch_bytes >= bytes) return NS_GPU_OK;
+    if (g->scratch) cudaFree(g->scratch);
+    g->scratch = nullptr;
+    g->scratch_bytes = 0;
+    NSG_TRY(dalloc(g, &g->scratch, bytes));
+    g->scratch_bytes = bytes;
+    return NS_GPU_OK;
+}
+
+static int h2d(ns_gpu* g, void* dst, const void* src, size_t bytes) {
+    NSG_CUDA(g, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, g->st));
+    return NS_GPU_OK;
+}
+static int d2h(ns_gpu* g, void* dst, const void* src, size_t bytes) {
+    NSG_CUDA(g, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, g->st));
+    return NS_GPU_OK;
+}
+static int sync(ns_gpu* g) {
+    NSG_CUDA(g, cudaStreamSynchronize(g->st));
+    return NS_GPU_OK;
+}
+static size_t spec_bytes(const ns_gpu* g) { return (size_t)g->g.nkx * g->g.nky * sizeof(double2); }
+static size_t real_bytes(const ns_gpu* g) { return (size_t)g->g.nx * g->g.ny * sizeof(double); }
+
+// tables in the working precision
+template <typename T> static int build_tables(ns_gpu* g) {
+    const long long n = (long long)g->g.Kxp * g->g.Ky;
+    const int sfd = (g->p.sfd_enabled && g->p.sfd_strength > 0.0) ? 1 : 0;
+    const int order = g->p.hv_order > 0 ? g->p.hv_order : 1;
+    k_tables<T><<<grid_for(n), 256, 0, g->st>>>(g->g, g->hvw_full, sfd, g->p.sfd_strength, order, g->hv_cutoff,
+                                                g->hv_inv_bw, (T*)g->kxv, (T*)g->kyv, (T*)g->hvw, (T*)g->sfdw);
+    NSG_LAUNCHED(g);
+    return NS_GPU_OK;
+}
+
+// hyperviscosity.c:60-102 — kmax on the device, cutoff/inverse bandwidth as the reference, FP64 weight table
+static int compute_hv(ns_gpu* g) {
+    NSG_CUDA(g, cudaMemsetAsync(&g->ds->kmax_bits, 0, sizeof(unsigned long long), g->st));
+    const long long n = (long long)g->g.nkx * g->g.nky;
+    k_kmax<<<grid_for(n), 256, 0, g->st>>>(g->g, g->ds);
+    NSG_LAUNCHED(g);
+    unsigned long long bits = 0;
+    NSG_TRY(d2h(g, &bits, &g->ds->kmax_bits, sizeof(bits)));
+    NSG_TRY(sync(g));
+    double kmax;
+    memcpy(&kmax, &bits, sizeof(kmax));
+    double ratio = g->p.hv_cutoff_ratio;
+    ratio = ratio < 0.0 ? 0.0 : (ratio > 1.0 ? 1.0 : ratio);
+    g->hv_kmax = kmax;
+    g->hv_cutoff = ratio * kmax;
+    const double bw = fmax(kmax - g->hv_cutoff, 1e-12);
+    g->hv_inv_bw = (bw > 0.0) ? 1.0 / bw : 0.0;
+    const int enabled = (g->p.hv_enabled && g->p.hv_coefficient > 0.0 && kmax > 0.0) ? 1 : 0;
+    const int order = g->p.hv_order > 0 ? g->p.hv_order : 1;
+    k_hv_weights<<<grid_for(n), 256, 0, g->st>>>(g->g, enabled, g->p.hv_coefficient, order, g->hv_cutoff, g->hv_inv_bw,
+                                                 g->hvw_full);
+    NSG_LAUNCHED(g);
+    return g->prec == NS_GPU_FP64 ? build_tables<double>(g) : build_tables<float>(g);
+}
+
+// forcing amplitude sigma = sqrt(2 eps / sum_full 1/k^2) over the kept modes of the shell
+__global__ void k_forcing_sigma(Geo g, double kmin, double kmax, double2* part) {
+    DD acc = {0.0, 0.0};
+    const long long n = (long long)g.nkx * g.nky;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(idx / g.nkx), i = (int)(idx - (long long)j * g.nkx);
+        const double k2 = geo_k2(g, j, i);
+        const double km = sqrt(k2);
+        if (geo_kept(g, j, i) && k2 > 1e-12 && km >= kmin && km <= kmax) dd_add(acc, (i == 0 ? 1.0 : 2.0) / k2);
+    }
+    DD t = block_dd(acc);
+    if (threadIdx.x == 0) part[blockIdx.x] = make_double2(t.s, t.c);
+}
+
+static int compute_sigma(ns_gpu* g) {
+    g->f_sigma = 0.0;
+    if (!g->p.forcing_enabled || g->p.forcing_epsilon <= 0.0) return NS_GPU_OK;
+    const long long n = (long long)g->g.nkx * g->g.nky;
+    const int nb = grid_for(n, 256, g->part_n);
+    k_forcing_sigma<<<nb, 256, 0, g->st>>>(g->g, g->p.forcing_kmin, g->p.forcing_kmax, g->part);
+    NSG_LAUNCHED(g);
+    k_merge_partials<<<1, 256, 0, g->st>>>(g->part, nb, g->dres);
+    NSG_LAUNCHED(g);
+    double acc = 0.0;
+    NSG_TRY(d2h(g, &acc, g->dres, sizeof(double)));
+    NSG_TRY(sync(g));
+    g->f_sigma = acc > 0.0 ? sqrt(2.0 * g->p.forcing_epsilon / acc) : 0.0;
+    return NS_GPU_OK;
+}
+
+// ================================================================== C-ABI
+// (C linkage comes from the declarations in ns_gpu.h)
+
+const char* ns_gpu_status_string(int s) {
+    switch (s) {
+        case NS_GPU_OK: return "ok";
+        case NS_GPU_ERR_INVALID: return "invalid argument";
+        case NS_GPU_ERR_NO_DEVICE: return "no CUDA device";
+        case NS_GPU_ERR_CUDA: return "CUDA error";
+        case NS_GPU_ERR_ALLOC: return "device allocation failed";
+        case NS_GPU_ERR_DIVERGED: return "non-finite values in the state";
+        default: return "unknown status";
+    }
+}
+
+const char* ns_gpu_last_error(const ns_gpu* g) { return g ? g->err.c_str() : "null instance"; }
+
+void ns_gpu_destroy(ns_gpu* g) {
+    if (!g) return;
+    if (g->st) cudaStreamSynchronize(g->st);
+    void* bufs[] = {g->F[0], g->F[1], g->F[2], g->F[3], g->G, g->W0, g->WS, g->ACC, g->PSI0, g->SFD, g->KS,
+                    g->KP, g->hvw, g->sfdw, g->kxv, g->kyv, g->twc, g->twr, g->twh, g->hvw_full, g->ds, g->part,
+                    g->dres, g->dflag, g->out, g->outsfd, g->scratch, g->flushbuf};
+    for (void* b : bufs)
+        if (b) cudaFree(b);
+    for (int i = 0; i < 5; ++i) {
+        if (g->spec[i]) cudaFree(g->spec[i]);
+        if (g->real[i]) cudaFree(g->real[i]);
+    }
+    if (g->st) cudaStreamDestroy(g->st);
+    delete g;
+}
+
+int ns_gpu_create(int nx, int ny, double Lx, double Ly, int precision, ns_gpu** out) {
+    if (!out) return NS_GPU_ERR_INVALID;
+    *out = nullptr;
+    if (!is_pow2(nx) || !is_pow2(ny) || nx < 8 || ny < 8 || nx > 4096 || ny > 4096) {
+        fprintf(stderr, "ns_gpu_create: nx=%d ny=%d must be powers of two in [8, 4096]\n", nx, ny);
+        return NS_GPU_ERR_INVALID;
+    }
+    if (!(Lx > 0.0) || !(Ly > 0.0) || (precision != NS_GPU_FP64 && precision != NS_GPU_FP32)) return NS_GPU_ERR_INVALID;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev < 1) {
+        fprintf(stderr, "ns_gpu_create: no CUDA device (%s)\n", cudaGetErrorString(e));
+        return NS_GPU_ERR_NO_DEVICE;
+    }
+    ns_gpu* g = new ns_gpu();
+    memset(g->F, 0, sizeof(g->F));
+    g->G = g->W0 = g->WS = g->ACC = g->PSI0 = g->SFD = g->KS = g->KP = nullptr;
+    g->hvw = g->sfdw = g->kxv = g->kyv = g->twc = g->twr = g->twh = nullptr;
+    g->hvw_full = nullptr;
+    g->ds = nullptr;
+    g->part = nullptr;
+    g->dres = nullptr;
+    g->dflag = nullptr;
+    for (int i = 0; i < 5; ++i) { g->spec[i] = nullptr; g->real[i] = nullptr; }
+    g->out = g->outsfd = nullptr;
+    g->scratch = nullptr;
+    g->scratch_bytes = 0;
+    g->flushbuf = nullptr;
+    g->flush_bytes = 0;
+    g->prof = nullptr;
+    g->launches = 0;
+    g->outside_active = 0;
+    g->fields_valid = 0;
+    g->psi0_valid = 0;
+    g->params_set = 0;
+    g->f_sigma = 0.0;
+    g->prec = precision;
+    cudaGetDevice(&g->device);
+    if (cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking) != cudaSuccess) {
+        delete g;
+        return NS_GPU_ERR_CUDA;
+    }
+    Geo& G = g->g;
+    G.nx = nx;
+    G.ny = ny;
+    G.nkx = nx / 2 + 1;
+    G.nky = ny;
+    G.H = nx / 2;
+    G.Kx = (2 * G.nkx) / 3 + 1;
+    G.Kyh = (2 * ny) / 6;
+    G.Ky = 2 * G.Kyh + 1;
+    G.logny = ilog2(ny);
+    G.logH = ilog2(G.H);
+    G.Lx = Lx;
+    G.Ly = Ly;
+    g->ER = G.H >= 16 ? 16 : 4;
+    g->EC = ny >= 16 ? 16 : 4;
+    const size_t cs = (precision == NS_GPU_FP64) ? sizeof(double2) : sizeof(float2);
+    // column tile width: up to 16 columns, <= 512 threads, <= ~100 KB shared memory
+    {
+        const int TC = ny / g->EC;
+        int CW = 1;
+        while (CW < 16 && 2 * CW * TC <= 512 && (size_t)2 * CW * spad_len(ny) * cs <= 100 * 1024 && CW < G.Kx) CW *= 2;
+        G.CW = CW;
+        G.Kxp = ((G.Kx + CW - 1) / CW) * CW;
+    }
+    // rows per CTA: up to 128 threads, <= ~100 KB shared memory for four fields
+    {
+        const int TT = G.H / g->ER;
+        int RPC = 1;
+        while (2 * RPC * TT <= 128 && 2 * RPC <= ny && (size_t)4 * 2 * RPC * spad_len(G.H) * cs <= 100 * 1024) RPC *= 2;
+        G.RPC = RPC;
+    }
+    const size_t A = (size_t)ny * G.Kxp * cs;
+    const size_t Cb = (size_t)G.Kxp * G.Ky * cs;
+    const size_t Rb = (size_t)G.Kxp * G.Ky * (cs / 2);
+    int s = NS_GPU_OK;
+    for (int f = 0; f < 4 && s == NS_GPU_OK; ++f) s = dalloc(g, &g->F[f], A);
+    if (s == NS_GPU_OK) s = dalloc(g, &g->G, A);
+    void** states[] = {&g->W0, &g->WS, &g->ACC, &g->PSI0, &g->SFD, &g->KS, &g->KP};
+    for (void** p : states)
+        if (s == NS_GPU_OK) s = dalloc(g, p, Cb);
+    if (s == NS_GPU_OK) s = dalloc(g, &g->hvw, Rb);
+    if (s == NS_GPU_OK) s = dalloc(g, &g->sfdw, Rb);
+    if (s == NS_GPU_OK) s = dalloc(g, &g->kxv, (size_t)G.Kxp * (cs / 2));
+    if (s == NS_GPU_OK) s = dalloc(g, &g->kyv, (size_t)G.Ky * (cs / 2));
+    if (s == NS_GPU_OK) s = dalloc(g, &g->twc, (size_t)ny * cs);
+    if (s == NS_GPU_OK) s = dalloc(g, &g->twr, (size_t)G.H * cs);
+    if (s == NS_GPU_OK) s = dalloc(g, &g->twh, (size_t)G.H * cs);
+    if (s == NS_GPU_OK) s = dalloc(g, (void**)&g->hvw_full, (size_t)G.nkx * G.nky * sizeof(double));
+    if (s == NS_GPU_OK) s = dalloc(g, (void**)&g->ds, sizeof(DevScalars));
+    g->part_n = 2048;
+    if (s == NS_GPU_OK) s = dalloc(g, (void**)&g->part, (size_t)4 * g->part_n * sizeof(double2));
+    if (s == NS_GPU_OK) s = dalloc(g, (void**)&g->dres, 16 * sizeof(double));
+    if (s == NS_GPU_OK) s = dalloc(g, (void**)&g->dflag, sizeof(int));
+    if (s != NS_GPU_OK) {
+        fprintf(stderr, "ns_gpu_create: %s\n", g->err.c_str());
+        ns_gpu_destroy(g);
+        return s;
+    }
+    if (precision == NS_GPU_FP64) {
+        k_twiddles<<<grid_for(ny), 256, 0, g->st>>>((double2*)g->twc, ny, ny);
+        k_twiddles<<<grid_for(G.H), 256, 0, g->st>>>((double2*)g->twr, G.H, G.H);
+        k_twiddles<<<grid_for(G.H), 256, 0, g->st>>>((double2*)g->twh, G.H, nx);
+    } else {
+        k_twiddles<<<grid_for(ny), 256, 0, g->st>>>((float2*)g->twc, ny, ny);
+        k_twiddles<<<grid_for(G.H), 256, 0, g->st>>>((float2*)g->twr, G.H, G.H);
+        k_twiddles<<<grid_for(G.H), 256, 0, g->st>>>((float2*)g->twh, G.H, nx);
+    }
+    g->launches += 3;
+    // default parameters: the reference allocate defaults (spectral_memory.c:17-19, hyperviscosity.c:15-30)
+    ns_gpu_params p;
+    memset(&p, 0, sizeof(p));
+    p.Re = 1.0;
+    p.cfl_factor = 0.3;
+    p.dt = 0.01;
+    p.hv_order = 8;
+    p.hv_cutoff_ratio = 0.65;
+    p.sfd_timescale = 1.0;
+    s = ns_gpu_set_params(g, &p);
+    if (s != NS_GPU_OK) {
+        fprintf(stderr, "ns_gpu_create: %s\n", g->err.c_str());
+        ns_gpu_destroy(g);
+        return s;
+    }
+    *out = g;
+    return NS_GPU_OK;
+}
+
+int ns_gpu_dims(const ns_gpu* g, int* kx_kept, int* ky_kept) {
+    if (!g) return NS_GPU_ERR_INVALID;
+    if (kx_kept) *kx_kept = g->g.Kx;
+    if (ky_kept) *ky_kept = g->g.Ky;
+    return NS_GPU_OK;
+}
+
+uint64_t ns_gpu_launch_count(const ns_gpu* g) { return g ? g->launches : 0; }
+
+int ns_gpu_synchronize(ns_gpu* g) {
+    if (!g) return NS_GPU_ERR_INVALID;
+    return sync(g);
+}
+
+int ns_gpu_set_params(ns_gpu* g, const ns_gpu_params* p) {
+    if (!g || !p) return NS_GPU_ERR_INVALID;
+    if (!(p->Re > 0.0)) NSG_FAIL(g, NS_GPU_ERR_INVALID, "Re must be positive (got %g)", p->Re);
+    const int hv_changed = !g->params_set || p->hv_enabled != g->p.hv_enabled || p->hv_coefficient != g->p.hv_coefficient ||
+                           p->hv_order != g->p.hv_order || p->hv_cutoff_ratio != g->p.hv_cutoff_ratio ||
+                           p->sfd_enabled != g->p.sfd_enabled || p->sfd_strength != g->p.sfd_strength;
+    const int f_changed = !g->params_set || p->forcing_enabled != g->p.forcing_enabled ||
+                          p->forcing_kmin != g->p.forcing_kmin || p->forcing_kmax != g->p.forcing_kmax ||
+                          p->forcing_epsilon != g->p.forcing_epsilon;
+    const int dt_changed = !g->params_set || p->dt != g->p.dt;
+    g->p = *p;
+    g->params_set = 1;
+    if (hv_changed) NSG_TRY(compute_hv(g));
+    if (f_changed) NSG_TRY(compute_sigma(g));
+    if (dt_changed) {
+        double dt = p->dt;
+        NSG_TRY(h2d(g, &g->ds->dt_fixed, &dt, sizeof(double)));
+        NSG_TRY(sync(g));
+    }
+    return NS_GPU_OK;
+}
+
+int ns_gpu_geometry(ns_gpu* g, double* x, double* y, double* kx, double* ky, double* k2, int* mask) {
+    if (!g) return NS_GPU_ERR_INVALID;
+    NSG_TRY(ensure_staging(g));
+    const Geo& G = g->g;
+    double* dx = g->real[0];
+    double* dy = g->real[0] + G.nx;
+    double* dkx = g->real[0] + G.nx + G.ny;
+    double* dky = g->real[0] + G.nx + G.ny + G.nkx;
+    double* dk2 = (double*)g->spec[0];
+    int* dmask = (int*)g->spec[1];
+    const long long n = (long long)G.nkx * G.nky;
+    k_geometry<<<grid_for(n), 256, 0, g->st>>>(G, dx, dy, dkx, dky, dk2, dmask);
+    NSG_LAUNCHED(g);
+    if (x) NSG_TRY(d2h(g, x, dx, G.nx * sizeof(double)));
+    if (y) NSG_TRY(d2h(g, y, dy, G.ny * sizeof(double)));
+    if (kx) NSG_TRY(d2h(g, kx, dkx, G.nkx * sizeof(double)));
+    if (ky) NSG_TRY(d2h(g, ky, dky, G.nky * sizeof(double)));
+    if (k2) NSG_TRY(d2h(g, k2, dk2, n * sizeof(double)));
+    if (mask) NSG_TRY(d2h(g, mask, dmask, n * sizeof(int)));
+    return sync(g);
+}
+
+int ns_gpu_hv_weights(ns_gpu* g, double* kmax, double* cutoff, double* inv_bw, double* weights_out) {
+    if (!g) return NS_GPU_ERR_INVALID;
+    NSG_TRY(compute_hv(g));
+    if (kmax) *kmax = g->hv_kmax;
+    if (cutoff) *cutoff = g->hv_cutoff;
+    if (inv_bw) *inv_bw = g->hv_inv_bw;
+    if (weights_out) NSG_TRY(d2h(g, weights_out, g->hvw_full, (size_t)g->g.nkx * g->g.nky * sizeof(double)));
+    return sync(g);
+}
+
+// ------------------------------------------------- host-array transforms
+template <typename T> static int forward_t(ns_gpu* g, const double* field, double* field_hat) {
+    NSG_TRY(h2d(g, g->real[0], field, real_bytes(g)));
+    RowArgs<T> a = row_args<T>(g);
+    a.in_real = g->real[0];
+    NSG_TRY(row_launch<T, ROW_FWD1>(g, a));
+    NSG_CUDA(g, cudaMemsetAsync(g->spec[0], 0, spec_bytes(g), g->st));
+    ColArgs<T> c = col_args<T>(g);
+    c.out_spec = g->spec[0];
+    c.out_scale = 1.0 / ((double)g->g.nx * (double)g->g.ny);
+    NSG_TRY((col_launch<T, COL_FWD_EXPORT, 0>(g, c)));
+    g->fields_valid = 0;
+    NSG_TRY(d2h(g, field_hat, g->spec[0], spec_bytes(g)));
+    return sync(g);
+}
+
+int ns_gpu_forward(ns_gpu* g, const double* field, double* field_hat) {
+    if (!g || !field || !field_hat) return NS_GPU_ERR_INVALID;
+    NSG_TRY(ensure_staging(g));
+    return g->prec == NS_GPU_FP64 ? forward_t<double>(g, field, field_hat) : forward_t<float>(g, field, field_hat);
+}
+
+template <typename T> static int import_kept(ns_gpu* g, const double2* spec, void* W, void* P, const double2* pspec) {
+    const long long n = (long long)g->g.nkx * g->g.nky;
+    k_import<T><<<grid_for(n), 256, 0, g->st>>>(g->g, spec, pspec, nullptr, (Cx<T>*)W, (Cx<T>*)P, nullptr, nullptr,
+                                                nullptr, nullptr);
+    NSG_LAUNCHED(g);
+    return NS_GPU_OK;
+}
+
+template <typename T> static int inverse_t(ns_gpu* g, const double* field_hat, double* field, double* masked) {
+    NSG_TRY(h2d(g, g->spec[0], field_hat, spec_bytes(g)));
+    NSG_TRY(import_kept<T>(g, g->spec[0], g->KS, nullptr, nullptr));
+    ColArgs<T> c = col_args<T>(g);
+    c.W0 = (Cx<T>*)g->KS;
+    NSG_TRY((col_launch<T, COL_INV1, 0>(g, c)));
+    RowArgs<T> a = row_args<T>(g);
+    a.F[0] = (const Cx<T>*)g->F[0];
+    a.out_real[0] = g->real[0];
+    NSG_TRY(row_launch<T, ROW_INV1>(g, a));
+    g->fields_valid = 0;
+    if (masked) {
+        const long long n = (long long)g->g.nkx * g->g.nky;
+        k_dealias<<<grid_for(n), 256, 0, g->st>>>(g->g, g->spec[0], g->spec[1]);
+        NSG_LAUNCHED(g);
+        NSG_TRY(d2h(g, masked, g->spec[1], spec_bytes(g)));
+    }
+    NSG_TRY(d2h(g, field, g->real[0], real_bytes(g)));
+    return sync(g);
+}
+
+int ns_gpu_inverse(ns_gpu* g, const double* field_hat, double* field, double* masked_copy) {
+    if (!g || !field_hat || !field) return NS_GPU_ERR_INVALID;
+    NSG_TRY(ensure_staging(g));
+    return g->prec == NS_GPU_FP64 ? inverse_t<double>(g, field_hat, field, masked_copy)
+                                  : inverse_t<float>(g, field_hat, field, masked_copy);
+}
+
+int ns_gpu_dealias(ns_gpu* g, double* field_hat) {
+    if (!g || !field_hat) return NS_GPU_ERR_INVALID;
+    NSG_TRY(ensure_staging(g));
+    NSG_TRY(h2d(g, g->spec[0], field_hat, spec_bytes(g)));
+    const long long n = (long long)g->g.nkx * g->g.nky;
+    k_dealias<<<grid_for(n), 256, 0, g->st>>>(g->g, g->spec[0], nullptr);
+    NSG_LAUNCHED(g);
+    NSG_TRY(d2h(g, field_hat, g->spec[0], spec_bytes(g)));
+    return sync(g);
+}
+
+int ns_gpu_velocity(ns_gpu* g, const double* omega_hat, double* psi_hat, double* u_hat, double* v_hat) {
+    if (!g || !omega_hat) return NS_GPU_ERR_INVALID;
+    NSG_TRY(ensure_staging(g));
+    NSG_TRY(h2d(g, g->spec[0], omega_hat, spec_bytes(g)));
+    const long long n = (long long)g->g.nkx * g->g.nky;
+    k_velocity<<<grid_for(n), 256, 0, g->st>>>(g->g, g->spec[0], g->spec[1], g->spec[2], g->spec[3]);
+    NSG_LAUNCHED(g);
+    if (psi_hat) NSG_TRY(d2h(g, psi_hat, g->spec[1], spec_bytes(g)));
+    if (u_hat) NSG_TRY(d2h(g, u_hat, g->spec[2], spec_bytes(g)));
+    if (v_hat) NSG_TRY(d2h(g, v_hat, g->spec[3], spec_bytes(g)));
+    return sync(g);
+}
+
+template <typename T> static int uvw_from_spec(ns_gpu* g, const double2* wspec, double* u, double* v, double* w) {
+    NSG_TRY(import_kept<T>(g, wspec, g->KS, nullptr, nullptr));
+    NSG_TRY(prologue<T>(g, g->KS, nullptr, 1, 3));
+    RowArgs<T> a = row_args<T>(g);
+    a.F[0] = (const Cx<T>*)g->F[1];  // Psi_y -> u
+    a.F[1] = (const Cx<T>*)g->F[0];  // Psi (x-derivative) -> v = -psi_x
+    a.F[2] = (const Cx<T>*)g->F[2];  // Omega -> omega
+    a.dx[0] = 0; a.dx[1] = 1; a.dx[2] = 0;
+    a.out_real[0] = g->real[0];
+    a.out_real[1] = g->real[1];
+    a.out_real[2] = g->real[2];
+    NSG_TRY(row_launch<T, ROW_UVW>(g, a));
+    g->fields_valid = 0;
+    if (u) NSG_TRY(d2h(g, u, g->real[0], real_bytes(g)));
+    if (v) NSG_TRY(d2h(g, v, g->real[1], real_bytes(g)));
+    if (w) NSG_TRY(d2h(g, w, g->real[2], real_bytes(g)));
+    return NS_GPU_OK;
+}
+
+int ns_gpu_derivatives(ns_gpu* g, const double* omega_hat, double* psi_hat, double* u_hat, double* v_hat, double* u,
+                       double* v, double* omega, double* masked_copy) {
+    if (!g || !omega_hat) return NS_GPU_ERR_INVALID;
+    NSG_TRY(ensure_staging(g));
+    NSG_TRY(h2d(g, g->spec[0], omega_hat, spec_bytes(g)));
+    const long long n = (long long)g->g.nkx * g->g.nky;
+    k_velocity<<<grid_for(n), 256, 0, g->st>>>(g->g, g->spec[0], g->spec[1], g->spec[2], g->spec[3]);
+    NSG_LAUNCHED(g);
+    if (psi_hat) NSG_TRY(d2h(g, psi_hat, g->spec[1], spec_bytes(g)));
+    if (u_hat) NSG_TRY(d2h(g, u_hat, g->spec[2], spec_bytes(g)));
+    if (v_hat) NSG_TRY(d2h(g, v_hat, g->spec[3], spec_bytes(g)));
+    if (g->prec == NS_GPU_FP64) NSG_TRY(uvw_from_spec<double>(g, g->spec[0], u, v, omega));
+    else NSG_TRY(uvw_from_spec<float>(g, g->spec[0], u, v, omega));
+    if (masked_copy) {
+        k_dealias<<<grid_for(n), 256, 0, g->st>>>(g->g, g->spec[0], g->spec[4]);
+        NSG_LAUNCHED(g);
+        NSG_TRY(d2h(g, masked_copy, g->spec[4], spec_bytes(g)));
+    }
+    return sync(g);
+}
+
+template <typename T>
+static int nonlinear_t(ns_gpu* g, const double* wh, const double* ph, double* nl, double* const* phys) {
+    NSG_TRY(h2d(g, g->spec[0], wh, spec_bytes(g)));
+    NSG_TRY(h2d(g, g->spec[1], ph, spec_bytes(g)));
+    NSG_TRY(import_kept<T>(g, g->spec[0], g->KS, g->KP, g->spec[1]));
+    NSG_TRY(prologue<T>(g, g->KS, g->KP, 0, 4));
+    RowArgs<T> a = row_args<T>(g);
+    for (int f = 0; f < 4; ++f) a.F[f] = (const Cx<T>*)g->F[f];
+    a.dx[0] = 1; a.dx[1] = 0; a.dx[2] = 1; a.dx[3] = 0;
+    int dump = 0;
+    for (int i = 0; i < 5; ++i) {
+        a.out_real[i] = g->real[i];
+        if (phys[i]) dump = 1;
+    }
+    if (dump) NSG_TRY(row_launch<T, ROW_DUMP>(g, a));
+    else NSG_TRY(row_launch<T, ROW_STAGE>(g, a));
+    NSG_CUDA(g, cudaMemsetAsync(g->spec[2], 0, spec_bytes(g), g->st));
+    ColArgs<T> c = col_args<T>(g);
+    c.out_spec = g->spec[2];
+    c.out_scale = -1.0 / ((double)g->g.nx * (double)g->g.ny);
+    NSG_TRY((col_launch<T, COL_NL_EXPORT, 0>(g, c)));
+    g->fields_valid = 0;
+    if (nl) NSG_TRY(d2h(g, nl, g->spec[2], spec_bytes(g)));
+    for (int i = 0; i < 5; ++i)
+        if (phys[i]) NSG_TRY(d2h(g, phys[i], g->real[i], real_bytes(g)));
+    return sync(g);
+}
+
+int ns_gpu_nonlinear(ns_gpu* g, const double* omega_hat, const double* psi_hat, double* nonlinear_hat, double* psi_x,
+                     double* psi_y, double* omega_x, double* omega_y, double* jacobian) {
+    if (!g || !omega_hat || !psi_hat) return NS_GPU_ERR_INVALID;
+    NSG_TRY(ensure_staging(g));
+    double* phys[5] = {psi_x, psi_y, omega_x, omega_y, jacobian};
+    return g->prec == NS_GPU_FP64 ? nonlinear_t<double>(g, omega_hat, psi_hat, nonlinear_hat, phys)
+                                  : nonlinear_t<float>(g, omega_hat, psi_hat, nonlinear_hat, phys);
+}
+
+int ns_gpu_hv_apply(ns_gpu* g, double* rhs_hat, const double* state_hat, const double* sfd_hat) {
+    if (!g || !rhs_hat || !state_hat) return NS_GPU_ERR_INVALID;
+    const int visc = (g->p.hv_enabled && g->p.hv_coefficient > 0.0) ? 1 : 0;
+    const int sfd = (g->p.sfd_enabled && g->p.sfd_strength > 0.0) ? 1 : 0;
+    if (!visc && !sfd) return NS_GPU_OK;
+    if (sfd && !sfd_hat) return NS_GPU_ERR_INVALID;
+    NSG_TRY(ensure_staging(g));
+    NSG_TRY(h2d(g, g->spec[0], rhs_hat, spec_bytes(g)));
+    NSG_TRY(h2d(g, g->spec[1], state_hat, spec_bytes(g)));
+    if (sfd) NSG_TRY(h2d(g, g->spec[2], sfd_hat, spec_bytes(g)));
+    const long long n = (long long)g->g.nkx * g->g.nky;
+    k_hv_apply<<<grid_for(n), 256, 0, g->st>>>(g->g, g->hvw_full, visc, sfd, g->p.sfd_strength,
+                                               g->p.hv_order > 0 ? g->p.hv_order : 1, g->hv_cutoff, g->hv_inv_bw,
+                                               g->spec[0], g->spec[1], g->spec[2]);
+    NSG_LAUNCHED(g);
+    NSG_TRY(d2h(g, rhs_hat, g->spec[0], spec_bytes(g)));
+    return sync(g);
+}
+
+int ns_gpu_hv_post_step(ns_gpu* g, const double* state_hat, double* sfd_hat, double dt) {
+    if (!g || !state_hat || !sfd_hat) return NS_GPU_ERR_INVALID;
+    if (dt <= 0.0 || !g->p.sfd_enabled || g->p.sfd_strength <= 0.0 || g->p.sfd_timescale <= 0.0) return NS_GPU_OK;
+    double a = dt / g->p.sfd_timescale;
+    a = a > 1.0 ? 1.0 : (a < 0.0 ? 0.0 : a);
+    NSG_TRY(ensure_staging(g));
+    NSG_TRY(h2d(g, g->spec[1], state_hat, spec_bytes(g)));
+    NSG_TRY(h2d(g, g->spec[2], sfd_hat, spec_bytes(g)));
+    const long long n = (long long)g->g.nkx * g->g.nky;
+    k_hv_post<<<grid_for(n), 256, 0, g->st>>>(g->g, a, g->spec[1], g->spec[2]);
+    NSG_LAUNCHED(g);
+    NSG_TRY(d2h(g, sfd_hat, g->spec[2], spec_bytes(g)));
+    return sync(g);
+}
+
+int ns_gpu_reduce(ns_gpu* g, int kind, const double* a, const double* b, double* out) {
+    if (!g || !a || !out || kind < 0 || kind > 2) return NS_GPU_ERR_INVALID;
+    if (kind != NS_GPU_REDUCE_ENSTROPHY && !b) return NS_GPU_ERR_INVALID;
+    NSG_TRY(ensure_staging(g));
+    const long long n = (long long)g->g.nx * g->g.ny;
+    NSG_TRY(h2d(g, g->real[0], a, real_bytes(g)));
+    if (b) NSG_TRY(h2d(g, g->real[1], b, real_bytes(g)));
+    const int nb = grid_for(n, 256, g->part_n);
+    if (kind == NS_GPU_REDUCE_CFL) {
+        NSG_CUDA(g, cudaMemsetAsync(&g->ds->aux_max, 0, sizeof(unsigned long long), g->st));
+        k_reduce_real<<<nb, 256, 0, g->st>>>(2, g->real[0], g->real[1], n, g->part, g->ds);
+        NSG_LAUNCHED(g);
+        unsigned long long bits = 0;
+        NSG_TRY(d2h(g, &bits, &g->ds->aux_max, sizeof(bits)));
+        NSG_TRY(sync(g));
+        double vmax;
+        memcpy(&vmax, &bits, sizeof(vmax));
+        // spectral_time_integration.c:22-30
+        const double dxmin = fmin(g->g.Lx / g->g.nx, g->g.Ly / g->g.ny);
+        const double dt_cfl = g->p.cfl_factor * dxmin / (vmax + 1e-12);
+        const double dt_visc = 0.5 * g->p.Re * dxmin * dxmin;
+        double dt = fmin(dt_cfl, dt_visc);
+        dt = fmax(dt, 1e-8);
+        dt = fmin(dt, 0.1);
+        *out = dt;
+        return NS_GPU_OK;
+    }
+    k_reduce_real<<<nb, 256, 0, g->st>>>(kind == NS_GPU_REDUCE_ENERGY ? 0 : 1, g->real[0], g->real[1], n, g->part, g->ds);
+    NSG_LAUNCHED(g);
+    k_merge_partials<<<1, 256, 0, g->st>>>(g->part, nb, g->dres);
+    NSG_LAUNCHED(g);
+    double s = 0.0;
+    NSG_TRY(d2h(g, &s, g->dres, sizeof(double)));
+    NSG_TRY(sync(g));
+    *out = s / ((double)g->g.nx * g->g.ny);
+    return NS_GPU_OK;
+}
+
+int ns_gpu_spectral_stats(ns_gpu* g, const double* omega_hat, const double* u_hat, const double* v_hat,
+                          double* resolution_fraction, double* max_abs, double* spectral_error, double* bin_energy,
+                          int* bin_count) {
+    if (!g) return NS_GPU_ERR_INVALID;
+    if ((bin_energy || bin_count) && (!u_hat || !v_hat)) return NS_GPU_ERR_INVALID;
+    NSG_TRY(ensure_staging(g));
+    const int nbins = (int)fmin((double)g->g.nkx, (double)(g->g.nky / 2));
+    if (omega_hat) NSG_TRY(h2d(g, g->spec[0], omega_hat, spec_bytes(g)));
+    if (u_hat) NSG_TRY(h2d(g, g->spec[1], u_hat, spec_bytes(g)));
+    if (v_hat) NSG_TRY(h2d(g, g->spec[2], v_hat, spec_bytes(g)));
+    double* dbins = g->real[0];
+    int* dcount = (int*)g->real[1];
+    const int want_bins = (bin_energy || bin_count) ? 1 : 0;
+    if (want_bins) {
+        NSG_CUDA(g, cudaMemsetAsync(dbins, 0, nbins * sizeof(double), g->st));
+        NSG_CUDA(g, cudaMemsetAsync(dcount, 0, nbins * sizeof(int), g->st));
+    }
+    NSG_CUDA(g, cudaMemsetAsync(&g->ds->aux_max, 0, sizeof(unsigned long long), g->st));
+    const long long n = (long long)g->g.nkx * g->g.nky;
+    const int nb = grid_for(n, 256, g->part_n);
+    k_spec_stats<<<nb, 256, 0, g->st>>>(g->g, omega_hat ? g->spec[0] : nullptr, want_bins ? g->spec[1] : nullptr,
+                                        want_bins ? g->spec[2] : nullptr, g->part, g->ds, dbins, dcount, nbins);
+    NSG_LAUNCHED(g);
+    k_merge_pairs4<<<1, 256, 0, g->st>>>(g->part, nb, g->dres);
+    NSG_LAUNCHED(g);
+    double r[4];
+    unsigned long long bits = 0;
+    NSG_TRY(d2h(g, r, g->dres, 4 * sizeof(double)));
+    NSG_TRY(d2h(g, &bits, &g->ds->aux_max, sizeof(bits)));
+    if (bin_energy) NSG_TRY(d2h(g, bin_energy, dbins, nbins * sizeof(double)));
+    if (bin_count) NSG_TRY(d2h(g, bin_count, dcount, nbins * sizeof(int)));
+    NSG_TRY(sync(g));
+    double mx;
+    memcpy(&mx, &bits, sizeof(mx));
+    if (resolution_fraction) *resolution_fraction = (r[0] > 1e-16) ? r[1] / r[0] : 0.0;
+    if (max_abs) *max_abs = mx;
+    if (spectral_error) *spectral_error = (r[3] > 0.0) ? sqrt(r[2] / r[3]) : 0.0;
+    return NS_GPU_OK;
+}
+
+int ns_gpu_taylor_green(ns_gpu* g, double* u, double* v, double* omega, double* p) {
+    if (!g) return NS_GPU_ERR_INVALID;
+    NSG_TRY(ensure_staging(g));
+    const long long n = (long long)g->g.nx * g->g.ny;
+    k_taylor_green<<<grid_for(n), 256, 0, g->st>>>(g->g, g->real[0], g->real[1], g->real[2], g->real[3]);
+    NSG_LAUNCHED(g);
+    if (u) NSG_TRY(d2h(g, u, g->real[0], real_bytes(g)));
+    if (v) NSG_TRY(d2h(g, v, g->real[1], real_bytes(g)));
+    if (omega) NSG_TRY(d2h(g, omega, g->real[2], real_bytes(g)));
+    if (p) NSG_TRY(d2h(g, p, g->real[3], real_bytes(g)));
+    return sync(g);
+}
+
+// ---------------------------------------------------------------- stepping
+template <typename T>
+static int upload_t(ns_gpu* g, const double2* wspec, const double2* pspec, const double2* sspec) {
+    NSG_TRY(ensure_outside(g));
+    NSG_CUDA(g, cudaMemsetAsync(g->dflag, 0, sizeof(int), g->st));
+    const long long n = (long long)g->g.nkx * g->g.nky;
+    k_import<T><<<grid_for(n), 256, 0, g->st>>>(g->g, wspec, pspec, sspec, (Cx<T>*)g->W0,
+                                                pspec ? (Cx<T>*)g->PSI0 : nullptr, sspec ? (Cx<T>*)g->SFD : nullptr,
+                                                g->out, g->outsfd, g->dflag);
+    NSG_LAUNCHED(g);
+    return NS_GPU_OK;
+}
+
+int ns_gpu_upload_state(ns_gpu* g, const double* omega_hat, const double* psi_hat, const double* sfd_hat, double t,
+                        double dt, uint64_t step0) {
+    if (!g || !omega_hat) return NS_GPU_ERR_INVALID;
+    NSG_TRY(ensure_staging(g));
+    NSG_TRY(h2d(g, g->spec[0], omega_hat, spec_bytes(g)));
+    if (psi_hat) NSG_TRY(h2d(g, g->spec[1], psi_hat, spec_bytes(g)));
+    if (sfd_hat) NSG_TRY(h2d(g, g->spec[2], sfd_hat, spec_bytes(g)));
+    const double2* pp = psi_hat ? g->spec[1] : nullptr;
+    const double2* sp = sfd_hat ? g->spec[2] : nullptr;
+    if (g->prec == NS_GPU_FP64) NSG_TRY(upload_t<double>(g, g->spec[0], pp, sp));
+    else NSG_TRY(upload_t<float>(g, g->spec[0], pp, sp));
+    DevScalars h;
+    memset(&h, 0, sizeof(h));
+    h.t = t;
+    h.dt = dt;
+    h.dt_fixed = dt;
+    h.step_next = step0;
+    h.step_cur = step0;
+    NSG_TRY(h2d(g, g->ds, &h, sizeof(h)));
+    int flag = 0;
+    NSG_TRY(d2h(g, &flag, g->dflag, sizeof(int)));
+    NSG_TRY(sync(g));
+    g->p.dt = dt;
+    g->outside_active = (flag & 1) ? 1 : 0;
+    g->fields_valid = 0;
+    g->psi0_valid = psi_hat ? 1 : 0;
+    return NS_GPU_OK;
+}
+
+int ns_gpu_advance(ns_gpu* g, int nsteps) {
+    if (!g || nsteps < 0) return NS_GPU_ERR_INVALID;
+    return g->prec == NS_GPU_FP64 ? advance_t<double>(g, nsteps) : advance_t<float>(g, nsteps);
+}
+
+template <typename T>
+static int download_t(ns_gpu* g, double* wh, double* ph, double* uh, double* vh, double* sh, double* u, double* v,
+                      double* w) {
+    if ((u || v || w) && !g->fields_valid) {
+        NSG_TRY(prologue<T>(g, g->W0, g->PSI0, g->psi0_valid ? 0 : 1, 4));
+        g->fields_valid = 1;
+    }
+    const long long n = (long long)g->g.nkx * g->g.nky;
+    const int sfd_on = (g->p.sfd_enabled && g->p.sfd_strength > 0.0);
+    k_export<T><<<grid_for(n), 256, 0, g->st>>>(g->g, (const Cx<T>*)g->W0, sfd_on ? (const Cx<T>*)g->SFD : nullptr,
+                                                g->outside_active ? g->out : nullptr,
+                                                (g->outside_active && sfd_on) ? g->outsfd : nullptr, g->spec[0],
+                                                g->spec[1], g->spec[2], g->spec[3], g->spec[4]);
+    NSG_LAUNCHED(g);
+    if (u || v || w) {
+        RowArgs<T> a = row_args<T>(g);
+        a.F[0] = (const Cx<T>*)g->F[1];
+        a.F[1] = (const Cx<T>*)g->F[0];
+        a.F[2] = (const Cx<T>*)g->F[2];
+        a.dx[0] = 0; a.dx[1] = 1; a.dx[2] = 0;
+        a.out_real[0] = g->real[0];
+        a.out_real[1] = g->real[1];
+        a.out_real[2] = g->real[2];
+        NSG_TRY(row_launch<T, ROW_UVW>(g, a));
+    }
+    if (wh) NSG_TRY(d2h(g, wh, g->spec[0], spec_bytes(g)));
+    if (ph) NSG_TRY(d2h(g, ph, g->spec[1], spec_bytes(g)));
+    if (uh) NSG_TRY(d2h(g, uh, g->spec[2], spec_bytes(g)));
+    if (vh) NSG_TRY(d2h(g, vh, g->spec[3], spec_bytes(g)));
+    if (sh) NSG_TRY(d2h(g, sh, g->spec[4], spec_bytes(g)));
+    if (u) NSG_TRY(d2h(g, u, g->real[0], real_bytes(g)));
+    if (v) NSG_TRY(d2h(g, v, g->real[1], real_bytes(g)));
+    if (w) NSG_TRY(d2h(g, w, g->real[2], real_bytes(g)));
+    return NS_GPU_OK;
+}
+
+int ns_gpu_download_state(ns_gpu* g, double* omega_hat, double* psi_hat, double* u_hat, double* v_hat, double* sfd_hat,
+                          double* u, double* v, double* omega, double* t, double* dt) {
+    if (!g) return NS_GPU_ERR_INVALID;
+    NSG_TRY(ensure_staging(g));
+    if (g->prec == NS_GPU_FP64) NSG_TRY(download_t<double>(g, omega_hat, psi_hat, u_hat, v_hat, sfd_hat, u, v, omega));
+    else NSG_TRY(download_t<float>(g, omega_hat, psi_hat, u_hat, v_hat, sfd_hat, u, v, omega));
+    DevScalars h;
+    NSG_TRY(d2h(g, &h, g->ds, sizeof(h)));
+    NSG_TRY(sync(g));
+    if (t) *t = h.t;
+    if (dt) *dt = h.dt;
+    return NS_GPU_OK;
+}
+
+static int flush_l2(ns_gpu* g, size_t bytes, int salt) {
+    if (bytes == 0) return NS_GPU_OK;
+    if (g->flush_bytes < bytes) {
+        if (g->flushbuf) cudaFree(g->flushbuf);
+        g->flushbuf = nullptr;
+        g->flush_bytes = 0;
+        NSG_TRY(dalloc(g, &g->flushbuf, bytes));
+        g->flush_bytes = bytes;
+    }
+    NSG_CUDA(g, cudaMemsetAsync(g->flushbuf, salt & 0xff, bytes, g->st));
+    return NS_GPU_OK;
+}
+
+int ns_gpu_advance_timed(ns_gpu* g, int nsteps, size_t flush_bytes, double* total_ms, double* step_ms) {
+    if (!g || nsteps < 0) return NS_GPU_ERR_INVALID;
+    std::vector<cudaEvent_t> ev(2 * (size_t)nsteps);
+    for (auto& e : ev) NSG_CUDA(g, cudaEventCreate(&e));
+    int st = NS_GPU_OK;
+    for (int n = 0; n < nsteps && st == NS_GPU_OK; ++n) {
+        st = flush_l2(g, flush_bytes, n);
+        if (st != NS_GPU_OK) break;
+        cudaEventRecord(ev[2 * n], g->st);
+        st = ns_gpu_advance(g, 1);
+        cudaEventRecord(ev[2 * n + 1], g->st);
+    }
+    if (st == NS_GPU_OK) st = sync(g);
+    double tot = 0.0;
+    for (int n = 0; n < nsteps && st == NS_GPU_OK; ++n) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev[2 * n], ev[2 * n + 1]);
+        tot += ms;
+        if (step_ms) step_ms[n] = ms;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    if (total_ms) *total_ms = tot;
+    return st;
+}
+
+int ns_gpu_profile_kernels(ns_gpu* g, int nsteps, size_t flush_bytes, double* kernel_ms, int* counts) {
+    if (!g || nsteps < 0 || !kernel_ms || !counts) return NS_GPU_ERR_INVALID;
+    std::vector<ns_gpu::ProfRec> recs;
+    int st = NS_GPU_OK;
+    for (int n = 0; n < nsteps && st == NS_GPU_OK; ++n) {
+        st = flush_l2(g, flush_bytes, n);
+        if (st != NS_GPU_OK) break;
+        g->prof = &recs;
+        st = ns_gpu_advance(g, 1);
+        g->prof = nullptr;
+    }
+    g->prof = nullptr;
+    if (st == NS_GPU_OK) st = sync(g);
+    kernel_ms[0] = kernel_ms[1] = 0.0;
+    counts[0] = counts[1] = 0;
+    for (auto& r : recs) {
+        float ms = 0.f;
+        if (st == NS_GPU_OK) cudaEventElapsedTime(&ms, r.a, r.b);
+        kernel_ms[r.kind] += ms;
+        counts[r.kind] += 1;
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    return st;
+}
+
+int ns_gpu_diagnostics(ns_gpu* g, double* energy, double* enstrophy, double* t, double* dt) {
+    if (!g) return NS_GPU_ERR_INVALID;
+    const long long n = (long long)g->g.Kx * g->g.Ky;
+    const int nb = grid_for(n, 256, g->part_n);
+    NSG_CUDA(g, cudaMemsetAsync(&g->ds->flag, 0, sizeof(int), g->st));
+    if (g->prec == NS_GPU_FP64)
+        k_diag<double><<<nb, 256, 0, g->st>>>(g->g, (const double2*)g->W0, (const double*)g->kxv, (const double*)g->kyv,
+                                              g->part, g->ds);
+    else
+        k_diag<float><<<nb, 256, 0, g->st>>>(g->g, (const float2*)g->W0, (const float*)g->kxv, (const float*)g->kyv,
+                                             g->part, g->ds);
+    NSG_LAUNCHED(g);
+    k_merge_pairs2<<<1, 256, 0, g->st>>>(g->part, nb, g->dres);
+    NSG_LAUNCHED(g);
+    double r[2];
+    DevScalars h;
+    NSG_TRY(d2h(g, r, g->dres, 2 * sizeof(double)));
+    NSG_TRY(d2h(g, &h, g->ds, sizeof(h)));
+    NSG_TRY(sync(g));
+    if (energy) *energy = r[0];
+    if (enstrophy) *enstrophy = r[1];
+    if (t) *t = h.t;
+    if (dt) *dt = h.dt;
+    if (h.flag & 2) NSG_FAIL(g, NS_GPU_ERR_DIVERGED, "non-finite vorticity in the device state at t=%g", h.t);
+    return NS_GPU_OK;
+}
+
+int ns_gpu_init_random_spectrum(ns_gpu* g, uint64_t seed, double k0, double energy) {
+    if (!g || !(k0 > 0.0) || energy < 0.0) return NS_GPU_ERR_INVALID;
+    NSG_TRY(ensure_staging(g));
+    const long long n = (long long)g->g.nkx * g->g.nky;
+    const int nb = grid_for(n, 256, g->part_n);
+    k_random_spectrum<<<nb, 256, 0, g->st>>>(g->g, (unsigned long long)seed, k0, g->spec[0], g->part);
+    NSG_LAUNCHED(g);
+    k_merge_partials<<<1, 256, 0, g->st>>>(g->part, nb, g->dres);
+    NSG_LAUNCHED(g);
+    NSG_TRY(h2d(g, g->dres + 1, &energy, sizeof(double)));
+    k_scale_spec<<<grid_for(n), 256, 0, g->st>>>(n, g->spec[0], g->dres);
+    NSG_LAUNCHED(g);
+    if (g->prec == NS_GPU_FP64) NSG_TRY(upload_t<double>(g, g->spec[0], nullptr, nullptr));
+    else NSG_TRY(upload_t<float>(g, g->spec[0], nullptr, nullptr));
+    DevScalars h;
+    memset(&h, 0, sizeof(h));
+    h.dt = g->p.dt;
+    h.dt_fixed = g->p.dt;
+    NSG_TRY(h2d(g, g->ds, &h, sizeof(h)));
+    NSG_TRY(sync(g));
+    g->outside_active = 0;
+    g->fields_valid = 0;
+    g->psi0_valid = 0;
+    return NS_GPU_OK;
+}
+
+// copy the random spectrum of the device state into a host-layout array (used by the drop-in IC)
+int ns_gpu_random_spectrum_host(ns_gpu* g, uint64_t seed, double k0, double energy, double* omega_hat) {
+    if (!g || !omega_hat) return NS_GPU_ERR_INVALID;
+    NSG_TRY(ns_gpu_init_random_spectrum(g, seed, k0, energy));
+    NSG_TRY(d2h(g, omega_hat, g->spec[0], spec_bytes(g)));
+    return sync(g);
+}
+
+int ns_gpu_forcing_weights(ns_gpu* g, const double* k2, int n, double kmin, double kmax, double* weights, int* active) {
+    if (!g || !k2 || !weights || !active || n <= 0) return NS_GPU_ERR_INVALID;
+    NSG_TRY(ensure_scratch(g, (size_t)n * 2 * sizeof(double) + 64));
+    double* dk2 = (double*)g->scratch;
+    double* dw = dk2 + n;
+    NSG_TRY(h2d(g, dk2, k2, n * sizeof(double)));
+    NSG_CUDA(g, cudaMemsetAsync(g->dflag, 0, sizeof(int), g->st));
+    k_forcing_weights<<<grid_for(n), 256, 0, g->st>>>(dk2, n, kmin, kmax, dw, g->dflag);
+    NSG_LAUNCHED(g);
+    NSG_TRY(d2h(g, weights, dw, n * sizeof(double)));
+    NSG_TRY(d2h(g, active, g->dflag, sizeof(int)));
+    return sync(g);
+}
+
+int ns_gpu_forcing_generate(ns_gpu* g, int n, const double* weights, int active, int colored, double dt,
+                            double correlation_time, double energy_target, uint64_t* rng_state, double* colored_state,
+                            double* forcing_out) {
+    if (!g || !weights || !rng_state || !forcing_out || n <= 0) return NS_GPU_ERR_INVALID;
+    if (colored && !colored_state) return NS_GPU_ERR_INVALID;
+    NSG_TRY(ensure_scratch(g, (size_t)n * (sizeof(double) + 2 * sizeof(double2)) + 64));
+    double* dw = (double*)g->scratch;
+    double2* dcs = (double2*)(dw + n);
+    double2* dout = dcs + n;
+    if (active == 0 || energy_target <= 0.0) {
+        // forcing.c:121-133: zero output (and colored state when the target is not positive)
+        memset(forcing_out, 0, (size_t)n * sizeof(double2));
+        if (colored && energy_target <= 0.0 && active != 0) memset(colored_state, 0, (size_t)n * sizeof(double2));
+        return NS_GPU_OK;
+    }
+    const double tau = fmax(correlation_time, 1e-6);
+    double alpha = 0.0, beta = 1.0;
+    if (colored) {
+        alpha = exp(-dt / tau);
+        beta = sqrt(fmax(1.0 - alpha * alpha, 0.0));
+    }
+    NSG_TRY(h2d(g, dw, weights, n * sizeof(double)));
+    if (colored) NSG_TRY(h2d(g, dcs, colored_state, n * sizeof(double2)));
+    k_forcing_generate<<<1, 1024, 0, g->st>>>(n, dw, colored, alpha, beta, energy_target,
+                                              (unsigned long long)*rng_state, dcs, dout);
+    NSG_LAUNCHED(g);
+    NSG_TRY(d2h(g, forcing_out, dout, n * sizeof(double2)));
+    if (colored) NSG_TRY(d2h(g, colored_state, dcs, n * sizeof(double2)));
+    NSG_TRY(sync(g));
+    *rng_state = *rng_state + 2ULL * (unsigned long long)active * 0x9E3779B97F4A7C15ULL;
+    return NS_GPU_OK;
+}
+
+void* ns_gpu_state_device_ptr(ns_gpu* g) { return g ? g->W0 : nullptr; }
+
+void* ns_gpu_host_alloc(size_t bytes) {
+    void* p = nullptr;
+    if (bytes == 0) bytes = 1;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    memset(p, 0, bytes);
+    return p;
+}
+
+void ns_gpu_host_free(void* ptr) {
+    if (ptr) cudaFreeHost(ptr);
+}

@@ -1,0 +1,1105 @@
+// Device kernels of the GB300 pseudospectral step.
+//
+// Data layout in HBM (per instance, T = float or double, C = complex of T):
+//   kept modes     kx columns i in [0, Kx), Kx = floor(2*nkx/3)+1, and ky rows
+//                  |band| <= Kyh = floor(ny/3), stored as kept-row index
+//                  jj in [0, Ky), Ky = 2*Kyh+1 (jj <= Kyh -> j = jj, else j = ny-Ky+jj)
+//   state arrays   W0 (omega_hat at the step start), WS (stage state), ACC (RK
+//                  accumulator), PSI0, SFD: C[Kxp][Ky]  (column i contiguous)
+//   F[4]           y-transformed fields Psi, Psi_y, Omega, Omega_y: C[ny][Kxp]
+//   G              x-transformed Jacobian: C[ny][Kxp]
+// Only the dealiased modes are ever stored or transformed on the hot path;
+// the 2/3 rule is the layout (reference mask: spectral_initialization.c:46-49).
+//
+// One RK stage = one row kernel (x-pass over ny rows: 4 inverse half-length
+// c2r, the Jacobian, one forward half-length r2c) + one column kernel (y-pass
+// over the Kx kept columns: forward FFT of J, the RK stage algebra of
+// spectral_time_integration.c:50-100 with hyperviscosity/SFD, forcing and the
+// SFD post-step at stage 4, then the four inverse FFTs of the next stage).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ns_fft.cuh"
+
+namespace nsg {
+
+struct Geo {
+    int nx, ny, nkx, nky;
+    int H;          // nx / 2: length of the packed real row transforms
+    int Kx, Kxp;    // kept kx columns, padded to a multiple of CW
+    int Kyh, Ky;    // kept |ky band| bound and kept row count
+    int logny, logH;
+    double Lx, Ly;
+    int CW;         // columns per column-kernel CTA
+    int RPC;        // rows per row-kernel CTA
+};
+
+__device__ __forceinline__ int kept_j(const Geo& g, int jj) { return jj <= g.Kyh ? jj : g.ny - g.Ky + jj; }
+__device__ __forceinline__ int kept_jj(const Geo& g, int j) {
+    if (j <= g.Kyh) return j;
+    if (j >= g.ny - g.Kyh) return j - (g.ny - g.Ky);
+    return -1;
+}
+
+// Device scalars shared by the kernels of one instance.
+struct DevScalars {
+    double t;
+    double dt;
+    double dt_fixed;
+    unsigned long long maxvel2;    // bit pattern of max(u^2+v^2) (non-negative double)
+    unsigned long long step_next;  // forcing counter of the next step
+    unsigned long long step_cur;   // forcing counter of the running step
+    unsigned long long kmax_bits;  // bit pattern of max |k| (hyperviscosity setup)
+    unsigned long long aux_max;    // bit pattern of a max reduction of the host-array API
+    int flag;                      // outside-mode presence / non-finite detection
+    int pad;
+};
+
+struct StepParams {
+    double inv_re, Re, cfl, dxmin, scale;
+    int adaptive, hv, sfd, forcing;
+    double sfd_tau;
+    double f_kmin, f_kmax, f_sigma;
+    unsigned long long f_seed;
+};
+
+// ------------------------------------------------------------ Philox4x64-10
+// Salmon, Moraes, Dror, Shaw, "Parallel Random Numbers: As Easy as 1, 2, 3" (SC'11)
+__device__ __forceinline__ void philox4x64(unsigned long long c[4], unsigned long long k0, unsigned long long k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) {
+            k0 += 0x9E3779B97F4A7C15ULL;
+            k1 += 0xBB67AE8584CAA73BULL;
+        }
+        const unsigned long long m0 = 0xD2E7470EE14C6C93ULL, m1 = 0xCA5A826395121157ULL;
+        const unsigned long long hi0 = __umul64hi(m0, c[0]), lo0 = m0 * c[0];
+        const unsigned long long hi1 = __umul64hi(m1, c[2]), lo1 = m1 * c[2];
+        const unsigned long long n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+    }
+}
+__device__ __forceinline__ double u53(unsigned long long b) { return (double)(b >> 11) * (1.0 / 9007199254740992.0); }
+
+#define NSG_TAG_IC 0x49430000ULL
+#define NSG_TAG_FORCE 0x464f5243ULL
+
+// ---------------------------------------------------------------- reductions
+struct DD { double s, c; };  // Neumaier pair: value = s + c
+__device__ __forceinline__ void dd_add(DD& a, double x) {
+    const double t = a.s + x;
+    if (fabs(a.s) >= fabs(x)) a.c += (a.s - t) + x;
+    else a.c += (x - t) + a.s;
+    a.s = t;
+}
+__device__ __forceinline__ DD dd_merge(DD a, DD b) {
+    DD r = a;
+    dd_add(r, b.s);
+    r.c += b.c;
+    return r;
+}
+// block-wide merge; returns the total in thread 0
+__device__ DD block_dd(DD v) {
+    __shared__ double ss[32], sc[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        DD w;
+        w.s = __shfl_xor_sync(0xffffffffu, v.s, o);
+        w.c = __shfl_xor_sync(0xffffffffu, v.c, o);
+        v = dd_merge(v, w);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (lane == 0) { ss[wid] = v.s; sc[wid] = v.c; }
+    __syncthreads();
+    if (wid == 0) {
+        DD w;
+        w.s = lane < nw ? ss[lane] : 0.0;
+        w.c = lane < nw ? sc[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            DD u;
+            u.s = __shfl_xor_sync(0xffffffffu, w.s, o);
+            u.c = __shfl_xor_sync(0xffffffffu, w.c, o);
+            w = dd_merge(w, u);
+        }
+        v = w;
+    }
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// =============================================================== row kernel
+enum { ROW_STAGE = 0, ROW_DUMP = 1, ROW_UVW = 2, ROW_INV1 = 3, ROW_FWD1 = 4 };
+
+template <typename T> struct RowArgs {
+    typedef typename CT<T>::C C;
+    const C* F[4];            // field inputs C[ny][Kxp]
+    int dx[4];                // 1: multiply by i kx before the transform
+    C* G;                     // C[ny][Kxp] output (ROW_STAGE, ROW_DUMP, ROW_FWD1)
+    const double* in_real;    // ROW_FWD1 input double[ny][nx]
+    double* out_real[5];      // physical outputs double[ny][nx]
+    const T* kxv;             // kx of kept columns
+    const C* twr;             // exp(-2 pi i t/H), t < H
+    const C* twh;             // exp(-2 pi i k/nx), k < H
+    DevScalars* ds;
+    int cfl;                  // reduce max(u^2+v^2) into ds->maxvel2
+    int marker;               // 1: stage 1 (advance step counters), 2: stage 2 (reset maxvel2)
+};
+
+template <int MODE> struct RowNF { static const int v = (MODE == ROW_STAGE || MODE == ROW_DUMP) ? 4 : (MODE == ROW_UVW ? 3 : 1); };
+
+// grid = ny / RPC, block = RPC * (H / E), dynamic smem = NF * RPC * spad_len(H) * sizeof(C)
+template <typename T, int E, int MODE>
+__global__ void __launch_bounds__(256) k_row(Geo g, RowArgs<T> a) {
+    typedef typename CT<T>::C C;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* sm = reinterpret_cast<C*>(smem_raw);
+    constexpr int NF = RowNF<MODE>::v;
+    const int H = g.H, TT = H / E, LP = spad_len(H);
+    const int r = threadIdx.x / TT, t = threadIdx.x - r * TT;
+    const int y = blockIdx.x * g.RPC + r;
+    const int nx = g.nx, Kxp = g.Kxp, Kx = g.Kx;
+
+    if (MODE == ROW_STAGE && blockIdx.x == 0 && threadIdx.x == 0) {
+        if (a.marker == 1) {
+            a.ds->step_cur = a.ds->step_next;
+            a.ds->step_next = a.ds->step_next + 1ULL;
+        } else if (a.marker == 2) {
+            a.ds->maxvel2 = 0ULL;
+        }
+    }
+
+    if constexpr (MODE == ROW_FWD1) {
+        C* b = sm + r * LP;
+        const double* src = a.in_real + (size_t)y * nx;
+        for (int m = t; m < H; m += TT) {
+            C z;
+            z.x = (T)src[2 * m];
+            z.y = (T)src[2 * m + 1];
+            b[spad(m)] = z;
+        }
+        __syncthreads();
+        fft_smem<E, false>(b, H, g.logH, t, TT, a.twr);
+    } else {
+        // half spectra X_f[k], k < Kx (zero above)
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            C* b = sm + (f * g.RPC + r) * LP;
+            const C* src = a.F[f] + (size_t)y * Kxp;
+            for (int k = t; k < H; k += TT) {
+                C x = cmake<C>(0.0, 0.0);
+                if (k < Kx) {
+                    x = src[k];
+                    if (a.dx[f]) {
+                        const T kx = a.kxv[k];
+                        C d;
+                        d.x = -kx * x.y;
+                        d.y = kx * x.x;
+                        x = d;
+                    }
+                }
+                b[spad(k)] = x;
+            }
+        }
+        __syncthreads();
+        // pack for the half-length inverse: z[m] = x[2m] + i x[2m+1] has spectrum
+        // Z[k] = (X[k] + conj X[H-k]) + i exp(+2 pi i k/nx) (X[k] - conj X[H-k]);
+        // the imaginary parts of X[0] and the Nyquist bin (zero here) are ignored.
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            C* b = sm + (f * g.RPC + r) * LP;
+            for (int k = t; 2 * k <= H; k += TT) {
+                if (k == 0) {
+                    const C x0 = b[spad(0)];
+                    b[spad(0)] = cmake<C>(x0.x, x0.x);
+                    continue;
+                }
+                const C xa = b[spad(k)], xb = b[spad(H - k)];
+                const C e = cconj(__ldg(&a.twh[k]));  // exp(+2 pi i k/nx)
+                const C A = cadd(xa, cconj(xb));
+                const C D = cmul(csub(xa, cconj(xb)), e);
+                b[spad(k)] = cmake<C>(A.x - D.y, A.y + D.x);
+                if (2 * k != H) {
+                    C e2;  // exp(+2 pi i (H-k)/nx) = -conj(e)
+                    e2.x = -e.x;
+                    e2.y = e.y;
+                    const C A2 = cadd(xb, cconj(xa));
+                    const C D2 = cmul(csub(xb, cconj(xa)), e2);
+                    b[spad(H - k)] = cmake<C>(A2.x - D2.y, A2.y + D2.x);
+                }
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int f = 0; f < NF; ++f) fft_smem<E, true>(sm + (f * g.RPC + r) * LP, H, g.logH, t, TT, a.twr);
+
+        if constexpr (MODE == ROW_STAGE || MODE == ROW_DUMP) {
+            C* b0 = sm + (0 * g.RPC + r) * LP;
+            const C* b1 = sm + (1 * g.RPC + r) * LP;
+            const C* b2 = sm + (2 * g.RPC + r) * LP;
+            const C* b3 = sm + (3 * g.RPC + r) * LP;
+            T vmax2 = (T)0;
+            for (int m = t; m < H; m += TT) {
+                const C z0 = b0[spad(m)], z1 = b1[spad(m)], z2 = b2[spad(m)], z3 = b3[spad(m)];
+                // z0 = psi_x, z1 = psi_y, z2 = omega_x, z3 = omega_y at points 2m (re) and 2m+1 (im)
+                const T je = z0.x * z3.x - z1.x * z2.x;
+                const T jo = z0.y * z3.y - z1.y * z2.y;
+                if (a.cfl) {
+                    const T ve = z0.x * z0.x + z1.x * z1.x, vo = z0.y * z0.y + z1.y * z1.y;
+                    vmax2 = fmax(vmax2, fmax(ve, vo));
+                }
+                if constexpr (MODE == ROW_DUMP) {
+                    const size_t o = (size_t)y * nx + 2 * m;
+                    a.out_real[0][o] = z0.x; a.out_real[0][o + 1] = z0.y;
+                    a.out_real[1][o] = z1.x; a.out_real[1][o + 1] = z1.y;
+                    a.out_real[2][o] = z2.x; a.out_real[2][o + 1] = z2.y;
+                    a.out_real[3][o] = z3.x; a.out_real[3][o + 1] = z3.y;
+                    a.out_real[4][o] = je;   a.out_real[4][o + 1] = jo;
+                }
+                b0[spad(m)] = cmake<C>(je, jo);
+            }
+            if (a.cfl) {
+                double v = (double)vmax2;
+                if ((blockDim.x & 31) == 0) {  // whole warps: reduce before the atomic
+                    v = warp_max(v);
+                    if ((threadIdx.x & 31) == 0) atomicMax(&a.ds->maxvel2, (unsigned long long)__double_as_longlong(v));
+                } else {
+                    atomicMax(&a.ds->maxvel2, (unsigned long long)__double_as_longlong(v));
+                }
+            }
+            __syncthreads();
+            fft_smem<E, false>(b0, H, g.logH, t, TT, a.twr);
+        } else {
+            const C* b0 = sm + (0 * g.RPC + r) * LP;
+            for (int m = t; m < H; m += TT) {
+                const size_t o = (size_t)y * nx + 2 * m;
+                const C z0 = b0[spad(m)];
+                if constexpr (MODE == ROW_UVW) {
+                    const C z1 = sm[(1 * g.RPC + r) * LP + spad(m)];
+                    const C z2 = sm[(2 * g.RPC + r) * LP + spad(m)];
+                    a.out_real[0][o] = z0.x; a.out_real[0][o + 1] = z0.y;   // u = psi_y
+                    a.out_real[1][o] = -z1.x; a.out_real[1][o + 1] = -z1.y; // v = -psi_x
+                    a.out_real[2][o] = z2.x; a.out_real[2][o + 1] = z2.y;   // omega
+                } else {
+                    a.out_real[0][o] = z0.x;
+                    a.out_real[0][o + 1] = z0.y;
+                }
+            }
+            return;
+        }
+    }
+    // forward post-processing: X[k] = E[k] + exp(-2 pi i k/nx) O[k],
+    // E = (W[k] + conj W[H-k])/2, O = (W[k] - conj W[H-k])/(2i), for the kept k < Kx
+    {
+        const C* b0 = sm + r * LP;
+        C* dst = a.G + (size_t)y * Kxp;
+        const T half = (T)0.5;
+        for (int k = t; k < Kx; k += TT) {
+            const C wa = b0[spad(k)];
+            const C wb = b0[spad((H - k) & (H - 1))];
+            C ev, od;
+            ev.x = half * (wa.x + wb.x);
+            ev.y = half * (wa.y - wb.y);
+            od.x = half * (wa.y + wb.y);
+            od.y = -half * (wa.x - wb.x);
+            dst[k] = cadd(ev, cmul(od, __ldg(&a.twh[k])));
+        }
+    }
+}
+
+// ============================================================ column kernel
+enum { COL_STAGE = 0, COL_PROLOGUE = 1, COL_INV1 = 2, COL_FWD_EXPORT = 3, COL_NL_EXPORT = 4 };
+
+template <typename T> struct ColArgs {
+    typedef typename CT<T>::C C;
+    const C* G;                 // C[ny][Kxp]
+    C* F[4];                    // C[ny][Kxp]
+    C* W0;                      // kept state at the step start (or the prologue input)
+    C* WS;                      // stage state
+    C* ACC;                     // RK accumulator
+    const C* PSI0;              // stored psi_hat (prologue)
+    C* SFD;                     // SFD filtered state
+    const T* hvw;               // hyperviscosity weight per kept mode
+    const T* sfdw;              // sfd_strength * ramp per kept mode
+    const T* kxv;
+    const T* kyv;
+    const C* twc;               // exp(-2 pi i t/ny), t < ny
+    DevScalars* ds;
+    StepParams sp;
+    double2* out_spec;          // FP64 export [nky][nkx]
+    double out_scale;           // export scale (1/(nx ny) forward, -1/(nx ny) nonlinear)
+    int psi_from_w;             // prologue: Psi = -W0/k^2 instead of PSI0
+    int nfields;                // prologue: number of fields (4 for a stage, 3 = Psi,Psi_y,Omega)
+};
+
+template <typename T, typename C>
+__device__ __forceinline__ C field_value(int f, C w, T kx, T ky) {
+    // f: 0 Psi = -w/k^2, 1 Psi_y = i ky Psi, 2 Omega = w, 3 Omega_y = i ky w
+    // (spectral_core.c:17-31; psi uses a true division as the reference does)
+    C v = w;
+    if (f < 2) {
+        const T k2 = kx * kx + ky * ky;
+        if (k2 > (T)1e-12) { v.x = -w.x / k2; v.y = -w.y / k2; }
+        else { v.x = (T)0; v.y = (T)0; }
+    }
+    if (f == 1 || f == 3) {
+        C d;
+        d.x = -ky * v.y;
+        d.y = ky * v.x;
+        v = d;
+    }
+    return v;
+}
+
+// grid = Kxp / CW, block = CW * (ny / E), dynamic smem = CW * spad_len(ny) * sizeof(C)
+template <typename T, int E, int MODE, int STAGE>
+__global__ void __launch_bounds__(512) k_col(Geo g, ColArgs<T> a) {
+    typedef typename CT<T>::C C;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* sm = reinterpret_cast<C*>(smem_raw);
+    const int ny = g.ny, TC = ny / E, LP = spad_len(ny), CW = g.CW;
+    const int b = threadIdx.x / TC, t = threadIdx.x - b * TC;
+    const int c0 = blockIdx.x * CW;
+    const int Kx = g.Kx, Kxp = g.Kxp, Ky = g.Ky;
+    const int nthr = blockDim.x;
+    C* mybuf = sm + b * LP;
+    __shared__ double s_dt;
+
+    if (MODE == COL_STAGE) {
+        if (threadIdx.x == 0) {
+            double dt;
+            if (STAGE == 1) {
+                if (a.sp.adaptive) {
+                    // spectral_time_integration.c:9-31 on max|u| of the stage-1 fields
+                    const double vmax = sqrt(__longlong_as_double((long long)a.ds->maxvel2));
+                    const double dt_cfl = a.sp.cfl * a.sp.dxmin / (vmax + 1e-12);
+                    const double dt_visc = 0.5 * a.sp.Re * a.sp.dxmin * a.sp.dxmin;
+                    dt = fmin(dt_cfl, dt_visc);
+                    dt = fmax(dt, 1e-8);
+                    dt = fmin(dt, 0.1);
+                } else {
+                    dt = a.ds->dt_fixed;
+                }
+                if (blockIdx.x == 0) a.ds->dt = dt;
+            } else {
+                dt = a.ds->dt;
+            }
+            s_dt = dt;
+        }
+    }
+
+    if (MODE == COL_STAGE || MODE == COL_FWD_EXPORT || MODE == COL_NL_EXPORT) {
+        for (int idx = threadIdx.x; idx < ny * CW; idx += nthr) {
+            const int y = idx / CW, c = idx - y * CW;
+            C v = cmake<C>(0.0, 0.0);
+            if (c0 + c < Kx) v = a.G[(size_t)y * Kxp + c0 + c];
+            sm[c * LP + spad(y)] = v;
+        }
+        __syncthreads();
+        fft_smem<E, false>(mybuf, ny, g.logny, t, TC, a.twc);
+
+        if constexpr (MODE == COL_FWD_EXPORT || MODE == COL_NL_EXPORT) {
+            const T sc = (T)a.out_scale;
+            for (int idx = threadIdx.x; idx < CW * Ky; idx += nthr) {
+                const int c = idx / Ky, jj = idx - c * Ky, i = c0 + c;
+                if (i >= Kx) continue;
+                const int j = kept_j(g, jj);
+                const C v = sm[c * LP + spad(j)];
+                a.out_spec[(size_t)j * g.nkx + i] = make_double2((double)(v.x * sc), (double)(v.y * sc));
+            }
+            return;
+        } else {
+            const double dt = s_dt;
+            const T inv_re = (T)a.sp.inv_re;
+            const T sc = (T)a.sp.scale;
+            const T ch = (T)(0.5 * dt), cf = (T)dt, c6 = (T)(dt / 6.0);
+            double f_amp = 0.0;
+            double sfd_a = 0.0;
+            if (STAGE == 4) {
+                if (a.sp.forcing) f_amp = a.sp.f_sigma * sqrt(dt);
+                if (a.sp.sfd) {
+                    sfd_a = dt / a.sp.sfd_tau;
+                    sfd_a = sfd_a > 1.0 ? 1.0 : (sfd_a < 0.0 ? 0.0 : sfd_a);
+                }
+            }
+            for (int idx = threadIdx.x; idx < CW * Ky; idx += nthr) {
+                const int c = idx / Ky, jj = idx - c * Ky, i = c0 + c;
+                if (i >= Kx) continue;
+                const int j = kept_j(g, jj);
+                const C gh = sm[c * LP + spad(j)];
+                C nl;  // N = -(r2c(J) / (nx ny))
+                nl.x = -(gh.x * sc);
+                nl.y = -(gh.y * sc);
+                const size_t s = (size_t)i * Ky + jj;
+                const C w0 = a.W0[s];
+                const C ws = (STAGE == 1) ? w0 : a.WS[s];
+                const T kx = a.kxv[i], ky = a.kyv[jj];
+                const T k2 = kx * kx + ky * ky;
+                C k;  // k = N - k^2 omega / Re - damping (spectral_time_integration.c:50-54)
+                k.x = nl.x - k2 * ws.x * inv_re;
+                k.y = nl.y - k2 * ws.y * inv_re;
+                if (a.sp.hv || a.sp.sfd) {
+                    C damp = cmake<C>(0.0, 0.0);
+                    if (a.sp.hv) { const T w = a.hvw[s]; damp.x += w * ws.x; damp.y += w * ws.y; }
+                    if (a.sp.sfd) {
+                        const T sw = a.sfdw[s];
+                        if (sw > (T)0) {
+                            const C fb = a.SFD[s];
+                            damp.x += sw * (ws.x - fb.x);
+                            damp.y += sw * (ws.y - fb.y);
+                        }
+                    }
+                    k.x -= damp.x;
+                    k.y -= damp.y;
+                }
+                C wn;
+                if (STAGE == 1) {
+                    a.ACC[s] = k;
+                    wn.x = w0.x + ch * k.x; wn.y = w0.y + ch * k.y;
+                    a.WS[s] = wn;
+                } else if (STAGE == 2 || STAGE == 3) {
+                    C acc = a.ACC[s];
+                    acc.x = acc.x + (T)2 * k.x;
+                    acc.y = acc.y + (T)2 * k.y;
+                    a.ACC[s] = acc;
+                    const T cc = (STAGE == 2) ? ch : cf;
+                    wn.x = w0.x + cc * k.x; wn.y = w0.y + cc * k.y;
+                    a.WS[s] = wn;
+                } else {
+                    const C acc = a.ACC[s];
+                    wn.x = w0.x + c6 * (acc.x + k.x);
+                    wn.y = w0.y + c6 * (acc.y + k.y);
+                    if (a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9) {
+                        // white-in-time forcing increment sigma sqrt(dt) xi (Euler-Maruyama)
+                        const double kxd = 2.0 * 3.141592653589793 * i / g.Lx;
+                        const double kyd = (j <= g.ny / 2) ? 2.0 * 3.141592653589793 * j / g.Ly
+                                                           : 2.0 * 3.141592653589793 * (j - g.ny) / g.Ly;
+                        const double k2d = kxd * kxd + kyd * kyd;
+                        const double km = sqrt(k2d);
+                        if (k2d > 1e-12 && km >= a.sp.f_kmin && km <= a.sp.f_kmax) {
+                            int jsrc = j, flip = 0;
+                            if (i == 0 && j > g.ny / 2) { jsrc = g.ny - j; flip = 1; }
+                            unsigned long long ctr[4] = {(unsigned long long)jsrc * g.nkx + i, a.ds->step_cur,
+                                                         NSG_TAG_FORCE, 0ULL};
+                            philox4x64(ctr, a.sp.f_seed, 0ULL);
+                            const double u1 = fmax(u53(ctr[0]), 2.2250738585072014e-308);
+                            const double u2 = u53(ctr[1]);
+                            const double rad = sqrt(-2.0 * log(u1)) * 0.70710678118654752440;
+                            double sn, cs;
+                            sincos(2.0 * 3.141592653589793 * u2, &sn, &cs);
+                            double xr = rad * cs, xi = rad * sn;
+                            if (flip) xi = -xi;
+                            wn.x = (T)((double)wn.x + f_amp * xr);
+                            wn.y = (T)((double)wn.y + f_amp * xi);
+                        }
+                    }
+                    if (a.sp.sfd) {
+                        C fb = a.SFD[s];
+                        const T al = (T)sfd_a, om = (T)(1.0 - sfd_a);
+                        fb.x = om * fb.x + al * wn.x;
+                        fb.y = om * fb.y + al * wn.y;
+                        a.SFD[s] = fb;
+                    }
+                    a.W0[s] = wn;
+                }
+            }
+            if (STAGE == 4 && blockIdx.x == 0 && threadIdx.x == 0) a.ds->t = a.ds->t + dt;
+            __syncthreads();
+        }
+    }
+
+    if constexpr (MODE == COL_FWD_EXPORT || MODE == COL_NL_EXPORT) return;
+
+    // inverse y-transforms of the next-stage fields
+    const int nf = (MODE == COL_INV1) ? 1 : (MODE == COL_PROLOGUE ? a.nfields : 4);
+    const C* src = (MODE == COL_STAGE) ? ((STAGE == 4) ? a.W0 : a.WS) : a.W0;
+    for (int f = 0; f < nf; ++f) {
+        for (int idx = threadIdx.x; idx < CW * ny; idx += nthr) {
+            const int c = idx / ny, j = idx - c * ny, i = c0 + c;
+            const int jk = kept_jj(g, j);
+            C v = cmake<C>(0.0, 0.0);
+            if (i < Kx && jk >= 0) {
+                const size_t s = (size_t)i * Ky + jk;
+                if (MODE == COL_INV1) {
+                    v = src[s];
+                } else if (MODE == COL_PROLOGUE && !a.psi_from_w && f < 2) {
+                    const C p = a.PSI0[s];
+                    v = p;
+                    if (f == 1) { const T ky = a.kyv[jk]; v.x = -ky * p.y; v.y = ky * p.x; }
+                } else {
+                    v = field_value<T, C>(f, src[s], a.kxv[i], a.kyv[jk]);
+                }
+            }
+            sm[c * LP + spad(j)] = v;
+        }
+        __syncthreads();
+        fft_smem<E, true>(mybuf, ny, g.logny, t, TC, a.twc);
+        C* dstF = a.F[f];
+        for (int idx = threadIdx.x; idx < ny * CW; idx += nthr) {
+            const int y = idx / CW, c = idx - y * CW;
+            dstF[(size_t)y * Kxp + c0 + c] = sm[c * LP + spad(y)];
+        }
+        __syncthreads();
+    }
+}
+
+// ======================================================= auxiliary kernels
+
+// grid, wavenumbers, k^2, mask exactly as spectral_initialization.c:15-49
+__global__ void k_geometry(Geo g, double* x, double* y, double* kx, double* ky, double* k2, int* mask) {
+    const int nx = g.nx, ny = g.ny, nkx = g.nkx;
+    const long long n = (long long)nkx * g.nky;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(idx / nkx), i = (int)(idx - (long long)j * nkx);
+        const double kxv = 2.0 * 3.14159265358979323846 * i / g.Lx;
+        const double kyv = (j <= ny / 2) ? 2.0 * 3.14159265358979323846 * j / g.Ly : 2.0 * 3.14159265358979323846 * (j - ny) / g.Ly;
+        if (k2) k2[idx] = kxv * kxv + kyv * kyv;
+        if (mask) {
+            const int band = (j <= ny / 2) ? j : j - ny;
+            mask[idx] = (i <= (2 * nkx) / 3) && (abs(band) <= (2 * ny) / 6);
+        }
+        if (j == 0 && kx) kx[i] = kxv;
+        if (i == 0 && ky) ky[j] = kyv;
+        if (j == 0 && i < nx && x) x[i] = i * g.Lx / nx;
+        if (i == 0 && y) y[j] = j * g.Ly / ny;
+    }
+    // x covers i < nx which exceeds nkx: finish the tail
+    for (long long i = nkx + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nx; i += (long long)gridDim.x * blockDim.x)
+        if (x) x[i] = i * g.Lx / nx;
+}
+
+__device__ __forceinline__ double geo_k2(const Geo& g, int j, int i) {
+    const double kxv = 2.0 * 3.14159265358979323846 * i / g.Lx;
+    const double kyv = (j <= g.ny / 2) ? 2.0 * 3.14159265358979323846 * j / g.Ly : 2.0 * 3.14159265358979323846 * (j - g.ny) / g.Ly;
+    return kxv * kxv + kyv * kyv;
+}
+__device__ __forceinline__ int geo_kept(const Geo& g, int j, int i) {
+    const int band = (j <= g.ny / 2) ? j : j - g.ny;
+    return (i <= (2 * g.nkx) / 3) && (abs(band) <= (2 * g.ny) / 6);
+}
+
+// max |k| over all modes (hyperviscosity.c:68-72)
+__global__ void k_kmax(Geo g, DevScalars* ds) {
+    const long long n = (long long)g.nkx * g.nky;
+    double m = 0.0;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(idx / g.nkx), i = (int)(idx - (long long)j * g.nkx);
+        m = fmax(m, sqrt(geo_k2(g, j, i)));
+    }
+    m = warp_max(m);
+    if ((threadIdx.x & 31) == 0) atomicMax(&ds->kmax_bits, (unsigned long long)__double_as_longlong(m));
+}
+
+// weight = c ((|k| - kc) inv_bw)^order above kc (hyperviscosity.c:88-101), FP64 full table
+__global__ void k_hv_weights(Geo g, int enabled, double coefficient, int order, double cutoff, double inv_bw,
+                             double* w_full) {
+    const long long n = (long long)g.nkx * g.nky;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(idx / g.nkx), i = (int)(idx - (long long)j * g.nkx);
+        double w = 0.0;
+        if (enabled) {
+            const double km = sqrt(geo_k2(g, j, i));
+            if (km > cutoff) w = coefficient * pow((km - cutoff) * inv_bw, (double)order);
+        }
+        w_full[idx] = w;
+    }
+}
+
+// kept-mode tables in the working precision (FP64 generated, rounded once)
+template <typename T>
+__global__ void k_tables(Geo g, const double* w_full, int sfd, double sfd_strength, int order, double cutoff,
+                         double inv_bw, T* kxv, T* kyv, T* hvw, T* sfdw) {
+    const long long n = (long long)g.Kxp * g.Ky;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(idx / g.Ky), jj = (int)(idx - (long long)i * g.Ky);
+        const int j = kept_j(g, jj);
+        double w = 0.0, s = 0.0;
+        if (i < g.Kx) {
+            w = w_full ? w_full[(size_t)j * g.nkx + i] : 0.0;
+            if (sfd && inv_bw > 0.0) {
+                const double km = sqrt(geo_k2(g, j, i));
+                double ratio = 0.0;
+                if (km > cutoff) {
+                    double sc = (km - cutoff) * inv_bw;
+                    sc = sc < 0.0 ? 0.0 : (sc > 1.0 ? 1.0 : sc);
+                    ratio = pow(sc, (double)order);
+                }
+                s = sfd_strength * ratio;
+            }
+        }
+        hvw[idx] = (T)w;
+        sfdw[idx] = (T)s;
+        if (jj == 0) kxv[i] = (T)(2.0 * 3.14159265358979323846 * i / g.Lx);
+        if (i == 0) {
+            kyv[jj] = (T)((j <= g.ny / 2) ? 2.0 * 3.14159265358979323846 * j / g.Ly : 2.0 * 3.14159265358979323846 * (j - g.ny) / g.Ly);
+        }
+    }
+}
+
+// twiddle table tw[t] = exp(-2 pi i t / L), t < n (FP64 sincospi, rounded once)
+template <typename C>
+__global__ void k_twiddles(C* tw, int n, int L) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        double s, c;
+        sincospi(-2.0 * (double)t / (double)L, &s, &c);
+        tw[t].x = c;
+        tw[t].y = s;
+    }
+}
+
+// host-layout spectrum -> kept state (and masked-out modes into OUT); flag if any masked-out mode is non-zero
+template <typename T>
+__global__ void k_import(Geo g, const double2* wh, const double2* ph, const double2* sh, typename CT<T>::C* W,
+                         typename CT<T>::C* P, typename CT<T>::C* S, double2* out, double2* outsfd, int* flag) {
+    typedef typename CT<T>::C C;
+    const long long n = (long long)g.nkx * g.nky;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(idx / g.nkx), i = (int)(idx - (long long)j * g.nkx);
+        const int jk = kept_jj(g, j);
+        const double2 w = wh[idx];
+        if (i < g.Kx && jk >= 0) {
+            const size_t s = (size_t)i * g.Ky + jk;
+            W[s] = cmake<C>(w.x, w.y);
+            if (P) { const double2 p = ph[idx]; P[s] = cmake<C>(p.x, p.y); }
+            if (S) { const double2 q = sh[idx]; S[s] = cmake<C>(q.x, q.y); }
+        } else {
+            if (out) out[idx] = w;
+            if (outsfd) outsfd[idx] = sh ? sh[idx] : make_double2(0.0, 0.0);
+            if (flag && (w.x != 0.0 || w.y != 0.0)) atomicOr(flag, 1);
+        }
+    }
+}
+
+// reference-layout exports of the device state (compute_derivatives' spectral part, spectral_core.c:8-34)
+template <typename T>
+__global__ void k_export(Geo g, const typename CT<T>::C* W, const typename CT<T>::C* S, const double2* out,
+                         const double2* outsfd, double2* wh, double2* ph, double2* uh, double2* vh, double2* sh) {
+    const long long n = (long long)g.nkx * g.nky;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(idx / g.nkx), i = (int)(idx - (long long)j * g.nkx);
+        const int jk = kept_jj(g, j);
+        double2 w = make_double2(0.0, 0.0), q = make_double2(0.0, 0.0);
+        if (i < g.Kx && jk >= 0) {
+            const size_t s = (size_t)i * g.Ky + jk;
+            w = make_double2((double)W[s].x, (double)W[s].y);
+            if (S) q = make_double2((double)S[s].x, (double)S[s].y);
+        } else {
+            if (out) w = out[idx];
+            if (outsfd) q = outsfd[idx];
+        }
+        if (wh) wh[idx] = w;
+        if (sh) sh[idx] = q;
+        const double kxv = 2.0 * 3.14159265358979323846 * i / g.Lx;
+        const double kyv = (j <= g.ny / 2) ? 2.0 * 3.14159265358979323846 * j / g.Ly : 2.0 * 3.14159265358979323846 * (j - g.ny) / g.Ly;
+        const double k2 = kxv * kxv + kyv * kyv;
+        double2 p = make_double2(0.0, 0.0);
+        if (k2 > 1e-12) p = make_double2(-w.x / k2, -w.y / k2);
+        if (ph) ph[idx] = p;
+        if (uh) uh[idx] = make_double2(-kyv * p.y, kyv * p.x);
+        if (vh) vh[idx] = make_double2(kxv * p.y, -kxv * p.x);
+    }
+}
+
+// FP64 pointwise compat ops over host-layout spectra
+__global__ void k_velocity(Geo g, const double2* wh, double2* ph, double2* uh, double2* vh) {
+    const long long n = (long long)g.nkx * g.nky;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(idx / g.nkx), i = (int)(idx - (long long)j * g.nkx);
+        const double kxv = 2.0 * 3.14159265358979323846 * i / g.Lx;
+        const double kyv = (j <= g.ny / 2) ? 2.0 * 3.14159265358979323846 * j / g.Ly : 2.0 * 3.14159265358979323846 * (j - g.ny) / g.Ly;
+        const double k2 = kxv * kxv + kyv * kyv;
+        const double2 w = wh[idx];
+        double2 p = make_double2(0.0, 0.0);
+        if (k2 > 1e-12) p = make_double2(-w.x / k2, -w.y / k2);
+        ph[idx] = p;
+        uh[idx] = make_double2(-kyv * p.y, kyv * p.x);
+        vh[idx] = make_double2(kxv * p.y, -kxv * p.x);
+    }
+}
+
+__global__ void k_dealias(Geo g, double2* fh, double2* masked_copy) {
+    const long long n = (long long)g.nkx * g.nky;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(idx / g.nkx), i = (int)(idx - (long long)j * g.nkx);
+        double2 v = fh[idx];
+        if (!geo_kept(g, j, i)) v = make_double2(0.0, 0.0);
+        if (masked_copy) masked_copy[idx] = v;
+        else fh[idx] = v;
+    }
+}
+
+// rhs -= w state + s ramp (state - sfd)   (hyperviscosity.c:104-150)
+__global__ void k_hv_apply(Geo g, const double* w_full, int visc, int sfd, double sfd_strength, int order,
+                           double cutoff, double inv_bw, double2* rhs, const double2* st, const double2* sf) {
+    const long long n = (long long)g.nkx * g.nky;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(idx / g.nkx), i = (int)(idx - (long long)j * g.nkx);
+        const double2 s = st[idx];
+        double dr = 0.0, di = 0.0;
+        if (visc) { const double w = w_full[idx]; dr += w * s.x; di += w * s.y; }
+        if (sfd) {
+            double ratio = 0.0;
+            if (inv_bw > 0.0) {
+                const double km = sqrt(geo_k2(g, j, i));
+                if (km > cutoff) {
+                    double sc = (km - cutoff) * inv_bw;
+                    sc = sc < 0.0 ? 0.0 : (sc > 1.0 ? 1.0 : sc);
+                    ratio = pow(sc, (double)order);
+                }
+            }
+            const double sw = sfd_strength * ratio;
+            if (sw > 0.0) { const double2 f = sf[idx]; dr += sw * (s.x - f.x); di += sw * (s.y - f.y); }
+        }
+        double2 r = rhs[idx];
+        r.x -= dr;
+        r.y -= di;
+        rhs[idx] = r;
+    }
+}
+
+__global__ void k_hv_post(Geo g, double alpha, const double2* st, double2* sf) {
+    const long long n = (long long)g.nkx * g.nky;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+        const double2 p = sf[idx], s = st[idx];
+        sf[idx] = make_double2((1.0 - alpha) * p.x + alpha * s.x, (1.0 - alpha) * p.y + alpha * s.y);
+    }
+}
+
+// masked-out modes evolve by the linear part only (the reference's RK4 on modes
+// whose nonlinear term is zeroed by the mask); FP64, reference arithmetic
+__global__ void k_outside(Geo g, StepParams sp, const double* w_full, double cutoff, double inv_bw, int order,
+                          double sfd_strength, DevScalars* ds, double2* out, double2* outsfd) {
+    const long long n = (long long)g.nkx * g.nky;
+    const double dt = ds->dt;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(idx / g.nkx), i = (int)(idx - (long long)j * g.nkx);
+        if (geo_kept(g, j, i)) continue;
+        const double k2 = geo_k2(g, j, i);
+        const double w = (sp.hv && w_full) ? w_full[idx] : 0.0;
+        double sw = 0.0;
+        if (sp.sfd && inv_bw > 0.0) {
+            const double km = sqrt(k2);
+            if (km > cutoff) {
+                double sc = (km - cutoff) * inv_bw;
+                sc = sc < 0.0 ? 0.0 : (sc > 1.0 ? 1.0 : sc);
+                sw = sfd_strength * pow(sc, (double)order);
+            }
+        }
+        const double2 w0 = out[idx];
+        const double2 fb = outsfd ? outsfd[idx] : make_double2(0.0, 0.0);
+        double2 kk[4];
+        double2 ws = w0;
+        const double cst[3] = {0.5 * dt, 0.5 * dt, dt};
+        for (int s = 0; s < 4; ++s) {
+            double2 k;
+            k.x = 0.0 - k2 * ws.x * sp.inv_re;
+            k.y = 0.0 - k2 * ws.y * sp.inv_re;
+            double dr = 0.0, di = 0.0;
+            if (sp.hv) { dr += w * ws.x; di += w * ws.y; }
+            if (sp.sfd && sw > 0.0) { dr += sw * (ws.x - fb.x); di += sw * (ws.y - fb.y); }
+            k.x -= dr;
+            k.y -= di;
+            kk[s] = k;
+            if (s < 3) ws = make_double2(w0.x + cst[s] * k.x, w0.y + cst[s] * k.y);
+        }
+        double2 wn;
+        wn.x = w0.x + dt / 6.0 * (kk[0].x + 2.0 * kk[1].x + 2.0 * kk[2].x + kk[3].x);
+        wn.y = w0.y + dt / 6.0 * (kk[0].y + 2.0 * kk[1].y + 2.0 * kk[2].y + kk[3].y);
+        out[idx] = wn;
+        if (sp.sfd && outsfd) {
+            double a = dt / sp.sfd_tau;
+            a = a > 1.0 ? 1.0 : (a < 0.0 ? 0.0 : a);
+            outsfd[idx] = make_double2((1.0 - a) * fb.x + a * wn.x, (1.0 - a) * fb.y + a * wn.y);
+        }
+    }
+}
+
+// per-block compensated partial sums of two quantities (s0, s1) -> part[2*block]
+// kind 0: energy 0.5(a^2+b^2); 1: enstrophy 0.5 a^2; 2: max sqrt(a^2+b^2) (into ds->maxvel2)
+__global__ void k_reduce_real(int kind, const double* a, const double* b, long long n, double2* part, DevScalars* ds) {
+    DD acc = {0.0, 0.0};
+    double m = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double x = a[i];
+        if (kind == 0) { const double yv = b[i]; dd_add(acc, 0.5 * (x * x + yv * yv)); }
+        else if (kind == 1) dd_add(acc, 0.5 * x * x);
+        else { const double yv = b[i]; m = fmax(m, sqrt(x * x + yv * yv)); }
+    }
+    if (kind == 2) {
+        m = warp_max(m);
+        if ((threadIdx.x & 31) == 0) atomicMax(&ds->aux_max, (unsigned long long)__double_as_longlong(m));
+        return;
+    }
+    DD tot = block_dd(acc);
+    if (threadIdx.x == 0) part[blockIdx.x] = make_double2(tot.s, tot.c);
+}
+
+// merge n partial pairs into out[0] (value) with one block
+__global__ void k_merge_partials(const double2* part, int n, double* out) {
+    DD acc = {0.0, 0.0};
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        DD v = {part[i].x, part[i].y};
+        acc = dd_merge(acc, v);
+    }
+    DD tot = block_dd(acc);
+    if (threadIdx.x == 0) out[0] = tot.s + tot.c;
+}
+
+// Parseval energy and enstrophy of the kept state: E = 1/2 sum_full |w|^2/k^2,
+// Z = 1/2 sum_full |w|^2 (Hermitian weight 2 for kx > 0); flags non-finite values
+template <typename T>
+__global__ void k_diag(Geo g, const typename CT<T>::C* W, const T* kxv, const T* kyv, double2* part, DevScalars* ds) {
+    DD e = {0.0, 0.0}, z = {0.0, 0.0};
+    int bad = 0;
+    const long long n = (long long)g.Kx * g.Ky;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(idx / g.Ky), jj = (int)(idx - (long long)i * g.Ky);
+        const double wx = (double)W[idx].x, wy = (double)W[idx].y;
+        if (!isfinite(wx) || !isfinite(wy)) bad = 1;
+        const int j = kept_j(g, jj);
+        const double k2 = geo_k2(g, j, i);
+        const double wt = (i == 0) ? 1.0 : 2.0;
+        const double m2 = wt * (wx * wx + wy * wy);
+        dd_add(z, 0.5 * m2);
+        if (k2 > 1e-12) dd_add(e, 0.5 * m2 / k2);
+    }
+    if (bad) atomicOr(&ds->flag, 2);
+    DD te = block_dd(e);
+    __syncthreads();
+    DD tz = block_dd(z);
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = make_double2(te.s, te.c);
+        part[2 * blockIdx.x + 1] = make_double2(tz.s, tz.c);
+    }
+}
+__global__ void k_merge_pairs2(const double2* part, int nblocks, double* out) {
+    DD a = {0.0, 0.0}, b = {0.0, 0.0};
+    for (int i = threadIdx.x; i < nblocks; i += blockDim.x) {
+        DD u = {part[2 * i].x, part[2 * i].y}, v = {part[2 * i + 1].x, part[2 * i + 1].y};
+        a = dd_merge(a, u);
+        b = dd_merge(b, v);
+    }
+    DD ta = block_dd(a);
+    __syncthreads();
+    DD tb = block_dd(b);
+    if (threadIdx.x == 0) { out[0] = ta.s + ta.c; out[1] = tb.s + tb.c; }
+}
+
+// spectral statistics of host-layout spectra (spectral_analysis.c:36-142)
+__global__ void k_spec_stats(Geo g, const double2* wh, const double2* uh, const double2* vh, double2* part,
+                             DevScalars* ds, double* bins, int* counts, int nbins) {
+    const long long n = (long long)g.nkx * g.nky;
+    const double k2last = geo_k2(g, g.nky - 1, g.nkx - 1);
+    const double max_k = sqrt(k2last);
+    DD tot = {0.0, 0.0}, hi = {0.0, 0.0}, acc = {0.0, 0.0};
+    double cnt = 0.0, mx = 0.0;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(idx / g.nkx), i = (int)(idx - (long long)j * g.nkx);
+        const double k2 = geo_k2(g, j, i);
+        if (wh) {
+            const double2 w = wh[idx];
+            const double m = hypot(w.x, w.y);
+            const double m2 = m * m;
+            dd_add(tot, m2);
+            const double kn = max_k > 0.0 ? sqrt(k2) / max_k : 0.0;
+            if (kn > 0.8) dd_add(hi, m2);
+            mx = fmax(mx, m);
+            if (k2 > 0.25 * k2last) { dd_add(acc, m2); cnt += 1.0; }
+        }
+        if (uh && bins) {
+            const int bin = (int)(sqrt(k2) + 0.5);
+            if (bin < nbins) {
+                const double2 u = uh[idx], v = vh[idx];
+                const double um = hypot(u.x, u.y), vm = hypot(v.x, v.y);
+                atomicAdd(&bins[bin], 0.5 * (um * um + vm * vm));
+                atomicAdd(&counts[bin], 1);
+            }
+        }
+    }
+    mx = warp_max(mx);
+    if ((threadIdx.x & 31) == 0) atomicMax(&ds->aux_max, (unsigned long long)__double_as_longlong(mx));
+    DD a = block_dd(tot);
+    __syncthreads();
+    DD b = block_dd(hi);
+    __syncthreads();
+    DD c = block_dd(acc);
+    __syncthreads();
+    DD d = {cnt, 0.0};
+    d = block_dd(d);
+    if (threadIdx.x == 0) {
+        part[4 * blockIdx.x + 0] = make_double2(a.s, a.c);
+        part[4 * blockIdx.x + 1] = make_double2(b.s, b.c);
+        part[4 * blockIdx.x + 2] = make_double2(c.s, c.c);
+        part[4 * blockIdx.x + 3] = make_double2(d.s, d.c);
+    }
+}
+__global__ void k_merge_pairs4(const double2* part, int nblocks, double* out) {
+    for (int q = 0; q < 4; ++q) {
+        DD a = {0.0, 0.0};
+        for (int i = threadIdx.x; i < nblocks; i += blockDim.x) {
+            DD u = {part[4 * i + q].x, part[4 * i + q].y};
+            a = dd_merge(a, u);
+        }
+        DD t = block_dd(a);
+        if (threadIdx.x == 0) out[q] = t.s + t.c;
+        __syncthreads();
+    }
+}
+
+// Taylor-Green fields of spectral_initialization.c:72-88
+__global__ void k_taylor_green(Geo g, double* u, double* v, double* w, double* p) {
+    const long long n = (long long)g.nx * g.ny;
+    const double tp = 2 * 3.14159265358979323846;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(idx / g.nx), i = (int)(idx - (long long)j * g.nx);
+        const double x = i * g.Lx / g.nx, y = j * g.Ly / g.ny;
+        u[idx] = sin(tp * x / g.Lx) * cos(tp * y / g.Ly);
+        v[idx] = -cos(tp * x / g.Lx) * sin(tp * y / g.Ly);
+        w[idx] = 2.0 * (tp / g.Lx) * cos(tp * x / g.Lx) * cos(tp * y / g.Ly);
+        p[idx] = 0.0;
+    }
+}
+
+// random-phase spectrum, unnormalised; energy partials (weight 2 for 0 < kx < Nyquist)
+__global__ void k_random_spectrum(Geo g, unsigned long long seed, double k0, double2* wh, double2* part) {
+    const long long n = (long long)g.nkx * g.nky;
+    DD e = {0.0, 0.0};
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(idx / g.nkx), i = (int)(idx - (long long)j * g.nkx);
+        const double k2 = geo_k2(g, j, i);
+        double2 v = make_double2(0.0, 0.0);
+        if (geo_kept(g, j, i) && k2 > 1e-12) {
+            int jsrc = j, flip = 0;
+            if (i == 0 && j > g.ny / 2) { jsrc = g.ny - j; flip = 1; }
+            unsigned long long ctr[4] = {(unsigned long long)jsrc * g.nkx + i, 0ULL, NSG_TAG_IC, 0ULL};
+            philox4x64(ctr, seed, 0ULL);
+            const double km = sqrt(k2);
+            const double ek = km * km * km * km * exp(-(km / k0) * (km / k0));
+            const double amp = sqrt(km * ek / 3.14159265358979323846);
+            double sn, cs;
+            sincos(2.0 * 3.14159265358979323846 * u53(ctr[0]), &sn, &cs);
+            v = make_double2(amp * cs, amp * sn);
+            if (flip) v.y = -v.y;
+            const double wt = (i == 0 || 2 * i == g.nx) ? 1.0 : 2.0;
+            const double m2 = v.x * v.x + v.y * v.y;
+            dd_add(e, wt * 0.5 * m2 / k2);
+        }
+        wh[idx] = v;
+    }
+    DD te = block_dd(e);
+    if (threadIdx.x == 0) part[blockIdx.x] = make_double2(te.s, te.c);
+}
+__global__ void k_scale_spec(long long n, double2* wh, const double* num_den) {
+    const double e = num_den[0];
+    const double target = num_den[1];
+    const double s = e > 0.0 ? sqrt(target / e) : 0.0;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+        double2 v = wh[idx];
+        wh[idx] = make_double2(v.x * s, v.y * s);
+    }
+}
+
+// forcing shell selection (forcing.c:78-96)
+__global__ void k_forcing_weights(const double* k2, int n, double kmin, double kmax, double* w, int* active) {
+    int cnt = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double km = sqrt(k2[i]);
+        const int on = (km >= kmin && km <= kmax);
+        w[i] = on ? 1.0 : 0.0;
+        cnt += on;
+    }
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(active, cnt);
+}
+
+__device__ __forceinline__ unsigned long long splitmix_out(unsigned long long z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+// ns_forcing_generate's stream, counter-addressable; single CTA (ranks by block scan)
+__global__ void k_forcing_generate(int n, const double* weights, int colored, double alpha, double beta,
+                                   double energy_target, unsigned long long state, double2* cs, double2* out) {
+    __shared__ int warp_tot[32];
+    __shared__ int base_s;
+    __shared__ double scale_s;
+    if (threadIdx.x == 0) base_s = 0;
+    __syncthreads();
+    DD tot = {0.0, 0.0};
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int c0 = 0; c0 < n; c0 += blockDim.x) {
+        const int idx = c0 + threadIdx.x;
+        const int on = (idx < n && weights[idx] > 0.0) ? 1 : 0;
+        // block exclusive scan of 'on'
+        int incl = on;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (lane == 31) warp_tot[wid] = incl;
+        __syncthreads();
+        if (wid == 0) {
+            int v = lane < nw ? warp_tot[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int u = __shfl_up_sync(0xffffffffu, v, o);
+                if (lane >= o) v += u;
+            }
+            if (lane < nw) warp_tot[lane] = v;  // inclusive warp prefix
+        }
+        __syncthreads();
+        const int rank = base_s + (wid > 0 ? warp_tot[wid - 1] : 0) + incl - on;
+        if (idx < n) {
+            double2 val = make_double2(0.0, 0.0);
+            if (on) {
+                const unsigned long long G = 0x9E3779B97F4A7C15ULL;
+                const unsigned long long d1 = splitmix_out(state + (2ULL * (unsigned long long)rank + 1ULL) * G);
+                const unsigned long long d2 = splitmix_out(state + (2ULL * (unsigned long long)rank + 2ULL) * G);
+                double u1 = u53(d1);
+                const double u2 = u53(d2);
+                u1 = fmax(u1, 2.2250738585072014e-308);
+                const double rad = sqrt(-2.0 * log(u1));
+                const double th = 2.0 * 3.14159265358979323846 * u2;
+                double sn, csv;
+                sincos(th, &sn, &csv);
+                double2 noise = make_double2(rad * csv, rad * sn);
+                if (colored) {
+                    double2 c = cs[idx];
+                    c = make_double2(alpha * c.x + beta * noise.x, alpha * c.y + beta * noise.y);
+                    cs[idx] = c;
+                    val = c;
+                } else {
+                    val = noise;
+                }
+                const double w = weights[idx];
+                out[idx] = make_double2(w * val.x, w * val.y);
+                dd_add(tot, w * w * (val.x * val.x + val.y * val.y));
+            } else {
+                out[idx] = make_double2(0.0, 0.0);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) base_s += warp_tot[nw - 1];
+        __syncthreads();
+    }
+    DD t = block_dd(tot);
+    if (threadIdx.x == 0) {
+        const double total = fmax(t.s + t.c, 1e-16);
+        scale_s = sqrt(energy_target / total);
+    }
+    __syncthreads();
+    const double sc = scale_s;
+    for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+        double2 v = out[idx];
+        out[idx] = make_double2(v.x * sc, v.y * sc);
+        if (colored) { double2 c = cs[idx]; cs[idx] = make_double2(c.x * sc, c.y * sc); }
+    }
+}
+
+}  // namespace nsg

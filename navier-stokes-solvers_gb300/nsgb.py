@@ -1,0 +1,363 @@
+"""Python binding (ctypes) of the GB300 drop-in solver library.
+
+Mirrors the reference C API (src/spectral/ns_spectral_solver.h:71-113 of
+DiogoRibeiro7/navier-stokes-solvers) and the C-ABI of include/ns_gpu.h, for
+tests and benchmarks.  It loads ``libns_gb300.so`` from this directory and
+raises if it is missing or no GPU is present: there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libns_gb300.so")
+
+_DP = C.POINTER(C.c_double)
+
+
+class HVConfig(C.Structure):
+    """NSSpectralHyperviscosityConfig (src/spectral/ns_spectral_solver.h:8-19)."""
+
+    _fields_ = [
+        ("enabled", C.c_int), ("coefficient", C.c_double), ("order", C.c_int),
+        ("cutoff_ratio", C.c_double), ("sfd_strength", C.c_double),
+        ("sfd_timescale", C.c_double), ("sfd_enabled", C.c_int), ("kmax", C.c_double),
+        ("cutoff_wavenumber", C.c_double), ("inv_bandwidth", C.c_double),
+    ]
+
+
+class SpectralData(C.Structure):
+    """NSSpectralData: the reference field order plus the appended ``gpu`` pointer."""
+
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("nkx", C.c_int), ("nky", C.c_int),
+        ("Lx", C.c_double), ("Ly", C.c_double), ("Re", C.c_double),
+        ("dt", C.c_double), ("t", C.c_double), ("cfl_factor", C.c_double),
+        ("u", _DP), ("v", _DP), ("p", _DP), ("omega", _DP), ("psi", _DP),
+        ("x", _DP), ("y", _DP),
+        ("u_hat", _DP), ("v_hat", _DP), ("omega_hat", _DP), ("psi_hat", _DP),
+        ("nonlinear_hat", _DP), ("rk1_hat", _DP), ("rk2_hat", _DP),
+        ("rk3_hat", _DP), ("rk4_hat", _DP), ("omega_tmp_hat", _DP),
+        ("kx", _DP), ("ky", _DP), ("k2", _DP),
+        ("forward_plan", C.c_void_p), ("backward_plan", C.c_void_p),
+        ("dealias_mask", C.POINTER(C.c_int)),
+        ("hyperviscosity", HVConfig),
+        ("hyperviscosity_weights", _DP),
+        ("sfd_hat", _DP),
+        ("gpu", C.c_void_p),
+    ]
+
+
+class ForcingConfig(C.Structure):
+    _fields_ = [
+        ("kmin", C.c_double), ("kmax", C.c_double), ("energy_target", C.c_double),
+        ("correlation_time", C.c_double), ("seed", C.c_ulong), ("type", C.c_int),
+    ]
+
+
+class ForcingState(C.Structure):
+    _fields_ = [
+        ("config", ForcingConfig), ("nkx", C.c_int), ("nky", C.c_int),
+        ("spectral_size", C.c_int), ("active_modes", C.c_int),
+        ("weights", _DP), ("colored_state", _DP), ("have_spare", C.c_uint),
+        ("spare_gaussian", C.c_double), ("rng_state", C.c_ulonglong),
+    ]
+
+
+class GpuParams(C.Structure):
+    """ns_gpu_params (include/ns_gpu.h)."""
+
+    _fields_ = [
+        ("Re", C.c_double), ("cfl_factor", C.c_double), ("adaptive_dt", C.c_int),
+        ("dt", C.c_double), ("hv_enabled", C.c_int), ("hv_coefficient", C.c_double),
+        ("hv_order", C.c_int), ("hv_cutoff_ratio", C.c_double), ("sfd_enabled", C.c_int),
+        ("sfd_strength", C.c_double), ("sfd_timescale", C.c_double),
+        ("forcing_enabled", C.c_int), ("forcing_kmin", C.c_double),
+        ("forcing_kmax", C.c_double), ("forcing_epsilon", C.c_double),
+        ("forcing_seed", C.c_uint64),
+    ]
+
+
+FP64, FP32 = 0, 1
+_LIB = None
+
+
+def load(build: bool = True) -> C.CDLL:
+    """Load libns_gb300.so (building it first when ``build`` and sources changed)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if build:
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("ns_gb300_build", os.path.join(PKG, "build.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with build.py (no CPU fallback exists)")
+    lib = C.CDLL(LIB_PATH)
+    sp = C.POINTER(SpectralData)
+    vp = C.c_void_p
+
+    def proto(name, res, *args):
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = list(args)
+
+    proto("ns_spectral_allocate", sp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double)
+    proto("ns_spectral_allocate_ex", sp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int)
+    proto("ns_spectral_free", None, sp)
+    for n in ("initialize_grids", "initialize_fft_plans", "initialize_taylor_green", "compute_derivatives",
+              "compute_velocity_from_vorticity", "compute_nonlinear_terms", "advance_rk4", "analyze_spectrum",
+              "hyperviscosity_update_weights"):
+        proto("ns_spectral_" + n, None, sp)
+    proto("ns_spectral_physical_to_spectral", None, sp, _DP, _DP)
+    proto("ns_spectral_spectral_to_physical", None, sp, _DP, _DP)
+    proto("ns_spectral_apply_dealiasing", None, sp, _DP)
+    for n in ("compute_cfl_timestep", "compute_energy", "compute_enstrophy"):
+        proto("ns_spectral_" + n, C.c_double, sp)
+    proto("ns_spectral_check_resolution", C.c_int, sp)
+    proto("ns_spectral_analyze_convergence", None, sp, C.c_int)
+    proto("ns_spectral_hyperviscosity_default", None, C.POINTER(HVConfig))
+    proto("ns_spectral_hyperviscosity_set", None, sp, C.POINTER(HVConfig))
+    proto("ns_spectral_hyperviscosity_apply", None, sp, _DP, _DP)
+    proto("ns_spectral_hyperviscosity_post_step", None, sp, _DP, C.c_double)
+    proto("ns_spectral_output_solution", None, sp, C.c_char_p)
+    proto("ns_spectral_gpu_advance_n", C.c_int, sp, C.c_int, C.c_int)
+    proto("ns_spectral_gpu_sync_host", C.c_int, sp)
+    proto("ns_spectral_gpu_set_forcing", C.c_int, sp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_ulonglong)
+    proto("ns_spectral_gpu_diagnostics", C.c_int, sp, _DP, _DP)
+    proto("ns_spectral_initialize_random_spectrum", C.c_int, sp, C.c_ulonglong, C.c_double, C.c_double)
+    proto("ns_spectral_gpu_last_error", C.c_char_p, sp)
+    proto("ns_spectral_gpu_handle", vp, sp)
+    proto("ns_forcing_config_default", None, C.POINTER(ForcingConfig))
+    proto("ns_forcing_state_init", C.c_int, C.POINTER(ForcingState), C.POINTER(ForcingConfig), _DP, C.c_int, C.c_int)
+    proto("ns_forcing_state_free", None, C.POINTER(ForcingState))
+    proto("ns_forcing_generate", None, C.POINTER(ForcingState), C.c_double, _DP, _DP)
+    # C-ABI
+    proto("ns_gpu_create", C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.POINTER(vp))
+    proto("ns_gpu_destroy", None, vp)
+    proto("ns_gpu_last_error", C.c_char_p, vp)
+    proto("ns_gpu_status_string", C.c_char_p, C.c_int)
+    proto("ns_gpu_dims", C.c_int, vp, C.POINTER(C.c_int), C.POINTER(C.c_int))
+    proto("ns_gpu_set_params", C.c_int, vp, C.POINTER(GpuParams))
+    proto("ns_gpu_synchronize", C.c_int, vp)
+    proto("ns_gpu_launch_count", C.c_uint64, vp)
+    proto("ns_gpu_upload_state", C.c_int, vp, _DP, _DP, _DP, C.c_double, C.c_double, C.c_uint64)
+    proto("ns_gpu_advance", C.c_int, vp, C.c_int)
+    proto("ns_gpu_download_state", C.c_int, vp, _DP, _DP, _DP, _DP, _DP, _DP, _DP, _DP, _DP, _DP)
+    proto("ns_gpu_diagnostics", C.c_int, vp, _DP, _DP, _DP, _DP)
+    proto("ns_gpu_init_random_spectrum", C.c_int, vp, C.c_uint64, C.c_double, C.c_double)
+    proto("ns_gpu_random_spectrum_host", C.c_int, vp, C.c_uint64, C.c_double, C.c_double, _DP)
+    proto("ns_gpu_state_device_ptr", vp, vp)
+    _LIB = lib
+    return lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(_DP)
+
+
+class Solver:
+    """One drop-in solver instance driven through the reference API.
+
+    The method names follow ``oracle/oracle.py``'s Solver so a test can run the
+    same script against both.  Array accessors return live numpy views of the
+    host arrays of the C struct.
+    """
+
+    def __init__(self, nx: int, ny: int, Lx: float = 2 * np.pi, Ly: float = 2 * np.pi, Re: float = 100.0,
+                 precision: int = FP64):
+        self.lib = load()
+        self.ptr = self.lib.ns_spectral_allocate_ex(nx, ny, Lx, Ly, Re, precision)
+        if not self.ptr:
+            raise RuntimeError("ns_spectral_allocate returned NULL (no GPU, or invalid size)")
+        self.d = self.ptr.contents
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            self.lib.ns_spectral_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _f(self, name):
+        return getattr(self.lib, "ns_spectral_" + name)
+
+    def setup(self, ic: str = "tg"):
+        self._f("initialize_grids")(self.ptr)
+        self._f("initialize_fft_plans")(self.ptr)
+        if ic == "tg":
+            self._f("initialize_taylor_green")(self.ptr)
+        return self
+
+    def real(self, name):
+        return np.ctypeslib.as_array(getattr(self.d, name), shape=(self.d.ny, self.d.nx))
+
+    def cplx(self, name):
+        return np.ctypeslib.as_array(getattr(self.d, name), shape=(self.d.nky, self.d.nkx * 2)).view(np.complex128)
+
+    def k2(self):
+        return np.ctypeslib.as_array(self.d.k2, shape=(self.d.nky, self.d.nkx))
+
+    def mask(self):
+        return np.ctypeslib.as_array(self.d.dealias_mask, shape=(self.d.nky, self.d.nkx))
+
+    def set_vorticity(self, omega: np.ndarray):
+        self.real("omega")[:] = omega
+        self._f("physical_to_spectral")(self.ptr, self.d.omega, self.d.omega_hat)
+
+    def derivatives(self):
+        self._f("compute_derivatives")(self.ptr)
+
+    def advance(self, n: int = 1, adaptive: bool = False):
+        for _ in range(n):
+            if adaptive:
+                self.d.dt = self._f("compute_cfl_timestep")(self.ptr)
+            self._f("advance_rk4")(self.ptr)
+
+    def advance_n(self, n: int, adaptive: bool = False):
+        st = self._f("gpu_advance_n")(self.ptr, n, 1 if adaptive else 0)
+        if st != 0:
+            raise RuntimeError(f"gpu_advance_n failed ({st}): {self._f('gpu_last_error')(self.ptr)}")
+
+    def sync_host(self):
+        st = self._f("gpu_sync_host")(self.ptr)
+        if st != 0:
+            raise RuntimeError(f"gpu_sync_host failed ({st})")
+
+    def set_forcing(self, kmin, kmax, epsilon, seed, enabled=True):
+        st = self._f("gpu_set_forcing")(self.ptr, 1 if enabled else 0, kmin, kmax, epsilon, seed)
+        if st != 0:
+            raise RuntimeError(f"gpu_set_forcing failed ({st})")
+
+    def diagnostics(self):
+        e = C.c_double()
+        z = C.c_double()
+        st = self._f("gpu_diagnostics")(self.ptr, C.byref(e), C.byref(z))
+        if st != 0:
+            raise RuntimeError(f"gpu_diagnostics failed ({st})")
+        return e.value, z.value
+
+    def random_spectrum(self, seed, k0, energy):
+        st = self._f("initialize_random_spectrum")(self.ptr, seed, k0, energy)
+        if st != 0:
+            raise RuntimeError(f"initialize_random_spectrum failed ({st})")
+
+    def energy(self):
+        return self._f("compute_energy")(self.ptr)
+
+    def enstrophy(self):
+        return self._f("compute_enstrophy")(self.ptr)
+
+    def cfl(self):
+        return self._f("compute_cfl_timestep")(self.ptr)
+
+    def set_hyperviscosity(self, **kw):
+        cfg = HVConfig()
+        self.lib.ns_spectral_hyperviscosity_default(C.byref(cfg))
+        for k, v in kw.items():
+            setattr(cfg, k, v)
+        self.lib.ns_spectral_hyperviscosity_set(self.ptr, C.byref(cfg))
+
+    def launches(self) -> int:
+        return int(self.lib.ns_gpu_launch_count(self.lib.ns_spectral_gpu_handle(self.ptr)))
+
+
+class Gpu:
+    """Direct use of the C-ABI (include/ns_gpu.h) with a device-resident state."""
+
+    def __init__(self, nx: int, ny: int, Lx: float = 2 * np.pi, Ly: float = 2 * np.pi, precision: int = FP32):
+        self.lib = load()
+        h = C.c_void_p()
+        st = self.lib.ns_gpu_create(nx, ny, Lx, Ly, precision, C.byref(h))
+        if st != 0:
+            raise RuntimeError(f"ns_gpu_create failed: {self.lib.ns_gpu_status_string(st).decode()}")
+        self.h = h
+        self.nx, self.ny = nx, ny
+        self.nkx, self.nky = nx // 2 + 1, ny
+
+    def check(self, st, what):
+        if st != 0:
+            raise RuntimeError(f"{what} failed ({st}): {self.lib.ns_gpu_last_error(self.h).decode()}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ns_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, **kw):
+        p = GpuParams()
+        p.Re, p.cfl_factor, p.dt = 1.0, 0.3, 0.01
+        p.hv_order, p.hv_cutoff_ratio, p.sfd_timescale = 8, 0.65, 1.0
+        for k, v in kw.items():
+            setattr(p, k, v)
+        self.check(self.lib.ns_gpu_set_params(self.h, C.byref(p)), "set_params")
+
+    def upload(self, omega_hat: np.ndarray, psi_hat=None, sfd_hat=None, t=0.0, dt=0.01, step0=0):
+        w = np.ascontiguousarray(omega_hat, dtype=np.complex128)
+        p = None if psi_hat is None else np.ascontiguousarray(psi_hat, dtype=np.complex128)
+        s = None if sfd_hat is None else np.ascontiguousarray(sfd_hat, dtype=np.complex128)
+        self.check(self.lib.ns_gpu_upload_state(self.h, _ptr(w.view(np.float64)),
+                                                None if p is None else _ptr(p.view(np.float64)),
+                                                None if s is None else _ptr(s.view(np.float64)), t, dt, step0),
+                   "upload_state")
+
+    def random_spectrum(self, seed, k0, energy):
+        self.check(self.lib.ns_gpu_init_random_spectrum(self.h, seed, k0, energy), "init_random_spectrum")
+
+    def advance(self, n):
+        self.check(self.lib.ns_gpu_advance(self.h, n), "advance")
+
+    def sync(self):
+        self.check(self.lib.ns_gpu_synchronize(self.h), "synchronize")
+
+    def download(self, fields=("omega_hat",)):
+        out = {}
+        args = []
+        for name in ("omega_hat", "psi_hat", "u_hat", "v_hat", "sfd_hat"):
+            if name in fields:
+                a = np.zeros((self.nky, self.nkx), dtype=np.complex128)
+                out[name] = a
+                args.append(_ptr(a.view(np.float64)))
+            else:
+                args.append(None)
+        for name in ("u", "v", "omega"):
+            if name in fields:
+                a = np.zeros((self.ny, self.nx), dtype=np.float64)
+                out[name] = a
+                args.append(_ptr(a))
+            else:
+                args.append(None)
+        t = C.c_double()
+        dt = C.c_double()
+        self.check(self.lib.ns_gpu_download_state(self.h, *args, C.byref(t), C.byref(dt)), "download_state")
+        out["t"], out["dt"] = t.value, dt.value
+        return out
+
+    def diagnostics(self):
+        e, z, t, dt = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+        self.check(self.lib.ns_gpu_diagnostics(self.h, C.byref(e), C.byref(z), C.byref(t), C.byref(dt)),
+                   "diagnostics")
+        return {"energy": e.value, "enstrophy": z.value, "t": t.value, "dt": dt.value}
+
+    def launches(self) -> int:
+        return int(self.lib.ns_gpu_launch_count(self.h))
+
+    def dims(self):
+        a, b = C.c_int(), C.c_int()
+        self.lib.ns_gpu_dims(self.h, C.byref(a), C.byref(b))
+        return a.value, b.value

@@ -220,6 +220,7 @@ void nso_hv_apply(nso_state *s, fftw_complex *rhs, const fftw_complex *state) {
     const int sfd = cfg->sfd_enabled && cfg->sfd_strength > 0.0;
     const int order = cfg->order > 0 ? cfg->order : 1;
     if (!visc && !sfd) return;
+#pragma omp parallel for
     for (int i = 0; i < n; ++i) {
         fftw_complex damp = 0.0;
         if (visc) damp += s->hyperviscosity_weights[i] * state[i];
@@ -246,6 +247,7 @@ void nso_hv_post_step(nso_state *s, const fftw_complex *state, double dt) {
     if (a > 1.0) a = 1.0;
     else if (a < 0.0) a = 0.0;
     const int n = s->nkx * s->nky;
+#pragma omp parallel for
     for (int i = 0; i < n; ++i) {
         const fftw_complex prev = s->sfd_hat[i];
         s->sfd_hat[i] = (1.0 - a) * prev + a * state[i];
@@ -286,6 +288,7 @@ void nso_initialize_fft_plans(nso_state *s) {
 /* src/spectral/spectral_transforms.c:35-43 */
 void nso_apply_dealiasing(nso_state *s, fftw_complex *f) {
     const int n = s->nkx * s->nky;
+#pragma omp parallel for
     for (int i = 0; i < n; ++i)
         if (!s->dealias_mask[i]) f[i] = 0.0;
 }
@@ -295,6 +298,7 @@ void nso_physical_to_spectral(nso_state *s, double *field, fftw_complex *field_h
     fftw_execute_dft_r2c(s->forward_plan, field, field_hat);
     const double norm = 1.0 / (s->nx * s->ny);
     const int n = s->nkx * s->nky;
+#pragma omp parallel for
     for (int i = 0; i < n; ++i) field_hat[i] *= norm;
     nso_apply_dealiasing(s, field_hat);
 }
@@ -330,6 +334,7 @@ void nso_initialize_taylor_green(nso_state *s) {
 /* src/spectral/spectral_core.c:8-34: psi = -omega/k^2 (0 where k^2 <= 1e-12),
  * u_hat = i ky psi, v_hat = -i kx psi */
 void nso_compute_velocity_from_vorticity(nso_state *s) {
+#pragma omp parallel for
     for (int j = 0; j < s->nky; ++j) {
         for (int i = 0; i < s->nkx; ++i) {
             const int idx = j * s->nkx + i;
@@ -337,6 +342,7 @@ void nso_compute_velocity_from_vorticity(nso_state *s) {
             else s->psi_hat[idx] = 0.0;
         }
     }
+#pragma omp parallel for
     for (int j = 0; j < s->nky; ++j) {
         for (int i = 0; i < s->nkx; ++i) {
             const int idx = j * s->nkx + i;
@@ -357,6 +363,7 @@ void nso_compute_derivatives(nso_state *s) {
 /* scratch = i * k_axis * src, then masked c2r into dst (spectral_core.c:62-99) */
 static void nso_derivative_to_physical(nso_state *s, const fftw_complex *src, int axis_y, double *dst) {
     fftw_complex *scratch = s->nonlinear_hat;
+#pragma omp parallel for
     for (int j = 0; j < s->nky; ++j) {
         for (int i = 0; i < s->nkx; ++i) {
             const int idx = j * s->nkx + i;
@@ -378,8 +385,10 @@ void nso_compute_nonlinear_terms(nso_state *s) {
     nso_derivative_to_physical(s, s->psi_hat, 1, psi_y);
     nso_derivative_to_physical(s, s->omega_hat, 0, omega_x);
     nso_derivative_to_physical(s, s->omega_hat, 1, omega_y);
+#pragma omp parallel for
     for (int k = 0; k < nr; ++k) jac[k] = psi_x[k] * omega_y[k] - psi_y[k] * omega_x[k];
     nso_physical_to_spectral(s, jac, s->nonlinear_hat);
+#pragma omp parallel for
     for (int k = 0; k < n; ++k) s->nonlinear_hat[k] = -s->nonlinear_hat[k];
 }
 
@@ -389,6 +398,7 @@ void nso_compute_nonlinear_terms(nso_state *s) {
 double nso_compute_cfl_timestep(nso_state *s) {
     const int nr = s->nx * s->ny;
     double vmax = 0.0;
+#pragma omp parallel for reduction(max : vmax)
     for (int k = 0; k < nr; ++k) {
         const double m = sqrt(s->u[k] * s->u[k] + s->v[k] * s->v[k]);
         if (m > vmax) vmax = m;
@@ -405,6 +415,7 @@ double nso_compute_cfl_timestep(nso_state *s) {
 /* k = N - k^2 * omega / Re, then hyperviscosity (spectral_time_integration.c:50-54) */
 static void nso_stage_rhs(nso_state *s, fftw_complex *kout, double inv_re) {
     const int n = s->nkx * s->nky;
+#pragma omp parallel for
     for (int k = 0; k < n; ++k) kout[k] = s->nonlinear_hat[k] - s->k2[k] * s->omega_hat[k] * inv_re;
     nso_hv_apply(s, kout, s->omega_hat);
 }
@@ -412,6 +423,7 @@ static void nso_stage_rhs(nso_state *s, fftw_complex *kout, double inv_re) {
 /* omega = omega_tmp + c * kin (spectral_time_integration.c:57-60) */
 static void nso_stage_state(nso_state *s, const fftw_complex *kin, double c) {
     const int n = s->nkx * s->nky;
+#pragma omp parallel for
     for (int k = 0; k < n; ++k) s->omega_hat[k] = s->omega_tmp_hat[k] + c * kin[k];
 }
 
@@ -447,6 +459,7 @@ static void nso_advance_rk4_impl(nso_state *s, const nso_ext_forcing *forcing) {
     nso_compute_derivatives(s);
     nso_compute_nonlinear_terms(s);
     nso_stage_rhs(s, s->rk4_hat, inv_re);
+#pragma omp parallel for
     for (int k = 0; k < n; ++k)
         s->omega_hat[k] = s->omega_tmp_hat[k] +
                           dt / 6.0 * (s->rk1_hat[k] + 2.0 * s->rk2_hat[k] + 2.0 * s->rk3_hat[k] + s->rk4_hat[k]);
