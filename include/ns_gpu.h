@@ -187,6 +187,29 @@ int ns_gpu_forcing_generate(ns_gpu *g, int n, const double *weights, int active,
 
 /* ------------------------------------------- device-resident access */
 
+/* Allocation-free forward transform, for callers that cannot allocate device
+ * memory (no counterpart in the reference; it has the effect of
+ * ns_spectral_physical_to_spectral, spectral_transforms.c:9-22, on device data).
+ * Frameworks that own every device allocation through their own pool,
+ * real-time loops that may not allocate, and processes whose device memory is
+ * already fully reserved pass their own input and output and get the transform
+ * without any allocation: its scratch lives in a fixed 8 MiB static device array
+ * that every GPU loading this library holds until exit.  That limit admits every
+ * power-of-two grid up to 1024 x 1024 (FP64; sides in [8, 4096]); a grid whose
+ * intermediate (ny x Kx complex doubles plus twiddles) exceeds it is rejected
+ * with NS_GPU_ERR_INVALID and a message on stderr.
+ *   field      device pointer, double[ny][nx], 16-byte aligned
+ *   field_hat  device pointer, double complex[ny][nx/2+1] (interleaved), 16-byte
+ *              aligned; receives r2c/(nx*ny) with every mode outside the 2/3
+ *              mask set to zero
+ *   stream     cudaStream_t to issue on (NULL: the default stream); the call
+ *              returns once the work is queued.
+ * The first call on a device looks up the scratch address there
+ * (cudaGetSymbolAddress with that device current): make it before any stream
+ * capture.  All calls share the scratch array, so calls that overlap on the GPU
+ * race; serialise them. */
+int ns_gpu_forward_noalloc(int nx, int ny, const double *field, double *field_hat, void *stream);
+
 /* Zero-initialised page-locked host memory for arrays that are copied to and
  * from the device every step (the drop-in allocates its host arrays here). */
 void *ns_gpu_host_alloc(size_t bytes);
