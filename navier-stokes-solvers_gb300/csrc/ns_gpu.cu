@@ -9,12 +9,14 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
 
 #include "ns_gpu.h"
 #include "ns_kernels.cuh"
+#include "ns_wkernels.cuh"
 
 using namespace nsg;
 
@@ -23,6 +25,9 @@ struct ns_gpu {
     int prec;
     int ER, EC;
     int device;
+    int num_sms;
+    int fast_row;       // radix-32 warp row kernel (nx = 2048)
+    int fast_col;       // radix-32 column kernel (ny = 2048)
     cudaStream_t st;
     std::string err;
     unsigned long long launches;
@@ -221,7 +226,29 @@ template <typename T> static int stage_row(ns_gpu* g, int stage) {
     a.dx[0] = 1; a.dx[1] = 0; a.dx[2] = 1; a.dx[3] = 0;  // psi_x, psi_y, omega_x, omega_y
     a.cfl = (stage == 1 && g->p.adaptive_dt) ? 1 : 0;
     a.marker = (stage == 1) ? 1 : (stage == 2 ? 2 : 0);
+    if (g->fast_row) {
+        const size_t smem = rw_smem_bytes<T>();
+        NSG_TRY(set_smem(g, k_row_w<T>, smem));
+        const int nw = rw_warps<T>();
+        int grid = g->g.ny / nw;
+        if (grid > g->num_sms) grid = g->num_sms;
+        k_row_w<T><<<grid, 32 * nw, smem, g->st>>>(g->g, a);
+        NSG_LAUNCHED(g);
+        return NS_GPU_OK;
+    }
     return row_launch<T, ROW_STAGE>(g, a);
+}
+
+template <typename T, int STAGE> static int stage_col(ns_gpu* g, const ColArgs<T>& a) {
+    ProfScope ps(g, 1);
+    if (g->fast_col) {
+        const size_t smem = cw_smem_bytes<T>();
+        NSG_TRY(set_smem(g, k_col_w<T, STAGE>, smem));
+        k_col_w<T, STAGE><<<(g->g.Kxp + NSG_CW_COLS - 1) / NSG_CW_COLS, 64 * NSG_CW_COLS, smem, g->st>>>(g->g, a);
+        NSG_LAUNCHED(g);
+        return NS_GPU_OK;
+    }
+    return col_launch<T, COL_STAGE, STAGE>(g, a);
 }
 
 template <typename T> static int advance_t(ns_gpu* g, int nsteps) {
@@ -233,13 +260,13 @@ template <typename T> static int advance_t(ns_gpu* g, int nsteps) {
     ColArgs<T> a = col_args<T>(g);
     for (int n = 0; n < nsteps; ++n) {
         NSG_TRY(stage_row<T>(g, 1));
-        { ProfScope ps(g, 1); NSG_TRY((col_launch<T, COL_STAGE, 1>(g, a))); }
+        NSG_TRY((stage_col<T, 1>(g, a)));
         NSG_TRY(stage_row<T>(g, 2));
-        { ProfScope ps(g, 1); NSG_TRY((col_launch<T, COL_STAGE, 2>(g, a))); }
+        NSG_TRY((stage_col<T, 2>(g, a)));
         NSG_TRY(stage_row<T>(g, 3));
-        { ProfScope ps(g, 1); NSG_TRY((col_launch<T, COL_STAGE, 3>(g, a))); }
+        NSG_TRY((stage_col<T, 3>(g, a)));
         NSG_TRY(stage_row<T>(g, 4));
-        { ProfScope ps(g, 1); NSG_TRY((col_launch<T, COL_STAGE, 4>(g, a))); }
+        NSG_TRY((stage_col<T, 4>(g, a)));
         if (g->outside_active) {
             const long long nn = (long long)g->g.nkx * g->g.nky;
             k_outside<<<grid_for(nn), 256, 0, g->st>>>(g->g, a.sp, g->hvw_full, g->hv_cutoff, g->hv_inv_bw,
@@ -442,6 +469,15 @@ int ns_gpu_create(int nx, int ny, double Lx, double Ly, int precision, ns_gpu** 
     g->f_sigma = 0.0;
     g->prec = precision;
     cudaGetDevice(&g->device);
+    g->num_sms = 1;
+    cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, g->device);
+    {
+        // NS_GB300_GENERIC_KERNELS=1 selects the generic Stockham stage kernels at every size
+        const char* gen = getenv("NS_GB300_GENERIC_KERNELS");
+        const int generic = gen && gen[0] == '1';
+        g->fast_row = (!generic && nx == 2048) ? 1 : 0;
+        g->fast_col = (!generic && ny == 2048) ? 1 : 0;
+    }
     if (cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking) != cudaSuccess) {
         delete g;
         return NS_GPU_ERR_CUDA;

@@ -1,0 +1,487 @@
+// Register-resident radix-32 stage kernels (the hot path at nx = 2048 / ny = 2048).
+//
+// Four-step FFT with 32 points per thread (N = N1 * N2, N1 = 32):
+//   forward   X[k1 + 32 k2] = sum_n2 W_N^{n2 k1} W_N2^{n2 k2} sum_n1 x[N2 n1 + n2] W_32^{n1 k1}
+//   pass A    thread n2 holds x[N2 n1 + n2] (n1 < 32), DFT32 over n1, times W_N^{n2 k1}
+//   exchange  shared-memory transpose (rows padded to 33 / 65 elements: conflict-free)
+//   pass B    DFT over n2 for each k1
+// The inverse runs the same steps in reverse order (decimation in frequency),
+// so it takes the forward's output layout and returns the forward's input
+// layout: no reordering pass exists anywhere.
+//
+// k_row_w  (nx = 2048, H = 1024 = 32 x 32): one warp per row, persistent over
+//          rows.  All five transforms of a row stay inside one warp, so the only
+//          synchronisation is __syncwarp.  The inverse outputs land in exactly
+//          the layout the forward transform reads, so the Jacobian is formed in
+//          registers between them.
+// k_col_w  (ny = 2048 = 32 x 64): two warps per kept kx column (N2 = 64 is
+//          split into even/odd halves, one per warp, joined by one radix-2
+//          exchange), two columns per CTA.  The RK stage algebra runs on the
+//          forward's output registers and the four inverse transforms start
+//          from registers.
+#pragma once
+#include "ns_kernels.cuh"
+
+namespace nsg {
+
+// ------------------------------------------------------------------ DFT32
+// cos(pi k/16), k = 0..8
+__device__ __forceinline__ double cpi16(int k) {
+    switch (k) {
+        case 0: return 1.0;
+        case 1: return 0.98078528040323044913;
+        case 2: return 0.92387953251128675613;
+        case 3: return 0.83146961230254523708;
+        case 4: return 0.70710678118654752440;
+        case 5: return 0.55557023301960222474;
+        case 6: return 0.38268343236508977173;
+        case 7: return 0.19509032201612826785;
+        default: return 0.0;
+    }
+}
+
+// y_k = E_k + W32^k O_k, y_{k+16} = E_k - W32^k O_k (E, O: DFT16 of even/odd inputs)
+template <bool INV, typename C> __device__ __forceinline__ void dft32(C* a) {
+    typedef decltype(a[0].x) T;
+    C e[16], o[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        e[k] = a[2 * k];
+        o[k] = a[2 * k + 1];
+    }
+    dft16<INV>(e);
+    dft16<INV>(o);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        C w;
+        if (k == 0) {
+            w = o[0];
+        } else if (k == 8) {
+            w = cmul_mi<INV>(o[8]);
+        } else {
+            // W32^k = cos(pi k/16) -+ i sin(pi k/16)
+            const T cr = (k < 8) ? (T)cpi16(k) : (T)-cpi16(16 - k);
+            const T si = (k < 8) ? (T)cpi16(8 - k) : (T)cpi16(k - 8);
+            C tw;
+            tw.x = cr;
+            tw.y = INV ? si : -si;
+            w = cmul(o[k], tw);
+        }
+        a[k] = cadd(e[k], w);
+        a[k + 16] = csub(e[k], w);
+    }
+}
+
+// ============================================================ k_row_w
+// grid = number of persistent CTAs, block = 32 * RW warps; dynamic smem:
+//   tw  [32][33]  W_1024^{t k1} at tw[k1*33 + t]
+//   per warp: S [32][33] exchange, R [1024] first result, Q [1024] second result (FP64 only)
+#define NSG_RW_WARPS_F32 8
+#define NSG_RW_WARPS_F64 4
+
+template <typename T> __host__ __device__ constexpr int rw_warps() { return sizeof(T) == 4 ? NSG_RW_WARPS_F32 : NSG_RW_WARPS_F64; }
+template <typename T> __host__ __device__ constexpr int rw_hold_in_smem() { return sizeof(T) == 8 ? 1 : 0; }
+template <typename T> __host__ __device__ constexpr size_t rw_smem_bytes() {
+    return (size_t)(32 * 33 + rw_warps<T>() * (32 * 33 + 1024 * (1 + rw_hold_in_smem<T>()))) *
+           (sizeof(T) == 4 ? sizeof(float2) : sizeof(double2));
+}
+
+// flat index k < 1024 inside a [32][33] exchange buffer
+__device__ __forceinline__ int sx(int k) { return (k >> 5) * 33 + (k & 31); }
+
+// one 1024-point transform inside a warp: a[] holds x[lane + 32 n1] on entry and
+// X[lane + 32 k2] on exit
+template <bool INV, typename C>
+__device__ __forceinline__ void warp_fft1024(C (&a)[32], C* S, const C* tw, int lane) {
+    dft32<INV>(a);
+#pragma unroll
+    for (int k1 = 1; k1 < 32; ++k1) {
+        C w = tw[k1 * 33 + lane];
+        if (INV) w.y = -w.y;
+        a[k1] = cmul(a[k1], w);
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < 32; ++k1) S[k1 * 33 + lane] = a[k1];
+    __syncwarp();
+#pragma unroll
+    for (int n2 = 0; n2 < 32; ++n2) a[n2] = S[lane * 33 + n2];
+    __syncwarp();
+    dft32<INV>(a);
+}
+
+// load half spectrum X_f[k] (k < Kx, times i kx when dx) of row y into S, then
+// pack the half-length inverse input Z[lane + 32 n1] into a[]
+template <typename T, typename C>
+__device__ __forceinline__ void row_pack(C (&a)[32], C* S, const C* __restrict__ src, int dx, const T* __restrict__ kxv,
+                                         const C* __restrict__ twh, int Kx, int lane) {
+    for (int k = lane; k < Kx; k += 32) {
+        C x = src[k];
+        if (dx) {
+            const T kx = kxv[k];
+            C d;
+            d.x = -kx * x.y;
+            d.y = kx * x.x;
+            x = d;
+        }
+        S[sx(k)] = x;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int n1 = 0; n1 < 32; ++n1) {
+        const int k = lane + 32 * n1;
+        const C zero = cmake<C>(0.0, 0.0);
+        const C xa = (k < Kx) ? S[sx(k)] : zero;
+        const int kb = 1024 - k;
+        const C xb = (k > 0 && kb < Kx) ? S[sx(kb)] : zero;
+        if (k == 0) {
+            a[n1] = cmake<C>(xa.x, xa.x);  // Re X[0] (1 + i); the Nyquist bin is masked
+        } else {
+            const C e = cconj(__ldg(&twh[k]));  // exp(+2 pi i k / nx)
+            const C A = cadd(xa, cconj(xb));
+            const C D = cmul(csub(xa, cconj(xb)), e);
+            a[n1] = cmake<C>(A.x - D.y, A.y + D.x);
+        }
+    }
+    __syncwarp();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32 * rw_warps<T>(), 1) k_row_w(Geo g, RowArgs<T> a) {
+    typedef typename CT<T>::C C;
+    constexpr int NW = rw_warps<T>();
+    constexpr int HOLD_SMEM = rw_hold_in_smem<T>();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* tw = reinterpret_cast<C*>(smem_raw);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    C* S = tw + 32 * 33 + warp * (32 * 33 + 1024 * (1 + HOLD_SMEM));
+    C* R = S + 32 * 33;
+    C* Q = R + 1024;  // FP64 only
+    const int Kx = g.Kx, Kxp = g.Kxp, nx = g.nx;
+
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (a.marker == 1) {
+            a.ds->step_cur = a.ds->step_next;
+            a.ds->step_next = a.ds->step_next + 1ULL;
+        } else if (a.marker == 2) {
+            a.ds->maxvel2 = 0ULL;
+        }
+    }
+    for (int i = threadIdx.x; i < 1024; i += blockDim.x) {
+        const int k1 = i >> 5, t = i & 31;
+        tw[k1 * 33 + t] = a.twr[t * k1];
+    }
+    __syncthreads();
+
+    T vmax2 = (T)0;
+    C v[32];
+    C hold[HOLD_SMEM ? 1 : 32];
+    for (int y = blockIdx.x * NW + warp; y < g.ny; y += gridDim.x * NW) {
+        const size_t roff = (size_t)y * Kxp;
+        // psi_x -> R
+        row_pack<T>(v, S, a.F[0] + roff, 1, a.kxv, a.twh, Kx, lane);
+        warp_fft1024<true>(v, S, tw, lane);
+#pragma unroll
+        for (int k = 0; k < 32; ++k) R[lane + 32 * k] = v[k];
+        // psi_y -> hold (registers, or Q for FP64); CFL max of psi_x^2 + psi_y^2
+        row_pack<T>(v, S, a.F[1] + roff, 0, a.kxv, a.twh, Kx, lane);
+        warp_fft1024<true>(v, S, tw, lane);
+#pragma unroll
+        for (int k = 0; k < 32; ++k) {
+            if (a.cfl) {
+                const C px = R[lane + 32 * k];
+                vmax2 = fmax(vmax2, fmax(px.x * px.x + v[k].x * v[k].x, px.y * px.y + v[k].y * v[k].y));
+            }
+            if (HOLD_SMEM) Q[lane + 32 * k] = v[k];
+            else hold[HOLD_SMEM ? 0 : k] = v[k];
+        }
+        // omega_y: R <- psi_x * omega_y (even and odd points)
+        row_pack<T>(v, S, a.F[3] + roff, 0, a.kxv, a.twh, Kx, lane);
+        warp_fft1024<true>(v, S, tw, lane);
+#pragma unroll
+        for (int k = 0; k < 32; ++k) {
+            const C px = R[lane + 32 * k];
+            R[lane + 32 * k] = cmake<C>(px.x * v[k].x, px.y * v[k].y);
+        }
+        // omega_x: J = psi_x omega_y - psi_y omega_x, packed as w[m] = J[2m] + i J[2m+1]
+        row_pack<T>(v, S, a.F[2] + roff, 1, a.kxv, a.twh, Kx, lane);
+        warp_fft1024<true>(v, S, tw, lane);
+#pragma unroll
+        for (int k = 0; k < 32; ++k) {
+            const C p = R[lane + 32 * k];
+            const C py = HOLD_SMEM ? Q[lane + 32 * k] : hold[HOLD_SMEM ? 0 : k];
+            v[k] = cmake<C>(p.x - py.x * v[k].x, p.y - py.y * v[k].y);
+        }
+        // forward half-length transform of J, then unpack the kept kx < Kx
+        warp_fft1024<false>(v, S, tw, lane);
+#pragma unroll
+        for (int k = 0; k < 32; ++k) S[k * 33 + lane] = v[k];
+        __syncwarp();
+        C* dst = a.G + roff;
+        const T half = (T)0.5;
+        for (int k = lane; k < Kx; k += 32) {
+            const C wa = S[sx(k)];
+            const C wb = S[sx((1024 - k) & 1023)];
+            C ev, od;
+            ev.x = half * (wa.x + wb.x);
+            ev.y = half * (wa.y - wb.y);
+            od.x = half * (wa.y + wb.y);
+            od.y = -half * (wa.x - wb.x);
+            dst[k] = cadd(ev, cmul(od, __ldg(&a.twh[k])));
+        }
+        __syncwarp();
+    }
+    (void)nx;
+    if (a.cfl) {
+        const double vm = warp_max((double)vmax2);
+        if (lane == 0) atomicMax(&a.ds->maxvel2, (unsigned long long)__double_as_longlong(vm));
+    }
+}
+
+// ============================================================ k_col_w
+// ny = 2048: 64 threads per column (two warps), 2 columns per CTA.
+// dynamic smem: tw [32][65] with W_2048^{t k1} at tw[k1*65 + t] (t < 64), then
+// per column a buffer of NSG_CW_LP elements (tile column / exchange area)
+#define NSG_CW_COLS 2
+#define NSG_CW_LP 2120
+
+template <typename T> __host__ __device__ constexpr size_t cw_smem_bytes() {
+    return (size_t)(32 * 65 + NSG_CW_COLS * NSG_CW_LP) * (sizeof(T) == 4 ? sizeof(float2) : sizeof(double2));
+}
+
+// forward 2048-point transform: a[] = x[64 n1 + t] on entry (t = 32 h + lane),
+// X[lane + 32 k2 + 1024 h] on exit; col is this column's shared buffer
+template <typename C>
+__device__ __forceinline__ void col_fwd2048(C (&a)[32], C* col, const C* tw, int t, int lane, int h) {
+    dft32<false>(a);
+#pragma unroll
+    for (int k1 = 1; k1 < 32; ++k1) a[k1] = cmul(a[k1], tw[k1 * 65 + t]);
+#pragma unroll
+    for (int k1 = 0; k1 < 32; ++k1) col[k1 * 65 + t] = a[k1];
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < 32; ++m) a[m] = col[lane * 65 + 2 * m + h];
+    __syncthreads();
+    dft32<false>(a);
+    if (h) {
+#pragma unroll
+        for (int k2 = 1; k2 < 32; ++k2) a[k2] = cmul(a[k2], tw[k2 * 65 + 32]);  // W_64^{k2} = W_2048^{32 k2}
+    }
+#pragma unroll
+    for (int k2 = 0; k2 < 32; ++k2) col[h * 1056 + k2 * 33 + lane] = a[k2];
+    __syncthreads();
+#pragma unroll
+    for (int k2 = 0; k2 < 32; ++k2) {
+        const C b = col[(1 - h) * 1056 + k2 * 33 + lane];
+        a[k2] = h ? csub(b, a[k2]) : cadd(a[k2], b);  // E + W O  |  E - W O
+    }
+    __syncthreads();
+}
+
+// inverse 2048-point transform: a[] = X[lane + 32 k2 + 1024 h] on entry,
+// x[64 n1 + t] on exit (unnormalised)
+template <typename C>
+__device__ __forceinline__ void col_inv2048(C (&a)[32], C* col, const C* tw, int t, int lane, int h) {
+#pragma unroll
+    for (int k2 = 0; k2 < 32; ++k2) col[h * 1056 + k2 * 33 + lane] = a[k2];
+    __syncthreads();
+#pragma unroll
+    for (int k2 = 0; k2 < 32; ++k2) {
+        const C b = col[(1 - h) * 1056 + k2 * 33 + lane];
+        if (h == 0) {
+            a[k2] = cadd(a[k2], b);  // E = X_lo + X_hi
+        } else {
+            C w = tw[k2 * 65 + 32];
+            w.y = -w.y;  // W_64^{-k2}
+            a[k2] = cmul(csub(b, a[k2]), w);  // O = (X_lo - X_hi) W_64^{-k2}
+        }
+    }
+    __syncthreads();
+    dft32<true>(a);
+#pragma unroll
+    for (int m = 0; m < 32; ++m) col[lane * 65 + 2 * m + h] = a[m];
+    __syncthreads();
+#pragma unroll
+    for (int k1 = 0; k1 < 32; ++k1) a[k1] = col[k1 * 65 + t];
+    __syncthreads();
+#pragma unroll
+    for (int k1 = 1; k1 < 32; ++k1) {
+        C w = tw[k1 * 65 + t];
+        w.y = -w.y;
+        a[k1] = cmul(a[k1], w);
+    }
+    dft32<true>(a);
+}
+
+template <typename T, int STAGE>
+__global__ void __launch_bounds__(64 * NSG_CW_COLS) k_col_w(Geo g, ColArgs<T> a) {
+    typedef typename CT<T>::C C;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* tw = reinterpret_cast<C*>(smem_raw);
+    C* tile = tw + 32 * 65;
+    const int p = threadIdx.x >> 6, t = threadIdx.x & 63, lane = threadIdx.x & 31, h = t >> 5;
+    const int c0 = blockIdx.x * NSG_CW_COLS;
+    const int i = c0 + p;
+    const int Kx = g.Kx, Kxp = g.Kxp, Ky = g.Ky;
+    C* col = tile + p * NSG_CW_LP;
+    __shared__ double s_dt;
+
+    for (int idx = threadIdx.x; idx < 32 * 64; idx += blockDim.x) {
+        const int k1 = idx >> 6, tt = idx & 63;
+        tw[k1 * 65 + tt] = a.twc[tt * k1];
+    }
+    if (threadIdx.x == 0) {
+        double dt;
+        if (STAGE == 1) {
+            if (a.sp.adaptive) {
+                const double vmax = sqrt(__longlong_as_double((long long)a.ds->maxvel2));
+                const double dt_cfl = a.sp.cfl * a.sp.dxmin / (vmax + 1e-12);
+                const double dt_visc = 0.5 * a.sp.Re * a.sp.dxmin * a.sp.dxmin;
+                dt = fmin(dt_cfl, dt_visc);
+                dt = fmax(dt, 1e-8);
+                dt = fmin(dt, 0.1);
+            } else {
+                dt = a.ds->dt_fixed;
+            }
+            if (blockIdx.x == 0) a.ds->dt = dt;
+        } else {
+            dt = a.ds->dt;
+        }
+        s_dt = dt;
+    }
+    // G tile -> shared (column-contiguous), coalesced along kx
+    for (int idx = threadIdx.x; idx < 2048 * NSG_CW_COLS; idx += blockDim.x) {
+        const int y = idx / NSG_CW_COLS, c = idx - y * NSG_CW_COLS;
+        C v = cmake<C>(0.0, 0.0);
+        if (c0 + c < Kx) v = a.G[(size_t)y * Kxp + c0 + c];
+        tile[c * NSG_CW_LP + y] = v;
+    }
+    __syncthreads();
+    C v[32];
+#pragma unroll
+    for (int n1 = 0; n1 < 32; ++n1) v[n1] = col[64 * n1 + t];
+    __syncthreads();
+    col_fwd2048(v, col, tw, t, lane, h);
+
+    // RK stage algebra on the kept modes held by this thread: j = lane + 32 k2 + 1024 h
+    const double dt = s_dt;
+    const T inv_re = (T)a.sp.inv_re;
+    const T sc = (T)a.sp.scale;
+    const T ch = (T)(0.5 * dt), cf = (T)dt, c6 = (T)(dt / 6.0);
+    double f_amp = 0.0, sfd_a = 0.0;
+    if (STAGE == 4) {
+        if (a.sp.forcing) f_amp = a.sp.f_sigma * sqrt(dt);
+        if (a.sp.sfd) {
+            sfd_a = dt / a.sp.sfd_tau;
+            sfd_a = sfd_a > 1.0 ? 1.0 : (sfd_a < 0.0 ? 0.0 : sfd_a);
+        }
+    }
+    const bool colok = (i < Kx);
+    const T kx = colok ? a.kxv[i] : (T)0;
+#pragma unroll
+    for (int k2 = 0; k2 < 32; ++k2) {
+        const int j = lane + 32 * k2 + 1024 * h;
+        const int jj = kept_jj(g, j);
+        if (!colok || jj < 0) continue;
+        const C gh = v[k2];
+        C nl;
+        nl.x = -(gh.x * sc);
+        nl.y = -(gh.y * sc);
+        const size_t s = (size_t)i * Ky + jj;
+        const C w0 = a.W0[s];
+        const C ws = (STAGE == 1) ? w0 : a.WS[s];
+        const T ky = a.kyv[jj];
+        const T k2v = kx * kx + ky * ky;
+        C k;
+        k.x = nl.x - k2v * ws.x * inv_re;
+        k.y = nl.y - k2v * ws.y * inv_re;
+        if (a.sp.hv || a.sp.sfd) {
+            C damp = cmake<C>(0.0, 0.0);
+            if (a.sp.hv) { const T w = a.hvw[s]; damp.x += w * ws.x; damp.y += w * ws.y; }
+            if (a.sp.sfd) {
+                const T sw = a.sfdw[s];
+                if (sw > (T)0) {
+                    const C fb = a.SFD[s];
+                    damp.x += sw * (ws.x - fb.x);
+                    damp.y += sw * (ws.y - fb.y);
+                }
+            }
+            k.x -= damp.x;
+            k.y -= damp.y;
+        }
+        C wn;
+        if (STAGE == 1) {
+            a.ACC[s] = k;
+            wn.x = w0.x + ch * k.x; wn.y = w0.y + ch * k.y;
+            a.WS[s] = wn;
+        } else if (STAGE == 2 || STAGE == 3) {
+            C acc = a.ACC[s];
+            acc.x = acc.x + (T)2 * k.x;
+            acc.y = acc.y + (T)2 * k.y;
+            a.ACC[s] = acc;
+            const T cc = (STAGE == 2) ? ch : cf;
+            wn.x = w0.x + cc * k.x; wn.y = w0.y + cc * k.y;
+            a.WS[s] = wn;
+        } else {
+            const C acc = a.ACC[s];
+            wn.x = w0.x + c6 * (acc.x + k.x);
+            wn.y = w0.y + c6 * (acc.y + k.y);
+            if (a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9) {
+                const double kxd = 2.0 * 3.141592653589793 * i / g.Lx;
+                const double kyd = (j <= g.ny / 2) ? 2.0 * 3.141592653589793 * j / g.Ly
+                                                   : 2.0 * 3.141592653589793 * (j - g.ny) / g.Ly;
+                const double k2d = kxd * kxd + kyd * kyd;
+                const double km = sqrt(k2d);
+                if (k2d > 1e-12 && km >= a.sp.f_kmin && km <= a.sp.f_kmax) {
+                    int jsrc = j, flip = 0;
+                    if (i == 0 && j > g.ny / 2) { jsrc = g.ny - j; flip = 1; }
+                    unsigned long long ctr[4] = {(unsigned long long)jsrc * g.nkx + i, a.ds->step_cur, NSG_TAG_FORCE, 0ULL};
+                    philox4x64(ctr, a.sp.f_seed, 0ULL);
+                    const double u1 = fmax(u53(ctr[0]), 2.2250738585072014e-308);
+                    const double u2 = u53(ctr[1]);
+                    const double rad = sqrt(-2.0 * log(u1)) * 0.70710678118654752440;
+                    double sn, cs;
+                    sincos(2.0 * 3.141592653589793 * u2, &sn, &cs);
+                    double xr = rad * cs, xi = rad * sn;
+                    if (flip) xi = -xi;
+                    wn.x = (T)((double)wn.x + f_amp * xr);
+                    wn.y = (T)((double)wn.y + f_amp * xi);
+                }
+            }
+            if (a.sp.sfd) {
+                C fb = a.SFD[s];
+                const T al = (T)sfd_a, om = (T)(1.0 - sfd_a);
+                fb.x = om * fb.x + al * wn.x;
+                fb.y = om * fb.y + al * wn.y;
+                a.SFD[s] = fb;
+            }
+            a.W0[s] = wn;
+        }
+    }
+    if (STAGE == 4 && blockIdx.x == 0 && threadIdx.x == 0) a.ds->t = a.ds->t + dt;
+
+    // inverse y-transforms of the next stage's Psi, Psi_y, Omega, Omega_y
+    const C* src = (STAGE == 4) ? a.W0 : a.WS;
+#pragma unroll 1
+    for (int f = 0; f < 4; ++f) {
+#pragma unroll
+        for (int k2 = 0; k2 < 32; ++k2) {
+            const int j = lane + 32 * k2 + 1024 * h;
+            const int jj = kept_jj(g, j);
+            C x = cmake<C>(0.0, 0.0);
+            if (colok && jj >= 0) x = field_value<T, C>(f, src[(size_t)i * Ky + jj], kx, a.kyv[jj]);
+            v[k2] = x;
+        }
+        col_inv2048(v, col, tw, t, lane, h);
+#pragma unroll
+        for (int n1 = 0; n1 < 32; ++n1) col[64 * n1 + t] = v[n1];
+        __syncthreads();
+        C* dstF = a.F[f];
+        for (int idx = threadIdx.x; idx < 2048 * NSG_CW_COLS; idx += blockDim.x) {
+            const int y = idx / NSG_CW_COLS, c = idx - y * NSG_CW_COLS;
+            if (c0 + c < Kxp) dstF[(size_t)y * Kxp + c0 + c] = tile[c * NSG_CW_LP + y];
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace nsg
