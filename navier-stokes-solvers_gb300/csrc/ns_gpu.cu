@@ -242,9 +242,9 @@ template <typename T> static int stage_row(ns_gpu* g, int stage) {
 template <typename T, int STAGE> static int stage_col(ns_gpu* g, const ColArgs<T>& a) {
     ProfScope ps(g, 1);
     if (g->fast_col) {
-        const size_t smem = cw_smem_bytes<T>();
+        const size_t smem = cw_smem_bytes2<T>(g->g.Ky);
         NSG_TRY(set_smem(g, k_col_w<T, STAGE>, smem));
-        k_col_w<T, STAGE><<<(g->g.Kxp + NSG_CW_COLS - 1) / NSG_CW_COLS, 64 * NSG_CW_COLS, smem, g->st>>>(g->g, a);
+        k_col_w<T, STAGE><<<g->g.Kx, 64, smem, g->st>>>(g->g, a);
         NSG_LAUNCHED(g);
         return NS_GPU_OK;
     }
@@ -495,6 +495,10 @@ int ns_gpu_create(int nx, int ny, double Lx, double Ly, int precision, ns_gpu** 
     G.logH = ilog2(G.H);
     G.Lx = Lx;
     G.Ly = Ly;
+    // F row-contiguous (the row pass reads whole rows), G column-contiguous (the
+    // column pass reads whole columns): scattered accesses fall on the store side
+    G.fTF = 0;
+    G.fTG = (g->fast_row || g->fast_col) ? 1 : 0;
     g->ER = G.H >= 16 ? 16 : 4;
     g->EC = ny >= 16 ? 16 : 4;
     const size_t cs = (precision == NS_GPU_FP64) ? sizeof(double2) : sizeof(float2);

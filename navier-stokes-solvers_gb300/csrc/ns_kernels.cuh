@@ -33,7 +33,17 @@ struct Geo {
     double Lx, Ly;
     int CW;         // columns per column-kernel CTA
     int RPC;        // rows per row-kernel CTA
+    int fTF;        // F stored kx-column-contiguous ([Kxp][ny]) instead of row-contiguous [ny][Kxp]
+    int fTG;        // G stored kx-column-contiguous
 };
+
+// element (row y, kept column c) of an F buffer / of the G buffer
+__device__ __forceinline__ size_t fidx(const Geo& g, int y, int c) {
+    return g.fTF ? (size_t)c * g.ny + y : (size_t)y * g.Kxp + c;
+}
+__device__ __forceinline__ size_t gidx(const Geo& g, int y, int c) {
+    return g.fTG ? (size_t)c * g.ny + y : (size_t)y * g.Kxp + c;
+}
 
 __device__ __forceinline__ int kept_j(const Geo& g, int jj) { return jj <= g.Kyh ? jj : g.ny - g.Ky + jj; }
 __device__ __forceinline__ int kept_jj(const Geo& g, int j) {
@@ -191,11 +201,11 @@ __global__ void __launch_bounds__(256) k_row(Geo g, RowArgs<T> a) {
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
             C* b = sm + (f * g.RPC + r) * LP;
-            const C* src = a.F[f] + (size_t)y * Kxp;
+            const C* src = a.F[f];
             for (int k = t; k < H; k += TT) {
                 C x = cmake<C>(0.0, 0.0);
                 if (k < Kx) {
-                    x = src[k];
+                    x = src[fidx(g, y, k)];
                     if (a.dx[f]) {
                         const T kx = a.kxv[k];
                         C d;
@@ -298,7 +308,7 @@ __global__ void __launch_bounds__(256) k_row(Geo g, RowArgs<T> a) {
     // E = (W[k] + conj W[H-k])/2, O = (W[k] - conj W[H-k])/(2i), for the kept k < Kx
     {
         const C* b0 = sm + r * LP;
-        C* dst = a.G + (size_t)y * Kxp;
+        C* dst = a.G;
         const T half = (T)0.5;
         for (int k = t; k < Kx; k += TT) {
             const C wa = b0[spad(k)];
@@ -308,7 +318,7 @@ __global__ void __launch_bounds__(256) k_row(Geo g, RowArgs<T> a) {
             ev.y = half * (wa.y - wb.y);
             od.x = half * (wa.y + wb.y);
             od.y = -half * (wa.x - wb.x);
-            dst[k] = cadd(ev, cmul(od, __ldg(&a.twh[k])));
+            dst[gidx(g, y, k)] = cadd(ev, cmul(od, __ldg(&a.twh[k])));
         }
     }
 }
@@ -338,14 +348,18 @@ template <typename T> struct ColArgs {
     int nfields;                // prologue: number of fields (4 for a stage, 3 = Psi,Psi_y,Omega)
 };
 
+// x / k2 for the Poisson solve: IEEE division in FP64 (as the reference), the
+// fast reciprocal-based divide in the FP32 bulk path
+__device__ __forceinline__ double kdiv(double x, double k2) { return x / k2; }
+__device__ __forceinline__ float kdiv(float x, float k2) { return __fdividef(x, k2); }
+
 template <typename T, typename C>
 __device__ __forceinline__ C field_value(int f, C w, T kx, T ky) {
-    // f: 0 Psi = -w/k^2, 1 Psi_y = i ky Psi, 2 Omega = w, 3 Omega_y = i ky w
-    // (spectral_core.c:17-31; psi uses a true division as the reference does)
+    // f: 0 Psi = -w/k^2, 1 Psi_y = i ky Psi, 2 Omega = w, 3 Omega_y = i ky w (spectral_core.c:17-31)
     C v = w;
     if (f < 2) {
         const T k2 = kx * kx + ky * ky;
-        if (k2 > (T)1e-12) { v.x = -w.x / k2; v.y = -w.y / k2; }
+        if (k2 > (T)1e-12) { v.x = -kdiv(w.x, k2); v.y = -kdiv(w.y, k2); }
         else { v.x = (T)0; v.y = (T)0; }
     }
     if (f == 1 || f == 3) {
@@ -396,9 +410,10 @@ __global__ void __launch_bounds__(512) k_col(Geo g, ColArgs<T> a) {
 
     if (MODE == COL_STAGE || MODE == COL_FWD_EXPORT || MODE == COL_NL_EXPORT) {
         for (int idx = threadIdx.x; idx < ny * CW; idx += nthr) {
-            const int y = idx / CW, c = idx - y * CW;
+            int y, c;
+            if (g.fTG) { c = idx / ny; y = idx - c * ny; } else { y = idx / CW; c = idx - y * CW; }
             C v = cmake<C>(0.0, 0.0);
-            if (c0 + c < Kx) v = a.G[(size_t)y * Kxp + c0 + c];
+            if (c0 + c < Kx) v = a.G[gidx(g, y, c0 + c)];
             sm[c * LP + spad(y)] = v;
         }
         __syncthreads();
@@ -542,8 +557,9 @@ __global__ void __launch_bounds__(512) k_col(Geo g, ColArgs<T> a) {
         fft_smem<E, true>(mybuf, ny, g.logny, t, TC, a.twc);
         C* dstF = a.F[f];
         for (int idx = threadIdx.x; idx < ny * CW; idx += nthr) {
-            const int y = idx / CW, c = idx - y * CW;
-            dstF[(size_t)y * Kxp + c0 + c] = sm[c * LP + spad(y)];
+            int y, c;
+            if (g.fTF) { c = idx / ny; y = idx - c * ny; } else { y = idx / CW; c = idx - y * CW; }
+            dstF[fidx(g, y, c0 + c)] = sm[c * LP + spad(y)];
         }
         __syncthreads();
     }

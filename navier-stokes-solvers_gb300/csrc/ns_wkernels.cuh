@@ -73,17 +73,19 @@ template <bool INV, typename C> __device__ __forceinline__ void dft32(C* a) {
 }
 
 // ============================================================ k_row_w
-// grid = number of persistent CTAs, block = 32 * RW warps; dynamic smem:
-//   tw  [32][33]  W_1024^{t k1} at tw[k1*33 + t]
-//   per warp: S [32][33] exchange, R [1024] first result, Q [1024] second result (FP64 only)
+// One warp per row (F row-contiguous), persistent over rows; the next field's
+// half spectrum is prefetched into registers while the current one transforms.
+// G is written column-contiguous ([Kx][ny]) for the column pass.
+// dynamic smem: tw [32][33] (W_1024^{t k1}); per warp S [32][33] exchange,
+//               R [1024] (psi_x, then psi_x * omega_y), Q [1024] (psi_y)
 #define NSG_RW_WARPS_F32 8
-#define NSG_RW_WARPS_F64 4
+#define NSG_RW_WARPS_F64 3
+#define NSG_RW_KXMAX 704   // kept kx columns at nx = 2048 (684) rounded up to 32
 
 template <typename T> __host__ __device__ constexpr int rw_warps() { return sizeof(T) == 4 ? NSG_RW_WARPS_F32 : NSG_RW_WARPS_F64; }
-template <typename T> __host__ __device__ constexpr int rw_hold_in_smem() { return sizeof(T) == 8 ? 1 : 0; }
 template <typename T> __host__ __device__ constexpr size_t rw_smem_bytes() {
-    return (size_t)(32 * 33 + rw_warps<T>() * (32 * 33 + 1024 * (1 + rw_hold_in_smem<T>()))) *
-           (sizeof(T) == 4 ? sizeof(float2) : sizeof(double2));
+    return (size_t)(32 * 33 + 1024 + rw_warps<T>() * (32 * 33 + 2048)) * (sizeof(T) == 4 ? sizeof(float2) : sizeof(double2)) +
+           (size_t)NSG_RW_KXMAX * sizeof(T);
 }
 
 // flat index k < 1024 inside a [32][33] exchange buffer
@@ -109,21 +111,33 @@ __device__ __forceinline__ void warp_fft1024(C (&a)[32], C* S, const C* tw, int 
     dft32<INV>(a);
 }
 
-// load half spectrum X_f[k] (k < Kx, times i kx when dx) of row y into S, then
-// pack the half-length inverse input Z[lane + 32 n1] into a[]
+// prefetch X_f[k], k = lane + 32 i < Kx, of one row into registers
+template <typename C>
+__device__ __forceinline__ void row_fetch(C (&pf)[NSG_RW_KXMAX / 32], const C* __restrict__ src, int Kx, int lane) {
+#pragma unroll
+    for (int i = 0; i < NSG_RW_KXMAX / 32; ++i) {
+        const int k = lane + 32 * i;
+        pf[i] = (k < Kx) ? __ldg(&src[k]) : cmake<C>(0.0, 0.0);
+    }
+}
+
+// stage the fetched half spectrum (times i kx when dx) in S and pack the
+// half-length inverse input Z[lane + 32 n1] = (X[k] + conj X[H-k]) + i e^{+2 pi i k/nx} (X[k] - conj X[H-k])
 template <typename T, typename C>
-__device__ __forceinline__ void row_pack(C (&a)[32], C* S, const C* __restrict__ src, int dx, const T* __restrict__ kxv,
-                                         const C* __restrict__ twh, int Kx, int lane) {
-    for (int k = lane; k < Kx; k += 32) {
-        C x = src[k];
-        if (dx) {
+__device__ __forceinline__ void row_pack(C (&a)[32], const C (&pf)[NSG_RW_KXMAX / 32], C* S, int dx,
+                                         const T* kxv, const C* twh, int Kx, int lane) {
+#pragma unroll
+    for (int i = 0; i < NSG_RW_KXMAX / 32; ++i) {
+        const int k = lane + 32 * i;
+        C x = pf[i];
+        if (dx && k < Kx) {
             const T kx = kxv[k];
             C d;
             d.x = -kx * x.y;
             d.y = kx * x.x;
             x = d;
         }
-        S[sx(k)] = x;
+        if (k < Kx) S[sx(k)] = x;
     }
     __syncwarp();
 #pragma unroll
@@ -136,7 +150,7 @@ __device__ __forceinline__ void row_pack(C (&a)[32], C* S, const C* __restrict__
         if (k == 0) {
             a[n1] = cmake<C>(xa.x, xa.x);  // Re X[0] (1 + i); the Nyquist bin is masked
         } else {
-            const C e = cconj(__ldg(&twh[k]));  // exp(+2 pi i k / nx)
+            const C e = cconj(twh[k]);
             const C A = cadd(xa, cconj(xb));
             const C D = cmul(csub(xa, cconj(xb)), e);
             a[n1] = cmake<C>(A.x - D.y, A.y + D.x);
@@ -149,14 +163,16 @@ template <typename T>
 __global__ void __launch_bounds__(32 * rw_warps<T>(), 1) k_row_w(Geo g, RowArgs<T> a) {
     typedef typename CT<T>::C C;
     constexpr int NW = rw_warps<T>();
-    constexpr int HOLD_SMEM = rw_hold_in_smem<T>();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* tw = reinterpret_cast<C*>(smem_raw);
+    C* twh_s = tw + 32 * 33;                          // exp(-2 pi i k/nx), k < 1024
+    C* S = twh_s + 1024 + (threadIdx.x >> 5) * (32 * 33 + 2048);
+    T* kx_s = reinterpret_cast<T*>(twh_s + 1024 + NW * (32 * 33 + 2048));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    C* S = tw + 32 * 33 + warp * (32 * 33 + 1024 * (1 + HOLD_SMEM));
     C* R = S + 32 * 33;
-    C* Q = R + 1024;  // FP64 only
-    const int Kx = g.Kx, Kxp = g.Kxp, nx = g.nx;
+    C* Q = R + 1024;
+    const int Kx = g.Kx, Kxp = g.Kxp, ny = g.ny;
+    (void)warp;
 
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (a.marker == 1) {
@@ -169,54 +185,62 @@ __global__ void __launch_bounds__(32 * rw_warps<T>(), 1) k_row_w(Geo g, RowArgs<
     for (int i = threadIdx.x; i < 1024; i += blockDim.x) {
         const int k1 = i >> 5, t = i & 31;
         tw[k1 * 33 + t] = a.twr[t * k1];
+        twh_s[i] = a.twh[i];
     }
+    for (int i = threadIdx.x; i < NSG_RW_KXMAX; i += blockDim.x) kx_s[i] = (i < Kx) ? a.kxv[i] : (T)0;
     __syncthreads();
 
+    // field order q = 0..3: psi_x (F[0], d/dx), psi_y (F[1]), omega_y (F[3]), omega_x (F[2], d/dx)
     T vmax2 = (T)0;
     C v[32];
-    C hold[HOLD_SMEM ? 1 : 32];
-    for (int y = blockIdx.x * NW + warp; y < g.ny; y += gridDim.x * NW) {
+    C pf[NSG_RW_KXMAX / 32];
+    const int ystep = gridDim.x * NW;
+    int y = blockIdx.x * NW + warp;
+    if (y < ny) row_fetch(pf, a.F[0] + (size_t)y * Kxp, Kx, lane);
+    for (; y < ny; y += ystep) {
         const size_t roff = (size_t)y * Kxp;
-        // psi_x -> R
-        row_pack<T>(v, S, a.F[0] + roff, 1, a.kxv, a.twh, Kx, lane);
-        warp_fft1024<true>(v, S, tw, lane);
+#pragma unroll 1
+        for (int q = 0; q < 4; ++q) {
+            const int f = (q < 2) ? q : 5 - q;
+            const int dx = (f == 0 || f == 2);
+            row_pack<T>(v, pf, S, dx, kx_s, twh_s, Kx, lane);
+            // prefetch the next field (or the next row's psi_x) while this one transforms
+            if (q < 3) row_fetch(pf, a.F[(q + 1 < 2) ? q + 1 : 4 - q] + roff, Kx, lane);
+            else if (y + ystep < ny) row_fetch(pf, a.F[0] + (size_t)(y + ystep) * Kxp, Kx, lane);
+            warp_fft1024<true>(v, S, tw, lane);
+            if (q == 0) {
 #pragma unroll
-        for (int k = 0; k < 32; ++k) R[lane + 32 * k] = v[k];
-        // psi_y -> hold (registers, or Q for FP64); CFL max of psi_x^2 + psi_y^2
-        row_pack<T>(v, S, a.F[1] + roff, 0, a.kxv, a.twh, Kx, lane);
-        warp_fft1024<true>(v, S, tw, lane);
+                for (int k = 0; k < 32; ++k) R[lane + 32 * k] = v[k];
+            } else if (q == 1) {
 #pragma unroll
-        for (int k = 0; k < 32; ++k) {
-            if (a.cfl) {
-                const C px = R[lane + 32 * k];
-                vmax2 = fmax(vmax2, fmax(px.x * px.x + v[k].x * v[k].x, px.y * px.y + v[k].y * v[k].y));
+                for (int k = 0; k < 32; ++k) {
+                    if (a.cfl) {
+                        const C px = R[lane + 32 * k];
+                        vmax2 = fmax(vmax2, fmax(px.x * px.x + v[k].x * v[k].x, px.y * px.y + v[k].y * v[k].y));
+                    }
+                    Q[lane + 32 * k] = v[k];
+                }
+            } else if (q == 2) {
+#pragma unroll
+                for (int k = 0; k < 32; ++k) {
+                    const C px = R[lane + 32 * k];
+                    R[lane + 32 * k] = cmake<C>(px.x * v[k].x, px.y * v[k].y);
+                }
+            } else {
+                // J = psi_x omega_y - psi_y omega_x, packed as w[m] = J[2m] + i J[2m+1]
+#pragma unroll
+                for (int k = 0; k < 32; ++k) {
+                    const C p = R[lane + 32 * k];
+                    const C py = Q[lane + 32 * k];
+                    v[k] = cmake<C>(p.x - py.x * v[k].x, p.y - py.y * v[k].y);
+                }
             }
-            if (HOLD_SMEM) Q[lane + 32 * k] = v[k];
-            else hold[HOLD_SMEM ? 0 : k] = v[k];
-        }
-        // omega_y: R <- psi_x * omega_y (even and odd points)
-        row_pack<T>(v, S, a.F[3] + roff, 0, a.kxv, a.twh, Kx, lane);
-        warp_fft1024<true>(v, S, tw, lane);
-#pragma unroll
-        for (int k = 0; k < 32; ++k) {
-            const C px = R[lane + 32 * k];
-            R[lane + 32 * k] = cmake<C>(px.x * v[k].x, px.y * v[k].y);
-        }
-        // omega_x: J = psi_x omega_y - psi_y omega_x, packed as w[m] = J[2m] + i J[2m+1]
-        row_pack<T>(v, S, a.F[2] + roff, 1, a.kxv, a.twh, Kx, lane);
-        warp_fft1024<true>(v, S, tw, lane);
-#pragma unroll
-        for (int k = 0; k < 32; ++k) {
-            const C p = R[lane + 32 * k];
-            const C py = HOLD_SMEM ? Q[lane + 32 * k] : hold[HOLD_SMEM ? 0 : k];
-            v[k] = cmake<C>(p.x - py.x * v[k].x, p.y - py.y * v[k].y);
         }
         // forward half-length transform of J, then unpack the kept kx < Kx
         warp_fft1024<false>(v, S, tw, lane);
 #pragma unroll
         for (int k = 0; k < 32; ++k) S[k * 33 + lane] = v[k];
         __syncwarp();
-        C* dst = a.G + roff;
         const T half = (T)0.5;
         for (int k = lane; k < Kx; k += 32) {
             const C wa = S[sx(k)];
@@ -226,11 +250,10 @@ __global__ void __launch_bounds__(32 * rw_warps<T>(), 1) k_row_w(Geo g, RowArgs<
             ev.y = half * (wa.y - wb.y);
             od.x = half * (wa.y + wb.y);
             od.y = -half * (wa.x - wb.x);
-            dst[k] = cadd(ev, cmul(od, __ldg(&a.twh[k])));
+            a.G[(size_t)k * ny + y] = cadd(ev, cmul(od, twh_s[k]));
         }
         __syncwarp();
     }
-    (void)nx;
     if (a.cfl) {
         const double vm = warp_max((double)vmax2);
         if (lane == 0) atomicMax(&a.ds->maxvel2, (unsigned long long)__double_as_longlong(vm));
@@ -241,12 +264,7 @@ __global__ void __launch_bounds__(32 * rw_warps<T>(), 1) k_row_w(Geo g, RowArgs<
 // ny = 2048: 64 threads per column (two warps), 2 columns per CTA.
 // dynamic smem: tw [32][65] with W_2048^{t k1} at tw[k1*65 + t] (t < 64), then
 // per column a buffer of NSG_CW_LP elements (tile column / exchange area)
-#define NSG_CW_COLS 2
-#define NSG_CW_LP 2120
 
-template <typename T> __host__ __device__ constexpr size_t cw_smem_bytes() {
-    return (size_t)(32 * 65 + NSG_CW_COLS * NSG_CW_LP) * (sizeof(T) == 4 ? sizeof(float2) : sizeof(double2));
-}
 
 // forward 2048-point transform: a[] = x[64 n1 + t] on entry (t = 32 h + lane),
 // X[lane + 32 k2 + 1024 h] on exit; col is this column's shared buffer
@@ -312,24 +330,52 @@ __device__ __forceinline__ void col_inv2048(C (&a)[32], C* col, const C* tw, int
     dft32<true>(a);
 }
 
+// white-in-time forcing increment of one kept mode (Philox4x64-10, Box-Muller)
+__device__ __noinline__ double2 forcing_increment(const Geo& g, int i, int j, unsigned long long step,
+                                                  unsigned long long seed, double kmin, double kmax, double amp) {
+    const double kxd = 2.0 * 3.141592653589793 * i / g.Lx;
+    const double kyd = (j <= g.ny / 2) ? 2.0 * 3.141592653589793 * j / g.Ly : 2.0 * 3.141592653589793 * (j - g.ny) / g.Ly;
+    const double k2d = kxd * kxd + kyd * kyd;
+    const double km = sqrt(k2d);
+    if (!(k2d > 1e-12 && km >= kmin && km <= kmax)) return make_double2(0.0, 0.0);
+    int jsrc = j, flip = 0;
+    if (i == 0 && j > g.ny / 2) { jsrc = g.ny - j; flip = 1; }
+    unsigned long long ctr[4] = {(unsigned long long)jsrc * g.nkx + i, step, NSG_TAG_FORCE, 0ULL};
+    philox4x64(ctr, seed, 0ULL);
+    const double u1 = fmax(u53(ctr[0]), 2.2250738585072014e-308);
+    const double u2 = u53(ctr[1]);
+    const double rad = sqrt(-2.0 * log(u1)) * 0.70710678118654752440;
+    double sn, cs;
+    sincos(2.0 * 3.141592653589793 * u2, &sn, &cs);
+    return make_double2(amp * rad * cs, amp * (flip ? -rad * sn : rad * sn));
+}
+
+// one kept kx column per CTA (64 threads); G and F columns are contiguous, so
+// layout-A values x[64 n1 + t] load and store straight from and to global memory
+#define NSG_CW_EX 2112
+
+template <typename T> __host__ __device__ constexpr size_t cw_smem_bytes2(int Ky) {
+    return (size_t)(32 * 65 + NSG_CW_EX) * (sizeof(T) == 4 ? sizeof(float2) : sizeof(double2)) + (size_t)Ky * sizeof(T);
+}
+
 template <typename T, int STAGE>
-__global__ void __launch_bounds__(64 * NSG_CW_COLS) k_col_w(Geo g, ColArgs<T> a) {
+__global__ void __launch_bounds__(64, (sizeof(T) == 4 ? 6 : 3)) k_col_w(Geo g, ColArgs<T> a) {
     typedef typename CT<T>::C C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* tw = reinterpret_cast<C*>(smem_raw);
-    C* tile = tw + 32 * 65;
-    const int p = threadIdx.x >> 6, t = threadIdx.x & 63, lane = threadIdx.x & 31, h = t >> 5;
-    const int c0 = blockIdx.x * NSG_CW_COLS;
-    const int i = c0 + p;
-    const int Kx = g.Kx, Kxp = g.Kxp, Ky = g.Ky;
-    C* col = tile + p * NSG_CW_LP;
+    C* ex = tw + 32 * 65;
+    T* kys = reinterpret_cast<T*>(ex + NSG_CW_EX);
+    const int t = threadIdx.x, lane = t & 31, h = t >> 5;
+    const int i = blockIdx.x;
+    const int Ky = g.Ky;
     __shared__ double s_dt;
 
-    for (int idx = threadIdx.x; idx < 32 * 64; idx += blockDim.x) {
+    for (int idx = t; idx < 32 * 64; idx += 64) {
         const int k1 = idx >> 6, tt = idx & 63;
-        tw[k1 * 65 + tt] = a.twc[tt * k1];
+        tw[k1 * 65 + tt] = __ldg(&a.twc[tt * k1]);
     }
-    if (threadIdx.x == 0) {
+    for (int jj = t; jj < Ky; jj += 64) kys[jj] = __ldg(&a.kyv[jj]);
+    if (t == 0) {
         double dt;
         if (STAGE == 1) {
             if (a.sp.adaptive) {
@@ -348,119 +394,125 @@ __global__ void __launch_bounds__(64 * NSG_CW_COLS) k_col_w(Geo g, ColArgs<T> a)
         }
         s_dt = dt;
     }
-    // G tile -> shared (column-contiguous), coalesced along kx
-    for (int idx = threadIdx.x; idx < 2048 * NSG_CW_COLS; idx += blockDim.x) {
-        const int y = idx / NSG_CW_COLS, c = idx - y * NSG_CW_COLS;
-        C v = cmake<C>(0.0, 0.0);
-        if (c0 + c < Kx) v = a.G[(size_t)y * Kxp + c0 + c];
-        tile[c * NSG_CW_LP + y] = v;
-    }
-    __syncthreads();
     C v[32];
+    const C* __restrict__ Gc = a.G + (size_t)i * 2048;
 #pragma unroll
-    for (int n1 = 0; n1 < 32; ++n1) v[n1] = col[64 * n1 + t];
+    for (int n1 = 0; n1 < 32; ++n1) v[n1] = __ldg(&Gc[64 * n1 + t]);
     __syncthreads();
-    col_fwd2048(v, col, tw, t, lane, h);
+    col_fwd2048(v, ex, tw, t, lane, h);
 
-    // RK stage algebra on the kept modes held by this thread: j = lane + 32 k2 + 1024 h
+    // RK stage algebra (spectral_time_integration.c:50-100) on this thread's modes j = lane + 32 k2 + 1024 h
     const double dt = s_dt;
     const T inv_re = (T)a.sp.inv_re;
     const T sc = (T)a.sp.scale;
-    const T ch = (T)(0.5 * dt), cf = (T)dt, c6 = (T)(dt / 6.0);
-    double f_amp = 0.0, sfd_a = 0.0;
-    if (STAGE == 4) {
-        if (a.sp.forcing) f_amp = a.sp.f_sigma * sqrt(dt);
-        if (a.sp.sfd) {
-            sfd_a = dt / a.sp.sfd_tau;
-            sfd_a = sfd_a > 1.0 ? 1.0 : (sfd_a < 0.0 ? 0.0 : sfd_a);
+    const T cst = (STAGE == 1 || STAGE == 2) ? (T)(0.5 * dt) : (STAGE == 3 ? (T)dt : (T)(dt / 6.0));
+    const T kx = __ldg(&a.kxv[i]);
+    C* __restrict__ W0 = a.W0;
+    C* __restrict__ WS = a.WS;
+    C* __restrict__ ACC = a.ACC;
+    const int hv = a.sp.hv, sfd = a.sp.sfd;
+    // NB modes at a time: issue every load of the batch, then compute and store
+    constexpr int NB = 4;
+#pragma unroll
+    for (int b0 = 0; b0 < 32; b0 += NB) {
+        C w0v[NB], wsv[NB], acv[NB], fbv[NB];
+        T hwv[NB], swv[NB];
+        int jjv[NB];
+#pragma unroll
+        for (int u = 0; u < NB; ++u) {
+            const int j = lane + 32 * (b0 + u) + 1024 * h;
+            const int jj = kept_jj(g, j);
+            jjv[u] = jj;
+            const size_t s = (size_t)i * Ky + (jj < 0 ? 0 : jj);
+            const bool ok = jj >= 0;
+            const C zero = cmake<C>(0.0, 0.0);
+            w0v[u] = ok ? ((STAGE == 4) ? W0[s] : __ldg(&W0[s])) : zero;
+            wsv[u] = (STAGE == 1) ? w0v[u] : (ok ? ((STAGE == 4) ? __ldg(&WS[s]) : WS[s]) : zero);
+            acv[u] = (STAGE == 1) ? zero : (ok ? ((STAGE == 4) ? __ldg(&ACC[s]) : ACC[s]) : zero);
+            hwv[u] = (hv && ok) ? __ldg(&a.hvw[s]) : (T)0;
+            swv[u] = (sfd && ok) ? __ldg(&a.sfdw[s]) : (T)0;
+            fbv[u] = (sfd && ok) ? a.SFD[s] : zero;
+        }
+#pragma unroll
+        for (int u = 0; u < NB; ++u) {
+            const int jj = jjv[u];
+            if (jj < 0) continue;
+            const int k2 = b0 + u;
+            const size_t s = (size_t)i * Ky + jj;
+            const C w0 = w0v[u], ws = wsv[u];
+            const T ky = kys[jj];
+            const T k2v = kx * kx + ky * ky;
+            C k;
+            k.x = -(v[k2].x * sc) - k2v * ws.x * inv_re;
+            k.y = -(v[k2].y * sc) - k2v * ws.y * inv_re;
+            if (hv || sfd) {
+                C damp = cmake<C>(0.0, 0.0);
+                if (hv) { damp.x += hwv[u] * ws.x; damp.y += hwv[u] * ws.y; }
+                if (sfd && swv[u] > (T)0) {
+                    damp.x += swv[u] * (ws.x - fbv[u].x);
+                    damp.y += swv[u] * (ws.y - fbv[u].y);
+                }
+                k.x -= damp.x;
+                k.y -= damp.y;
+            }
+            C wn;
+            if (STAGE == 1) {
+                ACC[s] = k;
+                wn.x = w0.x + cst * k.x; wn.y = w0.y + cst * k.y;
+                WS[s] = wn;
+            } else if (STAGE == 2 || STAGE == 3) {
+                C acc = acv[u];
+                acc.x = acc.x + (T)2 * k.x;
+                acc.y = acc.y + (T)2 * k.y;
+                ACC[s] = acc;
+                wn.x = w0.x + cst * k.x; wn.y = w0.y + cst * k.y;
+                WS[s] = wn;
+            } else {
+                const C acc = acv[u];
+                wn.x = w0.x + cst * (acc.x + k.x);
+                wn.y = w0.y + cst * (acc.y + k.y);
+                W0[s] = wn;
+            }
         }
     }
-    const bool colok = (i < Kx);
-    const T kx = colok ? a.kxv[i] : (T)0;
-#pragma unroll
-    for (int k2 = 0; k2 < 32; ++k2) {
-        const int j = lane + 32 * k2 + 1024 * h;
-        const int jj = kept_jj(g, j);
-        if (!colok || jj < 0) continue;
-        const C gh = v[k2];
-        C nl;
-        nl.x = -(gh.x * sc);
-        nl.y = -(gh.y * sc);
-        const size_t s = (size_t)i * Ky + jj;
-        const C w0 = a.W0[s];
-        const C ws = (STAGE == 1) ? w0 : a.WS[s];
-        const T ky = a.kyv[jj];
-        const T k2v = kx * kx + ky * ky;
-        C k;
-        k.x = nl.x - k2v * ws.x * inv_re;
-        k.y = nl.y - k2v * ws.y * inv_re;
-        if (a.sp.hv || a.sp.sfd) {
-            C damp = cmake<C>(0.0, 0.0);
-            if (a.sp.hv) { const T w = a.hvw[s]; damp.x += w * ws.x; damp.y += w * ws.y; }
-            if (a.sp.sfd) {
-                const T sw = a.sfdw[s];
-                if (sw > (T)0) {
-                    const C fb = a.SFD[s];
-                    damp.x += sw * (ws.x - fb.x);
-                    damp.y += sw * (ws.y - fb.y);
-                }
-            }
-            k.x -= damp.x;
-            k.y -= damp.y;
+    if (STAGE == 4 && (a.sp.forcing || sfd)) {
+        // forcing increment (few low-|k| modes), then the SFD post-step, on omega_hat^{n+1}
+        const double f_amp = a.sp.forcing ? a.sp.f_sigma * sqrt(dt) : 0.0;
+        double sa = 0.0;
+        if (sfd) {
+            sa = dt / a.sp.sfd_tau;
+            sa = sa > 1.0 ? 1.0 : (sa < 0.0 ? 0.0 : sa);
         }
-        C wn;
-        if (STAGE == 1) {
-            a.ACC[s] = k;
-            wn.x = w0.x + ch * k.x; wn.y = w0.y + ch * k.y;
-            a.WS[s] = wn;
-        } else if (STAGE == 2 || STAGE == 3) {
-            C acc = a.ACC[s];
-            acc.x = acc.x + (T)2 * k.x;
-            acc.y = acc.y + (T)2 * k.y;
-            a.ACC[s] = acc;
-            const T cc = (STAGE == 2) ? ch : cf;
-            wn.x = w0.x + cc * k.x; wn.y = w0.y + cc * k.y;
-            a.WS[s] = wn;
-        } else {
-            const C acc = a.ACC[s];
-            wn.x = w0.x + c6 * (acc.x + k.x);
-            wn.y = w0.y + c6 * (acc.y + k.y);
-            if (a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9) {
-                const double kxd = 2.0 * 3.141592653589793 * i / g.Lx;
-                const double kyd = (j <= g.ny / 2) ? 2.0 * 3.141592653589793 * j / g.Ly
-                                                   : 2.0 * 3.141592653589793 * (j - g.ny) / g.Ly;
-                const double k2d = kxd * kxd + kyd * kyd;
-                const double km = sqrt(k2d);
-                if (k2d > 1e-12 && km >= a.sp.f_kmin && km <= a.sp.f_kmax) {
-                    int jsrc = j, flip = 0;
-                    if (i == 0 && j > g.ny / 2) { jsrc = g.ny - j; flip = 1; }
-                    unsigned long long ctr[4] = {(unsigned long long)jsrc * g.nkx + i, a.ds->step_cur, NSG_TAG_FORCE, 0ULL};
-                    philox4x64(ctr, a.sp.f_seed, 0ULL);
-                    const double u1 = fmax(u53(ctr[0]), 2.2250738585072014e-308);
-                    const double u2 = u53(ctr[1]);
-                    const double rad = sqrt(-2.0 * log(u1)) * 0.70710678118654752440;
-                    double sn, cs;
-                    sincos(2.0 * 3.141592653589793 * u2, &sn, &cs);
-                    double xr = rad * cs, xi = rad * sn;
-                    if (flip) xi = -xi;
-                    wn.x = (T)((double)wn.x + f_amp * xr);
-                    wn.y = (T)((double)wn.y + f_amp * xi);
+        const bool force_col = a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9;
+#pragma unroll 1
+        for (int k2 = 0; k2 < 32; ++k2) {
+            const int j = lane + 32 * k2 + 1024 * h;
+            const int jj = kept_jj(g, j);
+            if (jj < 0) continue;
+            const size_t s = (size_t)i * Ky + jj;
+            C wn = W0[s];
+            if (force_col) {
+                const double2 df =
+                    forcing_increment(g, i, j, a.ds->step_cur, a.sp.f_seed, a.sp.f_kmin, a.sp.f_kmax, f_amp);
+                if (df.x != 0.0 || df.y != 0.0) {
+                    wn.x = (T)((double)wn.x + df.x);
+                    wn.y = (T)((double)wn.y + df.y);
+                    W0[s] = wn;
                 }
             }
-            if (a.sp.sfd) {
+            if (sfd) {
                 C fb = a.SFD[s];
-                const T al = (T)sfd_a, om = (T)(1.0 - sfd_a);
+                const T al = (T)sa, om = (T)(1.0 - sa);
                 fb.x = om * fb.x + al * wn.x;
                 fb.y = om * fb.y + al * wn.y;
                 a.SFD[s] = fb;
             }
-            a.W0[s] = wn;
         }
     }
-    if (STAGE == 4 && blockIdx.x == 0 && threadIdx.x == 0) a.ds->t = a.ds->t + dt;
+    if (STAGE == 4 && blockIdx.x == 0 && t == 0) a.ds->t = a.ds->t + dt;
 
     // inverse y-transforms of the next stage's Psi, Psi_y, Omega, Omega_y
-    const C* src = (STAGE == 4) ? a.W0 : a.WS;
+    const C* src = (STAGE == 4) ? W0 : WS;
 #pragma unroll 1
     for (int f = 0; f < 4; ++f) {
 #pragma unroll
@@ -468,19 +520,14 @@ __global__ void __launch_bounds__(64 * NSG_CW_COLS) k_col_w(Geo g, ColArgs<T> a)
             const int j = lane + 32 * k2 + 1024 * h;
             const int jj = kept_jj(g, j);
             C x = cmake<C>(0.0, 0.0);
-            if (colok && jj >= 0) x = field_value<T, C>(f, src[(size_t)i * Ky + jj], kx, a.kyv[jj]);
+            if (jj >= 0) x = field_value<T, C>(f, src[(size_t)i * Ky + jj], kx, kys[jj]);
             v[k2] = x;
         }
-        col_inv2048(v, col, tw, t, lane, h);
+        col_inv2048(v, ex, tw, t, lane, h);
+        C* __restrict__ Fc = a.F[f] + i;  // F row-contiguous: column i of [ny][Kxp]
+        const int Kxp = g.Kxp;
 #pragma unroll
-        for (int n1 = 0; n1 < 32; ++n1) col[64 * n1 + t] = v[n1];
-        __syncthreads();
-        C* dstF = a.F[f];
-        for (int idx = threadIdx.x; idx < 2048 * NSG_CW_COLS; idx += blockDim.x) {
-            const int y = idx / NSG_CW_COLS, c = idx - y * NSG_CW_COLS;
-            if (c0 + c < Kxp) dstF[(size_t)y * Kxp + c0 + c] = tile[c * NSG_CW_LP + y];
-        }
-        __syncthreads();
+        for (int n1 = 0; n1 < 32; ++n1) Fc[(size_t)(64 * n1 + t) * Kxp] = v[n1];
     }
 }
 
