@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(256) k_row(Geo g, RowArgs<T> a) {
     const int H = g.H, TT = H / E, LP = spad_len(H);
     const int r = threadIdx.x / TT, t = threadIdx.x - r * TT;
     const int y = blockIdx.x * g.RPC + r;
-    const int nx = g.nx, Kxp = g.Kxp, Kx = g.Kx;
+    const int nx = g.nx, Kx = g.Kx;
 
     if (MODE == ROW_STAGE && blockIdx.x == 0 && threadIdx.x == 0) {
         if (a.marker == 1) {
@@ -380,7 +380,7 @@ __global__ void __launch_bounds__(512) k_col(Geo g, ColArgs<T> a) {
     const int ny = g.ny, TC = ny / E, LP = spad_len(ny), CW = g.CW;
     const int b = threadIdx.x / TC, t = threadIdx.x - b * TC;
     const int c0 = blockIdx.x * CW;
-    const int Kx = g.Kx, Kxp = g.Kxp, Ky = g.Ky;
+    const int Kx = g.Kx, Ky = g.Ky;
     const int nthr = blockDim.x;
     C* mybuf = sm + b * LP;
     __shared__ double s_dt;

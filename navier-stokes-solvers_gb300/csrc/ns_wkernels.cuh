@@ -269,10 +269,10 @@ __global__ void __launch_bounds__(32 * rw_warps<T>(), 1) k_row_w(Geo g, RowArgs<
 // forward 2048-point transform: a[] = x[64 n1 + t] on entry (t = 32 h + lane),
 // X[lane + 32 k2 + 1024 h] on exit; col is this column's shared buffer
 template <typename C>
-__device__ __forceinline__ void col_fwd2048(C (&a)[32], C* col, const C* tw, int t, int lane, int h) {
+__device__ __forceinline__ void col_fwd2048(C (&a)[32], C* col, const C* __restrict__ twc, int t, int lane, int h) {
     dft32<false>(a);
 #pragma unroll
-    for (int k1 = 1; k1 < 32; ++k1) a[k1] = cmul(a[k1], tw[k1 * 65 + t]);
+    for (int k1 = 1; k1 < 32; ++k1) a[k1] = cmul(a[k1], __ldg(&twc[t * k1]));
 #pragma unroll
     for (int k1 = 0; k1 < 32; ++k1) col[k1 * 65 + t] = a[k1];
     __syncthreads();
@@ -282,7 +282,7 @@ __device__ __forceinline__ void col_fwd2048(C (&a)[32], C* col, const C* tw, int
     dft32<false>(a);
     if (h) {
 #pragma unroll
-        for (int k2 = 1; k2 < 32; ++k2) a[k2] = cmul(a[k2], tw[k2 * 65 + 32]);  // W_64^{k2} = W_2048^{32 k2}
+        for (int k2 = 1; k2 < 32; ++k2) a[k2] = cmul(a[k2], __ldg(&twc[32 * k2]));  // W_64^{k2} = W_2048^{32 k2}
     }
 #pragma unroll
     for (int k2 = 0; k2 < 32; ++k2) col[h * 1056 + k2 * 33 + lane] = a[k2];
@@ -298,7 +298,7 @@ __device__ __forceinline__ void col_fwd2048(C (&a)[32], C* col, const C* tw, int
 // inverse 2048-point transform: a[] = X[lane + 32 k2 + 1024 h] on entry,
 // x[64 n1 + t] on exit (unnormalised)
 template <typename C>
-__device__ __forceinline__ void col_inv2048(C (&a)[32], C* col, const C* tw, int t, int lane, int h) {
+__device__ __forceinline__ void col_inv2048(C (&a)[32], C* col, const C* __restrict__ twc, int t, int lane, int h) {
 #pragma unroll
     for (int k2 = 0; k2 < 32; ++k2) col[h * 1056 + k2 * 33 + lane] = a[k2];
     __syncthreads();
@@ -308,7 +308,7 @@ __device__ __forceinline__ void col_inv2048(C (&a)[32], C* col, const C* tw, int
         if (h == 0) {
             a[k2] = cadd(a[k2], b);  // E = X_lo + X_hi
         } else {
-            C w = tw[k2 * 65 + 32];
+            C w = __ldg(&twc[32 * k2]);
             w.y = -w.y;  // W_64^{-k2}
             a[k2] = cmul(csub(b, a[k2]), w);  // O = (X_lo - X_hi) W_64^{-k2}
         }
@@ -323,7 +323,7 @@ __device__ __forceinline__ void col_inv2048(C (&a)[32], C* col, const C* tw, int
     __syncthreads();
 #pragma unroll
     for (int k1 = 1; k1 < 32; ++k1) {
-        C w = tw[k1 * 65 + t];
+        C w = __ldg(&twc[t * k1]);
         w.y = -w.y;
         a[k1] = cmul(a[k1], w);
     }
@@ -355,26 +355,22 @@ __device__ __noinline__ double2 forcing_increment(const Geo& g, int i, int j, un
 #define NSG_CW_EX 2112
 
 template <typename T> __host__ __device__ constexpr size_t cw_smem_bytes2(int Ky) {
-    return (size_t)(32 * 65 + NSG_CW_EX) * (sizeof(T) == 4 ? sizeof(float2) : sizeof(double2)) + (size_t)Ky * sizeof(T);
+    return (size_t)(NSG_CW_EX + 2048) * (sizeof(T) == 4 ? sizeof(float2) : sizeof(double2));
 }
 
 template <typename T, int STAGE>
 __global__ void __launch_bounds__(64, (sizeof(T) == 4 ? 6 : 3)) k_col_w(Geo g, ColArgs<T> a) {
     typedef typename CT<T>::C C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    C* tw = reinterpret_cast<C*>(smem_raw);
-    C* ex = tw + 32 * 65;
-    T* kys = reinterpret_cast<T*>(ex + NSG_CW_EX);
+    C* ex = reinterpret_cast<C*>(smem_raw);
+    C* wb = ex + NSG_CW_EX;  // next-stage state of this thread's modes, wb[k2 * 64 + t]
+    const T* __restrict__ kys = a.kyv;
+    const C* __restrict__ tw = a.twc;  // W_2048^m, read through L1
     const int t = threadIdx.x, lane = t & 31, h = t >> 5;
     const int i = blockIdx.x;
     const int Ky = g.Ky;
     __shared__ double s_dt;
 
-    for (int idx = t; idx < 32 * 64; idx += 64) {
-        const int k1 = idx >> 6, tt = idx & 63;
-        tw[k1 * 65 + tt] = __ldg(&a.twc[tt * k1]);
-    }
-    for (int jj = t; jj < Ky; jj += 64) kys[jj] = __ldg(&a.kyv[jj]);
     if (t == 0) {
         double dt;
         if (STAGE == 1) {
@@ -436,11 +432,14 @@ __global__ void __launch_bounds__(64, (sizeof(T) == 4 ? 6 : 3)) k_col_w(Geo g, C
 #pragma unroll
         for (int u = 0; u < NB; ++u) {
             const int jj = jjv[u];
-            if (jj < 0) continue;
             const int k2 = b0 + u;
+            if (jj < 0) {
+                wb[k2 * 64 + t] = cmake<C>(0.0, 0.0);
+                continue;
+            }
             const size_t s = (size_t)i * Ky + jj;
             const C w0 = w0v[u], ws = wsv[u];
-            const T ky = kys[jj];
+            const T ky = __ldg(&kys[jj]);
             const T k2v = kx * kx + ky * ky;
             C k;
             k.x = -(v[k2].x * sc) - k2v * ws.x * inv_re;
@@ -473,6 +472,7 @@ __global__ void __launch_bounds__(64, (sizeof(T) == 4 ? 6 : 3)) k_col_w(Geo g, C
                 wn.y = w0.y + cst * (acc.y + k.y);
                 W0[s] = wn;
             }
+            wb[k2 * 64 + t] = wn;
         }
     }
     if (STAGE == 4 && (a.sp.forcing || sfd)) {
@@ -490,7 +490,7 @@ __global__ void __launch_bounds__(64, (sizeof(T) == 4 ? 6 : 3)) k_col_w(Geo g, C
             const int jj = kept_jj(g, j);
             if (jj < 0) continue;
             const size_t s = (size_t)i * Ky + jj;
-            C wn = W0[s];
+            C wn = wb[k2 * 64 + t];
             if (force_col) {
                 const double2 df =
                     forcing_increment(g, i, j, a.ds->step_cur, a.sp.f_seed, a.sp.f_kmin, a.sp.f_kmax, f_amp);
@@ -498,6 +498,7 @@ __global__ void __launch_bounds__(64, (sizeof(T) == 4 ? 6 : 3)) k_col_w(Geo g, C
                     wn.x = (T)((double)wn.x + df.x);
                     wn.y = (T)((double)wn.y + df.y);
                     W0[s] = wn;
+                    wb[k2 * 64 + t] = wn;
                 }
             }
             if (sfd) {
@@ -512,7 +513,6 @@ __global__ void __launch_bounds__(64, (sizeof(T) == 4 ? 6 : 3)) k_col_w(Geo g, C
     if (STAGE == 4 && blockIdx.x == 0 && t == 0) a.ds->t = a.ds->t + dt;
 
     // inverse y-transforms of the next stage's Psi, Psi_y, Omega, Omega_y
-    const C* src = (STAGE == 4) ? W0 : WS;
 #pragma unroll 1
     for (int f = 0; f < 4; ++f) {
 #pragma unroll
@@ -520,7 +520,7 @@ __global__ void __launch_bounds__(64, (sizeof(T) == 4 ? 6 : 3)) k_col_w(Geo g, C
             const int j = lane + 32 * k2 + 1024 * h;
             const int jj = kept_jj(g, j);
             C x = cmake<C>(0.0, 0.0);
-            if (jj >= 0) x = field_value<T, C>(f, src[(size_t)i * Ky + jj], kx, kys[jj]);
+            if (jj >= 0) x = field_value<T, C>(f, wb[k2 * 64 + t], kx, __ldg(&kys[jj]));
             v[k2] = x;
         }
         col_inv2048(v, ex, tw, t, lane, h);
