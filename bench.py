@@ -223,6 +223,11 @@ def reduce_max(x: float, ws: int):
     return float(t.item())
 
 
+def aggregate_value(n: int, steps: int, ws: int, ms_total: float) -> float:
+    """Whole-job grid-pt*steps/s: every replica's points over the slowest rank's time."""
+    return n * n * steps * ws / (ms_total * 1e-3)
+
+
 def barrier(ws: int):
     if ws > 1:
         import torch.distributed as dist
@@ -309,7 +314,7 @@ def main():
     ms_total = reduce_max(total.value, ws)
     barrier(ws)
     diag = g.diagnostics()
-    value = n * n * args.steps * ws / (ms_total * 1e-3)
+    value = aggregate_value(n, args.steps, ws, ms_total)
 
     # per-kernel CUDA-event timing for the roofline (separate pass, same flush)
     prof_steps = min(args.steps, 50)

@@ -45,6 +45,10 @@ __device__ __forceinline__ size_t gidx(const Geo& g, int y, int c) {
     return g.fTG ? (size_t)c * g.ny + y : (size_t)y * g.Kxp + c;
 }
 
+// kx^2 + ky^2 rounded as the reference's host code does (no fused multiply-add)
+__device__ __forceinline__ double k2sum(double kx, double ky) { return __dadd_rn(__dmul_rn(kx, kx), __dmul_rn(ky, ky)); }
+__device__ __forceinline__ float k2sum(float kx, float ky) { return kx * kx + ky * ky; }
+
 __device__ __forceinline__ int kept_j(const Geo& g, int jj) { return jj <= g.Kyh ? jj : g.ny - g.Ky + jj; }
 __device__ __forceinline__ int kept_jj(const Geo& g, int j) {
     if (j <= g.Kyh) return j;
@@ -358,7 +362,7 @@ __device__ __forceinline__ C field_value(int f, C w, T kx, T ky) {
     // f: 0 Psi = -w/k^2, 1 Psi_y = i ky Psi, 2 Omega = w, 3 Omega_y = i ky w (spectral_core.c:17-31)
     C v = w;
     if (f < 2) {
-        const T k2 = kx * kx + ky * ky;
+        const T k2 = k2sum(kx, ky);
         if (k2 > (T)1e-12) { v.x = -kdiv(w.x, k2); v.y = -kdiv(w.y, k2); }
         else { v.x = (T)0; v.y = (T)0; }
     }
@@ -455,7 +459,7 @@ __global__ void __launch_bounds__(512) k_col(Geo g, ColArgs<T> a) {
                 const C w0 = a.W0[s];
                 const C ws = (STAGE == 1) ? w0 : a.WS[s];
                 const T kx = a.kxv[i], ky = a.kyv[jj];
-                const T k2 = kx * kx + ky * ky;
+                const T k2 = k2sum(kx, ky);
                 C k;  // k = N - k^2 omega / Re - damping (spectral_time_integration.c:50-54)
                 k.x = nl.x - k2 * ws.x * inv_re;
                 k.y = nl.y - k2 * ws.y * inv_re;
@@ -575,7 +579,7 @@ __global__ void k_geometry(Geo g, double* x, double* y, double* kx, double* ky, 
         const int j = (int)(idx / nkx), i = (int)(idx - (long long)j * nkx);
         const double kxv = 2.0 * 3.14159265358979323846 * i / g.Lx;
         const double kyv = (j <= ny / 2) ? 2.0 * 3.14159265358979323846 * j / g.Ly : 2.0 * 3.14159265358979323846 * (j - ny) / g.Ly;
-        if (k2) k2[idx] = kxv * kxv + kyv * kyv;
+        if (k2) k2[idx] = k2sum(kxv, kyv);
         if (mask) {
             const int band = (j <= ny / 2) ? j : j - ny;
             mask[idx] = (i <= (2 * nkx) / 3) && (abs(band) <= (2 * ny) / 6);
@@ -593,7 +597,7 @@ __global__ void k_geometry(Geo g, double* x, double* y, double* kx, double* ky, 
 __device__ __forceinline__ double geo_k2(const Geo& g, int j, int i) {
     const double kxv = 2.0 * 3.14159265358979323846 * i / g.Lx;
     const double kyv = (j <= g.ny / 2) ? 2.0 * 3.14159265358979323846 * j / g.Ly : 2.0 * 3.14159265358979323846 * (j - g.ny) / g.Ly;
-    return kxv * kxv + kyv * kyv;
+    return k2sum(kxv, kyv);
 }
 __device__ __forceinline__ int geo_kept(const Geo& g, int j, int i) {
     const int band = (j <= g.ny / 2) ? j : j - g.ny;
@@ -713,7 +717,7 @@ __global__ void k_export(Geo g, const typename CT<T>::C* W, const typename CT<T>
         if (sh) sh[idx] = q;
         const double kxv = 2.0 * 3.14159265358979323846 * i / g.Lx;
         const double kyv = (j <= g.ny / 2) ? 2.0 * 3.14159265358979323846 * j / g.Ly : 2.0 * 3.14159265358979323846 * (j - g.ny) / g.Ly;
-        const double k2 = kxv * kxv + kyv * kyv;
+        const double k2 = k2sum(kxv, kyv);
         double2 p = make_double2(0.0, 0.0);
         if (k2 > 1e-12) p = make_double2(-w.x / k2, -w.y / k2);
         if (ph) ph[idx] = p;
@@ -729,7 +733,7 @@ __global__ void k_velocity(Geo g, const double2* wh, double2* ph, double2* uh, d
         const int j = (int)(idx / g.nkx), i = (int)(idx - (long long)j * g.nkx);
         const double kxv = 2.0 * 3.14159265358979323846 * i / g.Lx;
         const double kyv = (j <= g.ny / 2) ? 2.0 * 3.14159265358979323846 * j / g.Ly : 2.0 * 3.14159265358979323846 * (j - g.ny) / g.Ly;
-        const double k2 = kxv * kxv + kyv * kyv;
+        const double k2 = k2sum(kxv, kyv);
         const double2 w = wh[idx];
         double2 p = make_double2(0.0, 0.0);
         if (k2 > 1e-12) p = make_double2(-w.x / k2, -w.y / k2);

@@ -440,7 +440,7 @@ __global__ void __launch_bounds__(64, (sizeof(T) == 4 ? 6 : 3)) k_col_w(Geo g, C
             const size_t s = (size_t)i * Ky + jj;
             const C w0 = w0v[u], ws = wsv[u];
             const T ky = __ldg(&kys[jj]);
-            const T k2v = kx * kx + ky * ky;
+            const T k2v = k2sum(kx, ky);
             C k;
             k.x = -(v[k2].x * sc) - k2v * ws.x * inv_re;
             k.y = -(v[k2].y * sc) - k2v * ws.y * inv_re;

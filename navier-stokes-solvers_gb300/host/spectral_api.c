@@ -346,9 +346,9 @@ int ns_spectral_gpu_set_forcing(NSSpectralData *d, int enabled, double kmin, dou
 
 int ns_spectral_gpu_diagnostics(NSSpectralData *d, double *energy, double *enstrophy) {
     if (!d || !d->gpu) return SOLVER_INVALID_PARAM;
-    if (!d->gpu->device_current) {
-        int st = ns_host_sync(d);
-        if (st == NS_GPU_OK) st = ns_sync_params(d, 0);
+    /* the host arrays are the state unless device-resident steps are newer */
+    if (!d->gpu->host_stale) {
+        int st = ns_sync_params(d, 0);
         if (st == NS_GPU_OK)
             st = ns_gpu_upload_state(d->gpu->dev, (const double *)d->omega_hat, (const double *)d->psi_hat,
                                      ns_sfd_on(d) ? (const double *)d->sfd_hat : NULL, d->t, d->dt, d->gpu->step);
