@@ -12,6 +12,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "ns_gpu.h"
@@ -127,6 +128,29 @@ template <typename T> using Cx = typename CT<T>::C;
 
 
 // ------------------------------------------------------------- launchers
+// Launch a stage kernel with programmatic stream serialization: it may be
+// scheduled while the previous kernel on the stream drains, runs its
+// independent prologue, and waits (griddepcontrol.wait) before it touches
+// anything the previous kernel wrote.
+#ifndef NSG_PDL
+#define NSG_PDL 1
+#endif
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_stage(void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t st,
+                                Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = NSG_PDL;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
+
 template <typename K> static int set_smem(ns_gpu* g, K kernel, size_t bytes) {
     if (bytes > 48 * 1024) NSG_CUDA(g, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     return NS_GPU_OK;
@@ -232,7 +256,8 @@ template <typename T> static int stage_row(ns_gpu* g, int stage) {
         const int nw = rw_warps<T>();
         int grid = g->g.ny / nw;
         if (grid > g->num_sms) grid = g->num_sms;
-        k_row_w<T><<<grid, 32 * nw, smem, g->st>>>(g->g, a);
+        const cudaError_t e = launch_stage(k_row_w<T>, grid, 32 * nw, smem, g->st, g->g, a);
+        if (e != cudaSuccess) NSG_FAIL(g, NS_GPU_ERR_CUDA, "k_row_w launch: %s", cudaGetErrorString(e));
         NSG_LAUNCHED(g);
         return NS_GPU_OK;
     }
@@ -244,7 +269,8 @@ template <typename T, int STAGE> static int stage_col(ns_gpu* g, const ColArgs<T
     if (g->fast_col) {
         const size_t smem = cw_smem_bytes2<T>(g->g.Ky);
         NSG_TRY(set_smem(g, k_col_w<T, STAGE>, smem));
-        k_col_w<T, STAGE><<<g->g.Kx, 64, smem, g->st>>>(g->g, a);
+        const cudaError_t e = launch_stage(k_col_w<T, STAGE>, g->g.Kx, 64, smem, g->st, g->g, a);
+        if (e != cudaSuccess) NSG_FAIL(g, NS_GPU_ERR_CUDA, "k_col_w launch: %s", cudaGetErrorString(e));
         NSG_LAUNCHED(g);
         return NS_GPU_OK;
     }
@@ -495,10 +521,12 @@ int ns_gpu_create(int nx, int ny, double Lx, double Ly, int precision, ns_gpu** 
     G.logH = ilog2(G.H);
     G.Lx = Lx;
     G.Ly = Ly;
-    // F row-contiguous (the row pass reads whole rows), G column-contiguous (the
-    // column pass reads whole columns): scattered accesses fall on the store side
-    G.fTF = 0;
-    G.fTG = (g->fast_row || g->fast_col) ? 1 : 0;
+    // With the register-resident stage kernels F and G are both kx-column-contiguous
+    // (F in blocks of ny rows): the column pass reads G and writes F as whole
+    // columns, and the row pass reads F and writes G group-wide, as runs of one
+    // column over the group's consecutive rows.
+    G.fLB = (g->fast_row || g->fast_col) ? G.logny : 0;
+    G.fTG = G.fLB ? 1 : 0;
     g->ER = G.H >= 16 ? 16 : 4;
     g->EC = ny >= 16 ? 16 : 4;
     const size_t cs = (precision == NS_GPU_FP64) ? sizeof(double2) : sizeof(float2);

@@ -6,8 +6,10 @@
 //                  jj in [0, Ky), Ky = 2*Kyh+1 (jj <= Kyh -> j = jj, else j = ny-Ky+jj)
 //   state arrays   W0 (omega_hat at the step start), WS (stage state), ACC (RK
 //                  accumulator), PSI0, SFD: C[Kxp][Ky]  (column i contiguous)
-//   F[4]           y-transformed fields Psi, Psi_y, Omega, Omega_y: C[ny][Kxp]
-//   G              x-transformed Jacobian: C[ny][Kxp]
+//   F[4]           y-transformed fields Psi, Psi_y, Omega, Omega_y: C[ny/B][Kxp][B]
+//                  in blocks of B = 2^fLB rows (B = 1: row-contiguous, the
+//                  generic kernels; B = ny: kx-column-contiguous)
+//   G              x-transformed Jacobian: C[ny][Kxp] or C[Kxp][ny]
 // Only the dealiased modes are ever stored or transformed on the hot path;
 // the 2/3 rule is the layout (reference mask: spectral_initialization.c:46-49).
 //
@@ -33,13 +35,13 @@ struct Geo {
     double Lx, Ly;
     int CW;         // columns per column-kernel CTA
     int RPC;        // rows per row-kernel CTA
-    int fTF;        // F stored kx-column-contiguous ([Kxp][ny]) instead of row-contiguous [ny][Kxp]
+    int fLB;        // F stored in blocks of 2^fLB rows: [ny >> fLB][Kxp][1 << fLB]
     int fTG;        // G stored kx-column-contiguous
 };
 
 // element (row y, kept column c) of an F buffer / of the G buffer
 __device__ __forceinline__ size_t fidx(const Geo& g, int y, int c) {
-    return g.fTF ? (size_t)c * g.ny + y : (size_t)y * g.Kxp + c;
+    return (((size_t)(y >> g.fLB) * g.Kxp + c) << g.fLB) + (y & ((1 << g.fLB) - 1));
 }
 __device__ __forceinline__ size_t gidx(const Geo& g, int y, int c) {
     return g.fTG ? (size_t)c * g.ny + y : (size_t)y * g.Kxp + c;
@@ -494,7 +496,11 @@ __global__ void __launch_bounds__(512) k_col(Geo g, ColArgs<T> a) {
                     const C acc = a.ACC[s];
                     wn.x = w0.x + c6 * (acc.x + k.x);
                     wn.y = w0.y + c6 * (acc.y + k.y);
-                    if (a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9) {
+                    // FP32/FP64 |k|^2 screen (margin far beyond rounding) before the exact FP64 shell test
+                    const T k2s = kx * kx + ky * ky;
+                    if (a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9 &&
+                        k2s >= (T)(a.sp.f_kmin * a.sp.f_kmin * (1.0 - 1e-3)) &&
+                        k2s <= (T)(a.sp.f_kmax * a.sp.f_kmax * (1.0 + 1e-3))) {
                         // white-in-time forcing increment sigma sqrt(dt) xi (Euler-Maruyama)
                         const double kxd = 2.0 * 3.141592653589793 * i / g.Lx;
                         const double kyd = (j <= g.ny / 2) ? 2.0 * 3.141592653589793 * j / g.Ly
@@ -562,7 +568,7 @@ __global__ void __launch_bounds__(512) k_col(Geo g, ColArgs<T> a) {
         C* dstF = a.F[f];
         for (int idx = threadIdx.x; idx < ny * CW; idx += nthr) {
             int y, c;
-            if (g.fTF) { c = idx / ny; y = idx - c * ny; } else { y = idx / CW; c = idx - y * CW; }
+            if (g.fLB) { c = idx / ny; y = idx - c * ny; } else { y = idx / CW; c = idx - y * CW; }
             dstF[fidx(g, y, c0 + c)] = sm[c * LP + spad(y)];
         }
         __syncthreads();

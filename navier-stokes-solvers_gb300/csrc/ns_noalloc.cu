@@ -67,7 +67,7 @@ static void noalloc_geo(int nx, int ny, Geo& G, int& ER, int& EC) {
     G.logH = l;
     G.Lx = 1.0;
     G.Ly = 1.0;
-    G.fTF = 0;
+    G.fLB = 0;
     G.fTG = 0;
     ER = G.H >= 16 ? 16 : 4;
     EC = ny >= 16 ? 16 : 4;

@@ -24,6 +24,42 @@
 
 namespace nsg {
 
+// ------------------------------------------------------------ streamed loads
+// Global loads that do not allocate in L1: the column pass streams ~50 KB per
+// column through the SM, which would otherwise evict the twiddle and
+// wavenumber tables that every FFT pass re-reads from L1.
+#ifndef NSG_STREAM
+#define NSG_STREAM 1
+#endif
+#if NSG_STREAM
+__device__ __forceinline__ float2 ld_stream(const float2* p) {
+    float2 v;
+    asm("ld.global.L1::no_allocate.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ double2 ld_stream(const double2* p) {
+    double2 v;
+    asm("ld.global.L1::no_allocate.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ float ld_stream(const float* p) {
+    float v;
+    asm("ld.global.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ double ld_stream(const double* p) {
+    double v;
+    asm("ld.global.L1::no_allocate.f64 %0, [%1];" : "=d"(v) : "l"(p));
+    return v;
+}
+#else
+template <typename X> __device__ __forceinline__ X ld_stream(const X* p) { return *p; }
+#endif
+
+// wait until the kernel this one was launched after (programmatic stream
+// serialization) has completed and its writes are visible
+__device__ __forceinline__ void wait_previous_kernel() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // ------------------------------------------------------------------ DFT32
 // cos(pi k/16), k = 0..8
 __device__ __forceinline__ double cpi16(int k) {
@@ -73,19 +109,43 @@ template <bool INV, typename C> __device__ __forceinline__ void dft32(C* a) {
 }
 
 // ============================================================ k_row_w
-// One warp per row (F row-contiguous), persistent over rows; the next field's
-// half spectrum is prefetched into registers while the current one transforms.
-// G is written column-contiguous ([Kx][ny]) for the column pass.
-// dynamic smem: tw [32][33] (W_1024^{t k1}); per warp S [32][33] exchange,
-//               R [1024] (psi_x, then psi_x * omega_y), Q [1024] (psi_y)
+// NW warps per CTA, one row each (rows y0 .. y0 + NW - 1 of a round), persistent
+// over rounds.  F and G are kx-column-contiguous ([Kx][ny]), so the CTA moves
+// them together: thread (kb, w) = (tid / NW, tid % NW) handles columns
+// k = kb + 32 i of row y0 + w, and for each column the NW consecutive rows are
+// one run of NW elements (64 bytes in FP32).  The next field is fetched into
+// registers while the current one transforms, then deposited into the warps'
+// exchange buffers; every other step of a row stays inside its warp.
+// dynamic smem: tw [32][33] (W_1024^{t k1}), twh [1024]; per warp S [32][33]
+//               exchange, R [1024] (psi_x, then psi_x * omega_y), Q [1024] (psi_y);
+//               kx [704]
+#ifndef NSG_RW_WARPS_F32
 #define NSG_RW_WARPS_F32 8
+#endif
 #define NSG_RW_WARPS_F64 3
 #define NSG_RW_KXMAX 704   // kept kx columns at nx = 2048 (684) rounded up to 32
 
+// warps that share rows (and barriers): groups of NSG_RW_GROUP warps in FP32
+// (4 rows x 8 bytes: one 32-byte sector per column), the whole CTA in FP64
+#ifndef NSG_RW_GROUP
+#define NSG_RW_GROUP 4
+#endif
 template <typename T> __host__ __device__ constexpr int rw_warps() { return sizeof(T) == 4 ? NSG_RW_WARPS_F32 : NSG_RW_WARPS_F64; }
+template <typename T> __host__ __device__ constexpr int rw_group() { return sizeof(T) == 4 ? NSG_RW_GROUP : NSG_RW_WARPS_F64; }
+// per-warp block S | R | Q, padded so that group-wide accesses (GW lanes at one
+// offset in the GW warps' S, 32 / GW columns) hit distinct banks
+template <typename T> __host__ __device__ constexpr int rw_wstride() { return 32 * 33 + 2048 + 16 / rw_group<T>(); }
 template <typename T> __host__ __device__ constexpr size_t rw_smem_bytes() {
-    return (size_t)(32 * 33 + 1024 + rw_warps<T>() * (32 * 33 + 2048)) * (sizeof(T) == 4 ? sizeof(float2) : sizeof(double2)) +
+    return (size_t)(32 * 33 + 1024 + rw_warps<T>() * rw_wstride<T>()) * (sizeof(T) == 4 ? sizeof(float2) : sizeof(double2)) +
            (size_t)NSG_RW_KXMAX * sizeof(T);
+}
+// barrier over one group of GW warps (named barrier 1 + group; the CTA barrier when GW is the whole CTA)
+template <int GW, int NW> __device__ __forceinline__ void group_sync(int grp) {
+    if (GW == NW) {
+        __syncthreads();
+    } else {
+        asm volatile("bar.sync %0, %1;" ::"r"(grp + 1), "r"(32 * GW) : "memory");
+    }
 }
 
 // flat index k < 1024 inside a [32][33] exchange buffer
@@ -111,35 +171,42 @@ __device__ __forceinline__ void warp_fft1024(C (&a)[32], C* S, const C* tw, int 
     dft32<INV>(a);
 }
 
-// prefetch X_f[k], k = lane + 32 i < Kx, of one row into registers
+// fetch X_f[k] of row y, k = kb + 32 i < Kx, into registers (F kx-column-contiguous)
 template <typename C>
-__device__ __forceinline__ void row_fetch(C (&pf)[NSG_RW_KXMAX / 32], const C* __restrict__ src, int Kx, int lane) {
+__device__ __forceinline__ void rows_fetch(C (&pf)[NSG_RW_KXMAX / 32], const C* __restrict__ src, size_t ny, int y,
+                                           bool ok, int kb, int Kx) {
 #pragma unroll
     for (int i = 0; i < NSG_RW_KXMAX / 32; ++i) {
-        const int k = lane + 32 * i;
-        pf[i] = (k < Kx) ? __ldg(&src[k]) : cmake<C>(0.0, 0.0);
+        const int k = kb + 32 * i;
+        pf[i] = (ok && k < Kx) ? __ldg(&src[(size_t)k * ny + y]) : cmake<C>(0.0, 0.0);
     }
 }
 
-// stage the fetched half spectrum (times i kx when dx) in S and pack the
-// half-length inverse input Z[lane + 32 n1] = (X[k] + conj X[H-k]) + i e^{+2 pi i k/nx} (X[k] - conj X[H-k])
+// deposit the fetched values (times i kx when dx) into row w's exchange buffer Sw
 template <typename T, typename C>
-__device__ __forceinline__ void row_pack(C (&a)[32], const C (&pf)[NSG_RW_KXMAX / 32], C* S, int dx,
-                                         const T* kxv, const C* twh, int Kx, int lane) {
+__device__ __forceinline__ void rows_deposit(const C (&pf)[NSG_RW_KXMAX / 32], C* Sw, int dx, const T* kxv, int kb,
+                                             int Kx) {
 #pragma unroll
     for (int i = 0; i < NSG_RW_KXMAX / 32; ++i) {
-        const int k = lane + 32 * i;
-        C x = pf[i];
-        if (dx && k < Kx) {
-            const T kx = kxv[k];
-            C d;
-            d.x = -kx * x.y;
-            d.y = kx * x.x;
-            x = d;
+        const int k = kb + 32 * i;
+        if (k < Kx) {
+            C x = pf[i];
+            if (dx) {
+                const T kx = kxv[k];
+                C d;
+                d.x = -kx * x.y;
+                d.y = kx * x.x;
+                x = d;
+            }
+            Sw[i * 33 + kb] = x;
         }
-        if (k < Kx) S[sx(k)] = x;
     }
-    __syncwarp();
+}
+
+// pack the half-length inverse input Z[lane + 32 n1] = (X[k] + conj X[H-k]) + i e^{+2 pi i k/nx} (X[k] - conj X[H-k])
+// from the half spectrum X[k], k < Kx, held in S
+template <typename T, typename C>
+__device__ __forceinline__ void row_pack(C (&a)[32], const C* S, const C* twh, int Kx, int lane) {
 #pragma unroll
     for (int n1 = 0; n1 < 32; ++n1) {
         const int k = lane + 32 * n1;
@@ -163,17 +230,34 @@ template <typename T>
 __global__ void __launch_bounds__(32 * rw_warps<T>(), 1) k_row_w(Geo g, RowArgs<T> a) {
     typedef typename CT<T>::C C;
     constexpr int NW = rw_warps<T>();
+    constexpr int GW = rw_group<T>();
+    constexpr int WS = rw_wstride<T>();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* tw = reinterpret_cast<C*>(smem_raw);
     C* twh_s = tw + 32 * 33;                          // exp(-2 pi i k/nx), k < 1024
-    C* S = twh_s + 1024 + (threadIdx.x >> 5) * (32 * 33 + 2048);
-    T* kx_s = reinterpret_cast<T*>(twh_s + 1024 + NW * (32 * 33 + 2048));
+    C* S0 = twh_s + 1024;                             // warp w's block at S0 + w * WS
+    T* kx_s = reinterpret_cast<T*>(twh_s + 1024 + NW * WS);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    C* S = S0 + warp * WS;
     C* R = S + 32 * 33;
     C* Q = R + 1024;
-    const int Kx = g.Kx, Kxp = g.Kxp, ny = g.ny;
-    (void)warp;
+    const int Kx = g.Kx, ny = g.ny;
+    // group grp owns rows y0 + GW grp + w (w < GW); thread (kb, wme) of the group
+    // moves columns kb + 32 i of row wme
+    const int grp = warp / GW;
+    const int tg = threadIdx.x - grp * 32 * GW;
+    const int kb = tg / GW, wme = tg - kb * GW;
+    C* Sg = S0 + grp * GW * WS;                       // the group's first warp block
+    C* Sme = Sg + wme * WS;
 
+    // constant tables first (they do not depend on the previous kernel)
+    for (int i = threadIdx.x; i < 1024; i += blockDim.x) {
+        const int k1 = i >> 5, t = i & 31;
+        tw[k1 * 33 + t] = a.twr[t * k1];
+        twh_s[i] = a.twh[i];
+    }
+    for (int i = threadIdx.x; i < NSG_RW_KXMAX; i += blockDim.x) kx_s[i] = (i < Kx) ? a.kxv[i] : (T)0;
+    wait_previous_kernel();
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (a.marker == 1) {
             a.ds->step_cur = a.ds->step_next;
@@ -182,77 +266,88 @@ __global__ void __launch_bounds__(32 * rw_warps<T>(), 1) k_row_w(Geo g, RowArgs<
             a.ds->maxvel2 = 0ULL;
         }
     }
-    for (int i = threadIdx.x; i < 1024; i += blockDim.x) {
-        const int k1 = i >> 5, t = i & 31;
-        tw[k1 * 33 + t] = a.twr[t * k1];
-        twh_s[i] = a.twh[i];
-    }
-    for (int i = threadIdx.x; i < NSG_RW_KXMAX; i += blockDim.x) kx_s[i] = (i < Kx) ? a.kxv[i] : (T)0;
-    __syncthreads();
 
     // field order q = 0..3: psi_x (F[0], d/dx), psi_y (F[1]), omega_y (F[3]), omega_x (F[2], d/dx)
     T vmax2 = (T)0;
     C v[32];
     C pf[NSG_RW_KXMAX / 32];
     const int ystep = gridDim.x * NW;
-    int y = blockIdx.x * NW + warp;
-    if (y < ny) row_fetch(pf, a.F[0] + (size_t)y * Kxp, Kx, lane);
-    for (; y < ny; y += ystep) {
-        const size_t roff = (size_t)y * Kxp;
+    __syncthreads();  // tables in place
+    int y0 = blockIdx.x * NW + grp * GW;  // this group's first row of the round
+    rows_fetch(pf, a.F[0], (size_t)ny, y0 + wme, y0 + wme < ny, kb, Kx);
+    for (; y0 < ny; y0 += ystep) {
+        const int y = y0 + (warp - grp * GW);
 #pragma unroll 1
         for (int q = 0; q < 4; ++q) {
             const int f = (q < 2) ? q : 5 - q;
             const int dx = (f == 0 || f == 2);
-            row_pack<T>(v, pf, S, dx, kx_s, twh_s, Kx, lane);
-            // prefetch the next field (or the next row's psi_x) while this one transforms
-            if (q < 3) row_fetch(pf, a.F[(q + 1 < 2) ? q + 1 : 4 - q] + roff, Kx, lane);
-            else if (y + ystep < ny) row_fetch(pf, a.F[0] + (size_t)(y + ystep) * Kxp, Kx, lane);
-            warp_fft1024<true>(v, S, tw, lane);
-            if (q == 0) {
-#pragma unroll
-                for (int k = 0; k < 32; ++k) R[lane + 32 * k] = v[k];
-            } else if (q == 1) {
-#pragma unroll
-                for (int k = 0; k < 32; ++k) {
-                    if (a.cfl) {
-                        const C px = R[lane + 32 * k];
-                        vmax2 = fmax(vmax2, fmax(px.x * px.x + v[k].x * v[k].x, px.y * px.y + v[k].y * v[k].y));
-                    }
-                    Q[lane + 32 * k] = v[k];
-                }
-            } else if (q == 2) {
-#pragma unroll
-                for (int k = 0; k < 32; ++k) {
-                    const C px = R[lane + 32 * k];
-                    R[lane + 32 * k] = cmake<C>(px.x * v[k].x, px.y * v[k].y);
-                }
+            group_sync<GW, NW>(grp);  // every warp of the group is done with its exchange buffer
+            rows_deposit<T>(pf, Sme, dx, kx_s, kb, Kx);
+            group_sync<GW, NW>(grp);
+            // fetch the next field (or the next round's psi_x) while this one transforms
+            if (q < 3) {
+                rows_fetch(pf, a.F[(q + 1 < 2) ? q + 1 : 4 - q], (size_t)ny, y0 + wme, y0 + wme < ny, kb, Kx);
             } else {
-                // J = psi_x omega_y - psi_y omega_x, packed as w[m] = J[2m] + i J[2m+1]
+                const int yn = y0 + ystep + wme;
+                rows_fetch(pf, a.F[0], (size_t)ny, yn, yn < ny, kb, Kx);
+            }
+            if (y < ny) {
+                row_pack<T>(v, S, twh_s, Kx, lane);
+                warp_fft1024<true>(v, S, tw, lane);
+                if (q == 0) {
 #pragma unroll
-                for (int k = 0; k < 32; ++k) {
-                    const C p = R[lane + 32 * k];
-                    const C py = Q[lane + 32 * k];
-                    v[k] = cmake<C>(p.x - py.x * v[k].x, p.y - py.y * v[k].y);
+                    for (int k = 0; k < 32; ++k) R[lane + 32 * k] = v[k];
+                } else if (q == 1) {
+#pragma unroll
+                    for (int k = 0; k < 32; ++k) {
+                        if (a.cfl) {
+                            const C px = R[lane + 32 * k];
+                            vmax2 = fmax(vmax2, fmax(px.x * px.x + v[k].x * v[k].x, px.y * px.y + v[k].y * v[k].y));
+                        }
+                        Q[lane + 32 * k] = v[k];
+                    }
+                } else if (q == 2) {
+#pragma unroll
+                    for (int k = 0; k < 32; ++k) {
+                        const C px = R[lane + 32 * k];
+                        R[lane + 32 * k] = cmake<C>(px.x * v[k].x, px.y * v[k].y);
+                    }
+                } else {
+                    // J = psi_x omega_y - psi_y omega_x, packed as w[m] = J[2m] + i J[2m+1]
+#pragma unroll
+                    for (int k = 0; k < 32; ++k) {
+                        const C p = R[lane + 32 * k];
+                        const C py = Q[lane + 32 * k];
+                        v[k] = cmake<C>(p.x - py.x * v[k].x, p.y - py.y * v[k].y);
+                    }
                 }
             }
         }
-        // forward half-length transform of J, then unpack the kept kx < Kx
-        warp_fft1024<false>(v, S, tw, lane);
+        if (y < ny) {
+            // forward half-length transform of J
+            warp_fft1024<false>(v, S, tw, lane);
 #pragma unroll
-        for (int k = 0; k < 32; ++k) S[k * 33 + lane] = v[k];
-        __syncwarp();
+            for (int k = 0; k < 32; ++k) S[k * 33 + lane] = v[k];
+        }
+        group_sync<GW, NW>(grp);
+        // unpack the kept kx < Kx of the group's GW rows together: element e is
+        // (k = e / GW, row y0 + e % GW), so consecutive threads write the GW
+        // consecutive rows of one G column
         const T half = (T)0.5;
-        for (int k = lane; k < Kx; k += 32) {
-            const C wa = S[sx(k)];
-            const C wb = S[sx((1024 - k) & 1023)];
+        const int nrows = (ny - y0 < GW) ? ny - y0 : GW;
+        for (int e = tg; e < Kx * GW; e += 32 * GW) {
+            const int k = e / GW, w = e - k * GW;
+            if (w >= nrows) continue;
+            const C* Sw = Sg + w * WS;
+            const C wa = Sw[sx(k)];
+            const C wb = Sw[sx((1024 - k) & 1023)];
             C ev, od;
             ev.x = half * (wa.x + wb.x);
             ev.y = half * (wa.y - wb.y);
             od.x = half * (wa.y + wb.y);
             od.y = -half * (wa.x - wb.x);
-            a.G[(size_t)k * ny + y] = cadd(ev, cmul(od, twh_s[k]));
+            a.G[(size_t)k * ny + y0 + w] = cadd(ev, cmul(od, twh_s[k]));
         }
-        __syncwarp();
     }
     if (a.cfl) {
         const double vm = warp_max((double)vmax2);
@@ -350,16 +445,24 @@ __device__ __noinline__ double2 forcing_increment(const Geo& g, int i, int j, un
     return make_double2(amp * rad * cs, amp * (flip ? -rad * sn : rad * sn));
 }
 
-// one kept kx column per CTA (64 threads); G and F columns are contiguous, so
-// layout-A values x[64 n1 + t] load and store straight from and to global memory
+// one kept kx column per CTA (64 threads); layout-A values x[64 n1 + t] load
+// straight from the contiguous G column and store straight to F
 #define NSG_CW_EX 2112
+// resident CTAs per SM the FP32 column kernel is compiled for, and modes per
+// batch of its RK epilogue loads
+#ifndef NSG_CW_MINB
+#define NSG_CW_MINB 6
+#endif
+#ifndef NSG_CW_NB
+#define NSG_CW_NB 4
+#endif
 
 template <typename T> __host__ __device__ constexpr size_t cw_smem_bytes2(int Ky) {
     return (size_t)(NSG_CW_EX + 2048) * (sizeof(T) == 4 ? sizeof(float2) : sizeof(double2));
 }
 
 template <typename T, int STAGE>
-__global__ void __launch_bounds__(64, (sizeof(T) == 4 ? 6 : 3)) k_col_w(Geo g, ColArgs<T> a) {
+__global__ void __launch_bounds__(64, (sizeof(T) == 4 ? NSG_CW_MINB : 3)) k_col_w(Geo g, ColArgs<T> a) {
     typedef typename CT<T>::C C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* ex = reinterpret_cast<C*>(smem_raw);
@@ -371,6 +474,7 @@ __global__ void __launch_bounds__(64, (sizeof(T) == 4 ? 6 : 3)) k_col_w(Geo g, C
     const int Ky = g.Ky;
     __shared__ double s_dt;
 
+    wait_previous_kernel();
     if (t == 0) {
         double dt;
         if (STAGE == 1) {
@@ -391,128 +495,136 @@ __global__ void __launch_bounds__(64, (sizeof(T) == 4 ? 6 : 3)) k_col_w(Geo g, C
         s_dt = dt;
     }
     C v[32];
-    const C* __restrict__ Gc = a.G + (size_t)i * 2048;
-#pragma unroll
-    for (int n1 = 0; n1 < 32; ++n1) v[n1] = __ldg(&Gc[64 * n1 + t]);
     __syncthreads();
-    col_fwd2048(v, ex, tw, t, lane, h);
-
-    // RK stage algebra (spectral_time_integration.c:50-100) on this thread's modes j = lane + 32 k2 + 1024 h
-    const double dt = s_dt;
-    const T inv_re = (T)a.sp.inv_re;
-    const T sc = (T)a.sp.scale;
-    const T cst = (STAGE == 1 || STAGE == 2) ? (T)(0.5 * dt) : (STAGE == 3 ? (T)dt : (T)(dt / 6.0));
     const T kx = __ldg(&a.kxv[i]);
-    C* __restrict__ W0 = a.W0;
-    C* __restrict__ WS = a.WS;
-    C* __restrict__ ACC = a.ACC;
-    const int hv = a.sp.hv, sfd = a.sp.sfd;
-    // NB modes at a time: issue every load of the batch, then compute and store
-    constexpr int NB = 4;
+    {
+        const C* __restrict__ Gc = a.G + (size_t)i * 2048;
 #pragma unroll
-    for (int b0 = 0; b0 < 32; b0 += NB) {
-        C w0v[NB], wsv[NB], acv[NB], fbv[NB];
-        T hwv[NB], swv[NB];
-        int jjv[NB];
-#pragma unroll
-        for (int u = 0; u < NB; ++u) {
-            const int j = lane + 32 * (b0 + u) + 1024 * h;
-            const int jj = kept_jj(g, j);
-            jjv[u] = jj;
-            const size_t s = (size_t)i * Ky + (jj < 0 ? 0 : jj);
-            const bool ok = jj >= 0;
-            const C zero = cmake<C>(0.0, 0.0);
-            w0v[u] = ok ? ((STAGE == 4) ? W0[s] : __ldg(&W0[s])) : zero;
-            wsv[u] = (STAGE == 1) ? w0v[u] : (ok ? ((STAGE == 4) ? __ldg(&WS[s]) : WS[s]) : zero);
-            acv[u] = (STAGE == 1) ? zero : (ok ? ((STAGE == 4) ? __ldg(&ACC[s]) : ACC[s]) : zero);
-            hwv[u] = (hv && ok) ? __ldg(&a.hvw[s]) : (T)0;
-            swv[u] = (sfd && ok) ? __ldg(&a.sfdw[s]) : (T)0;
-            fbv[u] = (sfd && ok) ? a.SFD[s] : zero;
-        }
-#pragma unroll
-        for (int u = 0; u < NB; ++u) {
-            const int jj = jjv[u];
-            const int k2 = b0 + u;
-            if (jj < 0) {
-                wb[k2 * 64 + t] = cmake<C>(0.0, 0.0);
-                continue;
-            }
-            const size_t s = (size_t)i * Ky + jj;
-            const C w0 = w0v[u], ws = wsv[u];
-            const T ky = __ldg(&kys[jj]);
-            const T k2v = k2sum(kx, ky);
-            C k;
-            k.x = -(v[k2].x * sc) - k2v * ws.x * inv_re;
-            k.y = -(v[k2].y * sc) - k2v * ws.y * inv_re;
-            if (hv || sfd) {
-                C damp = cmake<C>(0.0, 0.0);
-                if (hv) { damp.x += hwv[u] * ws.x; damp.y += hwv[u] * ws.y; }
-                if (sfd && swv[u] > (T)0) {
-                    damp.x += swv[u] * (ws.x - fbv[u].x);
-                    damp.y += swv[u] * (ws.y - fbv[u].y);
-                }
-                k.x -= damp.x;
-                k.y -= damp.y;
-            }
-            C wn;
-            if (STAGE == 1) {
-                ACC[s] = k;
-                wn.x = w0.x + cst * k.x; wn.y = w0.y + cst * k.y;
-                WS[s] = wn;
-            } else if (STAGE == 2 || STAGE == 3) {
-                C acc = acv[u];
-                acc.x = acc.x + (T)2 * k.x;
-                acc.y = acc.y + (T)2 * k.y;
-                ACC[s] = acc;
-                wn.x = w0.x + cst * k.x; wn.y = w0.y + cst * k.y;
-                WS[s] = wn;
-            } else {
-                const C acc = acv[u];
-                wn.x = w0.x + cst * (acc.x + k.x);
-                wn.y = w0.y + cst * (acc.y + k.y);
-                W0[s] = wn;
-            }
-            wb[k2 * 64 + t] = wn;
-        }
-    }
-    if (STAGE == 4 && (a.sp.forcing || sfd)) {
-        // forcing increment (few low-|k| modes), then the SFD post-step, on omega_hat^{n+1}
-        const double f_amp = a.sp.forcing ? a.sp.f_sigma * sqrt(dt) : 0.0;
-        double sa = 0.0;
-        if (sfd) {
-            sa = dt / a.sp.sfd_tau;
-            sa = sa > 1.0 ? 1.0 : (sa < 0.0 ? 0.0 : sa);
-        }
-        const bool force_col = a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9;
-#pragma unroll 1
-        for (int k2 = 0; k2 < 32; ++k2) {
-            const int j = lane + 32 * k2 + 1024 * h;
-            const int jj = kept_jj(g, j);
-            if (jj < 0) continue;
-            const size_t s = (size_t)i * Ky + jj;
-            C wn = wb[k2 * 64 + t];
-            if (force_col) {
-                const double2 df =
-                    forcing_increment(g, i, j, a.ds->step_cur, a.sp.f_seed, a.sp.f_kmin, a.sp.f_kmax, f_amp);
-                if (df.x != 0.0 || df.y != 0.0) {
-                    wn.x = (T)((double)wn.x + df.x);
-                    wn.y = (T)((double)wn.y + df.y);
-                    W0[s] = wn;
-                    wb[k2 * 64 + t] = wn;
-                }
-            }
-            if (sfd) {
-                C fb = a.SFD[s];
-                const T al = (T)sa, om = (T)(1.0 - sa);
-                fb.x = om * fb.x + al * wn.x;
-                fb.y = om * fb.y + al * wn.y;
-                a.SFD[s] = fb;
-            }
-        }
-    }
-    if (STAGE == 4 && blockIdx.x == 0 && t == 0) a.ds->t = a.ds->t + dt;
+        for (int n1 = 0; n1 < 32; ++n1) v[n1] = ld_stream(&Gc[64 * n1 + t]);
+        col_fwd2048(v, ex, tw, t, lane, h);
 
-    // inverse y-transforms of the next stage's Psi, Psi_y, Omega, Omega_y
+        // RK stage algebra (spectral_time_integration.c:50-100) on this thread's modes j = lane + 32 k2 + 1024 h
+        const double dt = s_dt;
+        const T inv_re = (T)a.sp.inv_re;
+        const T sc = (T)a.sp.scale;
+        const T cst = (STAGE == 1 || STAGE == 2) ? (T)(0.5 * dt) : (STAGE == 3 ? (T)dt : (T)(dt / 6.0));
+        C* __restrict__ W0 = a.W0;
+        C* __restrict__ WS = a.WS;
+        C* __restrict__ ACC = a.ACC;
+        const int hv = a.sp.hv, sfd = a.sp.sfd;
+        // NB modes at a time: issue every load of the batch, then compute and store
+        constexpr int NB = NSG_CW_NB;
+#pragma unroll
+        for (int b0 = 0; b0 < 32; b0 += NB) {
+            C w0v[NB], wsv[NB], acv[NB], fbv[NB];
+            T hwv[NB], swv[NB];
+            int jjv[NB];
+#pragma unroll
+            for (int u = 0; u < NB; ++u) {
+                const int j = lane + 32 * (b0 + u) + 1024 * h;
+                const int jj = kept_jj(g, j);
+                jjv[u] = jj;
+                const size_t s = (size_t)i * Ky + (jj < 0 ? 0 : jj);
+                const bool ok = jj >= 0;
+                const C zero = cmake<C>(0.0, 0.0);
+                w0v[u] = ok ? ld_stream(&W0[s]) : zero;
+                wsv[u] = (STAGE == 1) ? w0v[u] : (ok ? ld_stream(&WS[s]) : zero);
+                acv[u] = (STAGE == 1) ? zero : (ok ? ld_stream(&ACC[s]) : zero);
+                hwv[u] = (hv && ok) ? ld_stream(&a.hvw[s]) : (T)0;
+                swv[u] = (sfd && ok) ? ld_stream(&a.sfdw[s]) : (T)0;
+                fbv[u] = (sfd && ok) ? ld_stream(&a.SFD[s]) : zero;
+            }
+#pragma unroll
+            for (int u = 0; u < NB; ++u) {
+                const int jj = jjv[u];
+                const int k2 = b0 + u;
+                if (jj < 0) {
+                    wb[k2 * 64 + t] = cmake<C>(0.0, 0.0);
+                    continue;
+                }
+                const size_t s = (size_t)i * Ky + jj;
+                const C w0 = w0v[u], ws = wsv[u];
+                const T ky = __ldg(&kys[jj]);
+                const T k2v = k2sum(kx, ky);
+                C k;
+                k.x = -(v[k2].x * sc) - k2v * ws.x * inv_re;
+                k.y = -(v[k2].y * sc) - k2v * ws.y * inv_re;
+                if (hv || sfd) {
+                    C damp = cmake<C>(0.0, 0.0);
+                    if (hv) { damp.x += hwv[u] * ws.x; damp.y += hwv[u] * ws.y; }
+                    if (sfd && swv[u] > (T)0) {
+                        damp.x += swv[u] * (ws.x - fbv[u].x);
+                        damp.y += swv[u] * (ws.y - fbv[u].y);
+                    }
+                    k.x -= damp.x;
+                    k.y -= damp.y;
+                }
+                C wn;
+                if (STAGE == 1) {
+                    ACC[s] = k;
+                    wn.x = w0.x + cst * k.x; wn.y = w0.y + cst * k.y;
+                    WS[s] = wn;
+                } else if (STAGE == 2 || STAGE == 3) {
+                    C acc = acv[u];
+                    acc.x = acc.x + (T)2 * k.x;
+                    acc.y = acc.y + (T)2 * k.y;
+                    ACC[s] = acc;
+                    wn.x = w0.x + cst * k.x; wn.y = w0.y + cst * k.y;
+                    WS[s] = wn;
+                } else {
+                    const C acc = acv[u];
+                    wn.x = w0.x + cst * (acc.x + k.x);
+                    wn.y = w0.y + cst * (acc.y + k.y);
+                    W0[s] = wn;
+                }
+                wb[k2 * 64 + t] = wn;
+            }
+        }
+        if (STAGE == 4 && (a.sp.forcing || sfd)) {
+            // forcing increment (few low-|k| modes), then the SFD post-step, on omega_hat^{n+1}
+            const double f_amp = a.sp.forcing ? a.sp.f_sigma * sqrt(dt) : 0.0;
+            double sa = 0.0;
+            if (sfd) {
+                sa = dt / a.sp.sfd_tau;
+                sa = sa > 1.0 ? 1.0 : (sa < 0.0 ? 0.0 : sa);
+            }
+            const bool force_col = a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9;
+            // |k|^2 window, widened far beyond FP32 rounding, that screens modes before the exact FP64 shell test
+            const T k2lo = (T)(a.sp.f_kmin * a.sp.f_kmin * (1.0 - 1e-3));
+            const T k2hi = (T)(a.sp.f_kmax * a.sp.f_kmax * (1.0 + 1e-3));
+#pragma unroll 1
+            for (int k2 = 0; k2 < 32 && (force_col || sfd); ++k2) {
+                const int j = lane + 32 * k2 + 1024 * h;
+                const int jj = kept_jj(g, j);
+                if (jj < 0) continue;
+                const size_t s = (size_t)i * Ky + jj;
+                C wn = wb[k2 * 64 + t];
+                const T ky = __ldg(&kys[jj]);
+                const T k2f = kx * kx + ky * ky;
+                if (force_col && k2f >= k2lo && k2f <= k2hi) {
+                    const double2 df =
+                        forcing_increment(g, i, j, a.ds->step_cur, a.sp.f_seed, a.sp.f_kmin, a.sp.f_kmax, f_amp);
+                    if (df.x != 0.0 || df.y != 0.0) {
+                        wn.x = (T)((double)wn.x + df.x);
+                        wn.y = (T)((double)wn.y + df.y);
+                        W0[s] = wn;
+                        wb[k2 * 64 + t] = wn;
+                    }
+                }
+                if (sfd) {
+                    C fb = a.SFD[s];
+                    const T al = (T)sa, om = (T)(1.0 - sa);
+                    fb.x = om * fb.x + al * wn.x;
+                    fb.y = om * fb.y + al * wn.y;
+                    a.SFD[s] = fb;
+                }
+            }
+        }
+        if (STAGE == 4 && blockIdx.x == 0 && t == 0) a.ds->t = a.ds->t + dt;
+    }
+
+    // inverse y-transforms of the next stage's Psi, Psi_y, Omega, Omega_y; F is
+    // kx-column-contiguous, so each column leaves as whole 256-byte runs
 #pragma unroll 1
     for (int f = 0; f < 4; ++f) {
 #pragma unroll
@@ -524,10 +636,9 @@ __global__ void __launch_bounds__(64, (sizeof(T) == 4 ? 6 : 3)) k_col_w(Geo g, C
             v[k2] = x;
         }
         col_inv2048(v, ex, tw, t, lane, h);
-        C* __restrict__ Fc = a.F[f] + i;  // F row-contiguous: column i of [ny][Kxp]
-        const int Kxp = g.Kxp;
+        C* __restrict__ Fc = a.F[f] + (size_t)i * 2048;
 #pragma unroll
-        for (int n1 = 0; n1 < 32; ++n1) Fc[(size_t)(64 * n1 + t) * Kxp] = v[n1];
+        for (int n1 = 0; n1 < 32; ++n1) Fc[64 * n1 + t] = v[n1];
     }
 }
 
