@@ -63,7 +63,14 @@ typedef struct {
     double forcing_kmax;
     double forcing_epsilon;
     uint64_t forcing_seed;
+    /* time scheme: NS_GPU_RK4 (the reference's classical RK4,
+     * spectral_time_integration.c:34-106) or NS_GPU_IFRK4 (integrating-factor
+     * RK4: viscous and hyperviscous decay exp(-(k^2/Re + w) t) integrated
+     * exactly, the Jacobian and SFD relaxation explicit; no reference counterpart) */
+    int scheme;
 } ns_gpu_params;
+
+enum { NS_GPU_RK4 = 0, NS_GPU_IFRK4 = 1 };
 
 /* ----------------------------------------------------------- lifetime */
 

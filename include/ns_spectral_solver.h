@@ -154,6 +154,13 @@ int ns_spectral_gpu_sync_host(NSSpectralData *data);
  * (Philox4x64-10 keyed by seed), applied after each RK4 step */
 int ns_spectral_gpu_set_forcing(NSSpectralData *data, int enabled, double kmin, double kmax, double epsilon,
                                 unsigned long long seed);
+/* time scheme of ns_spectral_advance_rk4 and ns_spectral_gpu_advance_n:
+ * NS_SPECTRAL_SCHEME_RK4 (default: the reference's classical RK4) or
+ * NS_SPECTRAL_SCHEME_IFRK4 (integrating-factor RK4, viscous and hyperviscous
+ * decay integrated exactly; no reference counterpart) */
+#define NS_SPECTRAL_SCHEME_RK4 0
+#define NS_SPECTRAL_SCHEME_IFRK4 1
+int ns_spectral_gpu_set_scheme(NSSpectralData *data, int scheme);
 /* Parseval energy and enstrophy of the device state (FP64 compensated);
  * SOLVER_DIVERGED when the state holds non-finite values */
 int ns_spectral_gpu_diagnostics(NSSpectralData *data, double *energy, double *enstrophy);

@@ -198,6 +198,7 @@ template <typename T> static StepParams step_params(const ns_gpu* g) {
     sp.f_kmax = g->p.forcing_kmax;
     sp.f_sigma = g->f_sigma;
     sp.f_seed = g->p.forcing_seed;
+    sp.ifrk = g->p.scheme == NS_GPU_IFRK4 ? 1 : 0;
     return sp;
 }
 
@@ -268,8 +269,9 @@ template <typename T, int STAGE> static int stage_col(ns_gpu* g, const ColArgs<T
     ProfScope ps(g, 1);
     if (g->fast_col) {
         const size_t smem = cw_smem_bytes2<T>(g->g.Ky);
-        NSG_TRY(set_smem(g, k_col_w<T, STAGE>, smem));
-        const cudaError_t e = launch_stage(k_col_w<T, STAGE>, g->g.Kx, 64, smem, g->st, g->g, a);
+        auto kern = a.sp.ifrk ? k_col_w<T, STAGE, true> : k_col_w<T, STAGE, false>;
+        NSG_TRY(set_smem(g, kern, smem));
+        const cudaError_t e = launch_stage(kern, g->g.Kx, 64, smem, g->st, g->g, a);
         if (e != cudaSuccess) NSG_FAIL(g, NS_GPU_ERR_CUDA, "k_col_w launch: %s", cudaGetErrorString(e));
         NSG_LAUNCHED(g);
         return NS_GPU_OK;
@@ -618,6 +620,8 @@ int ns_gpu_synchronize(ns_gpu* g) {
 int ns_gpu_set_params(ns_gpu* g, const ns_gpu_params* p) {
     if (!g || !p) return NS_GPU_ERR_INVALID;
     if (!(p->Re > 0.0)) NSG_FAIL(g, NS_GPU_ERR_INVALID, "Re must be positive (got %g)", p->Re);
+    if (p->scheme != NS_GPU_RK4 && p->scheme != NS_GPU_IFRK4)
+        NSG_FAIL(g, NS_GPU_ERR_INVALID, "unknown time scheme %d", p->scheme);
     const int hv_changed = !g->params_set || p->hv_enabled != g->p.hv_enabled || p->hv_coefficient != g->p.hv_coefficient ||
                            p->hv_order != g->p.hv_order || p->hv_cutoff_ratio != g->p.hv_cutoff_ratio ||
                            p->sfd_enabled != g->p.sfd_enabled || p->sfd_strength != g->p.sfd_strength;

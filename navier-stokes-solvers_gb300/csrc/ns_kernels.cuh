@@ -75,6 +75,7 @@ struct DevScalars {
 struct StepParams {
     double inv_re, Re, cfl, dxmin, scale;
     int adaptive, hv, sfd, forcing;
+    int ifrk;  // 1: integrating-factor RK4 stage algebra
     double sfd_tau;
     double f_kmin, f_kmax, f_sigma;
     unsigned long long f_seed;
@@ -462,40 +463,75 @@ __global__ void __launch_bounds__(512) k_col(Geo g, ColArgs<T> a) {
                 const C ws = (STAGE == 1) ? w0 : a.WS[s];
                 const T kx = a.kxv[i], ky = a.kyv[jj];
                 const T k2 = k2sum(kx, ky);
-                C k;  // k = N - k^2 omega / Re - damping (spectral_time_integration.c:50-54)
-                k.x = nl.x - k2 * ws.x * inv_re;
-                k.y = nl.y - k2 * ws.y * inv_re;
-                if (a.sp.hv || a.sp.sfd) {
-                    C damp = cmake<C>(0.0, 0.0);
-                    if (a.sp.hv) { const T w = a.hvw[s]; damp.x += w * ws.x; damp.y += w * ws.y; }
+                C wn;
+                if (a.sp.ifrk) {
+                    // integrating-factor RK4: explicit part N - SFD relaxation, decay
+                    // lam = k^2/Re + w integrated by E1 = exp(-lam dt/2), E2 = E1^2
+                    C k = nl;
                     if (a.sp.sfd) {
                         const T sw = a.sfdw[s];
                         if (sw > (T)0) {
                             const C fb = a.SFD[s];
-                            damp.x += sw * (ws.x - fb.x);
-                            damp.y += sw * (ws.y - fb.y);
+                            k.x -= sw * (ws.x - fb.x);
+                            k.y -= sw * (ws.y - fb.y);
                         }
                     }
-                    k.x -= damp.x;
-                    k.y -= damp.y;
-                }
-                C wn;
-                if (STAGE == 1) {
-                    a.ACC[s] = k;
-                    wn.x = w0.x + ch * k.x; wn.y = w0.y + ch * k.y;
-                    a.WS[s] = wn;
-                } else if (STAGE == 2 || STAGE == 3) {
-                    C acc = a.ACC[s];
-                    acc.x = acc.x + (T)2 * k.x;
-                    acc.y = acc.y + (T)2 * k.y;
-                    a.ACC[s] = acc;
-                    const T cc = (STAGE == 2) ? ch : cf;
-                    wn.x = w0.x + cc * k.x; wn.y = w0.y + cc * k.y;
-                    a.WS[s] = wn;
+                    const T lam = k2 * inv_re + (a.sp.hv ? a.hvw[s] : (T)0);
+                    const T e1 = exp(-lam * ch), e2 = e1 * e1;
+                    if (STAGE == 1) {
+                        a.ACC[s] = cmake<C>(e2 * k.x, e2 * k.y);
+                        wn.x = e1 * (w0.x + ch * k.x); wn.y = e1 * (w0.y + ch * k.y);
+                        a.WS[s] = wn;
+                    } else if (STAGE == 2 || STAGE == 3) {
+                        C acc = a.ACC[s];
+                        acc.x = acc.x + (T)2 * (e1 * k.x);
+                        acc.y = acc.y + (T)2 * (e1 * k.y);
+                        a.ACC[s] = acc;
+                        if (STAGE == 2) { wn.x = e1 * w0.x + ch * k.x; wn.y = e1 * w0.y + ch * k.y; }
+                        else { wn.x = e2 * w0.x + cf * (e1 * k.x); wn.y = e2 * w0.y + cf * (e1 * k.y); }
+                        a.WS[s] = wn;
+                    } else {
+                        const C acc = a.ACC[s];
+                        wn.x = e2 * w0.x + c6 * (acc.x + k.x);
+                        wn.y = e2 * w0.y + c6 * (acc.y + k.y);
+                    }
                 } else {
-                    const C acc = a.ACC[s];
-                    wn.x = w0.x + c6 * (acc.x + k.x);
-                    wn.y = w0.y + c6 * (acc.y + k.y);
+                    C k;  // k = N - k^2 omega / Re - damping (spectral_time_integration.c:50-54)
+                    k.x = nl.x - k2 * ws.x * inv_re;
+                    k.y = nl.y - k2 * ws.y * inv_re;
+                    if (a.sp.hv || a.sp.sfd) {
+                        C damp = cmake<C>(0.0, 0.0);
+                        if (a.sp.hv) { const T w = a.hvw[s]; damp.x += w * ws.x; damp.y += w * ws.y; }
+                        if (a.sp.sfd) {
+                            const T sw = a.sfdw[s];
+                            if (sw > (T)0) {
+                                const C fb = a.SFD[s];
+                                damp.x += sw * (ws.x - fb.x);
+                                damp.y += sw * (ws.y - fb.y);
+                            }
+                        }
+                        k.x -= damp.x;
+                        k.y -= damp.y;
+                    }
+                    if (STAGE == 1) {
+                        a.ACC[s] = k;
+                        wn.x = w0.x + ch * k.x; wn.y = w0.y + ch * k.y;
+                        a.WS[s] = wn;
+                    } else if (STAGE == 2 || STAGE == 3) {
+                        C acc = a.ACC[s];
+                        acc.x = acc.x + (T)2 * k.x;
+                        acc.y = acc.y + (T)2 * k.y;
+                        a.ACC[s] = acc;
+                        const T cc = (STAGE == 2) ? ch : cf;
+                        wn.x = w0.x + cc * k.x; wn.y = w0.y + cc * k.y;
+                        a.WS[s] = wn;
+                    } else {
+                        const C acc = a.ACC[s];
+                        wn.x = w0.x + c6 * (acc.x + k.x);
+                        wn.y = w0.y + c6 * (acc.y + k.y);
+                    }
+                }
+                if (STAGE == 4) {
                     // FP32/FP64 |k|^2 screen (margin far beyond rounding) before the exact FP64 shell test
                     const T k2s = kx * kx + ky * ky;
                     if (a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9 &&
@@ -819,24 +855,47 @@ __global__ void k_outside(Geo g, StepParams sp, const double* w_full, double cut
         }
         const double2 w0 = out[idx];
         const double2 fb = outsfd ? outsfd[idx] : make_double2(0.0, 0.0);
-        double2 kk[4];
-        double2 ws = w0;
-        const double cst[3] = {0.5 * dt, 0.5 * dt, dt};
-        for (int s = 0; s < 4; ++s) {
-            double2 k;
-            k.x = 0.0 - k2 * ws.x * sp.inv_re;
-            k.y = 0.0 - k2 * ws.y * sp.inv_re;
-            double dr = 0.0, di = 0.0;
-            if (sp.hv) { dr += w * ws.x; di += w * ws.y; }
-            if (sp.sfd && sw > 0.0) { dr += sw * (ws.x - fb.x); di += sw * (ws.y - fb.y); }
-            k.x -= dr;
-            k.y -= di;
-            kk[s] = k;
-            if (s < 3) ws = make_double2(w0.x + cst[s] * k.x, w0.y + cst[s] * k.y);
-        }
         double2 wn;
-        wn.x = w0.x + dt / 6.0 * (kk[0].x + 2.0 * kk[1].x + 2.0 * kk[2].x + kk[3].x);
-        wn.y = w0.y + dt / 6.0 * (kk[0].y + 2.0 * kk[1].y + 2.0 * kk[2].y + kk[3].y);
+        if (sp.ifrk) {
+            // integrating-factor RK4 with a zero (masked) nonlinear term: explicit part is the SFD relaxation
+            const double lam = k2 * sp.inv_re + w;
+            const double e1 = exp(-lam * (0.5 * dt)), e2 = e1 * e1;
+            double2 ws = w0, acc = make_double2(0.0, 0.0);
+            for (int s = 0; s < 4; ++s) {
+                double2 k = make_double2(0.0, 0.0);
+                if (sp.sfd && sw > 0.0) { k.x -= sw * (ws.x - fb.x); k.y -= sw * (ws.y - fb.y); }
+                if (s == 0) {
+                    acc = make_double2(e2 * k.x, e2 * k.y);
+                    ws = make_double2(e1 * (w0.x + (0.5 * dt) * k.x), e1 * (w0.y + (0.5 * dt) * k.y));
+                } else if (s == 1) {
+                    acc = make_double2(acc.x + 2.0 * (e1 * k.x), acc.y + 2.0 * (e1 * k.y));
+                    ws = make_double2(e1 * w0.x + (0.5 * dt) * k.x, e1 * w0.y + (0.5 * dt) * k.y);
+                } else if (s == 2) {
+                    acc = make_double2(acc.x + 2.0 * (e1 * k.x), acc.y + 2.0 * (e1 * k.y));
+                    ws = make_double2(e2 * w0.x + dt * (e1 * k.x), e2 * w0.y + dt * (e1 * k.y));
+                } else {
+                    wn = make_double2(e2 * w0.x + dt / 6.0 * (acc.x + k.x), e2 * w0.y + dt / 6.0 * (acc.y + k.y));
+                }
+            }
+        } else {
+            double2 kk[4];
+            double2 ws = w0;
+            const double cst[3] = {0.5 * dt, 0.5 * dt, dt};
+            for (int s = 0; s < 4; ++s) {
+                double2 k;
+                k.x = 0.0 - k2 * ws.x * sp.inv_re;
+                k.y = 0.0 - k2 * ws.y * sp.inv_re;
+                double dr = 0.0, di = 0.0;
+                if (sp.hv) { dr += w * ws.x; di += w * ws.y; }
+                if (sp.sfd && sw > 0.0) { dr += sw * (ws.x - fb.x); di += sw * (ws.y - fb.y); }
+                k.x -= dr;
+                k.y -= di;
+                kk[s] = k;
+                if (s < 3) ws = make_double2(w0.x + cst[s] * k.x, w0.y + cst[s] * k.y);
+            }
+            wn.x = w0.x + dt / 6.0 * (kk[0].x + 2.0 * kk[1].x + 2.0 * kk[2].x + kk[3].x);
+            wn.y = w0.y + dt / 6.0 * (kk[0].y + 2.0 * kk[1].y + 2.0 * kk[2].y + kk[3].y);
+        }
         out[idx] = wn;
         if (sp.sfd && outsfd) {
             double a = dt / sp.sfd_tau;

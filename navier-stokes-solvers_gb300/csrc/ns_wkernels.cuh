@@ -456,12 +456,17 @@ __device__ __noinline__ double2 forcing_increment(const Geo& g, int i, int j, un
 #ifndef NSG_CW_NB
 #define NSG_CW_NB 4
 #endif
+// 1: park the forward transform's output in shared memory (the thread's own wb
+// slots) so that its registers are free for deeper batches of epilogue loads
+#ifndef NSG_CW_EPI_SMEM
+#define NSG_CW_EPI_SMEM 0
+#endif
 
 template <typename T> __host__ __device__ constexpr size_t cw_smem_bytes2(int Ky) {
     return (size_t)(NSG_CW_EX + 2048) * (sizeof(T) == 4 ? sizeof(float2) : sizeof(double2));
 }
 
-template <typename T, int STAGE>
+template <typename T, int STAGE, bool IFRK>
 __global__ void __launch_bounds__(64, (sizeof(T) == 4 ? NSG_CW_MINB : 3)) k_col_w(Geo g, ColArgs<T> a) {
     typedef typename CT<T>::C C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -502,12 +507,18 @@ __global__ void __launch_bounds__(64, (sizeof(T) == 4 ? NSG_CW_MINB : 3)) k_col_
 #pragma unroll
         for (int n1 = 0; n1 < 32; ++n1) v[n1] = ld_stream(&Gc[64 * n1 + t]);
         col_fwd2048(v, ex, tw, t, lane, h);
+#if NSG_CW_EPI_SMEM
+#pragma unroll
+        for (int k2 = 0; k2 < 32; ++k2) wb[k2 * 64 + t] = v[k2];
+#endif
 
         // RK stage algebra (spectral_time_integration.c:50-100) on this thread's modes j = lane + 32 k2 + 1024 h
         const double dt = s_dt;
         const T inv_re = (T)a.sp.inv_re;
         const T sc = (T)a.sp.scale;
         const T cst = (STAGE == 1 || STAGE == 2) ? (T)(0.5 * dt) : (STAGE == 3 ? (T)dt : (T)(dt / 6.0));
+        const T ch = (T)(0.5 * dt), cf = (T)dt, c6 = (T)(dt / 6.0);
+        constexpr bool ifrk = IFRK;  // integrating-factor RK4 stage algebra
         C* __restrict__ W0 = a.W0;
         C* __restrict__ WS = a.WS;
         C* __restrict__ ACC = a.ACC;
@@ -546,9 +557,48 @@ __global__ void __launch_bounds__(64, (sizeof(T) == 4 ? NSG_CW_MINB : 3)) k_col_
                 const C w0 = w0v[u], ws = wsv[u];
                 const T ky = __ldg(&kys[jj]);
                 const T k2v = k2sum(kx, ky);
+#if NSG_CW_EPI_SMEM
+                const C jh = wb[k2 * 64 + t];
+#else
+                const C jh = v[k2];
+#endif
+                if (ifrk) {
+                    // integrating-factor RK4: explicit part N - SFD relaxation, exact
+                    // decay by E1 = exp(-(k^2/Re + w) dt/2), E2 = E1^2
+                    C k;
+                    k.x = -(jh.x * sc);
+                    k.y = -(jh.y * sc);
+                    if (sfd && swv[u] > (T)0) {
+                        k.x -= swv[u] * (ws.x - fbv[u].x);
+                        k.y -= swv[u] * (ws.y - fbv[u].y);
+                    }
+                    const T lam = k2v * inv_re + hwv[u];
+                    const T e1 = exp(-lam * ch), e2 = e1 * e1;
+                    C wn;
+                    if (STAGE == 1) {
+                        ACC[s] = cmake<C>(e2 * k.x, e2 * k.y);
+                        wn.x = e1 * (w0.x + ch * k.x); wn.y = e1 * (w0.y + ch * k.y);
+                        WS[s] = wn;
+                    } else if (STAGE == 2 || STAGE == 3) {
+                        C acc = acv[u];
+                        acc.x = acc.x + (T)2 * (e1 * k.x);
+                        acc.y = acc.y + (T)2 * (e1 * k.y);
+                        ACC[s] = acc;
+                        if (STAGE == 2) { wn.x = e1 * w0.x + ch * k.x; wn.y = e1 * w0.y + ch * k.y; }
+                        else { wn.x = e2 * w0.x + cf * (e1 * k.x); wn.y = e2 * w0.y + cf * (e1 * k.y); }
+                        WS[s] = wn;
+                    } else {
+                        const C acc = acv[u];
+                        wn.x = e2 * w0.x + c6 * (acc.x + k.x);
+                        wn.y = e2 * w0.y + c6 * (acc.y + k.y);
+                        W0[s] = wn;
+                    }
+                    wb[k2 * 64 + t] = wn;
+                    continue;
+                }
                 C k;
-                k.x = -(v[k2].x * sc) - k2v * ws.x * inv_re;
-                k.y = -(v[k2].y * sc) - k2v * ws.y * inv_re;
+                k.x = -(jh.x * sc) - k2v * ws.x * inv_re;
+                k.y = -(jh.y * sc) - k2v * ws.y * inv_re;
                 if (hv || sfd) {
                     C damp = cmake<C>(0.0, 0.0);
                     if (hv) { damp.x += hwv[u] * ws.x; damp.y += hwv[u] * ws.y; }

@@ -32,6 +32,7 @@ struct ns_spectral_gpu {
     int forcing_enabled;
     double forcing_kmin, forcing_kmax, forcing_epsilon;
     unsigned long long forcing_seed;
+    int scheme;
 };
 
 static void ns_report(NSSpectralData *d, const char *what, int status) {
@@ -90,6 +91,7 @@ static int ns_sync_params(NSSpectralData *d, int adaptive) {
     p.forcing_kmax = d->gpu->forcing_kmax;
     p.forcing_epsilon = d->gpu->forcing_epsilon;
     p.forcing_seed = d->gpu->forcing_seed;
+    p.scheme = d->gpu->scheme;
     return ns_gpu_set_params(d->gpu->dev, &p);
 }
 
@@ -341,6 +343,13 @@ int ns_spectral_gpu_set_forcing(NSSpectralData *d, int enabled, double kmin, dou
     d->gpu->forcing_kmax = kmax;
     d->gpu->forcing_epsilon = epsilon;
     d->gpu->forcing_seed = seed;
+    return ns_status_to_solver(ns_sync_params(d, 0));
+}
+
+int ns_spectral_gpu_set_scheme(NSSpectralData *d, int scheme) {
+    if (!d || !d->gpu) return SOLVER_INVALID_PARAM;
+    if (scheme != NS_SPECTRAL_SCHEME_RK4 && scheme != NS_SPECTRAL_SCHEME_IFRK4) return SOLVER_INVALID_PARAM;
+    d->gpu->scheme = scheme;
     return ns_status_to_solver(ns_sync_params(d, 0));
 }
 

@@ -77,7 +77,7 @@ class GpuParams(C.Structure):
         ("sfd_strength", C.c_double), ("sfd_timescale", C.c_double),
         ("forcing_enabled", C.c_int), ("forcing_kmin", C.c_double),
         ("forcing_kmax", C.c_double), ("forcing_epsilon", C.c_double),
-        ("forcing_seed", C.c_uint64),
+        ("forcing_seed", C.c_uint64), ("scheme", C.c_int),
     ]
 
 
@@ -129,6 +129,7 @@ def load(build: bool = True) -> C.CDLL:
     proto("ns_spectral_gpu_advance_n", C.c_int, sp, C.c_int, C.c_int)
     proto("ns_spectral_gpu_sync_host", C.c_int, sp)
     proto("ns_spectral_gpu_set_forcing", C.c_int, sp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_ulonglong)
+    proto("ns_spectral_gpu_set_scheme", C.c_int, sp, C.c_int)
     proto("ns_spectral_gpu_diagnostics", C.c_int, sp, _DP, _DP)
     proto("ns_spectral_initialize_random_spectrum", C.c_int, sp, C.c_ulonglong, C.c_double, C.c_double)
     proto("ns_spectral_gpu_last_error", C.c_char_p, sp)
@@ -237,6 +238,12 @@ class Solver:
         st = self._f("gpu_set_forcing")(self.ptr, 1 if enabled else 0, kmin, kmax, epsilon, seed)
         if st != 0:
             raise RuntimeError(f"gpu_set_forcing failed ({st})")
+
+    def set_scheme(self, scheme: int):
+        """0: the reference RK4, 1: integrating-factor RK4."""
+        st = self._f("gpu_set_scheme")(self.ptr, scheme)
+        if st != 0:
+            raise RuntimeError(f"gpu_set_scheme failed ({st})")
 
     def diagnostics(self):
         e = C.c_double()

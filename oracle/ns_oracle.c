@@ -838,6 +838,111 @@ static void nso_ext_apply_forcing(nso_state *s, const nso_ext_forcing *f, double
     }
 }
 
+/* ------------------------------------------- integrating-factor RK4 (extension)
+ * No reference counterpart.  Lawson's integrating-factor RK4 (J. D. Lawson,
+ * SIAM J. Numer. Anal. 4 (1967) 372-380): classical RK4 applied to
+ * v = exp(-L t) omega_hat, L = -lam, lam = k^2/Re + w (w: hyperviscosity
+ * weights when enabled), so the viscous and hyperviscous decay is integrated
+ * exactly.  The explicit part is the nonlinear term of the reference stage
+ * (spectral_core.c:46-112) minus the SFD relaxation of hyperviscosity.c:132-145.
+ * With E1 = exp(-lam h/2) and E2 = E1^2:
+ *   a = N(w_n)  u_a = E1 (w_n + h/2 a)       acc = E2 a
+ *   b = N(u_a)  u_b = E1 w_n + h/2 b         acc = acc + 2 (E1 b)
+ *   c = N(u_b)  u_c = E2 w_n + h (E1 c)      acc = acc + 2 (E1 c)
+ *   d = N(u_c)  w_{n+1} = E2 w_n + h/6 (acc + d)
+ * Forcing and the SFD post-step follow as in the explicit scheme. */
+static void nso_if_rhs(nso_state *s, fftw_complex *kout) {
+    const nso_hv_config *cfg = &s->hyperviscosity;
+    const int n = s->nkx * s->nky;
+    const int sfd = cfg->sfd_enabled && cfg->sfd_strength > 0.0;
+    const int order = cfg->order > 0 ? cfg->order : 1;
+#pragma omp parallel for
+    for (int i = 0; i < n; ++i) {
+        fftw_complex k = s->nonlinear_hat[i];
+        if (sfd) {
+            double ramp = 0.0;
+            if (cfg->inv_bandwidth > 0.0) {
+                const double km = sqrt(s->k2[i]);
+                if (km > cfg->cutoff_wavenumber)
+                    ramp = pow(nso_clamp((km - cfg->cutoff_wavenumber) * cfg->inv_bandwidth, 0.0, 1.0), order);
+            }
+            const double sw = cfg->sfd_strength * ramp;
+            if (sw > 0.0) k -= sw * (s->omega_hat[i] - s->sfd_hat[i]);
+        }
+        kout[i] = k;
+    }
+}
+
+static void nso_advance_ifrk4_impl(nso_state *s, const nso_ext_forcing *forcing) {
+    const int n = s->nkx * s->nky;
+    const double h = s->dt;
+    const double inv_re = 1.0 / s->Re;
+    const int visc = s->hyperviscosity.enabled && s->hyperviscosity.coefficient > 0.0;
+    double *e1 = (double *)malloc(sizeof(double) * (size_t)n);
+    fftw_complex *acc = s->rk4_hat;
+#pragma omp parallel for
+    for (int i = 0; i < n; ++i) {
+        const double lam = s->k2[i] * inv_re + (visc ? s->hyperviscosity_weights[i] : 0.0);
+        e1[i] = exp(-lam * (0.5 * h));
+    }
+    memcpy(s->omega_tmp_hat, s->omega_hat, (size_t)n * sizeof(fftw_complex));
+    nso_compute_nonlinear_terms(s);
+    nso_if_rhs(s, s->rk1_hat);
+#pragma omp parallel for
+    for (int i = 0; i < n; ++i) {
+        const double E2 = e1[i] * e1[i];
+        acc[i] = E2 * s->rk1_hat[i];
+        s->omega_hat[i] = e1[i] * (s->omega_tmp_hat[i] + (0.5 * h) * s->rk1_hat[i]);
+    }
+    nso_compute_derivatives(s);
+    nso_compute_nonlinear_terms(s);
+    nso_if_rhs(s, s->rk2_hat);
+#pragma omp parallel for
+    for (int i = 0; i < n; ++i) {
+        acc[i] = acc[i] + 2.0 * (e1[i] * s->rk2_hat[i]);
+        s->omega_hat[i] = e1[i] * s->omega_tmp_hat[i] + (0.5 * h) * s->rk2_hat[i];
+    }
+    nso_compute_derivatives(s);
+    nso_compute_nonlinear_terms(s);
+    nso_if_rhs(s, s->rk3_hat);
+#pragma omp parallel for
+    for (int i = 0; i < n; ++i) {
+        const double E2 = e1[i] * e1[i];
+        acc[i] = acc[i] + 2.0 * (e1[i] * s->rk3_hat[i]);
+        s->omega_hat[i] = E2 * s->omega_tmp_hat[i] + h * (e1[i] * s->rk3_hat[i]);
+    }
+    nso_compute_derivatives(s);
+    nso_compute_nonlinear_terms(s);
+    nso_if_rhs(s, s->rk2_hat);
+#pragma omp parallel for
+    for (int i = 0; i < n; ++i) {
+        const double E2 = e1[i] * e1[i];
+        s->omega_hat[i] = E2 * s->omega_tmp_hat[i] + h / 6.0 * (acc[i] + s->rk2_hat[i]);
+    }
+    free(e1);
+    if (forcing && forcing->enabled) nso_ext_apply_forcing(s, forcing, h);
+    nso_hv_post_step(s, s->omega_hat, h);
+    s->t += h;
+    nso_compute_derivatives(s);
+}
+
+/* n-step driver with a choice of scheme (0: the reference RK4, 1: IF-RK4) */
+void nso_ext_run_scheme(nso_state *s, int scheme, int nsteps, int adaptive, int forcing_on, double fkmin,
+                        double fkmax, double epsilon, uint64_t fseed, uint64_t step0) {
+    nso_ext_forcing f;
+    f.enabled = forcing_on;
+    f.kmin = fkmin;
+    f.kmax = fkmax;
+    f.epsilon = epsilon;
+    f.seed = fseed;
+    for (int n = 0; n < nsteps; ++n) {
+        if (adaptive) s->dt = nso_compute_cfl_timestep(s);
+        f.step = step0 + (uint64_t)n;
+        if (scheme == 1) nso_advance_ifrk4_impl(s, forcing_on ? &f : NULL);
+        else nso_advance_rk4_impl(s, forcing_on ? &f : NULL);
+    }
+}
+
 /* n-step driver: optional reference CFL dt per step (the loop of
  * tests/test_taylor_green.c:105-108), optional forcing with a per-step counter */
 void nso_ext_run(nso_state *s, int nsteps, int adaptive, int forcing_on, double fkmin, double fkmax,

@@ -144,6 +144,8 @@ def load(kind: str = "port") -> C.CDLL:
         proto("nso_ext_init_random_spectrum", None, sp, C.c_uint64, C.c_double, C.c_double)
         proto("nso_ext_run", None, sp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
               C.c_double, C.c_uint64, C.c_uint64)
+        proto("nso_ext_run_scheme", None, sp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+              C.c_double, C.c_uint64, C.c_uint64)
     else:
         proto("ns_spectral_check_resolution", C.c_int, sp)
     lib._prefix = p
