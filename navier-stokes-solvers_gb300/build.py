@@ -30,7 +30,8 @@ CFLAGS = ["-O2", "-std=gnu11", "-fPIC", "-ffp-contract=off", "-Wall", "-I", INCL
 def _sources():
     cu = sorted(glob.glob(os.path.join(PKG, "csrc", "*.cu")))
     c = sorted(glob.glob(os.path.join(PKG, "host", "*.c")))
-    deps = cu + c + glob.glob(os.path.join(PKG, "csrc", "*.cuh")) + glob.glob(os.path.join(INCLUDE, "*.h"))
+    deps = (cu + c + glob.glob(os.path.join(PKG, "csrc", "*.cuh")) + glob.glob(os.path.join(PKG, "csrc", "*.h"))
+            + glob.glob(os.path.join(INCLUDE, "*.h")))
     return cu, c, deps
 
 

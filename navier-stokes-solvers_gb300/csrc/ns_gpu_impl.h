@@ -1,0 +1,104 @@
+// Private host-side definition of an ns_gpu instance and the error-handling
+// macros shared by the translation units of the library (not installed).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "ns_gpu.h"
+#include "ns_kernels.cuh"
+
+using nsg::Geo;
+using nsg::DevScalars;
+
+struct ns_gpu {
+    Geo g;
+    int prec;
+    int ER, EC;
+    int device;
+    int num_sms;
+    int fast_row;       // radix-32 warp row kernel (nx = 2048)
+    int fast_col;       // radix-32 column kernel (ny = 2048)
+    cudaStream_t st;
+    std::string err;
+    unsigned long long launches;
+    ns_gpu_params p;
+    int params_set;
+    double hv_kmax, hv_cutoff, hv_inv_bw;
+    double f_sigma;
+    // device buffers (complex of the instance precision unless noted)
+    void* F[4];
+    void* G;
+    void *W0, *WS, *ACC, *PSI0, *SFD, *KS, *KP;
+    void *hvw, *sfdw, *kxv, *kyv, *twc, *twr, *twh;
+    double* hvw_full;   // FP64 [nky][nkx]
+    DevScalars* ds;
+    double2* part;      // reduction partials
+    int part_n;
+    double* dres;       // small FP64 results
+    int* dflag;
+    // host-layout FP64 staging (allocated on first use)
+    double2* spec[5];
+    double* real[5];
+    double2 *out, *outsfd;  // masked-out modes of the state (FP64)
+    int outside_active;
+    int fields_valid;   // F holds the stage-1 fields of the current state
+    int psi0_valid;     // PSI0 holds the caller's psi_hat for the next prologue
+    void* scratch;
+    size_t scratch_bytes;
+    void* flushbuf;     // L2 flush target of the timed entry points
+    size_t flush_bytes;
+    // kernel-level profiling: events around every launch while non-null
+    struct ProfRec { cudaEvent_t a, b; int kind; };
+    std::vector<ProfRec>* prof;
+};
+
+// record an event pair around one launch when kernel profiling is on
+struct ProfScope {
+    ns_gpu* g;
+    int kind;
+    cudaEvent_t a, b;
+    ProfScope(ns_gpu* g_, int kind_) : g(g_), kind(kind_), a(nullptr), b(nullptr) {
+        if (g->prof) {
+            cudaEventCreate(&a);
+            cudaEventCreate(&b);
+            cudaEventRecord(a, g->st);
+        }
+    }
+    ~ProfScope() {
+        if (g->prof) {
+            cudaEventRecord(b, g->st);
+            g->prof->push_back({a, b, kind});
+        }
+    }
+};
+
+#define NSG_FAIL(g, code, ...)                                             \
+    do {                                                                   \
+        char _b[512];                                                      \
+        snprintf(_b, sizeof(_b), __VA_ARGS__);                             \
+        if (g) (g)->err = _b;                                              \
+        return (code);                                                     \
+    } while (0)
+
+#define NSG_CUDA(g, call)                                                                    \
+    do {                                                                                     \
+        cudaError_t _e = (call);                                                             \
+        if (_e != cudaSuccess) NSG_FAIL(g, NS_GPU_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(_e)); \
+    } while (0)
+
+#define NSG_LAUNCHED(g)                                                                          \
+    do {                                                                                         \
+        (g)->launches++;                                                                         \
+        cudaError_t _e = cudaGetLastError();                                                     \
+        if (_e != cudaSuccess) NSG_FAIL(g, NS_GPU_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(_e)); \
+    } while (0)
+
+#define NSG_TRY(...)            \
+    do {                        \
+        int _s = (__VA_ARGS__); \
+        if (_s != NS_GPU_OK) return _s; \
+    } while (0)
+

@@ -172,18 +172,20 @@ template <typename T> struct RowArgs {
 template <int MODE> struct RowNF { static const int v = (MODE == ROW_STAGE || MODE == ROW_DUMP) ? 4 : (MODE == ROW_UVW ? 3 : 1); };
 
 // grid = ny / RPC, block = RPC * (H / E), dynamic smem = NF * RPC * spad_len(H) * sizeof(C)
+// body of the row pass for row block bx (rows bx*RPC .. bx*RPC + RPC - 1); the
+// block must have exactly RPC * (H / E) threads
 template <typename T, int E, int MODE>
-__global__ void __launch_bounds__(256) k_row(Geo g, RowArgs<T> a) {
+__device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, const int bx) {
     typedef typename CT<T>::C C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* sm = reinterpret_cast<C*>(smem_raw);
     constexpr int NF = RowNF<MODE>::v;
     const int H = g.H, TT = H / E, LP = spad_len(H);
     const int r = threadIdx.x / TT, t = threadIdx.x - r * TT;
-    const int y = blockIdx.x * g.RPC + r;
+    const int y = bx * g.RPC + r;
     const int nx = g.nx, Kx = g.Kx;
 
-    if (MODE == ROW_STAGE && blockIdx.x == 0 && threadIdx.x == 0) {
+    if (MODE == ROW_STAGE && bx == 0 && threadIdx.x == 0) {
         if (a.marker == 1) {
             a.ds->step_cur = a.ds->step_next;
             a.ds->step_next = a.ds->step_next + 1ULL;
@@ -330,6 +332,11 @@ __global__ void __launch_bounds__(256) k_row(Geo g, RowArgs<T> a) {
     }
 }
 
+template <typename T, int E, int MODE>
+__global__ void __launch_bounds__(256) k_row(Geo g, RowArgs<T> a) {
+    row_body<T, E, MODE>(g, a, blockIdx.x);
+}
+
 // ============================================================ column kernel
 enum { COL_STAGE = 0, COL_PROLOGUE = 1, COL_INV1 = 2, COL_FWD_EXPORT = 3, COL_NL_EXPORT = 4 };
 
@@ -379,14 +386,16 @@ __device__ __forceinline__ C field_value(int f, C w, T kx, T ky) {
 }
 
 // grid = Kxp / CW, block = CW * (ny / E), dynamic smem = CW * spad_len(ny) * sizeof(C)
+// body of the column pass for column block bx (kept columns bx*CW .. bx*CW + CW - 1);
+// the block must have exactly CW * (ny / E) threads
 template <typename T, int E, int MODE, int STAGE>
-__global__ void __launch_bounds__(512) k_col(Geo g, ColArgs<T> a) {
+__device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, const int bx) {
     typedef typename CT<T>::C C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* sm = reinterpret_cast<C*>(smem_raw);
     const int ny = g.ny, TC = ny / E, LP = spad_len(ny), CW = g.CW;
     const int b = threadIdx.x / TC, t = threadIdx.x - b * TC;
-    const int c0 = blockIdx.x * CW;
+    const int c0 = bx * CW;
     const int Kx = g.Kx, Ky = g.Ky;
     const int nthr = blockDim.x;
     C* mybuf = sm + b * LP;
@@ -407,7 +416,7 @@ __global__ void __launch_bounds__(512) k_col(Geo g, ColArgs<T> a) {
                 } else {
                     dt = a.ds->dt_fixed;
                 }
-                if (blockIdx.x == 0) a.ds->dt = dt;
+                if (bx == 0) a.ds->dt = dt;
             } else {
                 dt = a.ds->dt;
             }
@@ -570,7 +579,7 @@ __global__ void __launch_bounds__(512) k_col(Geo g, ColArgs<T> a) {
                     a.W0[s] = wn;
                 }
             }
-            if (STAGE == 4 && blockIdx.x == 0 && threadIdx.x == 0) a.ds->t = a.ds->t + dt;
+            if (STAGE == 4 && bx == 0 && threadIdx.x == 0) a.ds->t = a.ds->t + dt;
             __syncthreads();
         }
     }
@@ -609,6 +618,11 @@ __global__ void __launch_bounds__(512) k_col(Geo g, ColArgs<T> a) {
         }
         __syncthreads();
     }
+}
+
+template <typename T, int E, int MODE, int STAGE>
+__global__ void __launch_bounds__(512) k_col(Geo g, ColArgs<T> a) {
+    col_body<T, E, MODE, STAGE>(g, a, blockIdx.x);
 }
 
 // ======================================================= auxiliary kernels

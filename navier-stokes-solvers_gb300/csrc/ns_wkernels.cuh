@@ -171,25 +171,27 @@ __device__ __forceinline__ void warp_fft1024(C (&a)[32], C* S, const C* tw, int 
     dft32<INV>(a);
 }
 
-// fetch X_f[k] of row y, k = kb + 32 i < Kx, into registers (F kx-column-contiguous)
+// kept kx columns at nx = 2048: floor(2 * 1025 / 3) + 1 (spectral_initialization.c:46-49)
+#define NSG_RW_KX 684
+
+// fetch X_f[k] of row y, k = kb + 32 i < NSG_RW_KX, into registers (F kx-column-contiguous)
 template <typename C>
 __device__ __forceinline__ void rows_fetch(C (&pf)[NSG_RW_KXMAX / 32], const C* __restrict__ src, size_t ny, int y,
-                                           bool ok, int kb, int Kx) {
+                                           bool ok, int kb) {
 #pragma unroll
     for (int i = 0; i < NSG_RW_KXMAX / 32; ++i) {
         const int k = kb + 32 * i;
-        pf[i] = (ok && k < Kx) ? __ldg(&src[(size_t)k * ny + y]) : cmake<C>(0.0, 0.0);
+        pf[i] = (ok && k < NSG_RW_KX) ? __ldg(&src[(size_t)k * ny + y]) : cmake<C>(0.0, 0.0);
     }
 }
 
 // deposit the fetched values (times i kx when dx) into row w's exchange buffer Sw
 template <typename T, typename C>
-__device__ __forceinline__ void rows_deposit(const C (&pf)[NSG_RW_KXMAX / 32], C* Sw, int dx, const T* kxv, int kb,
-                                             int Kx) {
+__device__ __forceinline__ void rows_deposit(const C (&pf)[NSG_RW_KXMAX / 32], C* Sw, int dx, const T* kxv, int kb) {
 #pragma unroll
     for (int i = 0; i < NSG_RW_KXMAX / 32; ++i) {
         const int k = kb + 32 * i;
-        if (k < Kx) {
+        if (k < NSG_RW_KX) {
             C x = pf[i];
             if (dx) {
                 const T kx = kxv[k];
@@ -204,23 +206,29 @@ __device__ __forceinline__ void rows_deposit(const C (&pf)[NSG_RW_KXMAX / 32], C
 }
 
 // pack the half-length inverse input Z[lane + 32 n1] = (X[k] + conj X[H-k]) + i e^{+2 pi i k/nx} (X[k] - conj X[H-k])
-// from the half spectrum X[k], k < Kx, held in S
+// from the half spectrum X[k], k < NSG_RW_KX, held in S, and return conj Z (the
+// inverse transform runs as conj(DFT(conj Z))).  k = lane + 32 n1 sits at
+// S[33 n1 + lane]; H - k at S[33 (31 - n1) + ob] with ob = 32 - lane (lane > 0)
+// or 33 (lane = 0), so every address is a per-thread base plus a constant.
 template <typename T, typename C>
-__device__ __forceinline__ void row_pack(C (&a)[32], const C* S, const C* twh, int Kx, int lane) {
+__device__ __forceinline__ void row_pack(C (&a)[32], const C* S, const C* twh, int lane) {
+    const int ob = lane ? 32 - lane : 33;
+    const C zero = cmake<C>(0.0, 0.0);
 #pragma unroll
     for (int n1 = 0; n1 < 32; ++n1) {
         const int k = lane + 32 * n1;
-        const C zero = cmake<C>(0.0, 0.0);
-        const C xa = (k < Kx) ? S[sx(k)] : zero;
-        const int kb = 1024 - k;
-        const C xb = (k > 0 && kb < Kx) ? S[sx(kb)] : zero;
-        if (k == 0) {
-            a[n1] = cmake<C>(xa.x, xa.x);  // Re X[0] (1 + i); the Nyquist bin is masked
+        const C xa = (k < NSG_RW_KX) ? S[33 * n1 + lane] : zero;
+        const C xb = (k > 0 && 1024 - k < NSG_RW_KX) ? S[33 * (31 - n1) + ob] : zero;
+        if (n1 == 0 && lane == 0) {
+            a[n1] = cmake<C>(xa.x, -xa.x);  // conj of Re X[0] (1 + i); the Nyquist bin is masked
         } else {
-            const C e = cconj(twh[k]);
+            const C e = twh[k];  // exp(-2 pi i k/nx) = conj of the pack twiddle
             const C A = cadd(xa, cconj(xb));
-            const C D = cmul(csub(xa, cconj(xb)), e);
-            a[n1] = cmake<C>(A.x - D.y, A.y + D.x);
+            const C dd = csub(xa, cconj(xb));
+            // D = dd * conj(e); Z = (A.x - D.y, A.y + D.x); a = conj Z
+            const T Dx = dd.x * e.x + dd.y * e.y;
+            const T Dy = dd.y * e.x - dd.x * e.y;
+            a[n1] = cmake<C>(A.x - Dy, -(A.y + Dx));
         }
     }
     __syncwarp();
@@ -241,7 +249,7 @@ __global__ void __launch_bounds__(32 * rw_warps<T>(), 1) k_row_w(Geo g, RowArgs<
     C* S = S0 + warp * WS;
     C* R = S + 32 * 33;
     C* Q = R + 1024;
-    const int Kx = g.Kx, ny = g.ny;
+    const int ny = g.ny;
     // group grp owns rows y0 + GW grp + w (w < GW); thread (kb, wme) of the group
     // moves columns kb + 32 i of row wme
     const int grp = warp / GW;
@@ -256,7 +264,7 @@ __global__ void __launch_bounds__(32 * rw_warps<T>(), 1) k_row_w(Geo g, RowArgs<
         tw[k1 * 33 + t] = a.twr[t * k1];
         twh_s[i] = a.twh[i];
     }
-    for (int i = threadIdx.x; i < NSG_RW_KXMAX; i += blockDim.x) kx_s[i] = (i < Kx) ? a.kxv[i] : (T)0;
+    for (int i = threadIdx.x; i < NSG_RW_KXMAX; i += blockDim.x) kx_s[i] = (i < NSG_RW_KX) ? a.kxv[i] : (T)0;
     wait_previous_kernel();
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (a.marker == 1) {
@@ -274,58 +282,63 @@ __global__ void __launch_bounds__(32 * rw_warps<T>(), 1) k_row_w(Geo g, RowArgs<
     const int ystep = gridDim.x * NW;
     __syncthreads();  // tables in place
     int y0 = blockIdx.x * NW + grp * GW;  // this group's first row of the round
-    rows_fetch(pf, a.F[0], (size_t)ny, y0 + wme, y0 + wme < ny, kb, Kx);
+    rows_fetch(pf, a.F[0], (size_t)ny, y0 + wme, y0 + wme < ny, kb);
     for (; y0 < ny; y0 += ystep) {
         const int y = y0 + (warp - grp * GW);
+        // q = 0..3: inverse transforms (conj(DFT(conj Z))) of psi_x, psi_y,
+        // omega_y, omega_x; q = 4: forward transform of the packed Jacobian.
+        // One transform body serves all five.
 #pragma unroll 1
-        for (int q = 0; q < 4; ++q) {
-            const int f = (q < 2) ? q : 5 - q;
-            const int dx = (f == 0 || f == 2);
-            group_sync<GW, NW>(grp);  // every warp of the group is done with its exchange buffer
-            rows_deposit<T>(pf, Sme, dx, kx_s, kb, Kx);
-            group_sync<GW, NW>(grp);
-            // fetch the next field (or the next round's psi_x) while this one transforms
-            if (q < 3) {
-                rows_fetch(pf, a.F[(q + 1 < 2) ? q + 1 : 4 - q], (size_t)ny, y0 + wme, y0 + wme < ny, kb, Kx);
-            } else {
-                const int yn = y0 + ystep + wme;
-                rows_fetch(pf, a.F[0], (size_t)ny, yn, yn < ny, kb, Kx);
-            }
-            if (y < ny) {
-                row_pack<T>(v, S, twh_s, Kx, lane);
-                warp_fft1024<true>(v, S, tw, lane);
-                if (q == 0) {
-#pragma unroll
-                    for (int k = 0; k < 32; ++k) R[lane + 32 * k] = v[k];
-                } else if (q == 1) {
-#pragma unroll
-                    for (int k = 0; k < 32; ++k) {
-                        if (a.cfl) {
-                            const C px = R[lane + 32 * k];
-                            vmax2 = fmax(vmax2, fmax(px.x * px.x + v[k].x * v[k].x, px.y * px.y + v[k].y * v[k].y));
-                        }
-                        Q[lane + 32 * k] = v[k];
-                    }
-                } else if (q == 2) {
-#pragma unroll
-                    for (int k = 0; k < 32; ++k) {
-                        const C px = R[lane + 32 * k];
-                        R[lane + 32 * k] = cmake<C>(px.x * v[k].x, px.y * v[k].y);
-                    }
+        for (int q = 0; q < 5; ++q) {
+            if (q < 4) {
+                const int f = (q < 2) ? q : 5 - q;
+                const int dx = (f == 0 || f == 2);
+                group_sync<GW, NW>(grp);  // every warp of the group is done with its exchange buffer
+                rows_deposit<T>(pf, Sme, dx, kx_s, kb);
+                group_sync<GW, NW>(grp);
+                // fetch the next field (or the next round's psi_x) while this one transforms
+                if (q < 3) {
+                    rows_fetch(pf, a.F[(q + 1 < 2) ? q + 1 : 4 - q], (size_t)ny, y0 + wme, y0 + wme < ny, kb);
                 } else {
-                    // J = psi_x omega_y - psi_y omega_x, packed as w[m] = J[2m] + i J[2m+1]
+                    const int yn = y0 + ystep + wme;
+                    rows_fetch(pf, a.F[0], (size_t)ny, yn, yn < ny, kb);
+                }
+                if (y < ny) row_pack<T>(v, S, twh_s, lane);
+            }
+            if (y >= ny) continue;
+            warp_fft1024<false>(v, S, tw, lane);
+            if (q == 4) break;
 #pragma unroll
-                    for (int k = 0; k < 32; ++k) {
-                        const C p = R[lane + 32 * k];
-                        const C py = Q[lane + 32 * k];
-                        v[k] = cmake<C>(p.x - py.x * v[k].x, p.y - py.y * v[k].y);
+            for (int k = 0; k < 32; ++k) v[k].y = -v[k].y;
+            if (q == 0) {
+#pragma unroll
+                for (int k = 0; k < 32; ++k) R[lane + 32 * k] = v[k];
+            } else if (q == 1) {
+#pragma unroll
+                for (int k = 0; k < 32; ++k) {
+                    if (a.cfl) {
+                        const C px = R[lane + 32 * k];
+                        vmax2 = fmax(vmax2, fmax(px.x * px.x + v[k].x * v[k].x, px.y * px.y + v[k].y * v[k].y));
                     }
+                    Q[lane + 32 * k] = v[k];
+                }
+            } else if (q == 2) {
+#pragma unroll
+                for (int k = 0; k < 32; ++k) {
+                    const C px = R[lane + 32 * k];
+                    R[lane + 32 * k] = cmake<C>(px.x * v[k].x, px.y * v[k].y);
+                }
+            } else {
+                // J = psi_x omega_y - psi_y omega_x, packed as w[m] = J[2m] + i J[2m+1]
+#pragma unroll
+                for (int k = 0; k < 32; ++k) {
+                    const C p = R[lane + 32 * k];
+                    const C py = Q[lane + 32 * k];
+                    v[k] = cmake<C>(p.x - py.x * v[k].x, p.y - py.y * v[k].y);
                 }
             }
         }
         if (y < ny) {
-            // forward half-length transform of J
-            warp_fft1024<false>(v, S, tw, lane);
 #pragma unroll
             for (int k = 0; k < 32; ++k) S[k * 33 + lane] = v[k];
         }
@@ -335,7 +348,7 @@ __global__ void __launch_bounds__(32 * rw_warps<T>(), 1) k_row_w(Geo g, RowArgs<
         // consecutive rows of one G column
         const T half = (T)0.5;
         const int nrows = (ny - y0 < GW) ? ny - y0 : GW;
-        for (int e = tg; e < Kx * GW; e += 32 * GW) {
+        for (int e = tg; e < NSG_RW_KX * GW; e += 32 * GW) {
             const int k = e / GW, w = e - k * GW;
             if (w >= nrows) continue;
             const C* Sw = Sg + w * WS;
@@ -356,73 +369,42 @@ __global__ void __launch_bounds__(32 * rw_warps<T>(), 1) k_row_w(Geo g, RowArgs<
 }
 
 // ============================================================ k_col_w
-// ny = 2048: 64 threads per column (two warps), 2 columns per CTA.
-// dynamic smem: tw [32][65] with W_2048^{t k1} at tw[k1*65 + t] (t < 64), then
-// per column a buffer of NSG_CW_LP elements (tile column / exchange area)
+// ny = 2048: a team of 64 threads (two warps) per kept kx column.  The 2048-
+// point transforms below synchronise the team with a named barrier, so several
+// teams share one CTA (and its shared twiddle table) without waiting on each other.
 
+// barrier over one 64-thread team (named barrier bid, 1 <= bid <= 15)
+__device__ __forceinline__ void team_sync(int bid) { asm volatile("bar.sync %0, 64;" ::"r"(bid) : "memory"); }
 
 // forward 2048-point transform: a[] = x[64 n1 + t] on entry (t = 32 h + lane),
-// X[lane + 32 k2 + 1024 h] on exit; col is this column's shared buffer
+// X[lane + 32 k2 + 1024 h] on exit; col is this team's exchange buffer, tw the
+// shared table tw[k1 * 65 + t] = W_2048^{t k1} (k1 < 32, t < 64): consecutive
+// threads read consecutive entries, and column t = 32 holds W_64^{k1}
 template <typename C>
-__device__ __forceinline__ void col_fwd2048(C (&a)[32], C* col, const C* __restrict__ twc, int t, int lane, int h) {
+__device__ __forceinline__ void col_fwd2048(C (&a)[32], C* col, const C* tw, int t, int lane, int h, int bid) {
     dft32<false>(a);
 #pragma unroll
-    for (int k1 = 1; k1 < 32; ++k1) a[k1] = cmul(a[k1], __ldg(&twc[t * k1]));
+    for (int k1 = 1; k1 < 32; ++k1) a[k1] = cmul(a[k1], tw[k1 * 65 + t]);
 #pragma unroll
     for (int k1 = 0; k1 < 32; ++k1) col[k1 * 65 + t] = a[k1];
-    __syncthreads();
+    team_sync(bid);
 #pragma unroll
     for (int m = 0; m < 32; ++m) a[m] = col[lane * 65 + 2 * m + h];
-    __syncthreads();
+    team_sync(bid);
     dft32<false>(a);
     if (h) {
 #pragma unroll
-        for (int k2 = 1; k2 < 32; ++k2) a[k2] = cmul(a[k2], __ldg(&twc[32 * k2]));  // W_64^{k2} = W_2048^{32 k2}
+        for (int k2 = 1; k2 < 32; ++k2) a[k2] = cmul(a[k2], tw[k2 * 65 + 32]);  // W_64^{k2} = W_2048^{32 k2}
     }
 #pragma unroll
     for (int k2 = 0; k2 < 32; ++k2) col[h * 1056 + k2 * 33 + lane] = a[k2];
-    __syncthreads();
+    team_sync(bid);
 #pragma unroll
     for (int k2 = 0; k2 < 32; ++k2) {
         const C b = col[(1 - h) * 1056 + k2 * 33 + lane];
         a[k2] = h ? csub(b, a[k2]) : cadd(a[k2], b);  // E + W O  |  E - W O
     }
-    __syncthreads();
-}
-
-// inverse 2048-point transform: a[] = X[lane + 32 k2 + 1024 h] on entry,
-// x[64 n1 + t] on exit (unnormalised)
-template <typename C>
-__device__ __forceinline__ void col_inv2048(C (&a)[32], C* col, const C* __restrict__ twc, int t, int lane, int h) {
-#pragma unroll
-    for (int k2 = 0; k2 < 32; ++k2) col[h * 1056 + k2 * 33 + lane] = a[k2];
-    __syncthreads();
-#pragma unroll
-    for (int k2 = 0; k2 < 32; ++k2) {
-        const C b = col[(1 - h) * 1056 + k2 * 33 + lane];
-        if (h == 0) {
-            a[k2] = cadd(a[k2], b);  // E = X_lo + X_hi
-        } else {
-            C w = __ldg(&twc[32 * k2]);
-            w.y = -w.y;  // W_64^{-k2}
-            a[k2] = cmul(csub(b, a[k2]), w);  // O = (X_lo - X_hi) W_64^{-k2}
-        }
-    }
-    __syncthreads();
-    dft32<true>(a);
-#pragma unroll
-    for (int m = 0; m < 32; ++m) col[lane * 65 + 2 * m + h] = a[m];
-    __syncthreads();
-#pragma unroll
-    for (int k1 = 0; k1 < 32; ++k1) a[k1] = col[k1 * 65 + t];
-    __syncthreads();
-#pragma unroll
-    for (int k1 = 1; k1 < 32; ++k1) {
-        C w = __ldg(&twc[t * k1]);
-        w.y = -w.y;
-        a[k1] = cmul(a[k1], w);
-    }
-    dft32<true>(a);
+    team_sync(bid);
 }
 
 // white-in-time forcing increment of one kept mode (Philox4x64-10, Box-Muller)
@@ -445,45 +427,89 @@ __device__ __noinline__ double2 forcing_increment(const Geo& g, int i, int j, un
     return make_double2(amp * rad * cs, amp * (flip ? -rad * sn : rad * sn));
 }
 
-// one kept kx column per CTA (64 threads); layout-A values x[64 n1 + t] load
-// straight from the contiguous G column and store straight to F
-#define NSG_CW_EX 2112
-// resident CTAs per SM the FP32 column kernel is compiled for, and modes per
-// batch of its RK epilogue loads
-#ifndef NSG_CW_MINB
-#define NSG_CW_MINB 6
-#endif
-#ifndef NSG_CW_NB
-#define NSG_CW_NB 4
-#endif
-// 1: park the forward transform's output in shared memory (the thread's own wb
-// slots) so that its registers are free for deeper batches of epilogue loads
-#ifndef NSG_CW_EPI_SMEM
-#define NSG_CW_EPI_SMEM 0
-#endif
+// ------------------------------------------------------------ cp.async staging
+// Asynchronous global -> shared copies (no register staging); each thread
+// waits for its own copies with cp_async_wait_all, a barrier publishes them.
+__device__ __forceinline__ void cp_async(void* s, const float2* gp) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((unsigned)__cvta_generic_to_shared(s)), "l"(gp)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async(void* s, const double2* gp) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(s)), "l"(gp)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async(void* s, const float* gp) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((unsigned)__cvta_generic_to_shared(s)), "l"(gp)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async(void* s, const double* gp) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((unsigned)__cvta_generic_to_shared(s)), "l"(gp)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-template <typename T> __host__ __device__ constexpr size_t cw_smem_bytes2(int Ky) {
-    return (size_t)(NSG_CW_EX + 2048) * (sizeof(T) == 4 ? sizeof(float2) : sizeof(double2));
+// Persistent column pass: one CTA per SM, NT teams of 64 threads, team q of
+// CTA b takes the kept columns i = b + gridDim.x (q + NT r).  The CTA keeps the
+// twiddle table W_2048^m and the kept ky values in shared memory (every
+// transform reads 31-62 twiddles per thread, so they must not depend on L1
+// hits).  Each team stages its column's omega_hat and hyperviscosity weights
+// with cp.async before the kernel waits for the row pass, and the stage state
+// WS and accumulator ACC into its exchange buffer once the forward transform
+// has released it.  All five transforms of a column run through one forward
+// transform body (an inverse is conj(DFT(conj x))), which keeps the kernel
+// small enough for the instruction caches of five teams at different phases.
+//
+// dynamic smem: TW [32][65] C | per team: X [XL] C (FFT exchange, then WS | ACC),
+// NS [Kyp] C (omega_hat at the step start, then the next stage's state) |
+// per team SHV [Kyp] T | KYS [Kyp] T   (Kyp = Ky rounded up to a multiple of 4)
+#define NSG_CW_EX 2112
+#define NSG_CW_TW (32 * 65)
+__host__ __device__ constexpr int cw_kyp(int Ky) { return (Ky + 3) & ~3; }
+__host__ __device__ constexpr int cw_xl(int Ky) { return 2 * cw_kyp(Ky) > NSG_CW_EX ? 2 * cw_kyp(Ky) : NSG_CW_EX; }
+template <typename T> __host__ __device__ constexpr int cw_teams() { return sizeof(T) == 4 ? 5 : 2; }
+template <typename T> __host__ __device__ constexpr size_t cw_smem_bytes(int Ky) {
+    return (size_t)(NSG_CW_TW + cw_teams<T>() * (cw_xl(Ky) + cw_kyp(Ky))) * (sizeof(T) == 4 ? sizeof(float2) : sizeof(double2)) +
+           (size_t)(cw_teams<T>() + 1) * cw_kyp(Ky) * sizeof(T);
 }
 
 template <typename T, int STAGE, bool IFRK>
-__global__ void __launch_bounds__(64, (sizeof(T) == 4 ? NSG_CW_MINB : 3)) k_col_w(Geo g, ColArgs<T> a) {
+__global__ void __launch_bounds__(64 * cw_teams<T>(), 1) k_col_w(Geo g, ColArgs<T> a) {
     typedef typename CT<T>::C C;
+    constexpr int NT = cw_teams<T>();
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    C* ex = reinterpret_cast<C*>(smem_raw);
-    C* wb = ex + NSG_CW_EX;  // next-stage state of this thread's modes, wb[k2 * 64 + t]
-    const T* __restrict__ kys = a.kyv;
-    const C* __restrict__ tw = a.twc;  // W_2048^m, read through L1
-    const int t = threadIdx.x, lane = t & 31, h = t >> 5;
-    const int i = blockIdx.x;
-    const int Ky = g.Ky;
+    const int Ky = g.Ky, Kyp = cw_kyp(Ky), XL = cw_xl(Ky), Kx = g.Kx;
+    const int team = threadIdx.x >> 6, t = threadIdx.x & 63, lane = t & 31, h = t >> 5;
+    const int bid = 1 + team;
+    C* TW = reinterpret_cast<C*>(smem_raw);
+    C* X = TW + NSG_CW_TW + team * (XL + Kyp);
+    C* NS = X + XL;
+    T* SHV = reinterpret_cast<T*>(TW + NSG_CW_TW + NT * (XL + Kyp)) + team * Kyp;
+    T* KYS = reinterpret_cast<T*>(TW + NSG_CW_TW + NT * (XL + Kyp)) + NT * Kyp;
+    const int hv = a.sp.hv, sfd = a.sp.sfd;
     __shared__ double s_dt;
 
+    // constant tables, and the first column's omega_hat / weights: these were
+    // written before the previous kernel (the row pass, which waited for them)
+    for (int m = threadIdx.x; m < NSG_CW_TW; m += blockDim.x) {
+        const int k1 = m / 65, tt = m - 65 * k1;
+        TW[m] = a.twc[(tt * k1) & 2047];
+    }
+    for (int jj = threadIdx.x; jj < Ky; jj += blockDim.x) KYS[jj] = a.kyv[jj];
+    const int cstride = gridDim.x * NT;
+    int i = blockIdx.x + gridDim.x * team;
+    if (i < Kx) {
+        const size_t base = (size_t)i * Ky;
+        for (int jj = t; jj < Ky; jj += 64) {
+            cp_async(&NS[jj], &a.W0[base + jj]);
+            if (hv) cp_async(&SHV[jj], &a.hvw[base + jj]);
+        }
+    }
     wait_previous_kernel();
-    if (t == 0) {
+    if (threadIdx.x == 0) {
         double dt;
         if (STAGE == 1) {
             if (a.sp.adaptive) {
+                // spectral_time_integration.c:9-31 on max|u| of the stage-1 fields
                 const double vmax = sqrt(__longlong_as_double((long long)a.ds->maxvel2));
                 const double dt_cfl = a.sp.cfl * a.sp.dxmin / (vmax + 1e-12);
                 const double dt_visc = 0.5 * a.sp.Re * a.sp.dxmin * a.sp.dxmin;
@@ -499,88 +525,118 @@ __global__ void __launch_bounds__(64, (sizeof(T) == 4 ? NSG_CW_MINB : 3)) k_col_
         }
         s_dt = dt;
     }
-    C v[32];
-    __syncthreads();
-    const T kx = __ldg(&a.kxv[i]);
-    {
-        const C* __restrict__ Gc = a.G + (size_t)i * 2048;
-#pragma unroll
-        for (int n1 = 0; n1 < 32; ++n1) v[n1] = ld_stream(&Gc[64 * n1 + t]);
-        col_fwd2048(v, ex, tw, t, lane, h);
-#if NSG_CW_EPI_SMEM
-#pragma unroll
-        for (int k2 = 0; k2 < 32; ++k2) wb[k2 * 64 + t] = v[k2];
-#endif
+    __syncthreads();  // tables and dt
 
-        // RK stage algebra (spectral_time_integration.c:50-100) on this thread's modes j = lane + 32 k2 + 1024 h
-        const double dt = s_dt;
-        const T inv_re = (T)a.sp.inv_re;
-        const T sc = (T)a.sp.scale;
-        const T cst = (STAGE == 1 || STAGE == 2) ? (T)(0.5 * dt) : (STAGE == 3 ? (T)dt : (T)(dt / 6.0));
-        const T ch = (T)(0.5 * dt), cf = (T)dt, c6 = (T)(dt / 6.0);
-        constexpr bool ifrk = IFRK;  // integrating-factor RK4 stage algebra
-        C* __restrict__ W0 = a.W0;
-        C* __restrict__ WS = a.WS;
-        C* __restrict__ ACC = a.ACC;
-        const int hv = a.sp.hv, sfd = a.sp.sfd;
-        // NB modes at a time: issue every load of the batch, then compute and store
-        constexpr int NB = NSG_CW_NB;
-#pragma unroll
-        for (int b0 = 0; b0 < 32; b0 += NB) {
-            C w0v[NB], wsv[NB], acv[NB], fbv[NB];
-            T hwv[NB], swv[NB];
-            int jjv[NB];
-#pragma unroll
-            for (int u = 0; u < NB; ++u) {
-                const int j = lane + 32 * (b0 + u) + 1024 * h;
-                const int jj = kept_jj(g, j);
-                jjv[u] = jj;
-                const size_t s = (size_t)i * Ky + (jj < 0 ? 0 : jj);
-                const bool ok = jj >= 0;
-                const C zero = cmake<C>(0.0, 0.0);
-                w0v[u] = ok ? ld_stream(&W0[s]) : zero;
-                wsv[u] = (STAGE == 1) ? w0v[u] : (ok ? ld_stream(&WS[s]) : zero);
-                acv[u] = (STAGE == 1) ? zero : (ok ? ld_stream(&ACC[s]) : zero);
-                hwv[u] = (hv && ok) ? ld_stream(&a.hvw[s]) : (T)0;
-                swv[u] = (sfd && ok) ? ld_stream(&a.sfdw[s]) : (T)0;
-                fbv[u] = (sfd && ok) ? ld_stream(&a.SFD[s]) : zero;
+    const double dt = s_dt;
+    const T inv_re = (T)a.sp.inv_re;
+    const T sc = (T)a.sp.scale;
+    const T cst = (STAGE == 1 || STAGE == 2) ? (T)(0.5 * dt) : (STAGE == 3 ? (T)dt : (T)(dt / 6.0));
+    const T ch = (T)(0.5 * dt), cf = (T)dt, c6 = (T)(dt / 6.0);
+    C* __restrict__ W0 = a.W0;
+    C* __restrict__ WS = a.WS;
+    C* __restrict__ ACC = a.ACC;
+    const C zero = cmake<C>(0.0, 0.0);
+
+    for (bool first = true; i < Kx; i += cstride, first = false) {
+        if (!first) {
+            const size_t base = (size_t)i * Ky;
+            for (int jj = t; jj < Ky; jj += 64) {
+                cp_async(&NS[jj], &a.W0[base + jj]);
+                if (hv) cp_async(&SHV[jj], &a.hvw[base + jj]);
             }
+        }
+        const T kx = __ldg(&a.kxv[i]);
+        const size_t cbase = (size_t)i * Ky;
+        C v[32];
+        // q = -1: forward transform of the Jacobian column and the RK stage;
+        // q = 0..3: inverse transforms of Omega, Omega_y, Psi, Psi_y
+#pragma unroll 1
+        for (int q = -1; q < 4; ++q) {
+            const int f = (q + 2) & 3;
+            if (q < 0) {
+                const C* __restrict__ Gc = a.G + (size_t)i * 2048;
 #pragma unroll
-            for (int u = 0; u < NB; ++u) {
-                const int jj = jjv[u];
-                const int k2 = b0 + u;
-                if (jj < 0) {
-                    wb[k2 * 64 + t] = cmake<C>(0.0, 0.0);
-                    continue;
+                for (int n1 = 0; n1 < 32; ++n1) v[n1] = ld_stream(&Gc[64 * n1 + t]);
+            } else {
+                // thread t builds modes j = 64 n1 + t; Psi = -w/k^2 is formed once
+                // (written back to NS) and reused for Psi_y by the same thread
+#pragma unroll
+                for (int n1 = 0; n1 < 32; ++n1) {
+                    const int j = 64 * n1 + t;
+                    const int jj = kept_jj(g, j);
+                    C x = zero;
+                    if (jj >= 0) {
+                        const T ky = KYS[jj];
+                        C w = NS[jj];
+                        if (f == 0) {
+                            w = field_value<T, C>(0, w, kx, ky);
+                            NS[jj] = w;
+                        }
+                        if (f == 1 || f == 3) {
+                            x.x = -ky * w.y;
+                            x.y = ky * w.x;
+                        } else {
+                            x = w;
+                        }
+                    }
+                    v[n1] = cconj(x);
                 }
-                const size_t s = (size_t)i * Ky + jj;
-                const C w0 = w0v[u], ws = wsv[u];
-                const T ky = __ldg(&kys[jj]);
-                const T k2v = k2sum(kx, ky);
-#if NSG_CW_EPI_SMEM
-                const C jh = wb[k2 * 64 + t];
-#else
+            }
+            col_fwd2048(v, X, TW, t, lane, h, bid);  // ends with a team barrier: X is free
+            if (q >= 0) {
+                C* __restrict__ Fc = a.F[f] + (size_t)i * 2048;
+#pragma unroll
+                for (int k2 = 0; k2 < 32; ++k2) Fc[lane + 32 * k2 + 1024 * h] = cconj(v[k2]);
+                continue;
+            }
+            if (STAGE != 1) {
+                for (int jj = t; jj < Ky; jj += 64) {
+                    cp_async(&X[jj], &WS[cbase + jj]);
+                    cp_async(&X[Kyp + jj], &ACC[cbase + jj]);
+                }
+            }
+            cp_async_wait_all();
+            team_sync(bid);  // the team's staged omega_hat, weights, WS and ACC
+
+            // RK stage algebra (spectral_time_integration.c:50-100) on this
+            // thread's forward outputs, modes j = lane + 32 k2 + 1024 h
+#pragma unroll
+            for (int k2 = 0; k2 < 32; ++k2) {
+                const int j = lane + 32 * k2 + 1024 * h;
+                const int jj = kept_jj(g, j);
+                if (jj < 0) continue;
+                const size_t s = cbase + jj;
                 const C jh = v[k2];
-#endif
-                if (ifrk) {
+                const C w0 = NS[jj];
+                const C ws = (STAGE == 1) ? w0 : X[jj];
+                const C acc0 = (STAGE == 1) ? zero : X[Kyp + jj];
+                const T hw = hv ? SHV[jj] : (T)0;
+                T sw = (T)0;
+                C fb = zero;
+                if (sfd) {
+                    sw = a.sfdw[s];
+                    fb = a.SFD[s];
+                }
+                const T k2v = k2sum(kx, KYS[jj]);
+                C wn;
+                if (IFRK) {
                     // integrating-factor RK4: explicit part N - SFD relaxation, exact
                     // decay by E1 = exp(-(k^2/Re + w) dt/2), E2 = E1^2
                     C k;
                     k.x = -(jh.x * sc);
                     k.y = -(jh.y * sc);
-                    if (sfd && swv[u] > (T)0) {
-                        k.x -= swv[u] * (ws.x - fbv[u].x);
-                        k.y -= swv[u] * (ws.y - fbv[u].y);
+                    if (sfd && sw > (T)0) {
+                        k.x -= sw * (ws.x - fb.x);
+                        k.y -= sw * (ws.y - fb.y);
                     }
-                    const T lam = k2v * inv_re + hwv[u];
+                    const T lam = k2v * inv_re + hw;
                     const T e1 = exp(-lam * ch), e2 = e1 * e1;
-                    C wn;
                     if (STAGE == 1) {
                         ACC[s] = cmake<C>(e2 * k.x, e2 * k.y);
                         wn.x = e1 * (w0.x + ch * k.x); wn.y = e1 * (w0.y + ch * k.y);
                         WS[s] = wn;
                     } else if (STAGE == 2 || STAGE == 3) {
-                        C acc = acv[u];
+                        C acc = acc0;
                         acc.x = acc.x + (T)2 * (e1 * k.x);
                         acc.y = acc.y + (T)2 * (e1 * k.y);
                         ACC[s] = acc;
@@ -588,108 +644,87 @@ __global__ void __launch_bounds__(64, (sizeof(T) == 4 ? NSG_CW_MINB : 3)) k_col_
                         else { wn.x = e2 * w0.x + cf * (e1 * k.x); wn.y = e2 * w0.y + cf * (e1 * k.y); }
                         WS[s] = wn;
                     } else {
-                        const C acc = acv[u];
-                        wn.x = e2 * w0.x + c6 * (acc.x + k.x);
-                        wn.y = e2 * w0.y + c6 * (acc.y + k.y);
+                        wn.x = e2 * w0.x + c6 * (acc0.x + k.x);
+                        wn.y = e2 * w0.y + c6 * (acc0.y + k.y);
                         W0[s] = wn;
                     }
-                    wb[k2 * 64 + t] = wn;
-                    continue;
-                }
-                C k;
-                k.x = -(jh.x * sc) - k2v * ws.x * inv_re;
-                k.y = -(jh.y * sc) - k2v * ws.y * inv_re;
-                if (hv || sfd) {
-                    C damp = cmake<C>(0.0, 0.0);
-                    if (hv) { damp.x += hwv[u] * ws.x; damp.y += hwv[u] * ws.y; }
-                    if (sfd && swv[u] > (T)0) {
-                        damp.x += swv[u] * (ws.x - fbv[u].x);
-                        damp.y += swv[u] * (ws.y - fbv[u].y);
-                    }
-                    k.x -= damp.x;
-                    k.y -= damp.y;
-                }
-                C wn;
-                if (STAGE == 1) {
-                    ACC[s] = k;
-                    wn.x = w0.x + cst * k.x; wn.y = w0.y + cst * k.y;
-                    WS[s] = wn;
-                } else if (STAGE == 2 || STAGE == 3) {
-                    C acc = acv[u];
-                    acc.x = acc.x + (T)2 * k.x;
-                    acc.y = acc.y + (T)2 * k.y;
-                    ACC[s] = acc;
-                    wn.x = w0.x + cst * k.x; wn.y = w0.y + cst * k.y;
-                    WS[s] = wn;
                 } else {
-                    const C acc = acv[u];
-                    wn.x = w0.x + cst * (acc.x + k.x);
-                    wn.y = w0.y + cst * (acc.y + k.y);
-                    W0[s] = wn;
-                }
-                wb[k2 * 64 + t] = wn;
-            }
-        }
-        if (STAGE == 4 && (a.sp.forcing || sfd)) {
-            // forcing increment (few low-|k| modes), then the SFD post-step, on omega_hat^{n+1}
-            const double f_amp = a.sp.forcing ? a.sp.f_sigma * sqrt(dt) : 0.0;
-            double sa = 0.0;
-            if (sfd) {
-                sa = dt / a.sp.sfd_tau;
-                sa = sa > 1.0 ? 1.0 : (sa < 0.0 ? 0.0 : sa);
-            }
-            const bool force_col = a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9;
-            // |k|^2 window, widened far beyond FP32 rounding, that screens modes before the exact FP64 shell test
-            const T k2lo = (T)(a.sp.f_kmin * a.sp.f_kmin * (1.0 - 1e-3));
-            const T k2hi = (T)(a.sp.f_kmax * a.sp.f_kmax * (1.0 + 1e-3));
-#pragma unroll 1
-            for (int k2 = 0; k2 < 32 && (force_col || sfd); ++k2) {
-                const int j = lane + 32 * k2 + 1024 * h;
-                const int jj = kept_jj(g, j);
-                if (jj < 0) continue;
-                const size_t s = (size_t)i * Ky + jj;
-                C wn = wb[k2 * 64 + t];
-                const T ky = __ldg(&kys[jj]);
-                const T k2f = kx * kx + ky * ky;
-                if (force_col && k2f >= k2lo && k2f <= k2hi) {
-                    const double2 df =
-                        forcing_increment(g, i, j, a.ds->step_cur, a.sp.f_seed, a.sp.f_kmin, a.sp.f_kmax, f_amp);
-                    if (df.x != 0.0 || df.y != 0.0) {
-                        wn.x = (T)((double)wn.x + df.x);
-                        wn.y = (T)((double)wn.y + df.y);
+                    C k;
+                    k.x = -(jh.x * sc) - k2v * ws.x * inv_re;
+                    k.y = -(jh.y * sc) - k2v * ws.y * inv_re;
+                    if (hv || sfd) {
+                        C damp = zero;
+                        if (hv) { damp.x += hw * ws.x; damp.y += hw * ws.y; }
+                        if (sfd && sw > (T)0) {
+                            damp.x += sw * (ws.x - fb.x);
+                            damp.y += sw * (ws.y - fb.y);
+                        }
+                        k.x -= damp.x;
+                        k.y -= damp.y;
+                    }
+                    if (STAGE == 1) {
+                        ACC[s] = k;
+                        wn.x = w0.x + cst * k.x; wn.y = w0.y + cst * k.y;
+                        WS[s] = wn;
+                    } else if (STAGE == 2 || STAGE == 3) {
+                        C acc = acc0;
+                        acc.x = acc.x + (T)2 * k.x;
+                        acc.y = acc.y + (T)2 * k.y;
+                        ACC[s] = acc;
+                        wn.x = w0.x + cst * k.x; wn.y = w0.y + cst * k.y;
+                        WS[s] = wn;
+                    } else {
+                        wn.x = w0.x + cst * (acc0.x + k.x);
+                        wn.y = w0.y + cst * (acc0.y + k.y);
                         W0[s] = wn;
-                        wb[k2 * 64 + t] = wn;
                     }
                 }
+                NS[jj] = wn;
+            }
+            if (STAGE == 4 && (a.sp.forcing || sfd)) {
+                // forcing increment (few low-|k| modes), then the SFD post-step, on omega_hat^{n+1}
+                const double f_amp = a.sp.forcing ? a.sp.f_sigma * sqrt(dt) : 0.0;
+                double sa = 0.0;
                 if (sfd) {
-                    C fb = a.SFD[s];
-                    const T al = (T)sa, om = (T)(1.0 - sa);
-                    fb.x = om * fb.x + al * wn.x;
-                    fb.y = om * fb.y + al * wn.y;
-                    a.SFD[s] = fb;
+                    sa = dt / a.sp.sfd_tau;
+                    sa = sa > 1.0 ? 1.0 : (sa < 0.0 ? 0.0 : sa);
+                }
+                const bool force_col = a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9;
+                // |k|^2 window, widened far beyond FP32 rounding, that screens modes before the exact FP64 shell test
+                const T k2lo = (T)(a.sp.f_kmin * a.sp.f_kmin * (1.0 - 1e-3));
+                const T k2hi = (T)(a.sp.f_kmax * a.sp.f_kmax * (1.0 + 1e-3));
+#pragma unroll 1
+                for (int k2 = 0; k2 < 32 && (force_col || sfd); ++k2) {
+                    const int j = lane + 32 * k2 + 1024 * h;
+                    const int jj = kept_jj(g, j);
+                    if (jj < 0) continue;
+                    const size_t s = cbase + jj;
+                    C wn = NS[jj];
+                    const T ky = KYS[jj];
+                    const T k2f = kx * kx + ky * ky;
+                    if (force_col && k2f >= k2lo && k2f <= k2hi) {
+                        const double2 df =
+                            forcing_increment(g, i, j, a.ds->step_cur, a.sp.f_seed, a.sp.f_kmin, a.sp.f_kmax, f_amp);
+                        if (df.x != 0.0 || df.y != 0.0) {
+                            wn.x = (T)((double)wn.x + df.x);
+                            wn.y = (T)((double)wn.y + df.y);
+                            W0[s] = wn;
+                            NS[jj] = wn;
+                        }
+                    }
+                    if (sfd) {
+                        C fb = a.SFD[s];
+                        const T al = (T)sa, om = (T)(1.0 - sa);
+                        fb.x = om * fb.x + al * wn.x;
+                        fb.y = om * fb.y + al * wn.y;
+                        a.SFD[s] = fb;
+                    }
                 }
             }
+            team_sync(bid);  // NS complete for the inverse transforms; X is free again
         }
-        if (STAGE == 4 && blockIdx.x == 0 && t == 0) a.ds->t = a.ds->t + dt;
     }
-
-    // inverse y-transforms of the next stage's Psi, Psi_y, Omega, Omega_y; F is
-    // kx-column-contiguous, so each column leaves as whole 256-byte runs
-#pragma unroll 1
-    for (int f = 0; f < 4; ++f) {
-#pragma unroll
-        for (int k2 = 0; k2 < 32; ++k2) {
-            const int j = lane + 32 * k2 + 1024 * h;
-            const int jj = kept_jj(g, j);
-            C x = cmake<C>(0.0, 0.0);
-            if (jj >= 0) x = field_value<T, C>(f, wb[k2 * 64 + t], kx, __ldg(&kys[jj]));
-            v[k2] = x;
-        }
-        col_inv2048(v, ex, tw, t, lane, h);
-        C* __restrict__ Fc = a.F[f] + (size_t)i * 2048;
-#pragma unroll
-        for (int n1 = 0; n1 < 32; ++n1) Fc[64 * n1 + t] = v[n1];
-    }
+    if (STAGE == 4 && blockIdx.x == 0 && threadIdx.x == 0) a.ds->t = a.ds->t + dt;
 }
 
 }  // namespace nsg
