@@ -178,6 +178,72 @@ def model_bytes(n: int, elem: int):
     return {"row": 5 * A * elem, "col": (5 * A + 11 * Cc / 4) * elem, "step": (40 * A + 11 * Cc) * elem}
 
 
+# ------------------------------------------------------------ ensemble leg
+ENS_MIX = ((64, 128), (128, 96), (256, 32))   # (side, members): 4,194,304 points = 2048^2
+ENS_K0 = 4.0
+
+
+def ensemble_member_params(n: int, seed: int) -> dict:
+    return dict(Re=RE, cfl_factor=CFL, adaptive_dt=1, dt=1e-4, hv_enabled=1, hv_coefficient=hv_coefficient(n),
+                hv_order=4, hv_cutoff_ratio=0.0, forcing_enabled=1, forcing_kmin=F_KMIN, forcing_kmax=F_KMAX,
+                forcing_epsilon=F_EPS, forcing_seed=F_SEED + 7919 * seed)
+
+
+def ensemble_leg(steps: int, seq_steps: int = 10) -> dict:
+    """Config-3 ensemble: one persistent launch (CUDA graph) per `steps` steps versus
+    every member advanced alone, one member after another, with the same tiling."""
+    import nsgb
+
+    sizes = [n for n, cnt in ENS_MIX for _ in range(cnt)]
+    ens = nsgb.Ensemble(sizes, 2 * math.pi, config=(128, 16, 16, 1))
+    cache = os.path.join(ROOT, "navier-stokes-solvers_gb300", "_build", "ensemble_tune.jsonl")
+    os.makedirs(os.path.dirname(cache), exist_ok=True)
+    for i, (m, n) in enumerate(zip(ens.members, sizes)):
+        m.set_params(**ensemble_member_params(n, i))
+        m.random_spectrum(IC_SEED + i, ENS_K0, E0)
+    best, tune_ms = ens.autotune(steps=2, cache_path=cache)
+    for i, (m, n) in enumerate(zip(ens.members, sizes)):  # tuning advanced the members: restart
+        m.random_spectrum(IC_SEED + i, ENS_K0, E0)
+    ens.advance(3)
+    ms = ens.advance_timed(steps, 1)
+    points = sum(n * n for n in sizes)
+    energies = [m.diagnostics()["energy"] for m in ens.members]
+    info = ens.info()
+    ens.close()
+
+    # the same members one after another through the single-instance path
+    cfg = nsgb.EnsembleConfig(*best)
+    seq = []
+    for i, n in enumerate(sizes):
+        g = nsgb.Gpu(n, n, 2 * math.pi, 2 * math.pi, nsgb.FP32, ensemble_config=cfg)
+        g.set_params(**ensemble_member_params(n, i))
+        g.random_spectrum(IC_SEED + i, ENS_K0, E0)
+        g.advance(2)
+        g.sync()
+        seq.append(g)
+    t0 = time.perf_counter()
+    for g in seq:
+        g.advance(seq_steps)
+        g.sync()
+    seq_s = time.perf_counter() - t0
+    for g in seq:
+        g.close()
+    value = points * steps / (ms * 1e-3)
+    seq_value = points * seq_steps / seq_s
+    return {"workload": "ensemble of 256 members: 128 x 64^2, 96 x 128^2, 32 x 256^2 (4,194,304 points), FP32, "
+                        "RK4 + hyperviscosity p=2, own seeds for the k0=4 initial spectrum and the forcing, "
+                        "per-member adaptive dt at CFL 0.5",
+            "metric": "aggregate grid-pt*steps/s", "value": value, "steps": steps, "ms_per_step": ms / steps,
+            "launches_per_advance": 1, "graph": True, "tiling": {"threads": best[0], "row_radix": best[1],
+                                                                   "col_radix": best[2], "cluster": best[3]},
+            "grid": info["grid"], "smem_bytes": info["smem"], "autotune_ms_per_step": tune_ms,
+            "sequential": {"value": seq_value, "steps_per_member": seq_steps,
+                           "how": "each member alone (ns_gpu_advance, same tiling), one after another, host-synchronised"},
+            "speedup_vs_sequential": value / seq_value,
+            "energy_min_max": [min(energies), max(energies)],
+            "l2": "members stay resident in L2 (state ~ 2048^2 single field); no flush inside the persistent launch"}
+
+
 # ------------------------------------------------------------ CPU legs
 def cpu_sample(n: int, budget_s: float, max_steps: int):
     """Time the oracle restatement (FP64, OpenMP) on the workload for up to budget_s."""
@@ -264,6 +330,8 @@ def main():
     ap.add_argument("--kernels-only", action="store_true",
                     help="only warmup + timed steps (a short launch sequence for ncu captures); prints no JSON")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--ensemble-steps", type=int, default=100, help="steps of the timed ensemble launch (0: skip)")
+    ap.add_argument("--ensemble-only", action="store_true", help="run only the ensemble leg and print its JSON")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -283,6 +351,10 @@ def main():
 
     import numpy as np
     import nsgb
+
+    if args.ensemble_only:
+        print(json.dumps(ensemble_leg(max(1, args.ensemble_steps))), flush=True)
+        return 0
 
     n = args.n
     prec = nsgb.FP32 if args.precision == "fp32" else nsgb.FP64
@@ -376,6 +448,10 @@ def main():
                "path": "ns_spectral_compute_cfl_timestep + ns_spectral_advance_rk4 per step (FP32 instance)"}
         s.close()
 
+    ens = None
+    if args.ensemble_steps > 0 and not args.kernels_only:
+        ens = ensemble_leg(args.ensemble_steps)
+
     cpu = None
     if not args.no_cpu and rank == 0 and ws == 1:
         cpu = cpu_sample(n, float(os.environ.get("NS_BENCH_CPU_BUDGET_S", "15")), 20)
@@ -387,6 +463,7 @@ def main():
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
         "gpu_launches": launches, "wall_s_timed_region": t_wall,
         "fp32_vs_fp64": fp32_cmp,
+        "ensemble": ens,
         "diagnostics": {"energy": diag["energy"], "enstrophy": diag["enstrophy"], "t": diag["t"], "dt": diag["dt"]},
     }
     if rank == 0:

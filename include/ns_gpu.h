@@ -171,6 +171,14 @@ int ns_gpu_profile_kernels(ns_gpu *g, int nsteps, size_t flush_bytes, double *ke
 /* Energy, enstrophy (Parseval over the dealiased state, FP64 compensated),
  * and time of the device state. */
 int ns_gpu_diagnostics(ns_gpu *g, double *energy, double *enstrophy, double *t, double *dt);
+/* Shell-binned energy spectrum of the device state, the reference's
+ * ns_spectral_analyze_spectrum (spectral_analysis.c:103-142) without the print:
+ * bin b = (int)(|k| + 0.5) < nbins, energy_sum[b] = sum over the modes of the
+ * bin of 0.5 (|u_hat|^2 + |v_hat|^2), count[b] = modes of the half spectrum in
+ * the bin (dealiased or not, as the reference counts them), energy_mean[b] =
+ * energy_sum[b] / count[b] (the reference's printed E(k)).  FP64 sums; any
+ * output may be NULL. */
+int ns_gpu_energy_spectrum(ns_gpu *g, int nbins, double *energy_sum, double *energy_mean, int *count);
 /* Seeded random-phase vorticity with E(k) ~ k^4 exp(-(k/k0)^2) rescaled to the
  * given kinetic energy, written to the device state (no reference counterpart). */
 int ns_gpu_init_random_spectrum(ns_gpu *g, uint64_t seed, double k0, double energy);
@@ -225,6 +233,57 @@ void ns_gpu_host_free(void *ptr);
 /* Raw device pointer to the kept-mode vorticity state (layout [kx_kept][ky_kept]
  * complex of the instance precision) for callers that keep data on the GPU. */
 void *ns_gpu_state_device_ptr(ns_gpu *g);
+
+/* ----------------------------------------------------- batched ensembles */
+
+/* Many independent solvers of mixed sizes advanced together by one persistent
+ * kernel launch, replayed from a CUDA graph (no reference counterpart: the
+ * reference advances one NSSpectralData per ns_spectral_advance_rk4 call,
+ * spectral_time_integration.c:34-106).  Each member is an ordinary FP32
+ * ns_gpu instance with its own state, parameters, seeds and device-side dt;
+ * the ensemble runs the same stage arithmetic as that instance's own
+ * ns_gpu_advance, so a member advanced in the ensemble equals the same member
+ * advanced alone with the same tiling (ns_gpu_create_for_ensemble). */
+typedef struct ns_gpu_ensemble ns_gpu_ensemble;
+
+/* Tiling of the persistent kernel (chosen by ns_gpu_ensemble_autotune). */
+typedef struct {
+    int threads;    /* threads per CTA: a multiple of 32, at most 256 */
+    int row_radix;  /* complex values per thread in the row (x) transforms: 4 or 16 */
+    int col_radix;  /* complex values per thread in the column (y) transforms: 4 or 16 */
+    int cluster;    /* CTAs of a thread-block cluster that share one large member: 1, 2, 4 or 8 */
+} ns_gpu_ensemble_config;
+
+/* A standalone instance whose stage kernels use an ensemble tiling: the
+ * sequential reference run of one ensemble member.  nx == ny. */
+int ns_gpu_create_for_ensemble(int nx, int ny, double Lx, double Ly, int precision,
+                               const ns_gpu_ensemble_config *cfg, ns_gpu **out);
+/* nmembers FP32 members of side n[m] (powers of two in [16, 1024]) on
+ * [0, L]^2.  Set each member's parameters and initial state through
+ * ns_gpu_ensemble_member and the instance API before advancing. */
+int ns_gpu_ensemble_create(int nmembers, const int *n, double L, const ns_gpu_ensemble_config *cfg,
+                           ns_gpu_ensemble **out);
+void ns_gpu_ensemble_destroy(ns_gpu_ensemble *e);
+/* The instance of member m (owned by the ensemble; NULL when out of range). */
+ns_gpu *ns_gpu_ensemble_member(ns_gpu_ensemble *e, int m);
+/* Advance every member nsteps RK4 steps in one persistent launch.  Asynchronous:
+ * later calls on a member's instance wait for it. */
+int ns_gpu_ensemble_advance(ns_gpu_ensemble *e, int nsteps);
+int ns_gpu_ensemble_synchronize(ns_gpu_ensemble *e);
+/* reps launches of nsteps steps each, timed with CUDA events on the ensemble
+ * stream after one untimed launch; ms_per_rep receives the mean. */
+int ns_gpu_ensemble_advance_timed(ns_gpu_ensemble *e, int nsteps, int reps, double *ms_per_rep);
+/* Switch the tiling (members' state is kept). */
+int ns_gpu_ensemble_reconfigure(ns_gpu_ensemble *e, const ns_gpu_ensemble_config *cfg);
+/* Time every valid tiling for steps steps on this ensemble (which advances its
+ * members: tune before setting initial conditions), switch to the fastest and
+ * append it to the JSON-lines cache at cache_path (may be NULL); a cached entry
+ * for the same GPU and member mix is used without timing. */
+int ns_gpu_ensemble_autotune(ns_gpu_ensemble *e, int steps, const char *cache_path, ns_gpu_ensemble_config *best,
+                             double *best_ms_per_step);
+int ns_gpu_ensemble_info(const ns_gpu_ensemble *e, int *grid, int *threads, size_t *smem, int *cluster,
+                         uint64_t *launches);
+const char *ns_gpu_ensemble_last_error(const ns_gpu_ensemble *e);
 
 #ifdef __cplusplus
 }

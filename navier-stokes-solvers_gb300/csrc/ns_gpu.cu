@@ -221,6 +221,23 @@ template <typename T> static int advance_t(ns_gpu* g, int nsteps) {
     return NS_GPU_OK;
 }
 
+int nsg_prepare_fields(ns_gpu* g) {
+    if (g->prec != NS_GPU_FP32) return NS_GPU_ERR_INVALID;
+    if (!g->fields_valid) {
+        NSG_TRY(prologue<float>(g, g->W0, g->PSI0, g->psi0_valid ? 0 : 1, 4));
+        g->fields_valid = 1;
+        g->psi0_valid = 0;
+    }
+    return NS_GPU_OK;
+}
+
+void nsg_stage_args(ns_gpu* g, RowArgs<float>* ra, ColArgs<float>* ca) {
+    *ra = row_args<float>(g);
+    for (int f = 0; f < 4; ++f) ra->F[f] = (const float2*)g->F[f];
+    ra->dx[0] = 1; ra->dx[1] = 0; ra->dx[2] = 1; ra->dx[3] = 0;  // psi_x, psi_y, omega_x, omega_y
+    *ca = col_args<float>(g);
+}
+
 // ------------------------------------------------------------ allocation
 static int dalloc(ns_gpu* g, void** p, size_t bytes) {
     cudaError_t e = cudaMalloc(p, bytes);
@@ -374,7 +391,11 @@ void ns_gpu_destroy(ns_gpu* g) {
     delete g;
 }
 
-int ns_gpu_create(int nx, int ny, double Lx, double Ly, int precision, ns_gpu** out) {
+// Create an instance.  kc (may be NULL) fixes the generic stage kernels' tiling:
+// values per thread of the row / column transforms (er, ec), rows per row block
+// (rpc), kept columns per column block (cw), and the alignment of the padded
+// kept-column count Kxp; zero fields are chosen automatically.
+int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTiling* kc, ns_gpu** out) {
     if (!out) return NS_GPU_ERR_INVALID;
     *out = nullptr;
     if (!is_pow2(nx) || !is_pow2(ny) || nx < 8 || ny < 8 || nx > 4096 || ny > 4096) {
@@ -417,7 +438,7 @@ int ns_gpu_create(int nx, int ny, double Lx, double Ly, int precision, ns_gpu** 
     {
         // NS_GB300_GENERIC_KERNELS=1 selects the generic Stockham stage kernels at every size
         const char* gen = getenv("NS_GB300_GENERIC_KERNELS");
-        const int generic = gen && gen[0] == '1';
+        const int generic = (gen && gen[0] == '1') || (kc && (kc->er || kc->ec));
         g->fast_row = (!generic && nx == 2048) ? 1 : 0;
         g->fast_col = (!generic && ny == 2048) ? 1 : 0;
     }
@@ -444,22 +465,26 @@ int ns_gpu_create(int nx, int ny, double Lx, double Ly, int precision, ns_gpu** 
     // column over the group's consecutive rows.
     G.fLB = (g->fast_row || g->fast_col) ? G.logny : 0;
     G.fTG = G.fLB ? 1 : 0;
-    g->ER = G.H >= 16 ? 16 : 4;
-    g->EC = ny >= 16 ? 16 : 4;
+    g->ER = (kc && kc->er) ? kc->er : (G.H >= 16 ? 16 : 4);
+    g->EC = (kc && kc->ec) ? kc->ec : (ny >= 16 ? 16 : 4);
     const size_t cs = (precision == NS_GPU_FP64) ? sizeof(double2) : sizeof(float2);
     // column tile width: up to 16 columns, <= 512 threads, <= ~100 KB shared memory
     {
         const int TC = ny / g->EC;
         int CW = 1;
         while (CW < 16 && 2 * CW * TC <= 512 && (size_t)2 * CW * spad_len(ny) * cs <= 100 * 1024 && CW < G.Kx) CW *= 2;
+        if (kc && kc->cw) CW = kc->cw;
         G.CW = CW;
-        G.Kxp = ((G.Kx + CW - 1) / CW) * CW;
+        int al = CW;
+        if (kc && kc->kxp_align > al) al = kc->kxp_align;
+        G.Kxp = ((G.Kx + al - 1) / al) * al;
     }
     // rows per CTA: up to 128 threads, <= ~100 KB shared memory for four fields
     {
         const int TT = G.H / g->ER;
         int RPC = 1;
         while (2 * RPC * TT <= 128 && 2 * RPC <= ny && (size_t)4 * 2 * RPC * spad_len(G.H) * cs <= 100 * 1024) RPC *= 2;
+        if (kc && kc->rpc) RPC = kc->rpc;
         G.RPC = RPC;
     }
     const size_t A = (size_t)ny * G.Kxp * cs;
@@ -516,6 +541,10 @@ int ns_gpu_create(int nx, int ny, double Lx, double Ly, int precision, ns_gpu** 
     }
     *out = g;
     return NS_GPU_OK;
+}
+
+int ns_gpu_create(int nx, int ny, double Lx, double Ly, int precision, ns_gpu** out) {
+    return nsg_create(nx, ny, Lx, Ly, precision, nullptr, out);
 }
 
 int ns_gpu_dims(const ns_gpu* g, int* kx_kept, int* ky_kept) {
@@ -1057,6 +1086,41 @@ int ns_gpu_diagnostics(ns_gpu* g, double* energy, double* enstrophy, double* t, 
     if (t) *t = h.t;
     if (dt) *dt = h.dt;
     if (h.flag & 2) NSG_FAIL(g, NS_GPU_ERR_DIVERGED, "non-finite vorticity in the device state at t=%g", h.t);
+    return NS_GPU_OK;
+}
+
+int ns_gpu_energy_spectrum(ns_gpu* g, int nbins, double* energy_sum, double* energy_mean, int* count) {
+    if (!g || nbins < 1 || nbins > 65536) return NS_GPU_ERR_INVALID;
+    if (g->outside_active)
+        NSG_FAIL(g, NS_GPU_ERR_INVALID, "energy spectrum: the state has modes outside the 2/3 mask (host-array path only)");
+    const size_t need = (size_t)nbins * (sizeof(double) + sizeof(int));
+    NSG_TRY(ensure_scratch(g, need));
+    double* dbins = (double*)g->scratch;
+    int* dcnt = (int*)(dbins + nbins);
+    NSG_CUDA(g, cudaMemsetAsync(g->scratch, 0, need, g->st));
+    const long long n = (long long)g->g.Kx * g->g.Ky;
+    const size_t sm = (size_t)nbins * sizeof(double);
+    if (sm > 48 * 1024) {
+        if (g->prec == NS_GPU_FP64) NSG_CUDA(g, cudaFuncSetAttribute(k_energy_spectrum<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        else NSG_CUDA(g, cudaFuncSetAttribute(k_energy_spectrum<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    }
+    if (g->prec == NS_GPU_FP64)
+        k_energy_spectrum<double><<<grid_for(n, 256, 4 * g->num_sms), 256, sm, g->st>>>(g->g, (const double2*)g->W0, nbins, dbins);
+    else
+        k_energy_spectrum<float><<<grid_for(n, 256, 4 * g->num_sms), 256, sm, g->st>>>(g->g, (const float2*)g->W0, nbins, dbins);
+    NSG_LAUNCHED(g);
+    k_spectrum_counts<<<grid_for((long long)g->g.nkx * g->g.nky), 256, 0, g->st>>>(g->g, nbins, dcnt);
+    NSG_LAUNCHED(g);
+    std::vector<double> hs(nbins);
+    std::vector<int> hc(nbins);
+    NSG_TRY(d2h(g, hs.data(), dbins, (size_t)nbins * sizeof(double)));
+    NSG_TRY(d2h(g, hc.data(), dcnt, (size_t)nbins * sizeof(int)));
+    NSG_TRY(sync(g));
+    for (int b = 0; b < nbins; ++b) {
+        if (energy_sum) energy_sum[b] = hs[b];
+        if (energy_mean) energy_mean[b] = hc[b] > 0 ? hs[b] / hc[b] : 0.0;
+        if (count) count[b] = hc[b];
+    }
     return NS_GPU_OK;
 }
 

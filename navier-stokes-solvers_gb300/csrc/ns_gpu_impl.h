@@ -102,3 +102,15 @@ struct ProfScope {
         if (_s != NS_GPU_OK) return _s; \
     } while (0)
 
+// Tiling of the generic stage kernels (zero: automatic), see nsg_create.
+struct NsgTiling {
+    int er, ec;       // complex values per thread in the row / column transforms (4, 8 or 16)
+    int rpc, cw;      // rows per row block, kept columns per column block
+    int kxp_align;    // the padded kept-column count Kxp is a multiple of this
+};
+int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTiling* kc, ns_gpu** out);
+// Run the stage-1 field prologue of an instance if its fields are stale (FP32
+// generic kernels; instance stream, asynchronous).
+int nsg_prepare_fields(ns_gpu* g);
+// Kernel arguments of an FP32 instance as its stage kernels see them.
+void nsg_stage_args(ns_gpu* g, nsg::RowArgs<float>* ra, nsg::ColArgs<float>* ca);

@@ -117,7 +117,7 @@ __device__ __forceinline__ DD dd_merge(DD a, DD b) {
     return r;
 }
 // block-wide merge; returns the total in thread 0
-__device__ DD block_dd(DD v) {
+static __device__ DD block_dd(DD v) {
     __shared__ double ss[32], sc[32];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -626,6 +626,9 @@ __global__ void __launch_bounds__(512) k_col(Geo g, ColArgs<T> a) {
 }
 
 // ======================================================= auxiliary kernels
+// (left out of translation units that define NSG_NO_AUX_KERNELS: their host
+// stubs are defined once, by the instance engine)
+#ifndef NSG_NO_AUX_KERNELS
 
 // grid, wavenumbers, k^2, mask exactly as spectral_initialization.c:15-49
 __global__ void k_geometry(Geo g, double* x, double* y, double* kx, double* ky, double* k2, int* mask) {
@@ -1200,5 +1203,52 @@ __global__ void k_forcing_generate(int n, const double* weights, int colored, do
         if (colored) { double2 c = cs[idx]; cs[idx] = make_double2(c.x * sc, c.y * sc); }
     }
 }
+
+// Shell-binned energy spectrum of the kept-mode state with the reference's
+// binning (spectral_analysis.c:103-123): bin (int)(|k| + 0.5) for bins < nbins,
+// per-mode energy 0.5 (|u_hat|^2 + |v_hat|^2) with psi = -omega/k^2,
+// u_hat = i ky psi, v_hat = -i kx psi (spectral_core.c:17-31).  Wavenumbers in
+// FP64 as the reference's tables; per-block shared-memory bins, then one
+// atomic per bin and block.  dynamic smem = nbins doubles.
+template <typename T>
+__global__ void k_energy_spectrum(Geo g, const typename CT<T>::C* W, int nbins, double* bins) {
+    extern __shared__ double sbin[];
+    for (int b = threadIdx.x; b < nbins; b += blockDim.x) sbin[b] = 0.0;
+    __syncthreads();
+    const long long n = (long long)g.Kx * g.Ky;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(idx / g.Ky), jj = (int)(idx - (long long)i * g.Ky);
+        const int j = kept_j(g, jj);
+        const double kx = 2.0 * 3.14159265358979323846 * i / g.Lx;
+        const double ky = (j <= g.ny / 2) ? 2.0 * 3.14159265358979323846 * j / g.Ly
+                                          : 2.0 * 3.14159265358979323846 * (j - g.ny) / g.Ly;
+        const double k2 = k2sum(kx, ky);
+        const int bin = (int)(sqrt(k2) + 0.5);
+        if (bin >= nbins || k2 <= 1e-12) continue;
+        const typename CT<T>::C w = W[(size_t)i * g.Ky + jj];
+        const double px = -(double)w.x / k2, py = -(double)w.y / k2;
+        const double p2 = px * px + py * py;
+        atomicAdd(&sbin[bin], 0.5 * (ky * ky * p2 + kx * kx * p2));
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < nbins; b += blockDim.x)
+        if (sbin[b] != 0.0) atomicAdd(&bins[b], sbin[b]);
+}
+
+// modes per bin over the whole half spectrum [nky][nkx] (the reference counts
+// every mode, dealiased or not, spectral_analysis.c:116-121)
+__global__ void k_spectrum_counts(Geo g, int nbins, int* counts) {
+    const long long n = (long long)g.nkx * g.nky;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(idx / g.nkx), i = (int)(idx - (long long)j * g.nkx);
+        const double kx = 2.0 * 3.14159265358979323846 * i / g.Lx;
+        const double ky = (j <= g.ny / 2) ? 2.0 * 3.14159265358979323846 * j / g.Ly
+                                          : 2.0 * 3.14159265358979323846 * (j - g.ny) / g.Ly;
+        const int bin = (int)(sqrt(k2sum(kx, ky)) + 0.5);
+        if (bin < nbins) atomicAdd(&counts[bin], 1);
+    }
+}
+
+#endif  // NSG_NO_AUX_KERNELS
 
 }  // namespace nsg

@@ -22,18 +22,7 @@
 #include <string.h>
 
 #include "ns_gpu.h"
-
-struct ns_spectral_gpu {
-    ns_gpu *dev;
-    int precision;
-    int host_stale;      /* device state is newer than the host arrays */
-    int device_current;  /* device state equals the host arrays (no upload needed) */
-    unsigned long long step;
-    int forcing_enabled;
-    double forcing_kmin, forcing_kmax, forcing_epsilon;
-    unsigned long long forcing_seed;
-    int scheme;
-};
+#include "ns_spectral_internal.h"
 
 static void ns_report(NSSpectralData *d, const char *what, int status) {
     fprintf(stderr, "[ns-gb300] %s failed: %s (%s)\n", what, ns_gpu_status_string(status),

@@ -81,6 +81,15 @@ class GpuParams(C.Structure):
     ]
 
 
+class EnsembleConfig(C.Structure):
+    """ns_gpu_ensemble_config (include/ns_gpu.h)."""
+
+    _fields_ = [("threads", C.c_int), ("row_radix", C.c_int), ("col_radix", C.c_int), ("cluster", C.c_int)]
+
+    def as_tuple(self):
+        return (self.threads, self.row_radix, self.col_radix, self.cluster)
+
+
 FP64, FP32 = 0, 1
 _LIB = None
 
@@ -154,6 +163,20 @@ def load(build: bool = True) -> C.CDLL:
     proto("ns_gpu_init_random_spectrum", C.c_int, vp, C.c_uint64, C.c_double, C.c_double)
     proto("ns_gpu_random_spectrum_host", C.c_int, vp, C.c_uint64, C.c_double, C.c_double, _DP)
     proto("ns_gpu_state_device_ptr", vp, vp)
+    proto("ns_gpu_energy_spectrum", C.c_int, vp, C.c_int, _DP, _DP, C.POINTER(C.c_int))
+    ecp = C.POINTER(EnsembleConfig)
+    proto("ns_gpu_create_for_ensemble", C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, ecp, C.POINTER(vp))
+    proto("ns_gpu_ensemble_create", C.c_int, C.c_int, C.POINTER(C.c_int), C.c_double, ecp, C.POINTER(vp))
+    proto("ns_gpu_ensemble_destroy", None, vp)
+    proto("ns_gpu_ensemble_member", vp, vp, C.c_int)
+    proto("ns_gpu_ensemble_advance", C.c_int, vp, C.c_int)
+    proto("ns_gpu_ensemble_synchronize", C.c_int, vp)
+    proto("ns_gpu_ensemble_advance_timed", C.c_int, vp, C.c_int, C.c_int, _DP)
+    proto("ns_gpu_ensemble_reconfigure", C.c_int, vp, ecp)
+    proto("ns_gpu_ensemble_autotune", C.c_int, vp, C.c_int, C.c_char_p, ecp, _DP)
+    proto("ns_gpu_ensemble_info", C.c_int, vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_size_t),
+          C.POINTER(C.c_int), C.POINTER(C.c_uint64))
+    proto("ns_gpu_ensemble_last_error", C.c_char_p, vp)
     _LIB = lib
     return lib
 
@@ -281,12 +304,20 @@ class Solver:
 class Gpu:
     """Direct use of the C-ABI (include/ns_gpu.h) with a device-resident state."""
 
-    def __init__(self, nx: int, ny: int, Lx: float = 2 * np.pi, Ly: float = 2 * np.pi, precision: int = FP32):
+    def __init__(self, nx: int, ny: int, Lx: float = 2 * np.pi, Ly: float = 2 * np.pi, precision: int = FP32,
+                 ensemble_config: "EnsembleConfig | None" = None, handle=None):
         self.lib = load()
-        h = C.c_void_p()
-        st = self.lib.ns_gpu_create(nx, ny, Lx, Ly, precision, C.byref(h))
-        if st != 0:
-            raise RuntimeError(f"ns_gpu_create failed: {self.lib.ns_gpu_status_string(st).decode()}")
+        self.owned = handle is None
+        if handle is None:
+            h = C.c_void_p()
+            if ensemble_config is None:
+                st = self.lib.ns_gpu_create(nx, ny, Lx, Ly, precision, C.byref(h))
+            else:
+                st = self.lib.ns_gpu_create_for_ensemble(nx, ny, Lx, Ly, precision, C.byref(ensemble_config), C.byref(h))
+            if st != 0:
+                raise RuntimeError(f"ns_gpu_create failed: {self.lib.ns_gpu_status_string(st).decode()}")
+        else:
+            h = C.c_void_p(handle)
         self.h = h
         self.nx, self.ny = nx, ny
         self.nkx, self.nky = nx // 2 + 1, ny
@@ -297,7 +328,8 @@ class Gpu:
 
     def close(self):
         if getattr(self, "h", None):
-            self.lib.ns_gpu_destroy(self.h)
+            if self.owned:
+                self.lib.ns_gpu_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -364,7 +396,82 @@ class Gpu:
     def launches(self) -> int:
         return int(self.lib.ns_gpu_launch_count(self.h))
 
+    def energy_spectrum(self, nbins: int | None = None):
+        """Shell sums, per-shell means and mode counts (spectral_analysis.c:103-142)."""
+        if nbins is None:
+            nbins = min(self.nkx, self.nky // 2)
+        es = np.zeros(nbins)
+        em = np.zeros(nbins)
+        ct = np.zeros(nbins, dtype=np.int32)
+        self.check(self.lib.ns_gpu_energy_spectrum(self.h, nbins, _ptr(es), _ptr(em),
+                                                   ct.ctypes.data_as(C.POINTER(C.c_int))), "energy_spectrum")
+        return es, em, ct
+
     def dims(self):
         a, b = C.c_int(), C.c_int()
         self.lib.ns_gpu_dims(self.h, C.byref(a), C.byref(b))
         return a.value, b.value
+
+
+class Ensemble:
+    """Batched ensemble (ns_gpu_ensemble_*): members of mixed sizes advanced by one
+    persistent launch replayed from a CUDA graph."""
+
+    def __init__(self, sizes, L: float = 2 * np.pi, config=(128, 16, 16, 1)):
+        self.lib = load()
+        self.sizes = [int(n) for n in sizes]
+        cfg = EnsembleConfig(*config)
+        arr = (C.c_int * len(self.sizes))(*self.sizes)
+        h = C.c_void_p()
+        st = self.lib.ns_gpu_ensemble_create(len(self.sizes), arr, L, C.byref(cfg), C.byref(h))
+        if st != 0:
+            raise RuntimeError(f"ns_gpu_ensemble_create failed: {self.lib.ns_gpu_status_string(st).decode()}")
+        self.h = h
+        self.members = [Gpu(n, n, L, L, handle=self.lib.ns_gpu_ensemble_member(h, i)) for i, n in enumerate(self.sizes)]
+
+    def check(self, st, what):
+        if st != 0:
+            raise RuntimeError(f"{what} failed ({st}): {self.lib.ns_gpu_ensemble_last_error(self.h).decode()}")
+
+    def advance(self, n: int):
+        self.check(self.lib.ns_gpu_ensemble_advance(self.h, n), "ensemble_advance")
+
+    def sync(self):
+        self.check(self.lib.ns_gpu_ensemble_synchronize(self.h), "ensemble_synchronize")
+
+    def advance_timed(self, n: int, reps: int = 1) -> float:
+        ms = C.c_double()
+        self.check(self.lib.ns_gpu_ensemble_advance_timed(self.h, n, reps, C.byref(ms)), "ensemble_advance_timed")
+        return ms.value
+
+    def reconfigure(self, config):
+        cfg = EnsembleConfig(*config)
+        self.check(self.lib.ns_gpu_ensemble_reconfigure(self.h, C.byref(cfg)), "ensemble_reconfigure")
+
+    def autotune(self, steps: int = 2, cache_path: str | None = None):
+        best = EnsembleConfig()
+        ms = C.c_double()
+        self.check(self.lib.ns_gpu_ensemble_autotune(self.h, steps, cache_path.encode() if cache_path else None,
+                                                     C.byref(best), C.byref(ms)), "ensemble_autotune")
+        return best.as_tuple(), ms.value
+
+    def info(self) -> dict:
+        g, t, c = C.c_int(), C.c_int(), C.c_int()
+        sm = C.c_size_t()
+        ln = C.c_uint64()
+        self.check(self.lib.ns_gpu_ensemble_info(self.h, C.byref(g), C.byref(t), C.byref(sm), C.byref(c), C.byref(ln)),
+                   "ensemble_info")
+        return {"grid": g.value, "threads": t.value, "smem": sm.value, "cluster": c.value, "launches": ln.value}
+
+    def close(self):
+        if getattr(self, "h", None):
+            for m in self.members:
+                m.h = None
+            self.lib.ns_gpu_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
