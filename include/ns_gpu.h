@@ -234,6 +234,21 @@ void ns_gpu_host_free(void *ptr);
  * complex of the instance precision) for callers that keep data on the GPU. */
 void *ns_gpu_state_device_ptr(ns_gpu *g);
 
+/* ----------------------------------------- device-resident physical fields */
+
+/* Physical vorticity of the device state, omega[ny][nx] as float in a caller
+ * device buffer (the masked c2r of spectral_transforms.c:25-32 on the state). */
+int ns_gpu_vorticity_device(ns_gpu *g, float *omega_dev);
+/* omega += delta for a physical float field delta[ny][nx] on the device: the
+ * normalised, dealiased forward transform (spectral_transforms.c:9-22) of delta
+ * is added to the state's kept modes. */
+int ns_gpu_add_vorticity_device(ns_gpu *g, const float *delta_dev);
+/* Spectral truncation of a fine state onto a coarser instance of the same box
+ * and precision: the coarse kept modes take the fine values of the same (kx, ky)
+ * (forward transforms are normalised by 1/(nx ny), so amplitudes carry over);
+ * the coarse time is set to the fine time.  No reference counterpart. */
+int ns_gpu_filter_state(ns_gpu *fine, ns_gpu *coarse);
+
 /* ----------------------------------------------------- batched ensembles */
 
 /* Many independent solvers of mixed sizes advanced together by one persistent
@@ -284,6 +299,42 @@ int ns_gpu_ensemble_autotune(ns_gpu_ensemble *e, int steps, const char *cache_pa
 int ns_gpu_ensemble_info(const ns_gpu_ensemble *e, int *grid, int *threads, size_t *smem, int *cluster,
                          uint64_t *launches);
 const char *ns_gpu_ensemble_last_error(const ns_gpu_ensemble *e);
+
+/* -------------------------------------------------- learned corrector */
+
+/* A periodic 3x3 CNN that corrects coarse-grid steps (no reference
+ * counterpart): 6 layers, 2 -> 64 -> 64 -> 64 -> 64 -> 64 -> 1 channels, GELU
+ * between layers, BF16 weights (rounded from an FP32 master copy after every
+ * AdamW step), FP32 activations and accumulation, hand-written forward and
+ * backward kernels.  Input sample: [2][H][W] float = (coarse omega(t), plain
+ * coarse-step increment omega_plain(t+dt) - omega(t)); output [H][W]: the
+ * vorticity correction.  Parameters are one flat FP32 vector, per layer l the
+ * weights [3 dy + dx][ci][co] then the biases [co]. */
+typedef struct ns_cnn ns_cnn;
+/* H a multiple of 8, W a multiple of 16; activations for max_batch samples */
+int ns_cnn_create(int height, int width, int max_batch, uint64_t seed, ns_cnn **out);
+void ns_cnn_destroy(ns_cnn *c);
+const char *ns_cnn_last_error(const ns_cnn *c);
+int ns_cnn_param_count(const ns_cnn *c, size_t *n);
+uint64_t ns_cnn_launch_count(const ns_cnn *c);
+int ns_cnn_get_params(ns_cnn *c, float *host);
+/* sets the parameters and resets the AdamW moments */
+int ns_cnn_set_params(ns_cnn *c, const float *host);
+/* network input = (in0 * in_scale0, in1 * in_scale1); target = correction * out_scale */
+int ns_cnn_set_normalization(ns_cnn *c, float in_scale0, float in_scale1, float out_scale);
+/* training set on the device: inputs [n][2][H][W], targets [n][H][W] (host arrays) */
+int ns_cnn_set_dataset(ns_cnn *c, const float *inputs, const float *targets, int n);
+/* mean-squared-error loss (normalised units) and its parameter gradient for a host
+ * batch, parameters unchanged (gradient checks) */
+int ns_cnn_loss_and_grads(ns_cnn *c, const float *inputs, const float *targets, int batch, double *loss, float *grads);
+/* corrections [batch][H][W] (physical units) for a host batch */
+int ns_cnn_forward_host(ns_cnn *c, const float *inputs, int batch, float *out);
+/* iterations AdamW steps (beta 0.9 / 0.999, eps 1e-8, decoupled weight decay) on
+ * minibatches drawn from the dataset with a seeded generator; loss_history may be NULL */
+int ns_cnn_train(ns_cnn *c, int iterations, int batch, float lr, float weight_decay, uint64_t seed, double *loss_history);
+/* nsteps corrected steps of an instance on the network's grid: plain RK4 step
+ * (ns_gpu_advance), then omega += CNN(omega(t), omega(t+dt) - omega(t)) */
+int ns_cnn_correct_step(ns_cnn *c, ns_gpu *g, int nsteps);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,686 @@
+// Learned coarse-grid corrector: a 6-layer periodic 3x3 CNN (2 -> 64 x 5 -> 1
+// channels, GELU between layers) trained and applied with hand-written
+// forward and backward kernels.  No reference counterpart: the reference has
+// no learned component; the network corrects each coarse-grid step of this
+// library's own solver (include/ns_gpu.h, ns_cnn_*).
+//
+// Numerics: every convolution computes in FP32 from BF16 weights (the
+// AdamW update keeps an FP32 master copy and rounds it to BF16 after each
+// step); activations, gradients and accumulations are FP32.  Layout: NHWC,
+// activation [b][y][x][c]; weights [tap][ci][co] with tap = 3 dy + dx and
+// input offsets (dy - 1, dx - 1), periodic in both directions.
+//
+//   forward       k_conv3x3<CIN, COUT, CPT, GELU>: an 8 x 16 pixel tile per
+//                 CTA iteration (persistent grid), the tile's periodic halo and
+//                 the layer's weights in shared memory, CPT output channels per
+//                 thread, bias and GELU fused, pre-activation kept for backward
+//   input grad    the same kernel on the output gradient with the weights
+//                 flipped and transposed: wT[8 - tap][co][ci] = w[tap][ci][co]
+//   weight grad   k_conv_dw<CIN, COUT>: per-thread 3 x CBI x CBO blocks
+//                 accumulated over the CTA's tiles, one atomic per weight
+//   optimiser     AdamW with bias correction
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ns_gpu.h"
+
+namespace {
+
+constexpr int TH = 8, TW = 16, TP = TH * TW;  // pixel tile
+constexpr int NL = 6;                           // layers
+constexpr int HID = 64;                         // hidden channels
+constexpr int CIN_OF[NL] = {2, HID, HID, HID, HID, HID};
+constexpr int COUT_OF[NL] = {HID, HID, HID, HID, HID, 1};
+
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x) {
+    const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
+    return cdf + x * 0.39894228040143268f * expf(-0.5f * x * x);
+}
+__device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+template <int CIN, int COUT, int CPT> constexpr size_t conv_smem() {
+    return (size_t)(9 * CIN * COUT + (TH + 2) * (TW + 2) * (CIN + 1)) * sizeof(float);
+}
+
+// out = act(conv(in) + bias): in [B][H][W][CIN], pre/act [B][H][W][COUT]; act may be
+// null (pre only); bias may be null.  H % 8 == 0, W % 16 == 0.
+template <int CIN, int COUT, int CPT, bool GELU>
+__global__ void __launch_bounds__(TP*(COUT / CPT)) k_conv3x3(const float* __restrict__ in, const __nv_bfloat16* __restrict__ w,
+                                                             const float* __restrict__ bias, float* __restrict__ pre,
+                                                             float* __restrict__ act, int B, int H, int W) {
+    extern __shared__ float sm[];
+    float* sw = sm;                      // [9][CIN][COUT]
+    float* sx = sm + 9 * CIN * COUT;     // [(TH+2)(TW+2)][CIN + 1]
+    constexpr int CP = CIN + 1;
+    for (int i = threadIdx.x; i < 9 * CIN * COUT; i += blockDim.x) sw[i] = __bfloat162float(w[i]);
+    const int ntx = W / TW, nty = H / TH, ntiles = B * nty * ntx;
+    const int p = threadIdx.x % TP, g = threadIdx.x / TP;
+    const int py = p / TW, px = p - py * TW;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int b = tile / (nty * ntx), r = tile - b * nty * ntx;
+        const int y0 = (r / ntx) * TH, x0 = (r % ntx) * TW;
+        const float* inb = in + (size_t)b * H * W * CIN;
+        __syncthreads();  // previous tile done with sx (and sw written)
+        for (int i = threadIdx.x; i < (TH + 2) * (TW + 2) * CIN; i += blockDim.x) {
+            const int q = i / CIN, c = i - q * CIN;
+            const int hy = q / (TW + 2), hx = q - hy * (TW + 2);
+            sx[q * CP + c] = inb[((size_t)wrapi(y0 + hy - 1, H) * W + wrapi(x0 + hx - 1, W)) * CIN + c];
+        }
+        __syncthreads();
+        float acc[CPT];
+#pragma unroll
+        for (int k = 0; k < CPT; ++k) acc[k] = bias ? bias[g * CPT + k] : 0.0f;
+#pragma unroll 1
+        for (int tap = 0; tap < 9; ++tap) {
+            const int dy = tap / 3, dx = tap - 3 * dy;
+            const float* xs = sx + ((py + dy) * (TW + 2) + px + dx) * CP;
+            const float* ws = sw + tap * CIN * COUT + g * CPT;
+#pragma unroll 4
+            for (int ci = 0; ci < CIN; ++ci) {
+                const float xv = xs[ci];
+                const float* wr = ws + ci * COUT;
+#pragma unroll
+                for (int k = 0; k < CPT; ++k) acc[k] = fmaf(xv, wr[k], acc[k]);
+            }
+        }
+        const size_t o = (((size_t)b * H + y0 + py) * W + x0 + px) * COUT + g * CPT;
+#pragma unroll
+        for (int k = 0; k < CPT; ++k) {
+            pre[o + k] = acc[k];
+            if (act) act[o + k] = GELU ? gelu(acc[k]) : acc[k];
+        }
+    }
+}
+
+__host__ __device__ constexpr int cmin(int a, int b) { return a < b ? a : b; }
+template <int CIN, int COUT> __host__ __device__ constexpr int dw_threads() { return (CIN / cmin(4, CIN)) * (COUT / cmin(4, COUT)) * 3; }
+template <int CIN, int COUT> constexpr size_t dw_smem() {
+    return (size_t)((TH + 2) * (TW + 2) * (CIN + 4) + TP * COUT) * sizeof(float);
+}
+
+// dw[tap][ci][co] += sum over pixels of in[p + off(tap)][ci] * dpre[p][co]
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(dw_threads<CIN, COUT>()) k_conv_dw(const float* __restrict__ in, const float* __restrict__ dpre,
+                                                                     float* __restrict__ dw, int B, int H, int W) {
+    constexpr int CBI = cmin(4, CIN), CBO = cmin(4, COUT);
+    constexpr int NCIB = CIN / CBI, NCOB = COUT / CBO;
+    constexpr int CP = CIN + 4;
+    extern __shared__ float sm[];
+    float* sx = sm;                                 // [(TH+2)(TW+2)][CIN + 4]
+    float* sd = sm + (TH + 2) * (TW + 2) * CP;      // [TP][COUT]
+    const int dyi = threadIdx.x / (NCIB * NCOB);
+    const int rem = threadIdx.x - dyi * NCIB * NCOB;
+    const int cib = rem / NCOB, cob = rem - cib * NCOB;
+    float acc[3][CBI][CBO];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int i = 0; i < CBI; ++i)
+#pragma unroll
+            for (int j = 0; j < CBO; ++j) acc[d][i][j] = 0.0f;
+    const int ntx = W / TW, nty = H / TH, ntiles = B * nty * ntx;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int b = tile / (nty * ntx), r = tile - b * nty * ntx;
+        const int y0 = (r / ntx) * TH, x0 = (r % ntx) * TW;
+        const float* inb = in + (size_t)b * H * W * CIN;
+        __syncthreads();
+        for (int i = threadIdx.x; i < (TH + 2) * (TW + 2) * CIN; i += blockDim.x) {
+            const int q = i / CIN, c = i - q * CIN;
+            const int hy = q / (TW + 2), hx = q - hy * (TW + 2);
+            sx[q * CP + c] = inb[((size_t)wrapi(y0 + hy - 1, H) * W + wrapi(x0 + hx - 1, W)) * CIN + c];
+        }
+        for (int i = threadIdx.x; i < TP * COUT; i += blockDim.x) {
+            const int q = i / COUT, c = i - q * COUT;
+            const int qy = q / TW, qx = q - qy * TW;
+            sd[i] = dpre[(((size_t)b * H + y0 + qy) * W + x0 + qx) * COUT + c];
+        }
+        __syncthreads();
+#pragma unroll 2
+        for (int q = 0; q < TP; ++q) {
+            const int qy = q / TW, qx = q - qy * TW;
+            float dv[CBO];
+#pragma unroll
+            for (int j = 0; j < CBO; ++j) dv[j] = sd[q * COUT + cob * CBO + j];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const float* xs = sx + ((qy + dyi) * (TW + 2) + qx + d) * CP + cib * CBI;
+#pragma unroll
+                for (int i = 0; i < CBI; ++i) {
+                    const float xv = xs[i];
+#pragma unroll
+                    for (int j = 0; j < CBO; ++j) acc[d][i][j] = fmaf(xv, dv[j], acc[d][i][j]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int i = 0; i < CBI; ++i)
+#pragma unroll
+            for (int j = 0; j < CBO; ++j)
+                atomicAdd(&dw[((dyi * 3 + d) * CIN + cib * CBI + i) * COUT + cob * CBO + j], acc[d][i][j]);
+}
+
+// db[co] += sum over pixels of dpre[p][co]
+__global__ void k_bias_grad(const float* __restrict__ dpre, long long npix, int cout, float* __restrict__ db) {
+    extern __shared__ float sb[];
+    for (int c = threadIdx.x; c < cout; c += blockDim.x) sb[c] = 0.0f;
+    __syncthreads();
+    const long long n = npix * cout;
+    float acc = 0.0f;
+    // blockDim.x is a multiple of cout, so every thread sums one channel
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        acc += dpre[i];
+    atomicAdd(&sb[threadIdx.x % cout], acc);
+    __syncthreads();
+    for (int c = threadIdx.x; c < cout; c += blockDim.x) atomicAdd(&db[c], sb[c]);
+}
+
+// d <- d * gelu'(pre), in place
+__global__ void k_gelu_bwd(float* __restrict__ d, const float* __restrict__ pre, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        d[i] *= gelu_grad(pre[i]);
+}
+
+// loss += sum (out - tgt)^2 / n (FP64), grad = 2 (out - tgt) / n
+__global__ void k_mse(const float* __restrict__ out, const float* __restrict__ tgt, long long n, float* __restrict__ grad,
+                      double* __restrict__ loss) {
+    __shared__ double sl[32];
+    double acc = 0.0;
+    const float inv = 1.0f / (float)n;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float d = out[i] - tgt[i];
+        acc += (double)d * d;
+        if (grad) grad[i] = 2.0f * d * inv;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) sl[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sl[w];
+        atomicAdd(loss, s / (double)n);
+    }
+}
+
+// AdamW (decoupled weight decay), bias-corrected moments
+__global__ void k_adamw(float* __restrict__ p, float* __restrict__ m, float* __restrict__ v, const float* __restrict__ g,
+                        long long n, float lr, float b1, float b2, float eps, float wd, float bc1, float bc2) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.0f - b1) * gi;
+        const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        const float mh = mi / bc1, vh = vi / bc2;
+        p[i] -= lr * (mh / (sqrtf(vh) + eps) + wd * p[i]);
+    }
+}
+
+// BF16 compute copies of one layer: wb[tap][ci][co], wbT[8 - tap][co][ci]
+__global__ void k_round_weights(const float* __restrict__ w, int cin, int cout, __nv_bfloat16* __restrict__ wb,
+                                __nv_bfloat16* __restrict__ wbt) {
+    const int n = 9 * cin * cout;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int tap = i / (cin * cout), r = i - tap * cin * cout;
+        const int ci = r / cout, co = r - ci * cout;
+        const __nv_bfloat16 h = __float2bfloat16_rn(w[i]);
+        wb[i] = h;
+        wbt[((8 - tap) * cout + co) * cin + ci] = h;
+    }
+}
+
+// batch gather: x [B][H][W][2] = (in0 s0, in1 s1) of samples idx[b], tgt [B][H][W] = target s_out
+__global__ void k_gather(const float* __restrict__ din, const float* __restrict__ dtg, const int* __restrict__ idx, int B,
+                         int H, int W, float s0, float s1, float so, float* __restrict__ x, float* __restrict__ tgt) {
+    const long long hw = (long long)H * W, n = (long long)B * hw;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int b = (int)(i / hw);
+        const long long q = i - b * hw;
+        const long long s = idx[b];
+        x[2 * i] = din[(s * 2) * hw + q] * s0;
+        x[2 * i + 1] = din[(s * 2 + 1) * hw + q] * s1;
+        if (tgt) tgt[i] = dtg[s * hw + q] * so;
+    }
+}
+
+// x [H][W][2] = (w0 s0, (w1 - w0) s1) for a single coarse state
+__global__ void k_make_input(const float* __restrict__ w0, const float* __restrict__ w1, long long n, float s0, float s1,
+                             float* __restrict__ x) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        x[2 * i] = w0[i] * s0;
+        x[2 * i + 1] = (w1[i] - w0[i]) * s1;
+    }
+}
+
+__global__ void k_scale(float* __restrict__ a, long long n, float s) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) a[i] *= s;
+}
+
+// Philox-free deterministic init: uniform(-a, a) from splitmix64 of (seed, index)
+__host__ __device__ inline unsigned long long mix64(unsigned long long z) {
+    z += 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+int grid_of(long long n, int threads, int cap) {
+    long long b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > cap) b = cap;
+    return (int)b;
+}
+
+}  // namespace
+
+struct ns_cnn {
+    int H = 0, W = 0, maxB = 0;
+    int device = 0, num_sms = 1;
+    cudaStream_t st = nullptr;
+    size_t nparam = 0;
+    size_t woff[NL], boff[NL];     // offsets into the flat FP32 parameter vector
+    float *p = nullptr, *gp = nullptr, *m = nullptr, *v = nullptr;  // master, grad, moments
+    __nv_bfloat16 *wb[NL] = {}, *wbt[NL] = {};
+    float* x0 = nullptr;           // [B][H][W][2]
+    float *pre[NL] = {}, *act[NL] = {};
+    float *d0 = nullptr, *d1 = nullptr;  // gradient ping-pong [B][H][W][64]
+    float* tgt = nullptr;          // [B][H][W]
+    double* dloss = nullptr;       // loss history / scratch
+    int loss_cap = 0;
+    int* didx = nullptr;
+    float* data_in = nullptr;      // [N][2][H][W]
+    float* data_tg = nullptr;      // [N][H][W]
+    int ndata = 0;
+    float s0 = 1.0f, s1 = 1.0f, so = 1.0f;
+    long long step = 0;            // AdamW step counter
+    float *cw0 = nullptr, *cw1 = nullptr;  // corrector scratch [H][W]
+    unsigned long long launches = 0;
+    std::string err;
+};
+
+#define CNN_FAIL(c, code, ...)                   \
+    do {                                         \
+        char _b[512];                            \
+        snprintf(_b, sizeof(_b), __VA_ARGS__);   \
+        (c)->err = _b;                           \
+        return (code);                           \
+    } while (0)
+#define CNN_CUDA(c, call)                                                                              \
+    do {                                                                                               \
+        cudaError_t _e = (call);                                                                       \
+        if (_e != cudaSuccess) CNN_FAIL(c, NS_GPU_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(_e)); \
+    } while (0)
+#define CNN_LAUNCHED(c)                                                                                     \
+    do {                                                                                                    \
+        (c)->launches++;                                                                                    \
+        cudaError_t _e = cudaGetLastError();                                                                \
+        if (_e != cudaSuccess) CNN_FAIL(c, NS_GPU_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(_e)); \
+    } while (0)
+
+template <int CIN, int COUT, int CPT, bool GELU>
+static int conv(ns_cnn* c, cudaStream_t st, const float* in, const __nv_bfloat16* w, const float* bias, float* pre, float* act,
+                int B) {
+    constexpr size_t sm = conv_smem<CIN, COUT, CPT>();
+    auto k = k_conv3x3<CIN, COUT, CPT, GELU>;
+    if (sm > 48 * 1024) CNN_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    const int tiles = B * (c->H / TH) * (c->W / TW);
+    k<<<grid_of(tiles, 1, c->num_sms), TP * (COUT / CPT), sm, st>>>(in, w, bias, pre, act, B, c->H, c->W);
+    CNN_LAUNCHED(c);
+    return NS_GPU_OK;
+}
+
+template <int CIN, int COUT>
+static int conv_dw(ns_cnn* c, cudaStream_t st, const float* in, const float* dpre, float* dw, int B) {
+    constexpr size_t sm = dw_smem<CIN, COUT>();
+    auto k = k_conv_dw<CIN, COUT>;
+    if (sm > 48 * 1024) CNN_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    const int tiles = B * (c->H / TH) * (c->W / TW);
+    k<<<grid_of(tiles, 1, 2 * c->num_sms), dw_threads<CIN, COUT>(), sm, st>>>(in, dpre, dw, B, c->H, c->W);
+    CNN_LAUNCHED(c);
+    return NS_GPU_OK;
+}
+
+#define CNN_TRY(...)                    \
+    do {                                \
+        int _s = (__VA_ARGS__);         \
+        if (_s != NS_GPU_OK) return _s; \
+    } while (0)
+
+// forward of the whole network on x0 (B samples); output in pre[NL-1] ([B][H][W])
+static int forward(ns_cnn* c, cudaStream_t st, int B) {
+    const float* x = c->x0;
+    CNN_TRY((conv<2, HID, 32, true>(c, st, x, c->wb[0], c->p + c->boff[0], c->pre[0], c->act[0], B)));
+    for (int l = 1; l < NL - 1; ++l)
+        CNN_TRY((conv<HID, HID, 32, true>(c, st, c->act[l - 1], c->wb[l], c->p + c->boff[l], c->pre[l], c->act[l], B)));
+    CNN_TRY((conv<HID, 1, 1, false>(c, st, c->act[NL - 2], c->wb[NL - 1], c->p + c->boff[NL - 1], c->pre[NL - 1], nullptr, B)));
+    return NS_GPU_OK;
+}
+
+// loss into dloss[slot] and parameter gradients into gp (zeroed here)
+static int loss_and_backward(ns_cnn* c, cudaStream_t st, int B, int slot) {
+    const long long npix = (long long)B * c->H * c->W;
+    CNN_CUDA(c, cudaMemsetAsync(c->gp, 0, c->nparam * sizeof(float), st));
+    k_mse<<<grid_of(npix, 256, 4 * c->num_sms), 256, 0, st>>>(c->pre[NL - 1], c->tgt, npix, c->d0, c->dloss + slot);
+    CNN_LAUNCHED(c);
+    // last layer (64 -> 1): gradient of its output is d0 [B][H][W][1]
+    CNN_TRY((conv_dw<HID, 1>(c, st, c->act[NL - 2], c->d0, c->gp + c->woff[NL - 1], B)));
+    k_bias_grad<<<grid_of(npix, 256, 4 * c->num_sms), 256, sizeof(float), st>>>(c->d0, npix, 1, c->gp + c->boff[NL - 1]);
+    CNN_LAUNCHED(c);
+    CNN_TRY((conv<1, HID, 32, false>(c, st, c->d0, c->wbt[NL - 1], nullptr, c->d1, nullptr, B)));
+    float* dcur = c->d1;  // gradient of act[l]
+    float* dnext = c->d0;
+    for (int l = NL - 2; l >= 0; --l) {
+        k_gelu_bwd<<<grid_of(npix * HID, 256, 8 * c->num_sms), 256, 0, st>>>(dcur, c->pre[l], npix * HID);
+        CNN_LAUNCHED(c);
+        k_bias_grad<<<grid_of(npix * HID, 256, 4 * c->num_sms), 256, HID * sizeof(float), st>>>(dcur, npix, HID,
+                                                                                                  c->gp + c->boff[l]);
+        CNN_LAUNCHED(c);
+        if (l > 0) {
+            CNN_TRY((conv_dw<HID, HID>(c, st, c->act[l - 1], dcur, c->gp + c->woff[l], B)));
+            CNN_TRY((conv<HID, HID, 32, false>(c, st, dcur, c->wbt[l], nullptr, dnext, nullptr, B)));
+            float* t = dcur;
+            dcur = dnext;
+            dnext = t;
+        } else {
+            CNN_TRY((conv_dw<2, HID>(c, st, c->x0, dcur, c->gp + c->woff[0], B)));
+        }
+    }
+    return NS_GPU_OK;
+}
+
+static int round_weights(ns_cnn* c, cudaStream_t st) {
+    for (int l = 0; l < NL; ++l) {
+        k_round_weights<<<grid_of(9 * CIN_OF[l] * COUT_OF[l], 256, 256), 256, 0, st>>>(c->p + c->woff[l], CIN_OF[l],
+                                                                                      COUT_OF[l], c->wb[l], c->wbt[l]);
+        CNN_LAUNCHED(c);
+    }
+    return NS_GPU_OK;
+}
+
+extern "C" {
+
+int ns_cnn_create(int height, int width, int max_batch, uint64_t seed, ns_cnn** out) {
+    if (!out || height < TH || width < TW || height % TH || width % TW || max_batch < 1) return NS_GPU_ERR_INVALID;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return NS_GPU_ERR_NO_DEVICE;
+    ns_cnn* c = new ns_cnn();
+    c->H = height;
+    c->W = width;
+    c->maxB = max_batch;
+    cudaGetDevice(&c->device);
+    cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+    size_t off = 0;
+    for (int l = 0; l < NL; ++l) {
+        c->woff[l] = off;
+        off += (size_t)9 * CIN_OF[l] * COUT_OF[l];
+        c->boff[l] = off;
+        off += COUT_OF[l];
+    }
+    c->nparam = off;
+    const size_t npix = (size_t)max_batch * height * width;
+    bool ok = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) == cudaSuccess;
+    auto alloc = [&](void** pp, size_t bytes) {
+        if (ok && cudaMalloc(pp, bytes) != cudaSuccess) ok = false;
+    };
+    alloc((void**)&c->p, off * sizeof(float));
+    alloc((void**)&c->gp, off * sizeof(float));
+    alloc((void**)&c->m, off * sizeof(float));
+    alloc((void**)&c->v, off * sizeof(float));
+    for (int l = 0; l < NL; ++l) {
+        alloc((void**)&c->wb[l], (size_t)9 * CIN_OF[l] * COUT_OF[l] * sizeof(__nv_bfloat16));
+        alloc((void**)&c->wbt[l], (size_t)9 * CIN_OF[l] * COUT_OF[l] * sizeof(__nv_bfloat16));
+        alloc((void**)&c->pre[l], npix * COUT_OF[l] * sizeof(float));
+        if (l < NL - 1) alloc((void**)&c->act[l], npix * COUT_OF[l] * sizeof(float));
+    }
+    alloc((void**)&c->x0, npix * 2 * sizeof(float));
+    alloc((void**)&c->d0, npix * HID * sizeof(float));
+    alloc((void**)&c->d1, npix * HID * sizeof(float));
+    alloc((void**)&c->tgt, npix * sizeof(float));
+    alloc((void**)&c->didx, (size_t)max_batch * sizeof(int));
+    alloc((void**)&c->cw0, (size_t)height * width * sizeof(float));
+    alloc((void**)&c->cw1, (size_t)height * width * sizeof(float));
+    c->loss_cap = 1;
+    alloc((void**)&c->dloss, sizeof(double));
+    if (!ok) {
+        ns_cnn_destroy(c);
+        return NS_GPU_ERR_ALLOC;
+    }
+    // He-uniform hidden layers, a small last layer so the initial correction is near zero
+    std::vector<float> h(off, 0.0f);
+    for (int l = 0; l < NL; ++l) {
+        const double a = std::sqrt(6.0 / (9.0 * CIN_OF[l])) * (l == NL - 1 ? 0.1 : 1.0);
+        for (size_t i = 0; i < (size_t)9 * CIN_OF[l] * COUT_OF[l]; ++i) {
+            const unsigned long long r = mix64(seed * 0x100000001B3ULL + c->woff[l] + i);
+            h[c->woff[l] + i] = (float)(a * (2.0 * ((double)(r >> 11) * (1.0 / 9007199254740992.0)) - 1.0));
+        }
+    }
+    const int s = ns_cnn_set_params(c, h.data());
+    if (s != NS_GPU_OK) {
+        ns_cnn_destroy(c);
+        return s;
+    }
+    *out = c;
+    return NS_GPU_OK;
+}
+
+void ns_cnn_destroy(ns_cnn* c) {
+    if (!c) return;
+    if (c->st) cudaStreamSynchronize(c->st);
+    void* ptrs[] = {c->p, c->gp, c->m, c->v, c->x0, c->d0, c->d1, c->tgt, c->dloss, c->didx, c->data_in, c->data_tg, c->cw0, c->cw1};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    for (int l = 0; l < NL; ++l) {
+        if (c->wb[l]) cudaFree(c->wb[l]);
+        if (c->wbt[l]) cudaFree(c->wbt[l]);
+        if (c->pre[l]) cudaFree(c->pre[l]);
+        if (c->act[l]) cudaFree(c->act[l]);
+    }
+    if (c->st) cudaStreamDestroy(c->st);
+    delete c;
+}
+
+const char* ns_cnn_last_error(const ns_cnn* c) { return c ? c->err.c_str() : "null network"; }
+
+int ns_cnn_param_count(const ns_cnn* c, size_t* n) {
+    if (!c || !n) return NS_GPU_ERR_INVALID;
+    *n = c->nparam;
+    return NS_GPU_OK;
+}
+
+uint64_t ns_cnn_launch_count(const ns_cnn* c) { return c ? c->launches : 0; }
+
+int ns_cnn_get_params(ns_cnn* c, float* host) {
+    if (!c || !host) return NS_GPU_ERR_INVALID;
+    CNN_CUDA(c, cudaMemcpyAsync(host, c->p, c->nparam * sizeof(float), cudaMemcpyDeviceToHost, c->st));
+    CNN_CUDA(c, cudaStreamSynchronize(c->st));
+    return NS_GPU_OK;
+}
+
+int ns_cnn_set_params(ns_cnn* c, const float* host) {
+    if (!c || !host) return NS_GPU_ERR_INVALID;
+    CNN_CUDA(c, cudaMemcpyAsync(c->p, host, c->nparam * sizeof(float), cudaMemcpyHostToDevice, c->st));
+    CNN_CUDA(c, cudaMemsetAsync(c->m, 0, c->nparam * sizeof(float), c->st));
+    CNN_CUDA(c, cudaMemsetAsync(c->v, 0, c->nparam * sizeof(float), c->st));
+    c->step = 0;
+    CNN_TRY(round_weights(c, c->st));
+    CNN_CUDA(c, cudaStreamSynchronize(c->st));
+    return NS_GPU_OK;
+}
+
+int ns_cnn_set_normalization(ns_cnn* c, float in_scale0, float in_scale1, float out_scale) {
+    if (!c || !(in_scale0 > 0) || !(in_scale1 > 0) || !(out_scale > 0)) return NS_GPU_ERR_INVALID;
+    c->s0 = in_scale0;
+    c->s1 = in_scale1;
+    c->so = out_scale;
+    return NS_GPU_OK;
+}
+
+int ns_cnn_set_dataset(ns_cnn* c, const float* inputs, const float* targets, int n) {
+    if (!c || !inputs || !targets || n < 1) return NS_GPU_ERR_INVALID;
+    const size_t hw = (size_t)c->H * c->W;
+    if (c->data_in) cudaFree(c->data_in);
+    if (c->data_tg) cudaFree(c->data_tg);
+    c->data_in = c->data_tg = nullptr;
+    c->ndata = 0;
+    CNN_CUDA(c, cudaMalloc((void**)&c->data_in, (size_t)n * 2 * hw * sizeof(float)));
+    CNN_CUDA(c, cudaMalloc((void**)&c->data_tg, (size_t)n * hw * sizeof(float)));
+    CNN_CUDA(c, cudaMemcpy(c->data_in, inputs, (size_t)n * 2 * hw * sizeof(float), cudaMemcpyHostToDevice));
+    CNN_CUDA(c, cudaMemcpy(c->data_tg, targets, (size_t)n * hw * sizeof(float), cudaMemcpyHostToDevice));
+    c->ndata = n;
+    return NS_GPU_OK;
+}
+
+// Loss and parameter gradients of a host batch (inputs [B][2][H][W], targets
+// [B][H][W], both before normalisation), without updating the parameters.
+int ns_cnn_loss_and_grads(ns_cnn* c, const float* inputs, const float* targets, int B, double* loss, float* grads) {
+    if (!c || !inputs || !targets || B < 1 || B > c->maxB) return NS_GPU_ERR_INVALID;
+    const size_t hw = (size_t)c->H * c->W;
+    float *din = nullptr, *dtg = nullptr;
+    CNN_CUDA(c, cudaMalloc((void**)&din, (size_t)B * 2 * hw * sizeof(float)));
+    if (cudaMalloc((void**)&dtg, (size_t)B * hw * sizeof(float)) != cudaSuccess) {
+        cudaFree(din);
+        CNN_FAIL(c, NS_GPU_ERR_ALLOC, "loss_and_grads: allocation failed");
+    }
+    std::vector<int> idx(B);
+    for (int b = 0; b < B; ++b) idx[b] = b;
+    int s = NS_GPU_OK;
+    cudaStream_t st = c->st;
+    if (cudaMemcpyAsync(din, inputs, (size_t)B * 2 * hw * sizeof(float), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(dtg, targets, (size_t)B * hw * sizeof(float), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(c->didx, idx.data(), B * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemsetAsync(c->dloss, 0, sizeof(double), st) != cudaSuccess)
+        s = NS_GPU_ERR_CUDA;
+    if (s == NS_GPU_OK) {
+        k_gather<<<grid_of((long long)B * hw, 256, 1024), 256, 0, st>>>(din, dtg, c->didx, B, c->H, c->W, c->s0, c->s1, c->so,
+                                                                         c->x0, c->tgt);
+        c->launches++;
+        s = forward(c, st, B);
+    }
+    if (s == NS_GPU_OK) s = loss_and_backward(c, st, B, 0);
+    double l = 0.0;
+    if (s == NS_GPU_OK && loss) s = cudaMemcpyAsync(&l, c->dloss, sizeof(double), cudaMemcpyDeviceToHost, st) == cudaSuccess ? s : NS_GPU_ERR_CUDA;
+    if (s == NS_GPU_OK && grads)
+        s = cudaMemcpyAsync(grads, c->gp, c->nparam * sizeof(float), cudaMemcpyDeviceToHost, st) == cudaSuccess ? s : NS_GPU_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess && s == NS_GPU_OK) s = NS_GPU_ERR_CUDA;
+    cudaFree(din);
+    cudaFree(dtg);
+    if (s == NS_GPU_OK && loss) *loss = l;
+    return s;
+}
+
+// Network output for a host batch (inputs [B][2][H][W] before normalisation);
+// out [B][H][W] receives the correction in physical units (output / out_scale).
+int ns_cnn_forward_host(ns_cnn* c, const float* inputs, int B, float* out) {
+    if (!c || !inputs || !out || B < 1 || B > c->maxB) return NS_GPU_ERR_INVALID;
+    const size_t hw = (size_t)c->H * c->W;
+    float* din = nullptr;
+    CNN_CUDA(c, cudaMalloc((void**)&din, (size_t)B * 2 * hw * sizeof(float)));
+    std::vector<int> idx(B);
+    for (int b = 0; b < B; ++b) idx[b] = b;
+    cudaStream_t st = c->st;
+    int s = NS_GPU_OK;
+    if (cudaMemcpyAsync(din, inputs, (size_t)B * 2 * hw * sizeof(float), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(c->didx, idx.data(), B * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess)
+        s = NS_GPU_ERR_CUDA;
+    if (s == NS_GPU_OK) {
+        k_gather<<<grid_of((long long)B * hw, 256, 1024), 256, 0, st>>>(din, nullptr, c->didx, B, c->H, c->W, c->s0, c->s1,
+                                                                         c->so, c->x0, nullptr);
+        c->launches++;
+        s = forward(c, st, B);
+    }
+    if (s == NS_GPU_OK) {
+        k_scale<<<grid_of((long long)B * hw, 256, 1024), 256, 0, st>>>(c->pre[NL - 1], (long long)B * hw, 1.0f / c->so);
+        c->launches++;
+        if (cudaMemcpyAsync(out, c->pre[NL - 1], (size_t)B * hw * sizeof(float), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+            s = NS_GPU_ERR_CUDA;
+    }
+    if (cudaStreamSynchronize(st) != cudaSuccess && s == NS_GPU_OK) s = NS_GPU_ERR_CUDA;
+    cudaFree(din);
+    return s;
+}
+
+// iterations AdamW steps on random minibatches of the dataset; loss_history
+// (iterations doubles, may be NULL) receives each step's loss.
+int ns_cnn_train(ns_cnn* c, int iterations, int batch, float lr, float weight_decay, uint64_t seed, double* loss_history) {
+    if (!c || iterations < 1 || batch < 1 || batch > c->maxB || !(lr > 0)) return NS_GPU_ERR_INVALID;
+    if (c->ndata < 1) CNN_FAIL(c, NS_GPU_ERR_INVALID, "train: no dataset (ns_cnn_set_dataset)");
+    if (c->loss_cap < iterations) {
+        cudaFree(c->dloss);
+        c->dloss = nullptr;
+        c->loss_cap = 0;
+        CNN_CUDA(c, cudaMalloc((void**)&c->dloss, (size_t)iterations * sizeof(double)));
+        c->loss_cap = iterations;
+    }
+    cudaStream_t st = c->st;
+    CNN_CUDA(c, cudaMemsetAsync(c->dloss, 0, (size_t)iterations * sizeof(double), st));
+    const long long hw = (long long)c->H * c->W;
+    int* hidx = nullptr;
+    CNN_CUDA(c, cudaMallocHost((void**)&hidx, (size_t)iterations * batch * sizeof(int)));
+    unsigned long long state = seed;
+    for (long long i = 0; i < (long long)iterations * batch; ++i) {
+        state = mix64(state);
+        hidx[i] = (int)(state % (unsigned long long)c->ndata);
+    }
+    int* didx_all = nullptr;
+    int s = NS_GPU_OK;
+    if (cudaMalloc((void**)&didx_all, (size_t)iterations * batch * sizeof(int)) != cudaSuccess ||
+        cudaMemcpyAsync(didx_all, hidx, (size_t)iterations * batch * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess)
+        s = NS_GPU_ERR_CUDA;
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    for (int it = 0; it < iterations && s == NS_GPU_OK; ++it) {
+        k_gather<<<grid_of(batch * hw, 256, 2048), 256, 0, st>>>(c->data_in, c->data_tg, didx_all + (size_t)it * batch, batch,
+                                                                 c->H, c->W, c->s0, c->s1, c->so, c->x0, c->tgt);
+        c->launches++;
+        s = forward(c, st, batch);
+        if (s == NS_GPU_OK) s = loss_and_backward(c, st, batch, it);
+        if (s != NS_GPU_OK) break;
+        c->step++;
+        const float bc1 = 1.0f - powf(b1, (float)c->step), bc2 = 1.0f - powf(b2, (float)c->step);
+        k_adamw<<<grid_of((long long)c->nparam, 256, 1024), 256, 0, st>>>(c->p, c->m, c->v, c->gp, (long long)c->nparam, lr, b1,
+                                                                          b2, eps, weight_decay, bc1, bc2);
+        c->launches++;
+        s = round_weights(c, st);
+    }
+    if (s == NS_GPU_OK && loss_history &&
+        cudaMemcpyAsync(loss_history, c->dloss, (size_t)iterations * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        s = NS_GPU_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess && s == NS_GPU_OK) s = NS_GPU_ERR_CUDA;
+    if (cudaGetLastError() != cudaSuccess && s == NS_GPU_OK) s = NS_GPU_ERR_CUDA;
+    cudaFree(didx_all);
+    cudaFreeHost(hidx);
+    if (s != NS_GPU_OK && c->err.empty()) c->err = "train: CUDA error";
+    return s;
+}
+
+// One corrected coarse step of a FP32 instance whose grid matches the network:
+// w0 = omega(t); plain RK4 step; w1 = omega(t + dt); omega += CNN(w0, w1 - w0).
+int ns_cnn_correct_step(ns_cnn* c, ns_gpu* g, int nsteps) {
+    if (!c || !g || nsteps < 0) return NS_GPU_ERR_INVALID;
+    const long long hw = (long long)c->H * c->W;
+    for (int s = 0; s < nsteps; ++s) {
+        CNN_TRY(ns_gpu_vorticity_device(g, c->cw0));
+        CNN_TRY(ns_gpu_advance(g, 1));
+        CNN_TRY(ns_gpu_vorticity_device(g, c->cw1));
+        CNN_TRY(ns_gpu_synchronize(g));  // the network runs on its own stream
+        k_make_input<<<grid_of(hw, 256, 1024), 256, 0, c->st>>>(c->cw0, c->cw1, hw, c->s0, c->s1, c->x0);
+        CNN_LAUNCHED(c);
+        CNN_TRY(forward(c, c->st, 1));
+        k_scale<<<grid_of(hw, 256, 1024), 256, 0, c->st>>>(c->pre[NL - 1], hw, 1.0f / c->so);
+        CNN_LAUNCHED(c);
+        CNN_CUDA(c, cudaStreamSynchronize(c->st));
+        CNN_TRY(ns_gpu_add_vorticity_device(g, c->pre[NL - 1]));
+    }
+    return NS_GPU_OK;
+}
+
+}  // extern "C"

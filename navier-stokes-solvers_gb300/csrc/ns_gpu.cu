@@ -1124,6 +1124,74 @@ int ns_gpu_energy_spectrum(ns_gpu* g, int nbins, double* energy_sum, double* ene
     return NS_GPU_OK;
 }
 
+template <typename T> static int vorticity_t(ns_gpu* g, float* out) {
+    if (!g->fields_valid) {
+        NSG_TRY(prologue<T>(g, g->W0, g->PSI0, g->psi0_valid ? 0 : 1, 4));
+        g->fields_valid = 1;
+    }
+    RowArgs<T> a = row_args<T>(g);
+    a.F[0] = (const Cx<T>*)g->F[2];  // Omega, no derivative
+    a.dx[0] = 0;
+    a.out_real[0] = g->real[0];
+    NSG_TRY(row_launch<T, ROW_INV1>(g, a));
+    const long long n = (long long)g->g.nx * g->g.ny;
+    k_d2f<<<grid_for(n), 256, 0, g->st>>>(g->real[0], out, n);
+    NSG_LAUNCHED(g);
+    return NS_GPU_OK;
+}
+
+int ns_gpu_vorticity_device(ns_gpu* g, float* omega_dev) {
+    if (!g || !omega_dev) return NS_GPU_ERR_INVALID;
+    if (g->outside_active) NSG_FAIL(g, NS_GPU_ERR_INVALID, "vorticity_device: state has modes outside the 2/3 mask");
+    NSG_TRY(ensure_staging(g));
+    return g->prec == NS_GPU_FP64 ? vorticity_t<double>(g, omega_dev) : vorticity_t<float>(g, omega_dev);
+}
+
+template <typename T> static int add_vorticity_t(ns_gpu* g, const float* delta) {
+    const long long n = (long long)g->g.nx * g->g.ny;
+    k_f2d<<<grid_for(n), 256, 0, g->st>>>(delta, g->real[0], n);
+    NSG_LAUNCHED(g);
+    RowArgs<T> a = row_args<T>(g);
+    a.in_real = g->real[0];
+    NSG_TRY(row_launch<T, ROW_FWD1>(g, a));
+    NSG_CUDA(g, cudaMemsetAsync(g->spec[0], 0, spec_bytes(g), g->st));
+    ColArgs<T> c = col_args<T>(g);
+    c.out_spec = g->spec[0];
+    c.out_scale = 1.0 / ((double)g->g.nx * (double)g->g.ny);
+    NSG_TRY((col_launch<T, COL_FWD_EXPORT, 0>(g, c)));
+    const long long nk = (long long)g->g.Kx * g->g.Ky;
+    k_add_kept<T><<<grid_for(nk), 256, 0, g->st>>>(g->g, g->spec[0], (Cx<T>*)g->W0);
+    NSG_LAUNCHED(g);
+    g->fields_valid = 0;
+    g->psi0_valid = 0;
+    return NS_GPU_OK;
+}
+
+int ns_gpu_add_vorticity_device(ns_gpu* g, const float* delta_dev) {
+    if (!g || !delta_dev) return NS_GPU_ERR_INVALID;
+    NSG_TRY(ensure_staging(g));
+    return g->prec == NS_GPU_FP64 ? add_vorticity_t<double>(g, delta_dev) : add_vorticity_t<float>(g, delta_dev);
+}
+
+int ns_gpu_filter_state(ns_gpu* fine, ns_gpu* coarse) {
+    if (!fine || !coarse) return NS_GPU_ERR_INVALID;
+    if (fine->prec != coarse->prec || fine->g.nx < coarse->g.nx || fine->g.ny < coarse->g.ny ||
+        fine->g.Lx != coarse->g.Lx || fine->g.Ly != coarse->g.Ly)
+        NSG_FAIL(coarse, NS_GPU_ERR_INVALID, "filter_state: needs the same precision and box and a finer source grid");
+    NSG_CUDA(coarse, cudaStreamSynchronize(fine->st));
+    const long long n = (long long)coarse->g.Kx * coarse->g.Ky;
+    if (coarse->prec == NS_GPU_FP64)
+        k_filter<double><<<grid_for(n), 256, 0, coarse->st>>>(fine->g, (const double2*)fine->W0, coarse->g, (double2*)coarse->W0);
+    else
+        k_filter<float><<<grid_for(n), 256, 0, coarse->st>>>(fine->g, (const float2*)fine->W0, coarse->g, (float2*)coarse->W0);
+    NSG_LAUNCHED(coarse);
+    NSG_CUDA(coarse, cudaMemcpyAsync(&coarse->ds->t, &fine->ds->t, sizeof(double), cudaMemcpyDeviceToDevice, coarse->st));
+    coarse->fields_valid = 0;
+    coarse->psi0_valid = 0;
+    coarse->outside_active = 0;
+    return NS_GPU_OK;
+}
+
 int ns_gpu_init_random_spectrum(ns_gpu* g, uint64_t seed, double k0, double energy) {
     if (!g || !(k0 > 0.0) || energy < 0.0) return NS_GPU_ERR_INVALID;
     NSG_TRY(ensure_staging(g));

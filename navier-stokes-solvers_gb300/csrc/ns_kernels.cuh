@@ -1249,6 +1249,42 @@ __global__ void k_spectrum_counts(Geo g, int nbins, int* counts) {
     }
 }
 
+// spectral truncation of a fine state onto a coarse grid of the same box: the
+// coarse kept modes are a subset of the fine kept modes (same physical kx, ky)
+template <typename T>
+__global__ void k_filter(Geo gf, const typename CT<T>::C* Wf, Geo gc, typename CT<T>::C* Wc) {
+    const long long n = (long long)gc.Kx * gc.Ky;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(idx / gc.Ky), jj = (int)(idx - (long long)i * gc.Ky);
+        const int j = kept_j(gc, jj);
+        const int ky = (j <= gc.ny / 2) ? j : j - gc.ny;
+        const int jf = ky >= 0 ? ky : ky + gf.ny;
+        const int jjf = kept_jj(gf, jf);
+        Wc[idx] = (i < gf.Kx && jjf >= 0) ? Wf[(size_t)i * gf.Ky + jjf] : cmake<typename CT<T>::C>(0.0, 0.0);
+    }
+}
+
+// W[kept] += spec[j][i] (an FP64 half spectrum in the reference layout)
+template <typename T>
+__global__ void k_add_kept(Geo g, const double2* spec, typename CT<T>::C* W) {
+    const long long n = (long long)g.Kx * g.Ky;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(idx / g.Ky), jj = (int)(idx - (long long)i * g.Ky);
+        const double2 a = spec[(size_t)kept_j(g, jj) * g.nkx + i];
+        typename CT<T>::C w = W[idx];
+        w.x = (T)((double)w.x + a.x);
+        w.y = (T)((double)w.y + a.y);
+        W[idx] = w;
+    }
+}
+
+__global__ void k_d2f(const double* a, float* b, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) b[i] = (float)a[i];
+}
+__global__ void k_f2d(const float* a, double* b, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) b[i] = (double)a[i];
+}
+
 #endif  // NSG_NO_AUX_KERNELS
 
 }  // namespace nsg

@@ -347,7 +347,6 @@ int ns_checkpoint_read_spectral(const char *filename, NSSpectralData *state) {
         d->dt = dt;
         /* optional entries: absent in files from other writers */
         npz_get(&r, "fields/psi_hat.npy", "<c16", nc, sizeof(fftw_complex), d->psi_hat);
-        npz_get(&r, "fields/sfd_hat.npy", "<c16", nc, sizeof(fftw_complex), d->sfd_hat);
         npz_get(&r, "cfl_factor.npy", "<f8", 1, sizeof(double), &d->cfl_factor);
         double hv[10];
         if (npz_get(&r, "hyperviscosity.npy", "<f8", 10, sizeof(double), hv) == 0) {
@@ -360,7 +359,12 @@ int ns_checkpoint_read_spectral(const char *filename, NSSpectralData *state) {
             c.sfd_timescale = hv[5];
             c.sfd_enabled = (int)hv[6];
             if (d->gpu) {
-                ns_spectral_hyperviscosity_set(d, &c);  /* recomputes kmax, cutoff and the weights */
+                /* not ns_spectral_hyperviscosity_set: it re-seeds the SFD filter
+                 * with omega_hat (hyperviscosity.c:38-57), and the filter state is
+                 * part of the checkpoint */
+                d->hyperviscosity = c;
+                if (!c.enabled) memset(d->hyperviscosity_weights, 0, nc * sizeof(double));
+                ns_spectral_hyperviscosity_update_weights(d);  /* kmax, cutoff and the weights */
             } else {
                 c.kmax = hv[7];
                 c.cutoff_wavenumber = hv[8];
@@ -368,6 +372,7 @@ int ns_checkpoint_read_spectral(const char *filename, NSSpectralData *state) {
                 d->hyperviscosity = c;
             }
         }
+        if (!d->gpu) npz_get(&r, "fields/sfd_hat.npy", "<c16", nc, sizeof(fftw_complex), d->sfd_hat);
         if (d->gpu) {
             double fc[4];
             uint64_t seed = 0, step = 0;
@@ -377,6 +382,7 @@ int ns_checkpoint_read_spectral(const char *filename, NSSpectralData *state) {
                 ns_spectral_gpu_set_forcing(d, (int)fc[0], fc[1], fc[2], fc[3], (unsigned long long)seed);
             if (npz_get(&r, "gpu/step.npy", "<u8", 1, sizeof(uint64_t), &step) == 0) d->gpu->step = step;
             if (npz_get(&r, "gpu/scheme.npy", "<i4", 1, sizeof(int), &scheme) == 0) ns_spectral_gpu_set_scheme(d, scheme);
+            npz_get(&r, "fields/sfd_hat.npy", "<c16", nc, sizeof(fftw_complex), d->sfd_hat);
             /* the host arrays are the state: the next call uploads them */
             d->gpu->host_stale = 0;
             d->gpu->device_current = 0;

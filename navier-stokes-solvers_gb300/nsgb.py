@@ -143,6 +143,8 @@ def load(build: bool = True) -> C.CDLL:
     proto("ns_spectral_initialize_random_spectrum", C.c_int, sp, C.c_ulonglong, C.c_double, C.c_double)
     proto("ns_spectral_gpu_last_error", C.c_char_p, sp)
     proto("ns_spectral_gpu_handle", vp, sp)
+    proto("ns_checkpoint_write_spectral", C.c_int, C.c_char_p, sp)
+    proto("ns_checkpoint_read_spectral", C.c_int, C.c_char_p, sp)
     proto("ns_forcing_config_default", None, C.POINTER(ForcingConfig))
     proto("ns_forcing_state_init", C.c_int, C.POINTER(ForcingState), C.POINTER(ForcingConfig), _DP, C.c_int, C.c_int)
     proto("ns_forcing_state_free", None, C.POINTER(ForcingState))
