@@ -57,7 +57,9 @@ typedef struct {
     double sfd_strength;
     double sfd_timescale;
     /* white-in-time forcing on the shell kmin <= |k| <= kmax with energy
-     * injection rate epsilon (Philox4x64-10 counter RNG keyed by seed) */
+     * injection rate epsilon (Philox4x64-10 counter RNG keyed by seed; the
+     * counter is the physical mode (kx, ky) and the forcing step, so every grid
+     * that resolves the shell draws the same noise for the same step) */
     int forcing_enabled;
     double forcing_kmin;
     double forcing_kmax;
@@ -68,6 +70,11 @@ typedef struct {
      * RK4: viscous and hyperviscous decay exp(-(k^2/Re + w) t) integrated
      * exactly, the Jacobian and SFD relaxation explicit; no reference counterpart) */
     int scheme;
+    /* forcing draws per step (0 or 1: one): a step of M draws adds
+     * sigma sqrt(dt/M) (xi_c + ... + xi_{c+M-1}) and advances the forcing counter
+     * by M, so a coarse step of M fine steps receives exactly the fine run's
+     * forcing over those steps */
+    int forcing_substeps;
 } ns_gpu_params;
 
 enum { NS_GPU_RK4 = 0, NS_GPU_IFRK4 = 1 };
@@ -246,7 +253,8 @@ int ns_gpu_add_vorticity_device(ns_gpu *g, const float *delta_dev);
 /* Spectral truncation of a fine state onto a coarser instance of the same box
  * and precision: the coarse kept modes take the fine values of the same (kx, ky)
  * (forward transforms are normalised by 1/(nx ny), so amplitudes carry over);
- * the coarse time is set to the fine time.  No reference counterpart. */
+ * the coarse time and forcing counter are set to the fine ones.  No reference
+ * counterpart. */
 int ns_gpu_filter_state(ns_gpu *fine, ns_gpu *coarse);
 
 /* ----------------------------------------------------- batched ensembles */

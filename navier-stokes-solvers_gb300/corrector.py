@@ -1,0 +1,159 @@
+"""Learned coarse-grid corrector: training data from this solver, training with the
+library's own kernels (ns_cnn_*), evaluation against the filtered fine solution.
+
+No reference counterpart.  The fine solver runs at FINE^2, its state is spectrally
+truncated to COARSE^2 (ns_gpu_filter_state) every RATIO fine steps, and the
+network learns the difference between the filtered fine state and one plain
+coarse step of RATIO x the fine time step:
+
+    input   (omega_c(t), omega_plain(t + D) - omega_c(t))     omega_c = filtered fine
+    target  omega_c(t + D) - omega_plain(t + D)
+
+Applied online, every coarse step is a plain RK4 step followed by
+omega += CNN(...) (ns_cnn_correct_step); the plain fine solver is the judge of
+its error.  All numerics run in the library (ns_gpu_*, ns_cnn_*); this module
+only sequences the calls and keeps host copies of the samples.
+"""
+from __future__ import annotations
+
+import math
+import time
+
+import numpy as np
+
+import nsgb
+
+L = 2 * math.pi
+
+
+def hv_coefficient(n: int, cfl: float = 0.5) -> float:
+    """nu_h |k|^4 in the reference ramp form (cutoff 0, order 4): damping O(1) per
+    CFL-limited step at 2/3 of the grid's largest wavenumber."""
+    kmax = math.hypot(n / 2, n / 2)
+    dt_ref = cfl * (2 * math.pi / n) / 3.0
+    kd = 2.0 / 3.0 * kmax
+    return kmax ** 4 / (kd ** 4 * dt_ref)
+
+
+def params(n: int, dt: float, Re: float = 1e5, forcing_seed: int | None = None, epsilon: float = 1e-3) -> dict:
+    p = dict(Re=Re, cfl_factor=0.5, adaptive_dt=0, dt=dt, hv_enabled=1, hv_coefficient=hv_coefficient(n),
+             hv_order=4, hv_cutoff_ratio=0.0)
+    if forcing_seed is not None:
+        p.update(forcing_enabled=1, forcing_kmin=4.0, forcing_kmax=6.0, forcing_epsilon=epsilon,
+                 forcing_seed=forcing_seed)
+    return p
+
+
+def _omega(g: "nsgb.Gpu") -> np.ndarray:
+    return g.download(("omega",))["omega"].astype(np.float32)
+
+
+def _filter(fine: "nsgb.Gpu", coarse: "nsgb.Gpu"):
+    fine.check(fine.lib.ns_gpu_filter_state(fine.h, coarse.h), "filter_state")
+
+
+def fine_dt(fine_n: int, seed: int, k0: float, cfl: float = 0.4) -> float:
+    """Fixed fine time step: the reference CFL rule at the initial state, factor cfl."""
+    g = nsgb.Gpu(fine_n, fine_n, L, L, nsgb.FP32)
+    g.set_params(**dict(params(fine_n, 1e-4), adaptive_dt=1, cfl_factor=cfl))
+    g.random_spectrum(seed, k0, 0.5)
+    g.advance(1)
+    dt = g.diagnostics()["dt"]
+    g.close()
+    return dt
+
+
+def generate(seeds, fine_n=1024, coarse_n=256, ratio=8, spinup=200, snapshots=32, k0=8.0, dt_f=None,
+             forcing=False):
+    """Samples (inputs [N][2][c][c], targets [N][c][c]) from seeded fine runs."""
+    if dt_f is None:
+        dt_f = fine_dt(fine_n, seeds[0], k0)
+    fine = nsgb.Gpu(fine_n, fine_n, L, L, nsgb.FP32)
+    coarse = nsgb.Gpu(coarse_n, coarse_n, L, L, nsgb.FP32)
+    xs, ts = [], []
+    for seed in seeds:
+        fine.set_params(**params(fine_n, dt_f, forcing_seed=(1000 + seed) if forcing else None))
+        coarse.set_params(**params(coarse_n, ratio * dt_f))
+        fine.random_spectrum(seed, k0, 0.5)
+        fine.advance(spinup)
+        for _ in range(snapshots):
+            _filter(fine, coarse)
+            w0 = _omega(coarse)
+            coarse.advance(1)
+            wp = _omega(coarse)
+            fine.advance(ratio)
+            _filter(fine, coarse)
+            wt = _omega(coarse)
+            xs.append(np.stack([w0, wp - w0]))
+            ts.append(wt - wp)
+    fine.close()
+    coarse.close()
+    return np.asarray(xs, dtype=np.float32), np.asarray(ts, dtype=np.float32), dt_f
+
+
+def normalisation(inputs: np.ndarray, targets: np.ndarray):
+    """Per-channel scales that make inputs and targets of unit RMS."""
+    s0 = 1.0 / max(float(np.sqrt(np.mean(inputs[:, 0] ** 2))), 1e-30)
+    s1 = 1.0 / max(float(np.sqrt(np.mean(inputs[:, 1] ** 2))), 1e-30)
+    so = 1.0 / max(float(np.sqrt(np.mean(targets ** 2))), 1e-30)
+    return s0, s1, so
+
+
+def rel_l2(a, b) -> float:
+    return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
+
+
+def evaluate(net: "nsgb.Corrector", seeds, horizon, fine_n=1024, coarse_n=256, ratio=8, spinup=200, k0=8.0,
+             dt_f=None, forcing=False, every=1):
+    """Relative L2 of plain and corrected coarse runs against the filtered fine run
+    over `horizon` coarse steps, energy-spectrum error at the end, and wall times."""
+    if dt_f is None:
+        dt_f = fine_dt(fine_n, seeds[0], k0)
+    fine = nsgb.Gpu(fine_n, fine_n, L, L, nsgb.FP32)
+    plain = nsgb.Gpu(coarse_n, coarse_n, L, L, nsgb.FP32)
+    learned = nsgb.Gpu(coarse_n, coarse_n, L, L, nsgb.FP32)
+    out = []
+    for seed in seeds:
+        fine.set_params(**params(fine_n, dt_f, forcing_seed=(1000 + seed) if forcing else None))
+        for g in (plain, learned):
+            g.set_params(**params(coarse_n, ratio * dt_f))
+        fine.random_spectrum(seed, k0, 0.5)
+        fine.advance(spinup)
+        _filter(fine, plain)
+        _filter(fine, learned)
+        errs_p, errs_l = [], []
+        t_fine = t_plain = t_learned = 0.0
+        for k in range(1, horizon + 1):
+            fine.sync()
+            t0 = time.perf_counter()
+            fine.advance(ratio)
+            fine.sync()
+            t_fine += time.perf_counter() - t0
+            t0 = time.perf_counter()
+            plain.advance(1)
+            plain.sync()
+            t_plain += time.perf_counter() - t0
+            t0 = time.perf_counter()
+            net.correct_step(learned, 1)
+            learned.sync()
+            t_learned += time.perf_counter() - t0
+            if k % every == 0 or k == horizon:
+                truth = nsgb.Gpu(coarse_n, coarse_n, L, L, nsgb.FP32)
+                truth.set_params(**params(coarse_n, ratio * dt_f))
+                _filter(fine, truth)
+                wt = _omega(truth)
+                et = truth.energy_spectrum()[1]
+                truth.close()
+                errs_p.append(rel_l2(_omega(plain), wt))
+                errs_l.append(rel_l2(_omega(learned), wt))
+        ep = plain.energy_spectrum()[1]
+        el = learned.energy_spectrum()[1]
+        band = slice(1, coarse_n // 3)
+        spec = lambda e: float(np.mean(np.abs(np.log(np.maximum(e[band], 1e-300) / np.maximum(et[band], 1e-300)))))
+        out.append({"seed": int(seed), "rel_l2_plain": errs_p, "rel_l2_learned": errs_l,
+                    "log_spectrum_error_plain": spec(ep), "log_spectrum_error_learned": spec(el),
+                    "wall_s_fine": t_fine, "wall_s_plain": t_plain, "wall_s_learned": t_learned})
+    fine.close()
+    plain.close()
+    learned.close()
+    return out, dt_f

@@ -112,6 +112,7 @@ template <typename T> static StepParams step_params(const ns_gpu* g) {
     sp.f_sigma = g->f_sigma;
     sp.f_seed = g->p.forcing_seed;
     sp.ifrk = g->p.scheme == NS_GPU_IFRK4 ? 1 : 0;
+    sp.fsub = g->p.forcing_substeps > 1 ? g->p.forcing_substeps : 1;
     return sp;
 }
 
@@ -573,6 +574,9 @@ int ns_gpu_set_params(ns_gpu* g, const ns_gpu_params* p) {
                           p->forcing_kmin != g->p.forcing_kmin || p->forcing_kmax != g->p.forcing_kmax ||
                           p->forcing_epsilon != g->p.forcing_epsilon;
     const int dt_changed = !g->params_set || p->dt != g->p.dt;
+    const int fsub_changed = !g->params_set || p->forcing_substeps != g->p.forcing_substeps;
+    if (p->forcing_substeps < 0 || p->forcing_substeps > 1024)
+        NSG_FAIL(g, NS_GPU_ERR_INVALID, "forcing_substeps %d not in [0, 1024]", p->forcing_substeps);
     g->p = *p;
     g->params_set = 1;
     if (hv_changed) NSG_TRY(compute_hv(g));
@@ -580,6 +584,11 @@ int ns_gpu_set_params(ns_gpu* g, const ns_gpu_params* p) {
     if (dt_changed) {
         double dt = p->dt;
         NSG_TRY(h2d(g, &g->ds->dt_fixed, &dt, sizeof(double)));
+        NSG_TRY(sync(g));
+    }
+    if (fsub_changed) {
+        unsigned long long m = p->forcing_substeps > 1 ? (unsigned long long)p->forcing_substeps : 1ULL;
+        NSG_TRY(h2d(g, &g->ds->fsub, &m, sizeof(m)));
         NSG_TRY(sync(g));
     }
     return NS_GPU_OK;
@@ -932,6 +941,7 @@ int ns_gpu_upload_state(ns_gpu* g, const double* omega_hat, const double* psi_ha
     h.dt_fixed = dt;
     h.step_next = step0;
     h.step_cur = step0;
+    h.fsub = g->p.forcing_substeps > 1 ? (unsigned long long)g->p.forcing_substeps : 1ULL;
     NSG_TRY(h2d(g, g->ds, &h, sizeof(h)));
     int flag = 0;
     NSG_TRY(d2h(g, &flag, g->dflag, sizeof(int)));
@@ -1186,6 +1196,8 @@ int ns_gpu_filter_state(ns_gpu* fine, ns_gpu* coarse) {
         k_filter<float><<<grid_for(n), 256, 0, coarse->st>>>(fine->g, (const float2*)fine->W0, coarse->g, (float2*)coarse->W0);
     NSG_LAUNCHED(coarse);
     NSG_CUDA(coarse, cudaMemcpyAsync(&coarse->ds->t, &fine->ds->t, sizeof(double), cudaMemcpyDeviceToDevice, coarse->st));
+    NSG_CUDA(coarse, cudaMemcpyAsync(&coarse->ds->step_next, &fine->ds->step_next, sizeof(unsigned long long),
+                                     cudaMemcpyDeviceToDevice, coarse->st));
     coarse->fields_valid = 0;
     coarse->psi0_valid = 0;
     coarse->outside_active = 0;
@@ -1210,6 +1222,7 @@ int ns_gpu_init_random_spectrum(ns_gpu* g, uint64_t seed, double k0, double ener
     memset(&h, 0, sizeof(h));
     h.dt = g->p.dt;
     h.dt_fixed = g->p.dt;
+    h.fsub = g->p.forcing_substeps > 1 ? (unsigned long long)g->p.forcing_substeps : 1ULL;
     NSG_TRY(h2d(g, g->ds, &h, sizeof(h)));
     NSG_TRY(sync(g));
     g->outside_active = 0;

@@ -70,12 +70,14 @@ struct DevScalars {
     unsigned long long aux_max;    // bit pattern of a max reduction of the host-array API
     int flag;                      // outside-mode presence / non-finite detection
     int pad;
+    unsigned long long fsub;       // forcing draws per step (counter advance per step; 0 means 1)
 };
 
 struct StepParams {
     double inv_re, Re, cfl, dxmin, scale;
     int adaptive, hv, sfd, forcing;
     int ifrk;  // 1: integrating-factor RK4 stage algebra
+    int fsub;  // forcing draws summed per step (>= 1)
     double sfd_tau;
     double f_kmin, f_kmax, f_sigma;
     unsigned long long f_seed;
@@ -101,6 +103,32 @@ __device__ __forceinline__ double u53(unsigned long long b) { return (double)(b 
 
 #define NSG_TAG_IC 0x49430000ULL
 #define NSG_TAG_FORCE 0x464f5243ULL
+
+// Forcing noise of the kept mode (kx index i, row j): the sum over s < M of
+// xi(base + s), xi = (g1 + i g2) / sqrt 2 from Box-Muller on Philox4x64-10 keyed
+// by the seed with counter (mode id, base + s, TAG, 0).  The mode id is
+// (signed ky) << 32 | kx, so a physical mode draws the same noise on every grid;
+// kx = 0 rows with ky < 0 take the conjugate of the ky > 0 row (Hermitian).
+__device__ __forceinline__ double2 forcing_xi_sum(int i, int j, int ny, unsigned long long base, int M,
+                                                  unsigned long long seed) {
+    int ky = (j <= ny / 2) ? j : j - ny;
+    int flip = 0;
+    if (i == 0 && ky < 0) { ky = -ky; flip = 1; }
+    const unsigned long long id = ((unsigned long long)(unsigned int)ky << 32) | (unsigned int)i;
+    double sx = 0.0, sy = 0.0;
+    for (int s = 0; s < M; ++s) {
+        unsigned long long ctr[4] = {id, base + (unsigned long long)s, NSG_TAG_FORCE, 0ULL};
+        philox4x64(ctr, seed, 0ULL);
+        const double u1 = fmax(u53(ctr[0]), 2.2250738585072014e-308);
+        const double u2 = u53(ctr[1]);
+        const double rad = sqrt(-2.0 * log(u1)) * 0.70710678118654752440;
+        double sn, cs;
+        sincos(2.0 * 3.141592653589793 * u2, &sn, &cs);
+        sx += rad * cs;
+        sy += rad * sn;
+    }
+    return make_double2(sx, flip ? -sy : sy);
+}
 
 // ---------------------------------------------------------------- reductions
 struct DD { double s, c; };  // Neumaier pair: value = s + c
@@ -188,7 +216,7 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
     if (MODE == ROW_STAGE && bx == 0 && threadIdx.x == 0) {
         if (a.marker == 1) {
             a.ds->step_cur = a.ds->step_next;
-            a.ds->step_next = a.ds->step_next + 1ULL;
+            a.ds->step_next = a.ds->step_next + (a.ds->fsub ? a.ds->fsub : 1ULL);
         } else if (a.marker == 2) {
             a.ds->maxvel2 = 0ULL;
         }
@@ -453,7 +481,7 @@ __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, cons
             double f_amp = 0.0;
             double sfd_a = 0.0;
             if (STAGE == 4) {
-                if (a.sp.forcing) f_amp = a.sp.f_sigma * sqrt(dt);
+                if (a.sp.forcing) f_amp = a.sp.f_sigma * sqrt(dt / a.sp.fsub);
                 if (a.sp.sfd) {
                     sfd_a = dt / a.sp.sfd_tau;
                     sfd_a = sfd_a > 1.0 ? 1.0 : (sfd_a < 0.0 ? 0.0 : sfd_a);
@@ -553,20 +581,10 @@ __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, cons
                         const double k2d = kxd * kxd + kyd * kyd;
                         const double km = sqrt(k2d);
                         if (k2d > 1e-12 && km >= a.sp.f_kmin && km <= a.sp.f_kmax) {
-                            int jsrc = j, flip = 0;
-                            if (i == 0 && j > g.ny / 2) { jsrc = g.ny - j; flip = 1; }
-                            unsigned long long ctr[4] = {(unsigned long long)jsrc * g.nkx + i, a.ds->step_cur,
-                                                         NSG_TAG_FORCE, 0ULL};
-                            philox4x64(ctr, a.sp.f_seed, 0ULL);
-                            const double u1 = fmax(u53(ctr[0]), 2.2250738585072014e-308);
-                            const double u2 = u53(ctr[1]);
-                            const double rad = sqrt(-2.0 * log(u1)) * 0.70710678118654752440;
-                            double sn, cs;
-                            sincos(2.0 * 3.141592653589793 * u2, &sn, &cs);
-                            double xr = rad * cs, xi = rad * sn;
-                            if (flip) xi = -xi;
+                            const double2 xi = forcing_xi_sum(i, j, g.ny, a.ds->step_cur, a.sp.fsub, a.sp.f_seed);
+                            const double xr = xi.x, xi_im = xi.y;
                             wn.x = (T)((double)wn.x + f_amp * xr);
-                            wn.y = (T)((double)wn.y + f_amp * xi);
+                            wn.y = (T)((double)wn.y + f_amp * xi_im);
                         }
                     }
                     if (a.sp.sfd) {

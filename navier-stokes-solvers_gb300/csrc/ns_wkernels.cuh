@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(32 * rw_warps<T>(), 1) k_row_w(Geo g, RowArgs<
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (a.marker == 1) {
             a.ds->step_cur = a.ds->step_next;
-            a.ds->step_next = a.ds->step_next + 1ULL;
+            a.ds->step_next = a.ds->step_next + (a.ds->fsub ? a.ds->fsub : 1ULL);
         } else if (a.marker == 2) {
             a.ds->maxvel2 = 0ULL;
         }
@@ -407,24 +407,17 @@ __device__ __forceinline__ void col_fwd2048(C (&a)[32], C* col, const C* tw, int
     team_sync(bid);
 }
 
-// white-in-time forcing increment of one kept mode (Philox4x64-10, Box-Muller)
-__device__ __noinline__ double2 forcing_increment(const Geo& g, int i, int j, unsigned long long step,
+// white-in-time forcing increment of one kept mode: amp times the mode's noise
+// (forcing_xi_sum) when kmin <= |k| <= kmax (FP64 shell test as the reference's k2)
+__device__ __noinline__ double2 forcing_increment(const Geo& g, int i, int j, unsigned long long step, int M,
                                                   unsigned long long seed, double kmin, double kmax, double amp) {
     const double kxd = 2.0 * 3.141592653589793 * i / g.Lx;
     const double kyd = (j <= g.ny / 2) ? 2.0 * 3.141592653589793 * j / g.Ly : 2.0 * 3.141592653589793 * (j - g.ny) / g.Ly;
     const double k2d = kxd * kxd + kyd * kyd;
     const double km = sqrt(k2d);
     if (!(k2d > 1e-12 && km >= kmin && km <= kmax)) return make_double2(0.0, 0.0);
-    int jsrc = j, flip = 0;
-    if (i == 0 && j > g.ny / 2) { jsrc = g.ny - j; flip = 1; }
-    unsigned long long ctr[4] = {(unsigned long long)jsrc * g.nkx + i, step, NSG_TAG_FORCE, 0ULL};
-    philox4x64(ctr, seed, 0ULL);
-    const double u1 = fmax(u53(ctr[0]), 2.2250738585072014e-308);
-    const double u2 = u53(ctr[1]);
-    const double rad = sqrt(-2.0 * log(u1)) * 0.70710678118654752440;
-    double sn, cs;
-    sincos(2.0 * 3.141592653589793 * u2, &sn, &cs);
-    return make_double2(amp * rad * cs, amp * (flip ? -rad * sn : rad * sn));
+    const double2 xi = forcing_xi_sum(i, j, g.ny, step, M, seed);
+    return make_double2(amp * xi.x, amp * xi.y);
 }
 
 // ------------------------------------------------------------ cp.async staging
@@ -683,7 +676,7 @@ __global__ void __launch_bounds__(64 * cw_teams<T>(), 1) k_col_w(Geo g, ColArgs<
             }
             if (STAGE == 4 && (a.sp.forcing || sfd)) {
                 // forcing increment (few low-|k| modes), then the SFD post-step, on omega_hat^{n+1}
-                const double f_amp = a.sp.forcing ? a.sp.f_sigma * sqrt(dt) : 0.0;
+                const double f_amp = a.sp.forcing ? a.sp.f_sigma * sqrt(dt / a.sp.fsub) : 0.0;
                 double sa = 0.0;
                 if (sfd) {
                     sa = dt / a.sp.sfd_tau;
@@ -704,7 +697,7 @@ __global__ void __launch_bounds__(64 * cw_teams<T>(), 1) k_col_w(Geo g, ColArgs<
                     const T k2f = kx * kx + ky * ky;
                     if (force_col && k2f >= k2lo && k2f <= k2hi) {
                         const double2 df =
-                            forcing_increment(g, i, j, a.ds->step_cur, a.sp.f_seed, a.sp.f_kmin, a.sp.f_kmax, f_amp);
+                            forcing_increment(g, i, j, a.ds->step_cur, a.sp.fsub, a.sp.f_seed, a.sp.f_kmin, a.sp.f_kmax, f_amp);
                         if (df.x != 0.0 || df.y != 0.0) {
                             wn.x = (T)((double)wn.x + df.x);
                             wn.y = (T)((double)wn.y + df.y);

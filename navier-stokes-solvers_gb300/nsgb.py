@@ -77,7 +77,7 @@ class GpuParams(C.Structure):
         ("sfd_strength", C.c_double), ("sfd_timescale", C.c_double),
         ("forcing_enabled", C.c_int), ("forcing_kmin", C.c_double),
         ("forcing_kmax", C.c_double), ("forcing_epsilon", C.c_double),
-        ("forcing_seed", C.c_uint64), ("scheme", C.c_int),
+        ("forcing_seed", C.c_uint64), ("scheme", C.c_int), ("forcing_substeps", C.c_int),
     ]
 
 
@@ -166,6 +166,23 @@ def load(build: bool = True) -> C.CDLL:
     proto("ns_gpu_random_spectrum_host", C.c_int, vp, C.c_uint64, C.c_double, C.c_double, _DP)
     proto("ns_gpu_state_device_ptr", vp, vp)
     proto("ns_gpu_energy_spectrum", C.c_int, vp, C.c_int, _DP, _DP, C.POINTER(C.c_int))
+    fp = C.POINTER(C.c_float)
+    proto("ns_gpu_vorticity_device", C.c_int, vp, vp)
+    proto("ns_gpu_add_vorticity_device", C.c_int, vp, vp)
+    proto("ns_gpu_filter_state", C.c_int, vp, vp)
+    proto("ns_cnn_create", C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64, C.POINTER(vp))
+    proto("ns_cnn_destroy", None, vp)
+    proto("ns_cnn_last_error", C.c_char_p, vp)
+    proto("ns_cnn_param_count", C.c_int, vp, C.POINTER(C.c_size_t))
+    proto("ns_cnn_launch_count", C.c_uint64, vp)
+    proto("ns_cnn_get_params", C.c_int, vp, fp)
+    proto("ns_cnn_set_params", C.c_int, vp, fp)
+    proto("ns_cnn_set_normalization", C.c_int, vp, C.c_float, C.c_float, C.c_float)
+    proto("ns_cnn_set_dataset", C.c_int, vp, fp, fp, C.c_int)
+    proto("ns_cnn_loss_and_grads", C.c_int, vp, fp, fp, C.c_int, _DP, fp)
+    proto("ns_cnn_forward_host", C.c_int, vp, fp, C.c_int, fp)
+    proto("ns_cnn_train", C.c_int, vp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_uint64, _DP)
+    proto("ns_cnn_correct_step", C.c_int, vp, vp, C.c_int)
     ecp = C.POINTER(EnsembleConfig)
     proto("ns_gpu_create_for_ensemble", C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, ecp, C.POINTER(vp))
     proto("ns_gpu_ensemble_create", C.c_int, C.c_int, C.POINTER(C.c_int), C.c_double, ecp, C.POINTER(vp))
@@ -470,6 +487,84 @@ class Ensemble:
             for m in self.members:
                 m.h = None
             self.lib.ns_gpu_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class Corrector:
+    """Learned coarse-grid corrector network (ns_cnn_*)."""
+
+    def __init__(self, height: int, width: int, max_batch: int, seed: int = 1):
+        self.lib = load()
+        h = C.c_void_p()
+        st = self.lib.ns_cnn_create(height, width, max_batch, seed, C.byref(h))
+        if st != 0:
+            raise RuntimeError(f"ns_cnn_create failed: {self.lib.ns_gpu_status_string(st).decode()}")
+        self.h = h
+        self.H, self.W = height, width
+        n = C.c_size_t()
+        self.lib.ns_cnn_param_count(h, C.byref(n))
+        self.nparam = n.value
+
+    def check(self, st, what):
+        if st != 0:
+            raise RuntimeError(f"{what} failed ({st}): {self.lib.ns_cnn_last_error(self.h).decode()}")
+
+    def params(self) -> np.ndarray:
+        p = np.zeros(self.nparam, dtype=np.float32)
+        self.check(self.lib.ns_cnn_get_params(self.h, _fptr(p)), "get_params")
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        self.check(self.lib.ns_cnn_set_params(self.h, _fptr(p)), "set_params")
+
+    def set_normalization(self, s0, s1, so):
+        self.check(self.lib.ns_cnn_set_normalization(self.h, s0, s1, so), "set_normalization")
+
+    def set_dataset(self, inputs, targets):
+        i = np.ascontiguousarray(inputs, dtype=np.float32)
+        t = np.ascontiguousarray(targets, dtype=np.float32)
+        self.check(self.lib.ns_cnn_set_dataset(self.h, _fptr(i), _fptr(t), i.shape[0]), "set_dataset")
+
+    def loss_and_grads(self, inputs, targets):
+        i = np.ascontiguousarray(inputs, dtype=np.float32)
+        t = np.ascontiguousarray(targets, dtype=np.float32)
+        g = np.zeros(self.nparam, dtype=np.float32)
+        loss = C.c_double()
+        self.check(self.lib.ns_cnn_loss_and_grads(self.h, _fptr(i), _fptr(t), i.shape[0], C.byref(loss), _fptr(g)),
+                   "loss_and_grads")
+        return loss.value, g
+
+    def forward(self, inputs):
+        i = np.ascontiguousarray(inputs, dtype=np.float32)
+        out = np.zeros((i.shape[0], self.H, self.W), dtype=np.float32)
+        self.check(self.lib.ns_cnn_forward_host(self.h, _fptr(i), i.shape[0], _fptr(out)), "forward")
+        return out
+
+    def train(self, iterations, batch, lr, weight_decay=0.0, seed=1):
+        hist = np.zeros(iterations)
+        self.check(self.lib.ns_cnn_train(self.h, iterations, batch, lr, weight_decay, seed, _ptr(hist)), "train")
+        return hist
+
+    def correct_step(self, gpu: "Gpu", n: int = 1):
+        self.check(self.lib.ns_cnn_correct_step(self.h, gpu.h, n), "correct_step")
+
+    def launches(self) -> int:
+        return int(self.lib.ns_cnn_launch_count(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ns_cnn_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -806,8 +806,9 @@ static double nso_ext_forcing_sigma(const nso_state *s, const nso_ext_forcing *f
 }
 
 /* omega_hat += sigma sqrt(dt) xi, xi = (g1 + i g2)/sqrt(2) from Box-Muller on
- * Philox(counter = (j*nkx+i, step, TAG_FORCE, 0), key = (seed, 0)) outputs 0,1;
- * kx = 0 rows ny-j take the conjugate of row j. */
+ * Philox(counter = (mode id, step, TAG_FORCE, 0), key = (seed, 0)) outputs 0,1;
+ * mode id = (signed ky) << 32 | kx (the same noise for a physical mode on every
+ * grid); kx = 0 rows with ky < 0 take the conjugate of the ky > 0 row. */
 static void nso_ext_apply_forcing(nso_state *s, const nso_ext_forcing *f, double dt) {
     const double sigma = nso_ext_forcing_sigma(s, f);
     const double amp = sigma * sqrt(dt);
@@ -817,12 +818,13 @@ static void nso_ext_apply_forcing(nso_state *s, const nso_ext_forcing *f, double
             const int idx = j * s->nkx + i;
             const double km = sqrt(s->k2[idx]);
             if (!s->dealias_mask[idx] || s->k2[idx] <= 1e-12 || km < f->kmin || km > f->kmax) continue;
-            int jsrc = j, flip = 0;
-            if (i == 0 && j > ny / 2) {
-                jsrc = ny - j;
+            int ky = (j <= ny / 2) ? j : j - ny, flip = 0;
+            if (i == 0 && ky < 0) {
+                ky = -ky;
                 flip = 1;
             }
-            const uint64_t ctr[4] = {(uint64_t)(jsrc * s->nkx + i), f->step, NSO_TAG_FORCE, 0};
+            const uint64_t id = ((uint64_t)(uint32_t)ky << 32) | (uint32_t)i;
+            const uint64_t ctr[4] = {id, f->step, NSO_TAG_FORCE, 0};
             const uint64_t key[2] = {f->seed, 0};
             uint64_t r[4];
             nso_ext_philox4x64(ctr, key, r);

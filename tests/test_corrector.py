@@ -1,0 +1,88 @@
+"""Learned corrector network (ns_cnn_*): the hand-written forward and backward
+kernels against the CPU FP64 oracle (oracle/cnn_oracle.py) on the same BF16-rounded
+weights, and the oracle's own gradients against finite differences.
+
+Tolerances: the device accumulates in FP32, so losses agree to 1e-5 and each
+layer's weight and bias gradients to 2e-4 relative L2."""
+import numpy as np
+import pytest
+
+import cnn_oracle as CO
+
+
+def rand_params(seed, scale=1.0):
+    rng = np.random.default_rng(seed)
+    parts = []
+    for ci, co in CO.CHANNELS:
+        a = np.sqrt(6.0 / (9 * ci)) * scale
+        parts.append(rng.uniform(-a, a, 9 * ci * co))
+        parts.append(rng.uniform(-0.1, 0.1, co))
+    return np.concatenate(parts)
+
+
+def test_oracle_gradients_match_finite_differences():
+    rng = np.random.default_rng(0)
+    p = rand_params(1)
+    x = rng.standard_normal((1, 2, 8, 16))
+    t = 0.1 * rng.standard_normal((1, 8, 16))
+    loss, g = CO.loss_and_grads(p, x, t, bf16_weights=False)
+    offs = np.cumsum([0] + [9 * ci * co + co for ci, co in CO.CHANNELS])
+    picks = [offs[l] + k for l in range(6) for k in (0, 9 * CO.CHANNELS[l][0] * CO.CHANNELS[l][1] - 1,
+                                                     9 * CO.CHANNELS[l][0] * CO.CHANNELS[l][1])]
+    for i in picks:
+        h = 1e-5
+        pp, pm = p.copy(), p.copy()
+        pp[i] += h
+        pm[i] -= h
+        fd = (CO.loss_and_grads(pp, x, t, bf16_weights=False)[0] - CO.loss_and_grads(pm, x, t, bf16_weights=False)[0]) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(g).max()), (i, fd, g[i])
+
+
+def test_bf16_rounding_is_nearest_even():
+    x = np.array([1.0, 1.00390625, 1.005859375, -3.14159, 65504.0], dtype=np.float32)
+    r = CO.bf16(x)
+    assert r[0] == 1.0 and r[1] == 1.0 and r[2] == 1.0078125
+    assert abs(r[3] + 3.140625) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape,batch", [((8, 16), 2), ((16, 32), 3)])
+def test_device_gradients_match_oracle(nsgb, shape, batch):
+    H, W = shape
+    net = nsgb.Corrector(H, W, max_batch=4, seed=3)
+    p = rand_params(7).astype(np.float32)
+    net.set_params(p)
+    s0, s1, so = 0.5, 2.0, 3.0
+    net.set_normalization(s0, s1, so)
+    rng = np.random.default_rng(11)
+    x = rng.standard_normal((batch, 2, H, W)).astype(np.float32)
+    t = (0.2 * rng.standard_normal((batch, H, W))).astype(np.float32)
+    loss, g = net.loss_and_grads(x, t)
+    lo, go = CO.loss_and_grads(p.astype(np.float64), x.astype(np.float64), t.astype(np.float64), s0, s1, so)
+    assert abs(loss - lo) <= 1e-5 * lo
+    off = 0
+    for ci, co in CO.CHANNELS:
+        for n in (9 * ci * co, co):
+            a, b = g[off:off + n].astype(np.float64), go[off:off + n]
+            err = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+            assert err <= 2e-4, (ci, co, n, err)
+            off += n
+    out = net.forward(x)
+    ref = CO.forward(p.astype(np.float64), x.astype(np.float64), s0, s1, so)
+    assert np.linalg.norm(out - ref) / np.linalg.norm(ref) <= 1e-5
+    net.close()
+
+
+@pytest.mark.gpu
+def test_training_reduces_the_loss_on_a_learnable_map(nsgb):
+    """The target is a fixed linear stencil of the inputs: AdamW must fit it."""
+    H, W, N = 16, 32, 64
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal((N, 2, H, W)).astype(np.float32)
+    t = (0.5 * (np.roll(x[:, 0], 1, axis=2) - np.roll(x[:, 0], -1, axis=2)) + 0.3 * x[:, 1]).astype(np.float32)
+    net = nsgb.Corrector(H, W, max_batch=8, seed=2)
+    net.set_dataset(x, t)
+    hist = net.train(300, 8, 2e-3, 1e-4, seed=9)
+    assert np.isfinite(hist).all()
+    assert hist[-20:].mean() < 0.1 * hist[:5].mean(), (hist[:5], hist[-20:])
+    net.close()
