@@ -35,12 +35,17 @@ def hv_coefficient(n: int, cfl: float = 0.5) -> float:
     return kmax ** 4 / (kd ** 4 * dt_ref)
 
 
-def params(n: int, dt: float, Re: float = 1e5, forcing_seed: int | None = None, epsilon: float = 1e-3) -> dict:
+def params(n: int, dt: float, Re: float = 1e5, forcing_seed: int | None = None, epsilon: float = 1e-3,
+           substeps: int = 1) -> dict:
+    """Config-2 physics on an n^2 grid with a fixed dt.  With forcing, a coarse
+    instance takes `substeps` forcing draws per step: the forcing noise is keyed
+    by the physical mode and the fine step, so a coarse step of `substeps` fine
+    steps receives the fine run's forcing exactly (ns_gpu_params.forcing_substeps)."""
     p = dict(Re=Re, cfl_factor=0.5, adaptive_dt=0, dt=dt, hv_enabled=1, hv_coefficient=hv_coefficient(n),
              hv_order=4, hv_cutoff_ratio=0.0)
     if forcing_seed is not None:
         p.update(forcing_enabled=1, forcing_kmin=4.0, forcing_kmax=6.0, forcing_epsilon=epsilon,
-                 forcing_seed=forcing_seed)
+                 forcing_seed=forcing_seed, forcing_substeps=substeps)
     return p
 
 
@@ -72,8 +77,9 @@ def generate(seeds, fine_n=1024, coarse_n=256, ratio=8, spinup=200, snapshots=32
     coarse = nsgb.Gpu(coarse_n, coarse_n, L, L, nsgb.FP32)
     xs, ts = [], []
     for seed in seeds:
-        fine.set_params(**params(fine_n, dt_f, forcing_seed=(1000 + seed) if forcing else None))
-        coarse.set_params(**params(coarse_n, ratio * dt_f))
+        fseed = (1000 + seed) if forcing else None
+        fine.set_params(**params(fine_n, dt_f, forcing_seed=fseed))
+        coarse.set_params(**params(coarse_n, ratio * dt_f, forcing_seed=fseed, substeps=ratio))
         fine.random_spectrum(seed, k0, 0.5)
         fine.advance(spinup)
         for _ in range(snapshots):
@@ -114,9 +120,10 @@ def evaluate(net: "nsgb.Corrector", seeds, horizon, fine_n=1024, coarse_n=256, r
     learned = nsgb.Gpu(coarse_n, coarse_n, L, L, nsgb.FP32)
     out = []
     for seed in seeds:
-        fine.set_params(**params(fine_n, dt_f, forcing_seed=(1000 + seed) if forcing else None))
+        fseed = (1000 + seed) if forcing else None
+        fine.set_params(**params(fine_n, dt_f, forcing_seed=fseed))
         for g in (plain, learned):
-            g.set_params(**params(coarse_n, ratio * dt_f))
+            g.set_params(**params(coarse_n, ratio * dt_f, forcing_seed=fseed, substeps=ratio))
         fine.random_spectrum(seed, k0, 0.5)
         fine.advance(spinup)
         _filter(fine, plain)
@@ -157,3 +164,68 @@ def evaluate(net: "nsgb.Corrector", seeds, horizon, fine_n=1024, coarse_n=256, r
     plain.close()
     learned.close()
     return out, dt_f
+
+
+def main(argv=None):
+    """Config-4 experiment: generate, train, evaluate; one JSON document on stdout."""
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--fine", type=int, default=1024)
+    ap.add_argument("--coarse", type=int, default=256)
+    ap.add_argument("--ratio", type=int, default=8)
+    ap.add_argument("--train-seeds", type=int, default=64)
+    ap.add_argument("--snapshots", type=int, default=32)
+    ap.add_argument("--spinup", type=int, default=200)
+    ap.add_argument("--iters", type=int, default=20000)
+    ap.add_argument("--batch", type=int, default=32)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--weight-decay", type=float, default=1e-4)
+    ap.add_argument("--eval-seeds", type=int, default=16)
+    ap.add_argument("--horizon", type=int, default=2000)
+    ap.add_argument("--every", type=int, default=50)
+    ap.add_argument("--forcing", action="store_true", help="forced runs (shells 4-6, eps 1e-3)")
+    ap.add_argument("--save", default=None, help="write the trained parameters (.npy)")
+    a = ap.parse_args(argv)
+    t0 = time.time()
+    x, t, dt_f = generate(list(range(a.train_seeds)), a.fine, a.coarse, a.ratio, a.spinup, a.snapshots,
+                          forcing=a.forcing)
+    t_gen = time.time() - t0
+    s0, s1, so = normalisation(x, t)
+    net = nsgb.Corrector(a.coarse, a.coarse, max_batch=a.batch, seed=1)
+    net.set_normalization(s0, s1, so)
+    net.set_dataset(x, t)
+    t0 = time.time()
+    hist = net.train(a.iters, a.batch, a.lr, a.weight_decay, seed=7)
+    t_train = time.time() - t0
+    if a.save:
+        np.save(a.save, net.params())
+    eval_seeds = list(range(10000, 10000 + a.eval_seeds))
+    res, _ = evaluate(net, eval_seeds, a.horizon, a.fine, a.coarse, a.ratio, a.spinup, dt_f=dt_f,
+                      forcing=a.forcing, every=a.every)
+    mean = lambda key, i: float(np.mean([r[key][i] for r in res]))
+    n_eval = len(res[0]["rel_l2_plain"])
+    summary = {
+        "config": {"fine": a.fine, "coarse": a.coarse, "ratio": a.ratio, "train_seeds": a.train_seeds,
+                   "samples": int(x.shape[0]), "iters": a.iters, "batch": a.batch, "horizon": a.horizon,
+                   "eval_seeds": a.eval_seeds, "forcing": a.forcing, "dt_fine": dt_f},
+        "seconds": {"generate": t_gen, "train": t_train},
+        "loss": {"first": float(hist[:10].mean()), "last": float(hist[-100:].mean())},
+        "rel_l2_vs_filtered_fine": {
+            "coarse_steps": [min((i + 1) * a.every, a.horizon) for i in range(n_eval)],
+            "plain": [mean("rel_l2_plain", i) for i in range(n_eval)],
+            "learned": [mean("rel_l2_learned", i) for i in range(n_eval)]},
+        "log_spectrum_error_end": {"plain": float(np.mean([r["log_spectrum_error_plain"] for r in res])),
+                                   "learned": float(np.mean([r["log_spectrum_error_learned"] for r in res]))},
+        "wall_s_per_coarse_step": {k: float(np.sum([r[f"wall_s_{k}"] for r in res]) / (a.horizon * len(res)))
+                                   for k in ("fine", "plain", "learned")},
+        "network_launches": net.launches(),
+    }
+    net.close()
+    print(json.dumps(summary))
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
