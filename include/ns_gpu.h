@@ -340,6 +340,10 @@ int ns_cnn_forward_host(ns_cnn *c, const float *inputs, int batch, float *out);
 /* iterations AdamW steps (beta 0.9 / 0.999, eps 1e-8, decoupled weight decay) on
  * minibatches drawn from the dataset with a seeded generator; loss_history may be NULL */
 int ns_cnn_train(ns_cnn *c, int iterations, int batch, float lr, float weight_decay, uint64_t seed, double *loss_history);
+/* The four 64 -> 64 layers run on the tcgen05 tensor cores (BF16 activations and
+ * weights, FP32 accumulation in tensor memory) when W is a multiple of 128 (the
+ * default there); 0 selects the FP32 SIMT kernels for every layer. */
+int ns_cnn_set_tensor_cores(ns_cnn *c, int enable);
 /* nsteps corrected steps of an instance on the network's grid: plain RK4 step
  * (ns_gpu_advance), then omega += CNN(omega(t), omega(t+dt) - omega(t)) */
 int ns_cnn_correct_step(ns_cnn *c, ns_gpu *g, int nsteps);

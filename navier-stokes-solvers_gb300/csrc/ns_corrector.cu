@@ -99,6 +99,183 @@ __global__ void __launch_bounds__(TP*(COUT / CPT)) k_conv3x3(const float* __rest
     }
 }
 
+// ----------------------------------------------------- tcgen05 convolution
+// The 64 -> 64 layers as an implicit GEMM on the 5th-generation tensor cores:
+// D[128 pixels][64 co] (FP32, in tensor memory) += A[128 pixels][16 ci] x
+// B[16 ci][64 co] (BF16), 9 taps x 4 K-steps = 36 tcgen05.mma per tile.  A tile
+// is 128 consecutive pixels of one image row (W % 128 == 0).  The periodic halo
+// of the tile (3 rows x 130 pixels x 64 channels, BF16) sits in shared memory
+// as [row][8-channel chunk][130 px][8 ch], which is the canonical K-major,
+// no-swizzle operand layout (core matrix = 8 pixels x 16 bytes, 8-pixel groups
+// 128 B apart, K chunks 2080 B apart); the operand of tap (dy, dx) therefore
+// starts dx x 16 B and dy rows into the halo, with no im2col copy.  The weights
+// (B operand) stay in shared memory as [tap][chunk][64 co][8 ci].  One thread
+// issues the MMAs and commits them to an mbarrier; all four warps then read
+// their 32 rows of the accumulator with tcgen05.ld and run the epilogue (bias,
+// GELU, FP32 and BF16 stores).  Every wait is bounded by a clock budget: on
+// expiry the kernel records an error, frees its tensor memory and returns.
+constexpr int TC_W = 128;                                  // pixels per tile
+constexpr int TC_HP = TC_W + 2;                            // halo pixels per row
+constexpr int TC_WB_BYTES = 9 * 8 * 64 * 16;               // 73,728
+constexpr int TC_HX_BYTES = 3 * 8 * TC_HP * 16;            // 49,920
+constexpr int TC_SMEM = TC_WB_BYTES + TC_HX_BYTES + 64;    // + mbarrier and tmem address
+constexpr long long TC_WAIT_CYCLES = 4000000000LL;         // about 2 s
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: K-major, no swizzle (sm_100 family layout)
+__device__ __forceinline__ unsigned long long umma_desc(unsigned addr, unsigned lbo, unsigned sbo) {
+    unsigned long long d = 0;
+    d |= (unsigned long long)((addr >> 4) & 0x3FFF);
+    d |= (unsigned long long)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (unsigned long long)((sbo >> 4) & 0x3FFF) << 32;
+    d |= 1ULL << 46;  // descriptor version
+    return d;         // base offset 0, swizzle none
+}
+
+// instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major, N = 64, M = 128
+constexpr unsigned TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void tc_mma(unsigned taddr, unsigned long long a, unsigned long long b, unsigned accum) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(taddr),
+        "l"(a), "l"(b), "r"(TC_IDESC), "r"(accum));
+}
+
+__device__ __forceinline__ bool mbar_wait(unsigned mbar, unsigned parity) {
+    const long long t0 = clock64();
+    for (;;) {
+        unsigned done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (clock64() - t0 > TC_WAIT_CYCLES) return false;
+    }
+}
+
+// 32 consecutive accumulator columns of this thread's row
+__device__ __forceinline__ void tc_ld32(unsigned taddr, float (&v)[32]) {
+    unsigned r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// in: BF16 activations [B][H][W][64]; w: BF16 weights [9][64 ci][64 co];
+// outputs (each may be null): pre FP32, actf FP32, actb BF16, all [B][H][W][64]
+template <bool GELU>
+__global__ void __launch_bounds__(128, 1) k_conv_tc(const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ w,
+                                                    const float* __restrict__ bias, float* __restrict__ pre,
+                                                    float* __restrict__ actf, __nv_bfloat16* __restrict__ actb, int B, int H,
+                                                    int W, int* __restrict__ err) {
+    extern __shared__ __align__(128) unsigned char tsm[];
+    unsigned char* WB = tsm;                            // [9][8][64][8] bf16
+    unsigned char* HX = tsm + TC_WB_BYTES;              // [3][8][130][8] bf16
+    unsigned long long* mbar = reinterpret_cast<unsigned long long*>(tsm + TC_WB_BYTES + TC_HX_BYTES);
+    unsigned* tslot = reinterpret_cast<unsigned*>(tsm + TC_WB_BYTES + TC_HX_BYTES + 16);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    // weights into the B-operand layout: WB[tap][kc][co][j] = w[tap][8 kc + j][co]
+    for (int i = tid; i < 9 * 64 * 64; i += 128) {
+        const int tap = i >> 12, r = i & 4095, ci = r >> 6, co = r & 63;
+        reinterpret_cast<__nv_bfloat16*>(WB)[((tap * 8 + (ci >> 3)) * 64 + co) * 8 + (ci & 7)] = w[i];
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(smem_u32(tslot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const unsigned taddr = *tslot;
+    const unsigned mb = smem_u32(mbar);
+    const unsigned hx = smem_u32(HX), wbs = smem_u32(WB);
+    const int ntx = W / TC_W;
+    const int ntiles = B * H * ntx;
+    unsigned phase = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const int b = tile / (H * ntx), r = tile - b * H * ntx;
+        const int y = r / ntx, x0 = (r - y * ntx) * TC_W;
+        // halo: HX[row][kc][px][8] = in[b][y + row - 1][x0 + px - 1][8 kc .. 8 kc + 7]
+        for (int i = tid; i < 3 * TC_HP * 8; i += 128) {
+            const int row = i / (TC_HP * 8), q = i - row * TC_HP * 8;
+            const int px = q >> 3, kc = q & 7;
+            const int gy = wrapi(y + row - 1, H), gx = wrapi(x0 + px - 1, W);
+            const __nv_bfloat16* src = in + (((size_t)b * H + gy) * W + gx) * 64 + kc * 8;
+            const unsigned dst = hx + (unsigned)(((row * 8 + kc) * TC_HP + px) * 16);
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic-proxy writes -> tensor-core reads
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll 1
+            for (int tap = 0; tap < 9; ++tap) {
+                const int dy = tap / 3, dx = tap - 3 * dy;
+#pragma unroll
+                for (int s = 0; s < 4; ++s) {
+                    const unsigned a = hx + (unsigned)(((dy * 8 + 2 * s) * TC_HP + dx) * 16);
+                    const unsigned bb = wbs + (unsigned)((tap * 8 + 2 * s) * 64 * 16);
+                    tc_mma(taddr, umma_desc(a, TC_HP * 16, 128), umma_desc(bb, 64 * 16, 128), (tap | s) ? 1u : 0u);
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb) : "memory");
+        }
+        // every thread must take the same branch (barriers follow): the tile
+        // succeeds only if every thread saw the MMAs complete in time
+        ok = __syncthreads_and(mbar_wait(mb, phase) ? 1 : 0) != 0;
+        phase ^= 1u;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (ok) {
+            const int px = x0 + warp * 32 + lane;
+            const size_t o = (((size_t)b * H + y) * W + px) * 64;
+#pragma unroll
+            for (int half = 0; half < 2; ++half) {
+                float v[32];
+                tc_ld32(taddr + ((unsigned)(warp * 32) << 16) + (unsigned)(half * 32), v);
+#pragma unroll
+                for (int k = 0; k < 32; ++k) {
+                    const int co = half * 32 + k;
+                    const float pv = v[k] + bias[co];
+                    const float av = GELU ? gelu(pv) : pv;
+                    if (pre) pre[o + co] = pv;
+                    if (actf) actf[o + co] = av;
+                    if (actb) actb[o + co] = __float2bfloat16_rn(av);
+                }
+            }
+        } else if (tid == 0) {
+            atomicExch(err, 1);
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();  // accumulator read and halo consumed before the next tile
+    }
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(taddr));
+}
+
+__global__ void k_to_bf16(const float* __restrict__ a, __nv_bfloat16* __restrict__ b, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b[i] = __float2bfloat16_rn(a[i]);
+}
+
 __host__ __device__ constexpr int cmin(int a, int b) { return a < b ? a : b; }
 template <int CIN, int COUT> __host__ __device__ constexpr int dw_threads() { return (CIN / cmin(4, CIN)) * (COUT / cmin(4, COUT)) * 3; }
 template <int CIN, int COUT> constexpr size_t dw_smem() {
@@ -303,6 +480,9 @@ struct ns_cnn {
     float s0 = 1.0f, s1 = 1.0f, so = 1.0f;
     long long step = 0;            // AdamW step counter
     float *cw0 = nullptr, *cw1 = nullptr;  // corrector scratch [H][W]
+    __nv_bfloat16 *ab0 = nullptr, *ab1 = nullptr;  // BF16 activations of the tensor-core layers
+    int tc = 0;                    // 64 -> 64 layers on tcgen05 (W % 128 == 0)
+    int* derr = nullptr;           // device error flag of the tensor-core kernel
     unsigned long long launches = 0;
     std::string err;
 };
@@ -355,13 +535,52 @@ static int conv_dw(ns_cnn* c, cudaStream_t st, const float* in, const float* dpr
         if (_s != NS_GPU_OK) return _s; \
     } while (0)
 
-// forward of the whole network on x0 (B samples); output in pre[NL-1] ([B][H][W])
-static int forward(ns_cnn* c, cudaStream_t st, int B) {
+static int conv_tc(ns_cnn* c, cudaStream_t st, int l, const __nv_bfloat16* in, float* pre, float* actf, __nv_bfloat16* actb,
+                   int B) {
+    auto k = k_conv_tc<true>;
+    CNN_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+    const int tiles = B * c->H * (c->W / TC_W);
+    k<<<grid_of(tiles, 1, c->num_sms), 128, TC_SMEM, st>>>(in, c->wb[l], c->p + c->boff[l], pre, actf, actb, B, c->H, c->W,
+                                                           c->derr);
+    CNN_LAUNCHED(c);
+    return NS_GPU_OK;
+}
+
+// forward of the whole network on x0 (B samples); output in pre[NL-1] ([B][H][W]).
+// With tensor cores the hidden 64 -> 64 layers run on tcgen05 from BF16
+// activations; `training` keeps every layer's FP32 pre-activation and
+// activation for the backward pass, otherwise only what the next layer reads.
+static int forward(ns_cnn* c, cudaStream_t st, int B, bool training = true) {
     const float* x = c->x0;
     CNN_TRY((conv<2, HID, 32, true>(c, st, x, c->wb[0], c->p + c->boff[0], c->pre[0], c->act[0], B)));
-    for (int l = 1; l < NL - 1; ++l)
-        CNN_TRY((conv<HID, HID, 32, true>(c, st, c->act[l - 1], c->wb[l], c->p + c->boff[l], c->pre[l], c->act[l], B)));
+    if (c->tc) {
+        const long long n = (long long)B * c->H * c->W * HID;
+        k_to_bf16<<<grid_of(n, 256, 8 * c->num_sms), 256, 0, st>>>(c->act[0], c->ab0, n);
+        CNN_LAUNCHED(c);
+        __nv_bfloat16* ain = c->ab0;
+        __nv_bfloat16* aout = c->ab1;
+        for (int l = 1; l < NL - 1; ++l) {
+            const bool last = (l == NL - 2);
+            CNN_TRY(conv_tc(c, st, l, ain, training ? c->pre[l] : nullptr, (training || last) ? c->act[l] : nullptr,
+                            last ? nullptr : aout, B));
+            __nv_bfloat16* t = ain;
+            ain = aout;
+            aout = t;
+        }
+    } else {
+        for (int l = 1; l < NL - 1; ++l)
+            CNN_TRY((conv<HID, HID, 32, true>(c, st, c->act[l - 1], c->wb[l], c->p + c->boff[l], c->pre[l], c->act[l], B)));
+    }
     CNN_TRY((conv<HID, 1, 1, false>(c, st, c->act[NL - 2], c->wb[NL - 1], c->p + c->boff[NL - 1], c->pre[NL - 1], nullptr, B)));
+    return NS_GPU_OK;
+}
+
+// the tensor-core kernel's bounded waits record expiry in derr
+static int check_tc(ns_cnn* c) {
+    if (!c->tc) return NS_GPU_OK;
+    int e = 0;
+    CNN_CUDA(c, cudaMemcpy(&e, c->derr, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) CNN_FAIL(c, NS_GPU_ERR_CUDA, "tensor-core convolution: an MMA completion wait timed out");
     return NS_GPU_OK;
 }
 
@@ -448,6 +667,13 @@ int ns_cnn_create(int height, int width, int max_batch, uint64_t seed, ns_cnn** 
     alloc((void**)&c->tgt, npix * sizeof(float));
     alloc((void**)&c->didx, (size_t)max_batch * sizeof(int));
     alloc((void**)&c->cw0, (size_t)height * width * sizeof(float));
+    c->tc = (width % TC_W == 0) ? 1 : 0;
+    if (c->tc) {
+        alloc((void**)&c->ab0, npix * HID * sizeof(__nv_bfloat16));
+        alloc((void**)&c->ab1, npix * HID * sizeof(__nv_bfloat16));
+    }
+    alloc((void**)&c->derr, sizeof(int));
+    if (ok && cudaMemset(c->derr, 0, sizeof(int)) != cudaSuccess) ok = false;
     alloc((void**)&c->cw1, (size_t)height * width * sizeof(float));
     c->loss_cap = 1;
     alloc((void**)&c->dloss, sizeof(double));
@@ -476,7 +702,8 @@ int ns_cnn_create(int height, int width, int max_batch, uint64_t seed, ns_cnn** 
 void ns_cnn_destroy(ns_cnn* c) {
     if (!c) return;
     if (c->st) cudaStreamSynchronize(c->st);
-    void* ptrs[] = {c->p, c->gp, c->m, c->v, c->x0, c->d0, c->d1, c->tgt, c->dloss, c->didx, c->data_in, c->data_tg, c->cw0, c->cw1};
+    void* ptrs[] = {c->p,   c->gp,     c->m,       c->v,       c->x0,  c->d0,  c->d1,  c->tgt,
+                    c->dloss, c->didx, c->data_in, c->data_tg, c->cw0, c->cw1, c->ab0, c->ab1, c->derr};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     for (int l = 0; l < NL; ++l) {
@@ -606,6 +833,7 @@ int ns_cnn_forward_host(ns_cnn* c, const float* inputs, int B, float* out) {
     }
     if (cudaStreamSynchronize(st) != cudaSuccess && s == NS_GPU_OK) s = NS_GPU_ERR_CUDA;
     cudaFree(din);
+    if (s == NS_GPU_OK) s = check_tc(c);
     return s;
 }
 
@@ -659,6 +887,7 @@ int ns_cnn_train(ns_cnn* c, int iterations, int batch, float lr, float weight_de
     cudaFree(didx_all);
     cudaFreeHost(hidx);
     if (s != NS_GPU_OK && c->err.empty()) c->err = "train: CUDA error";
+    if (s == NS_GPU_OK) s = check_tc(c);
     return s;
 }
 
@@ -674,12 +903,19 @@ int ns_cnn_correct_step(ns_cnn* c, ns_gpu* g, int nsteps) {
         CNN_TRY(ns_gpu_synchronize(g));  // the network runs on its own stream
         k_make_input<<<grid_of(hw, 256, 1024), 256, 0, c->st>>>(c->cw0, c->cw1, hw, c->s0, c->s1, c->x0);
         CNN_LAUNCHED(c);
-        CNN_TRY(forward(c, c->st, 1));
+        CNN_TRY(forward(c, c->st, 1, false));
         k_scale<<<grid_of(hw, 256, 1024), 256, 0, c->st>>>(c->pre[NL - 1], hw, 1.0f / c->so);
         CNN_LAUNCHED(c);
         CNN_CUDA(c, cudaStreamSynchronize(c->st));
         CNN_TRY(ns_gpu_add_vorticity_device(g, c->pre[NL - 1]));
     }
+    return check_tc(c);
+}
+
+int ns_cnn_set_tensor_cores(ns_cnn* c, int enable) {
+    if (!c) return NS_GPU_ERR_INVALID;
+    if (enable && (c->W % TC_W != 0 || !c->ab0)) CNN_FAIL(c, NS_GPU_ERR_INVALID, "tensor cores need W %% %d == 0", TC_W);
+    c->tc = enable ? 1 : 0;
     return NS_GPU_OK;
 }
 

@@ -183,6 +183,7 @@ def load(build: bool = True) -> C.CDLL:
     proto("ns_cnn_forward_host", C.c_int, vp, fp, C.c_int, fp)
     proto("ns_cnn_train", C.c_int, vp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_uint64, _DP)
     proto("ns_cnn_correct_step", C.c_int, vp, vp, C.c_int)
+    proto("ns_cnn_set_tensor_cores", C.c_int, vp, C.c_int)
     ecp = C.POINTER(EnsembleConfig)
     proto("ns_gpu_create_for_ensemble", C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, ecp, C.POINTER(vp))
     proto("ns_gpu_ensemble_create", C.c_int, C.c_int, C.POINTER(C.c_int), C.c_double, ecp, C.POINTER(vp))
@@ -555,6 +556,9 @@ class Corrector:
         hist = np.zeros(iterations)
         self.check(self.lib.ns_cnn_train(self.h, iterations, batch, lr, weight_decay, seed, _ptr(hist)), "train")
         return hist
+
+    def set_tensor_cores(self, enable: bool):
+        self.check(self.lib.ns_cnn_set_tensor_cores(self.h, 1 if enable else 0), "set_tensor_cores")
 
     def correct_step(self, gpu: "Gpu", n: int = 1):
         self.check(self.lib.ns_cnn_correct_step(self.h, gpu.h, n), "correct_step")

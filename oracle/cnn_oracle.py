@@ -108,10 +108,14 @@ def loss_and_grads(params, inputs, targets, s0=1.0, s1=1.0, so=1.0, bf16_weights
     return loss, flat
 
 
-def forward(params, inputs, s0=1.0, s1=1.0, so=1.0):
+def forward(params, inputs, s0=1.0, s1=1.0, so=1.0, bf16_hidden_inputs=False):
+    """Network output; bf16_hidden_inputs rounds the inputs of the four 64 -> 64
+    layers to bfloat16, as the library's tensor-core path stores them."""
     layers = [(bf16(w), b) for w, b in unflatten(np.asarray(params, dtype=np.float64))]
     x = np.stack([inputs[:, 0] * s0, inputs[:, 1] * s1], axis=-1).astype(np.float64)
     for l, (w, b) in enumerate(layers):
+        if bf16_hidden_inputs and 1 <= l <= len(layers) - 2:
+            x = bf16(x.astype(np.float32))
         x = conv(x, w, b)
         if l < len(layers) - 1:
             x = gelu(x)

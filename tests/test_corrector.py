@@ -86,3 +86,38 @@ def test_training_reduces_the_loss_on_a_learnable_map(nsgb):
     assert np.isfinite(hist).all()
     assert hist[-20:].mean() < 0.1 * hist[:5].mean(), (hist[:5], hist[-20:])
     net.close()
+
+
+@pytest.mark.gpu
+def test_tensor_core_layers_match_oracle_with_bf16_activations(nsgb):
+    """W = 128: the four 64 -> 64 layers run on tcgen05 (BF16 operands, FP32
+    accumulation in tensor memory); the oracle rounds the same activations to BF16."""
+    H, W, B = 8, 128, 2
+    net = nsgb.Corrector(H, W, max_batch=2, seed=4)
+    p = rand_params(21).astype(np.float32)
+    net.set_params(p)
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal((B, 2, H, W)).astype(np.float32)
+    out_tc = net.forward(x)
+    ref = CO.forward(p.astype(np.float64), x.astype(np.float64), bf16_hidden_inputs=True)
+    assert np.linalg.norm(out_tc - ref) / np.linalg.norm(ref) <= 2e-3
+    net.set_tensor_cores(False)
+    out_simt = net.forward(x)
+    ref32 = CO.forward(p.astype(np.float64), x.astype(np.float64))
+    assert np.linalg.norm(out_simt - ref32) / np.linalg.norm(ref32) <= 1e-5
+    # the two paths differ by the BF16 rounding of the hidden activations only
+    assert np.linalg.norm(out_tc - out_simt) / np.linalg.norm(out_simt) <= 2e-2
+    net.close()
+
+
+@pytest.mark.gpu
+def test_tensor_core_training_reduces_the_loss(nsgb):
+    H, W, N = 8, 128, 32
+    rng = np.random.default_rng(8)
+    x = rng.standard_normal((N, 2, H, W)).astype(np.float32)
+    t = (0.5 * (np.roll(x[:, 0], 1, axis=2) - np.roll(x[:, 0], -1, axis=2)) + 0.3 * x[:, 1]).astype(np.float32)
+    net = nsgb.Corrector(H, W, max_batch=8, seed=2)
+    net.set_dataset(x, t)
+    hist = net.train(200, 8, 2e-3, 1e-4, seed=9)
+    assert np.isfinite(hist).all() and hist[-20:].mean() < 0.2 * hist[:5].mean(), (hist[:5], hist[-20:])
+    net.close()
