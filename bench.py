@@ -244,6 +244,100 @@ def ensemble_leg(steps: int, seq_steps: int = 10) -> dict:
             "l2": "members stay resident in L2 (state ~ 2048^2 single field); no flush inside the persistent launch"}
 
 
+# ----------------------------------------------------- corrector / config-5 legs
+def corrector_leg(steps: int = 20, batch: int = 32) -> dict:
+    """Wall time of the learned-corrected 256^2 step against the 8 fine 1024^2 steps it
+    replaces (timing does not depend on the weights), and the tensor-core roofline of
+    the network's dominant kernel (one 64 -> 64 hidden layer on a training batch)."""
+    import nsgb
+    import corrector as CR
+
+    fine_n, coarse_n, ratio = 1024, 256, 8
+    dt_f = CR.fine_dt(fine_n, IC_SEED, K0)
+    fine = nsgb.Gpu(fine_n, fine_n, 2 * math.pi, 2 * math.pi, nsgb.FP32)
+    plain = nsgb.Gpu(coarse_n, coarse_n, 2 * math.pi, 2 * math.pi, nsgb.FP32)
+    learned = nsgb.Gpu(coarse_n, coarse_n, 2 * math.pi, 2 * math.pi, nsgb.FP32)
+    fine.set_params(**CR.params(fine_n, dt_f, forcing_seed=F_SEED))
+    for g in (plain, learned):
+        g.set_params(**CR.params(coarse_n, ratio * dt_f, forcing_seed=F_SEED, substeps=ratio))
+    fine.random_spectrum(IC_SEED, K0, E0)
+    fine.advance(2)
+    for g in (plain, learned):
+        fine.check(fine.lib.ns_gpu_filter_state(fine.h, g.h), "filter_state")
+    net = nsgb.Corrector(coarse_n, coarse_n, max_batch=batch, seed=1)
+    fine.advance(ratio)
+    plain.advance(1)
+    net.correct_step(learned, 1)
+    for g in (fine, plain, learned):
+        g.sync()
+
+    def wall(fn):
+        t0 = time.perf_counter()
+        fn()
+        return time.perf_counter() - t0
+
+    t_fine = wall(lambda: (fine.advance(ratio * steps), fine.sync()))
+    t_plain = wall(lambda: (plain.advance(steps), plain.sync()))
+    t_learned = wall(lambda: (net.correct_step(learned, steps), learned.sync()))
+    ms_tc = net.time_hidden_layer(batch, 10)
+    net.set_tensor_cores(False)
+    ms_simt = net.time_hidden_layer(batch, 2)
+    net.set_tensor_cores(True)
+    flops = 2.0 * batch * coarse_n * coarse_n * 64 * 576
+    tflops = flops / (ms_tc * 1e-3) / 1e12
+    peak = None
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak = float(json.load(f)["bf16_tflops"])
+        peak_src = "measured"
+    except (OSError, KeyError, ValueError):
+        peak, peak_src = 1900.0, "fallback"
+    for x in (fine, plain, learned):
+        x.close()
+    net.close()
+    return {"workload": "learned-corrected 256^2 step (plain RK4 + CNN) vs 8 steps of 1024^2 (config-2 physics, "
+                        "matched forcing)", "steps": steps,
+            "ms_per_coarse_step": {"fine_1024_x8": t_fine / steps * 1e3, "plain_256": t_plain / steps * 1e3,
+                                   "learned_256": t_learned / steps * 1e3},
+            "wall_ratio_fine_over_learned": t_fine / t_learned,
+            "tensor_roofline": {"kernel": "k_conv_tc (64->64 3x3, tcgen05 BF16 -> FP32 TMEM)", "bound": "tensor",
+                                "batch": batch, "flops_per_launch": flops, "mean_launch_ms": ms_tc,
+                                "achieved": tflops, "peak": peak, "unit": "TFLOP/s", "frac": tflops / peak,
+                                "peak_source": peak_src},
+            "simt_same_layer_ms": ms_simt,
+            "accuracy": "profiles/corrector_config4.md (trained by navier-stokes-solvers_gb300/corrector.py)"}
+
+
+def config5_leg(steps: int = 10) -> dict:
+    """4096^2 forced run (FP32 bulk, p=4 hyperviscosity, CFL 0.4) on the generic
+    stage kernels, with the energy spectrum of the device state."""
+    import nsgb
+
+    n = 4096
+    g = nsgb.Gpu(n, n, 2 * math.pi, 2 * math.pi, nsgb.FP32)
+    kmax = math.hypot(n / 2, n / 2)
+    dt_ref = 0.4 * (2 * math.pi / n) / 3.0
+    c8 = kmax ** 8 / ((2.0 / 3.0 * kmax) ** 8 * dt_ref)
+    g.set_params(Re=RE, cfl_factor=0.4, adaptive_dt=1, dt=1e-4, hv_enabled=1, hv_coefficient=c8, hv_order=8,
+                 hv_cutoff_ratio=0.0, forcing_enabled=1, forcing_kmin=F_KMIN, forcing_kmax=F_KMAX,
+                 forcing_epsilon=F_EPS, forcing_seed=F_SEED)
+    g.random_spectrum(IC_SEED, K0, E0)
+    g.advance(3)
+    import ctypes as C
+
+    total = C.c_double()
+    g.check(g.lib.ns_gpu_advance_timed(g.h, steps, C.c_size_t(0), C.byref(total), None), "advance_timed")
+    t0 = time.perf_counter()
+    es, em, ct = g.energy_spectrum()
+    t_spec = time.perf_counter() - t0
+    d = g.diagnostics()
+    g.close()
+    return {"workload": "forced 4096^2, FP32, RK4, hyperviscosity p=4 (order 8), CFL 0.4, generic stage kernels",
+            "value": n * n * steps / (total.value * 1e-3), "unit": UNIT, "ms_per_step": total.value / steps,
+            "spectrum_ms": t_spec * 1e3, "spectrum_bins": int(len(es)), "energy": d["energy"],
+            "l2": "working set above L2; no flush"}
+
+
 # ------------------------------------------------------------ CPU legs
 def cpu_sample(n: int, budget_s: float, max_steps: int):
     """Time the oracle restatement (FP64, OpenMP) on the workload for up to budget_s."""
@@ -332,6 +426,8 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--ensemble-steps", type=int, default=100, help="steps of the timed ensemble launch (0: skip)")
     ap.add_argument("--ensemble-only", action="store_true", help="run only the ensemble leg and print its JSON")
+    ap.add_argument("--no-extra", action="store_true", help="skip the corrector and 4096^2 legs")
+    ap.add_argument("--extra-only", action="store_true", help="run only the corrector and 4096^2 legs")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -354,6 +450,9 @@ def main():
 
     if args.ensemble_only:
         print(json.dumps(ensemble_leg(max(1, args.ensemble_steps))), flush=True)
+        return 0
+    if args.extra_only:
+        print(json.dumps({"corrector": corrector_leg(), "config5_4096": config5_leg()}), flush=True)
         return 0
 
     n = args.n
@@ -451,6 +550,8 @@ def main():
     ens = None
     if args.ensemble_steps > 0 and not args.kernels_only:
         ens = ensemble_leg(args.ensemble_steps)
+    corr = corrector_leg() if not args.no_extra else None
+    c5 = config5_leg() if not args.no_extra else None
 
     cpu = None
     if not args.no_cpu and rank == 0 and ws == 1:
@@ -464,6 +565,8 @@ def main():
         "gpu_launches": launches, "wall_s_timed_region": t_wall,
         "fp32_vs_fp64": fp32_cmp,
         "ensemble": ens,
+        "corrector": corr,
+        "config5_4096": c5,
         "diagnostics": {"energy": diag["energy"], "enstrophy": diag["enstrophy"], "t": diag["t"], "dt": diag["dt"]},
     }
     if rank == 0:

@@ -344,6 +344,9 @@ int ns_cnn_train(ns_cnn *c, int iterations, int batch, float lr, float weight_de
  * weights, FP32 accumulation in tensor memory) when W is a multiple of 128 (the
  * default there); 0 selects the FP32 SIMT kernels for every layer. */
 int ns_cnn_set_tensor_cores(ns_cnn *c, int enable);
+/* Mean CUDA-event time of one 64 -> 64 hidden layer (the network's dominant
+ * kernel) on batch samples, over reps launches after one untimed launch. */
+int ns_cnn_time_hidden_layer(ns_cnn *c, int batch, int reps, double *ms_per_launch);
 /* nsteps corrected steps of an instance on the network's grid: plain RK4 step
  * (ns_gpu_advance), then omega += CNN(omega(t), omega(t+dt) - omega(t)) */
 int ns_cnn_correct_step(ns_cnn *c, ns_gpu *g, int nsteps);

@@ -28,7 +28,9 @@
 #include <string>
 #include <vector>
 
+#define NSG_NO_AUX_KERNELS
 #include "ns_gpu.h"
+#include "ns_gpu_impl.h"
 
 namespace {
 
@@ -173,8 +175,9 @@ __device__ __forceinline__ void tc_ld32(unsigned taddr, float (&v)[32]) {
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// in: BF16 activations [B][H][W][64]; w: BF16 weights [9][64 ci][64 co];
-// outputs (each may be null): pre FP32, actf FP32, actb BF16, all [B][H][W][64]
+// in: BF16 activations [B][H][W][64]; w: BF16 weights [9][64 ci][64 co]; bias
+// may be null; outputs (each may be null): pre FP32, actf FP32, actb BF16, all
+// [B][H][W][64]
 template <bool GELU>
 __global__ void __launch_bounds__(128, 1) k_conv_tc(const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ w,
                                                     const float* __restrict__ bias, float* __restrict__ pre,
@@ -254,7 +257,7 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __nv_bfloat16* __restr
 #pragma unroll
                 for (int k = 0; k < 32; ++k) {
                     const int co = half * 32 + k;
-                    const float pv = v[k] + bias[co];
+                    const float pv = bias ? v[k] + bias[co] : v[k];
                     const float av = GELU ? gelu(pv) : pv;
                     if (pre) pre[o + co] = pv;
                     if (actf) actf[o + co] = av;
@@ -535,13 +538,13 @@ static int conv_dw(ns_cnn* c, cudaStream_t st, const float* in, const float* dpr
         if (_s != NS_GPU_OK) return _s; \
     } while (0)
 
-static int conv_tc(ns_cnn* c, cudaStream_t st, int l, const __nv_bfloat16* in, float* pre, float* actf, __nv_bfloat16* actb,
-                   int B) {
-    auto k = k_conv_tc<true>;
+template <bool GELU>
+static int conv_tc(ns_cnn* c, cudaStream_t st, const __nv_bfloat16* in, const __nv_bfloat16* w, const float* bias, float* pre,
+                   float* actf, __nv_bfloat16* actb, int B) {
+    auto k = k_conv_tc<GELU>;
     CNN_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
     const int tiles = B * c->H * (c->W / TC_W);
-    k<<<grid_of(tiles, 1, c->num_sms), 128, TC_SMEM, st>>>(in, c->wb[l], c->p + c->boff[l], pre, actf, actb, B, c->H, c->W,
-                                                           c->derr);
+    k<<<grid_of(tiles, 1, c->num_sms), 128, TC_SMEM, st>>>(in, w, bias, pre, actf, actb, B, c->H, c->W, c->derr);
     CNN_LAUNCHED(c);
     return NS_GPU_OK;
 }
@@ -561,8 +564,8 @@ static int forward(ns_cnn* c, cudaStream_t st, int B, bool training = true) {
         __nv_bfloat16* aout = c->ab1;
         for (int l = 1; l < NL - 1; ++l) {
             const bool last = (l == NL - 2);
-            CNN_TRY(conv_tc(c, st, l, ain, training ? c->pre[l] : nullptr, (training || last) ? c->act[l] : nullptr,
-                            last ? nullptr : aout, B));
+            CNN_TRY(conv_tc<true>(c, st, ain, c->wb[l], c->p + c->boff[l], training ? c->pre[l] : nullptr,
+                                  (training || last) ? c->act[l] : nullptr, last ? nullptr : aout, B));
             __nv_bfloat16* t = ain;
             ain = aout;
             aout = t;
@@ -605,7 +608,16 @@ static int loss_and_backward(ns_cnn* c, cudaStream_t st, int B, int slot) {
         CNN_LAUNCHED(c);
         if (l > 0) {
             CNN_TRY((conv_dw<HID, HID>(c, st, c->act[l - 1], dcur, c->gp + c->woff[l], B)));
-            CNN_TRY((conv<HID, HID, 32, false>(c, st, dcur, c->wbt[l], nullptr, dnext, nullptr, B)));
+            if (c->tc) {
+                // input gradient on the tensor cores: BF16 output gradient, flipped
+                // and transposed BF16 weights, FP32 result
+                const long long n = npix * HID;
+                k_to_bf16<<<grid_of(n, 256, 8 * c->num_sms), 256, 0, st>>>(dcur, c->ab0, n);
+                CNN_LAUNCHED(c);
+                CNN_TRY(conv_tc<false>(c, st, c->ab0, c->wbt[l], nullptr, nullptr, dnext, nullptr, B));
+            } else {
+                CNN_TRY((conv<HID, HID, 32, false>(c, st, dcur, c->wbt[l], nullptr, dnext, nullptr, B)));
+            }
             float* t = dcur;
             dcur = dnext;
             dnext = t;
@@ -893,22 +905,25 @@ int ns_cnn_train(ns_cnn* c, int iterations, int batch, float lr, float weight_de
 
 // One corrected coarse step of a FP32 instance whose grid matches the network:
 // w0 = omega(t); plain RK4 step; w1 = omega(t + dt); omega += CNN(w0, w1 - w0).
+// Everything runs on the instance's stream, with no host synchronisation
+// between steps.
 int ns_cnn_correct_step(ns_cnn* c, ns_gpu* g, int nsteps) {
     if (!c || !g || nsteps < 0) return NS_GPU_ERR_INVALID;
+    if (g->g.nx != c->W || g->g.ny != c->H) CNN_FAIL(c, NS_GPU_ERR_INVALID, "correct_step: grid differs from the network's");
     const long long hw = (long long)c->H * c->W;
+    cudaStream_t st = g->st;
     for (int s = 0; s < nsteps; ++s) {
         CNN_TRY(ns_gpu_vorticity_device(g, c->cw0));
         CNN_TRY(ns_gpu_advance(g, 1));
         CNN_TRY(ns_gpu_vorticity_device(g, c->cw1));
-        CNN_TRY(ns_gpu_synchronize(g));  // the network runs on its own stream
-        k_make_input<<<grid_of(hw, 256, 1024), 256, 0, c->st>>>(c->cw0, c->cw1, hw, c->s0, c->s1, c->x0);
+        k_make_input<<<grid_of(hw, 256, 1024), 256, 0, st>>>(c->cw0, c->cw1, hw, c->s0, c->s1, c->x0);
         CNN_LAUNCHED(c);
-        CNN_TRY(forward(c, c->st, 1, false));
-        k_scale<<<grid_of(hw, 256, 1024), 256, 0, c->st>>>(c->pre[NL - 1], hw, 1.0f / c->so);
+        CNN_TRY(forward(c, st, 1, false));
+        k_scale<<<grid_of(hw, 256, 1024), 256, 0, st>>>(c->pre[NL - 1], hw, 1.0f / c->so);
         CNN_LAUNCHED(c);
-        CNN_CUDA(c, cudaStreamSynchronize(c->st));
         CNN_TRY(ns_gpu_add_vorticity_device(g, c->pre[NL - 1]));
     }
+    CNN_CUDA(c, cudaStreamSynchronize(st));
     return check_tc(c);
 }
 
@@ -917,6 +932,40 @@ int ns_cnn_set_tensor_cores(ns_cnn* c, int enable) {
     if (enable && (c->W % TC_W != 0 || !c->ab0)) CNN_FAIL(c, NS_GPU_ERR_INVALID, "tensor cores need W %% %d == 0", TC_W);
     c->tc = enable ? 1 : 0;
     return NS_GPU_OK;
+}
+
+// Mean time of one 64 -> 64 hidden layer (the network's dominant kernel:
+// tcgen05 when tensor cores are on, else the SIMT kernel) over reps launches
+// on a batch of `batch` samples of the current activations, timed with CUDA
+// events on the network's stream after one untimed launch.
+int ns_cnn_time_hidden_layer(ns_cnn* c, int batch, int reps, double* ms_per_launch) {
+    if (!c || batch < 1 || batch > c->maxB || reps < 1 || !ms_per_launch) return NS_GPU_ERR_INVALID;
+    cudaStream_t st = c->st;
+    const long long n = (long long)batch * c->H * c->W * HID;
+    CNN_CUDA(c, cudaMemsetAsync(c->act[0], 0, (size_t)n * sizeof(float), st));
+    if (c->tc) {
+        k_to_bf16<<<grid_of(n, 256, 8 * c->num_sms), 256, 0, st>>>(c->act[0], c->ab0, n);
+        CNN_LAUNCHED(c);
+    }
+    cudaEvent_t a, b;
+    CNN_CUDA(c, cudaEventCreate(&a));
+    CNN_CUDA(c, cudaEventCreate(&b));
+    int s = NS_GPU_OK;
+    for (int r = 0; r <= reps && s == NS_GPU_OK; ++r) {
+        if (r == 1) cudaEventRecord(a, st);
+        if (c->tc) s = conv_tc<true>(c, st, c->ab0, c->wb[1], c->p + c->boff[1], c->pre[1], c->act[1], c->ab1, batch);
+        else s = conv<HID, HID, 32, true>(c, st, c->act[0], c->wb[1], c->p + c->boff[1], c->pre[1], c->act[1], batch);
+    }
+    cudaEventRecord(b, st);
+    const cudaError_t e = cudaEventSynchronize(b);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (s != NS_GPU_OK) return s;
+    if (e != cudaSuccess) CNN_FAIL(c, NS_GPU_ERR_CUDA, "time_hidden_layer: %s", cudaGetErrorString(e));
+    *ms_per_launch = ms / reps;
+    return check_tc(c);
 }
 
 }  // extern "C"

@@ -184,6 +184,7 @@ def load(build: bool = True) -> C.CDLL:
     proto("ns_cnn_train", C.c_int, vp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_uint64, _DP)
     proto("ns_cnn_correct_step", C.c_int, vp, vp, C.c_int)
     proto("ns_cnn_set_tensor_cores", C.c_int, vp, C.c_int)
+    proto("ns_cnn_time_hidden_layer", C.c_int, vp, C.c_int, C.c_int, _DP)
     ecp = C.POINTER(EnsembleConfig)
     proto("ns_gpu_create_for_ensemble", C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, ecp, C.POINTER(vp))
     proto("ns_gpu_ensemble_create", C.c_int, C.c_int, C.POINTER(C.c_int), C.c_double, ecp, C.POINTER(vp))
@@ -556,6 +557,11 @@ class Corrector:
         hist = np.zeros(iterations)
         self.check(self.lib.ns_cnn_train(self.h, iterations, batch, lr, weight_decay, seed, _ptr(hist)), "train")
         return hist
+
+    def time_hidden_layer(self, batch: int, reps: int = 10) -> float:
+        ms = C.c_double()
+        self.check(self.lib.ns_cnn_time_hidden_layer(self.h, batch, reps, C.byref(ms)), "time_hidden_layer")
+        return ms.value
 
     def set_tensor_cores(self, enable: bool):
         self.check(self.lib.ns_cnn_set_tensor_cores(self.h, 1 if enable else 0), "set_tensor_cores")

@@ -121,3 +121,29 @@ def test_tensor_core_training_reduces_the_loss(nsgb):
     hist = net.train(200, 8, 2e-3, 1e-4, seed=9)
     assert np.isfinite(hist).all() and hist[-20:].mean() < 0.2 * hist[:5].mean(), (hist[:5], hist[-20:])
     net.close()
+
+
+@pytest.mark.gpu
+def test_tensor_core_gradients_track_the_oracle(nsgb):
+    """W = 128 with tensor cores: forward and input-gradient convolutions use BF16
+    activations and output gradients, so each layer's gradient stays within a few
+    per cent of the FP64 oracle; the SIMT path on the same batch stays at FP32 rounding."""
+    H, W, B = 8, 128, 2
+    net = nsgb.Corrector(H, W, max_batch=2, seed=6)
+    p = rand_params(31).astype(np.float32)
+    net.set_params(p)
+    rng = np.random.default_rng(17)
+    x = rng.standard_normal((B, 2, H, W)).astype(np.float32)
+    t = (0.2 * rng.standard_normal((B, H, W))).astype(np.float32)
+    lo, go = CO.loss_and_grads(p.astype(np.float64), x.astype(np.float64), t.astype(np.float64))
+    for tc, tol in ((True, 3e-2), (False, 2e-4)):
+        net.set_tensor_cores(tc)
+        loss, g = net.loss_and_grads(x, t)
+        assert abs(loss - lo) <= (1e-2 if tc else 1e-5) * lo
+        off = 0
+        for ci, co in CO.CHANNELS:
+            n = 9 * ci * co
+            a, b = g[off:off + n].astype(np.float64), go[off:off + n]
+            assert np.linalg.norm(a - b) / np.linalg.norm(b) <= tol, (tc, ci, co)
+            off += n + co
+    net.close()
