@@ -119,9 +119,11 @@ __global__ void __launch_bounds__(TP*(COUT / CPT)) k_conv3x3(const float* __rest
 constexpr int TC_W = 128;                                  // pixels per tile
 constexpr int TC_HP = TC_W + 2;                            // halo pixels per row
 constexpr int TC_WB_BYTES = 9 * 8 * 64 * 16;               // 73,728
-constexpr int TC_HX_BYTES = 3 * 8 * TC_HP * 16;            // 49,920
-constexpr int TC_SMEM = TC_WB_BYTES + TC_HX_BYTES + 64;    // + mbarrier and tmem address
+constexpr int TC_HX_BYTES = 3 * 8 * TC_HP * 16;            // 49,920 per halo buffer
+constexpr int TC_ST = 65;                                  // staged output row pitch (floats)
+constexpr int TC_SMEM = TC_WB_BYTES + 2 * TC_HX_BYTES + 64;  // + mbarrier and tmem address
 constexpr long long TC_WAIT_CYCLES = 4000000000LL;         // about 2 s
+static_assert(TC_W * TC_ST * 4 <= TC_HX_BYTES, "output staging must fit in a halo buffer");
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -175,9 +177,44 @@ __device__ __forceinline__ void tc_ld32(unsigned taddr, float (&v)[32]) {
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// halo of tile `tile` into buffer at shared address hx (cp.async, 16-byte chunks)
+__device__ __forceinline__ void tc_load_halo(const __nv_bfloat16* __restrict__ in, unsigned hx, int tile, int H, int W,
+                                             int ntx, int tid) {
+    const int b = tile / (H * ntx), r = tile - b * H * ntx;
+    const int y = r / ntx, x0 = (r - y * ntx) * TC_W;
+    for (int i = tid; i < 3 * TC_HP * 8; i += 128) {
+        const int row = i / (TC_HP * 8), q = i - row * TC_HP * 8;
+        const int px = q >> 3, kc = q & 7;
+        const int gy = wrapi(y + row - 1, H), gx = wrapi(x0 + px - 1, W);
+        const __nv_bfloat16* src = in + (((size_t)b * H + gy) * W + gx) * 64 + kc * 8;
+        const unsigned dst = hx + (unsigned)(((row * 8 + kc) * TC_HP + px) * 16);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+// 36 MMAs of one tile from halo buffer hx into the accumulator, committed to mbar (one thread)
+__device__ __forceinline__ void tc_issue(unsigned taddr, unsigned hx, unsigned wbs, unsigned mb) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll 1
+    for (int tap = 0; tap < 9; ++tap) {
+        const int dy = tap / 3, dx = tap - 3 * dy;
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+            const unsigned a = hx + (unsigned)(((dy * 8 + 2 * s) * TC_HP + dx) * 16);
+            const unsigned bb = wbs + (unsigned)((tap * 8 + 2 * s) * 64 * 16);
+            tc_mma(taddr, umma_desc(a, TC_HP * 16, 128), umma_desc(bb, 64 * 16, 128), (tap | s) ? 1u : 0u);
+        }
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb) : "memory");
+}
+
 // in: BF16 activations [B][H][W][64]; w: BF16 weights [9][64 ci][64 co]; bias
 // may be null; outputs (each may be null): pre FP32, actf FP32, actb BF16, all
-// [B][H][W][64]
+// [B][H][W][64].  Two halo buffers: the next tile's halo loads while the
+// current tile's MMAs and epilogue run; the epilogue stages the accumulator
+// through the current tile's (consumed) halo buffer so that every output of a
+// tile leaves as one contiguous, coalesced block.
 template <bool GELU>
 __global__ void __launch_bounds__(128, 1) k_conv_tc(const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ w,
                                                     const float* __restrict__ bias, float* __restrict__ pre,
@@ -185,10 +222,12 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __nv_bfloat16* __restr
                                                     int W, int* __restrict__ err) {
     extern __shared__ __align__(128) unsigned char tsm[];
     unsigned char* WB = tsm;                            // [9][8][64][8] bf16
-    unsigned char* HX = tsm + TC_WB_BYTES;              // [3][8][130][8] bf16
-    unsigned long long* mbar = reinterpret_cast<unsigned long long*>(tsm + TC_WB_BYTES + TC_HX_BYTES);
-    unsigned* tslot = reinterpret_cast<unsigned*>(tsm + TC_WB_BYTES + TC_HX_BYTES + 16);
+    unsigned char* HXB = tsm + TC_WB_BYTES;             // 2 x [3][8][130][8] bf16
+    unsigned long long* mbar = reinterpret_cast<unsigned long long*>(tsm + TC_WB_BYTES + 2 * TC_HX_BYTES);
+    unsigned* tslot = reinterpret_cast<unsigned*>(tsm + TC_WB_BYTES + 2 * TC_HX_BYTES + 16);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int ntx = W / TC_W;
+    const int ntiles = B * H * ntx;
 
     // weights into the B-operand layout: WB[tap][kc][co][j] = w[tap][8 kc + j][co]
     for (int i = tid; i < 9 * 64 * 64; i += 128) {
@@ -203,73 +242,64 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __nv_bfloat16* __restr
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    const unsigned hxb = smem_u32(HXB), wbs = smem_u32(WB), mb = smem_u32(mbar);
+    int tile = blockIdx.x;
+    if (tile < ntiles) tc_load_halo(in, hxb, tile, H, W, ntx, tid);
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic-proxy writes -> tensor-core reads
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const unsigned taddr = *tslot;
-    const unsigned mb = smem_u32(mbar);
-    const unsigned hx = smem_u32(HX), wbs = smem_u32(WB);
-    const int ntx = W / TC_W;
-    const int ntiles = B * H * ntx;
+    if (tile < ntiles && tid == 0) tc_issue(taddr, hxb, wbs, mb);
     unsigned phase = 0;
-    bool ok = true;
-    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        const int b = tile / (H * ntx), r = tile - b * H * ntx;
-        const int y = r / ntx, x0 = (r - y * ntx) * TC_W;
-        // halo: HX[row][kc][px][8] = in[b][y + row - 1][x0 + px - 1][8 kc .. 8 kc + 7]
-        for (int i = tid; i < 3 * TC_HP * 8; i += 128) {
-            const int row = i / (TC_HP * 8), q = i - row * TC_HP * 8;
-            const int px = q >> 3, kc = q & 7;
-            const int gy = wrapi(y + row - 1, H), gx = wrapi(x0 + px - 1, W);
-            const __nv_bfloat16* src = in + (((size_t)b * H + gy) * W + gx) * 64 + kc * 8;
-            const unsigned dst = hx + (unsigned)(((row * 8 + kc) * TC_HP + px) * 16);
-            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-        }
-        asm volatile("cp.async.wait_all;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic-proxy writes -> tensor-core reads
-        __syncthreads();
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll 1
-            for (int tap = 0; tap < 9; ++tap) {
-                const int dy = tap / 3, dx = tap - 3 * dy;
-#pragma unroll
-                for (int s = 0; s < 4; ++s) {
-                    const unsigned a = hx + (unsigned)(((dy * 8 + 2 * s) * TC_HP + dx) * 16);
-                    const unsigned bb = wbs + (unsigned)((tap * 8 + 2 * s) * 64 * 16);
-                    tc_mma(taddr, umma_desc(a, TC_HP * 16, 128), umma_desc(bb, 64 * 16, 128), (tap | s) ? 1u : 0u);
-                }
-            }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb) : "memory");
-        }
+    int buf = 0;
+    for (; tile < ntiles; tile += gridDim.x, buf ^= 1) {
+        const int next = tile + gridDim.x;
+        const unsigned hx_next = hxb + (unsigned)((buf ^ 1) * TC_HX_BYTES);
+        if (next < ntiles) tc_load_halo(in, hx_next, next, H, W, ntx, tid);  // overlaps this tile's MMAs and epilogue
         // every thread must take the same branch (barriers follow): the tile
         // succeeds only if every thread saw the MMAs complete in time
-        ok = __syncthreads_and(mbar_wait(mb, phase) ? 1 : 0) != 0;
+        const bool ok = __syncthreads_and(mbar_wait(mb, phase) ? 1 : 0) != 0;
         phase ^= 1u;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        if (ok) {
-            const int px = x0 + warp * 32 + lane;
-            const size_t o = (((size_t)b * H + y) * W + px) * 64;
+        if (!ok) {
+            if (tid == 0) atomicExch(err, 1);
+            break;
+        }
+        // epilogue: accumulator row of this thread = pixel warp*32 + lane of the tile
+        const int b = tile / (H * ntx), r = tile - b * H * ntx;
+        const int y = r / ntx, x0 = (r - y * ntx) * TC_W;
+        const size_t obase = (((size_t)b * H + y) * W + x0) * 64;  // the tile's 128 x 64 outputs are contiguous
+        float* stg = reinterpret_cast<float*>(HXB + buf * TC_HX_BYTES);  // this tile's halo is consumed
+        const int prow = warp * 32 + lane;
 #pragma unroll
-            for (int half = 0; half < 2; ++half) {
-                float v[32];
-                tc_ld32(taddr + ((unsigned)(warp * 32) << 16) + (unsigned)(half * 32), v);
+        for (int half = 0; half < 2; ++half) {
+            float v[32];
+            tc_ld32(taddr + ((unsigned)(warp * 32) << 16) + (unsigned)(half * 32), v);
 #pragma unroll
-                for (int k = 0; k < 32; ++k) {
-                    const int co = half * 32 + k;
-                    const float pv = bias ? v[k] + bias[co] : v[k];
-                    const float av = GELU ? gelu(pv) : pv;
-                    if (pre) pre[o + co] = pv;
-                    if (actf) actf[o + co] = av;
-                    if (actb) actb[o + co] = __float2bfloat16_rn(av);
-                }
+            for (int k = 0; k < 32; ++k) {
+                const int co = half * 32 + k;
+                stg[prow * TC_ST + co] = bias ? v[k] + bias[co] : v[k];
             }
-        } else if (tid == 0) {
-            atomicExch(err, 1);
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();  // accumulator read and halo consumed before the next tile
+        __syncthreads();  // staged; the accumulator may be overwritten
+        for (int i = tid; i < TC_W * 64; i += 128) {
+            const float pv = stg[(i >> 6) * TC_ST + (i & 63)];
+            const float av = GELU ? gelu(pv) : pv;
+            if (pre) pre[obase + i] = pv;
+            if (actf) actf[obase + i] = av;
+            if (actb) actb[obase + i] = __float2bfloat16_rn(av);
+        }
+        // the next tile's halo must have landed before its MMAs start
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();  // staging read done (the buffer takes a halo again), next halo visible
+        if (next < ntiles && tid == 0) tc_issue(taddr, hx_next, wbs, mb);
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(taddr));
 }

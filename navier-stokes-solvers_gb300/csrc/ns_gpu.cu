@@ -466,14 +466,19 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
     // column over the group's consecutive rows.
     G.fLB = (g->fast_row || g->fast_col) ? G.logny : 0;
     G.fTG = G.fLB ? 1 : 0;
-    g->ER = (kc && kc->er) ? kc->er : (G.H >= 16 ? 16 : 4);
-    g->EC = (kc && kc->ec) ? kc->ec : (ny >= 16 ? 16 : 4);
+    // automatic tiling: 16 values per thread from 512-point transforms up (a
+    // row or column keeps at least 32 threads), 4 values per thread below, so
+    // that small grids still fill warps and spread over the SMs
+    g->ER = (kc && kc->er) ? kc->er : (G.H >= 512 ? 16 : 4);
+    g->EC = (kc && kc->ec) ? kc->ec : (ny >= 512 ? 16 : 4);
     const size_t cs = (precision == NS_GPU_FP64) ? sizeof(double2) : sizeof(float2);
     // column tile width: up to 16 columns, <= 512 threads, <= ~100 KB shared memory
     {
         const int TC = ny / g->EC;
         int CW = 1;
-        while (CW < 16 && 2 * CW * TC <= 512 && (size_t)2 * CW * spad_len(ny) * cs <= 100 * 1024 && CW < G.Kx) CW *= 2;
+        while (CW < 16 && 2 * CW * TC <= 512 && (size_t)2 * CW * spad_len(ny) * cs <= 100 * 1024 && CW < G.Kx &&
+               G.Kx / (2 * CW) >= g->num_sms)
+            CW *= 2;
         if (kc && kc->cw) CW = kc->cw;
         G.CW = CW;
         int al = CW;
@@ -484,7 +489,9 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
     {
         const int TT = G.H / g->ER;
         int RPC = 1;
-        while (2 * RPC * TT <= 128 && 2 * RPC <= ny && (size_t)4 * 2 * RPC * spad_len(G.H) * cs <= 100 * 1024) RPC *= 2;
+        while (2 * RPC * TT <= 128 && 2 * RPC <= ny && (size_t)4 * 2 * RPC * spad_len(G.H) * cs <= 100 * 1024 &&
+               ny / (2 * RPC) >= g->num_sms)
+            RPC *= 2;
         if (kc && kc->rpc) RPC = kc->rpc;
         G.RPC = RPC;
     }
