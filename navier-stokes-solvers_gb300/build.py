@@ -21,6 +21,7 @@ ROOT = os.path.dirname(PKG)
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libns_gb300.so")
+RUNNER = os.path.join(PKG, "ns_run")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE]
@@ -31,7 +32,7 @@ def _sources():
     cu = sorted(glob.glob(os.path.join(PKG, "csrc", "*.cu")))
     c = sorted(glob.glob(os.path.join(PKG, "host", "*.c")))
     deps = (cu + c + glob.glob(os.path.join(PKG, "csrc", "*.cuh")) + glob.glob(os.path.join(PKG, "csrc", "*.h"))
-            + glob.glob(os.path.join(INCLUDE, "*.h")))
+            + glob.glob(os.path.join(PKG, "host", "*.h")) + glob.glob(os.path.join(INCLUDE, "*.h")))
     return cu, c, deps
 
 
@@ -49,9 +50,18 @@ def _run(cmd):
     return r
 
 
+def build_runner(force: bool = False) -> str:
+    """The config-driven runner (driver/ns_run.c), linked against the library."""
+    src = os.path.join(PKG, "driver", "ns_run.c")
+    if force or _stale(RUNNER, [src, LIB] + glob.glob(os.path.join(INCLUDE, "*.h"))):
+        _run(["gcc"] + CFLAGS + [src, "-L", PKG, "-lns_gb300", "-Wl,-rpath,$ORIGIN", "-lm", "-o", RUNNER])
+    return RUNNER
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     cu, c, deps = _sources()
     if not force and not _stale(LIB, deps + [__file__]):
+        build_runner()
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     jobs = []
@@ -69,6 +79,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
             if verbose and (r.stdout or r.stderr):
                 print(r.stdout + r.stderr, file=sys.stderr)
     _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lm"])
+    build_runner(force=True)
     return LIB
 
 
