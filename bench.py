@@ -547,11 +547,14 @@ def main():
                "path": "ns_spectral_compute_cfl_timestep + ns_spectral_advance_rk4 per step (FP32 instance)"}
         s.close()
 
-    ens = None
-    if args.ensemble_steps > 0 and not args.kernels_only:
-        ens = ensemble_leg(args.ensemble_steps)
-    corr = corrector_leg() if not args.no_extra else None
-    c5 = config5_leg() if not args.no_extra else None
+    # the secondary workloads run once, on rank 0 (replicas add nothing to them)
+    ens = corr = c5 = None
+    if rank == 0:
+        if args.ensemble_steps > 0:
+            ens = ensemble_leg(args.ensemble_steps)
+        if not args.no_extra:
+            corr = corrector_leg()
+            c5 = config5_leg()
 
     cpu = None
     if not args.no_cpu and rank == 0 and ws == 1:
