@@ -36,13 +36,16 @@ def hv_coefficient(n: int, cfl: float = 0.5) -> float:
 
 
 def params(n: int, dt: float, Re: float = 1e5, forcing_seed: int | None = None, epsilon: float = 1e-3,
-           substeps: int = 1) -> dict:
+           substeps: int = 1, hv_order: int = 4) -> dict:
     """Config-2 physics on an n^2 grid with a fixed dt.  With forcing, a coarse
     instance takes `substeps` forcing draws per step: the forcing noise is keyed
     by the physical mode and the fine step, so a coarse step of `substeps` fine
     steps receives the fine run's forcing exactly (ns_gpu_params.forcing_substeps)."""
-    p = dict(Re=Re, cfl_factor=0.5, adaptive_dt=0, dt=dt, hv_enabled=1, hv_coefficient=hv_coefficient(n),
-             hv_order=4, hv_cutoff_ratio=0.0)
+    kmax = math.hypot(n / 2, n / 2)
+    dt_ref = 0.5 * (2 * math.pi / n) / 3.0
+    c = kmax ** hv_order / ((2.0 / 3.0 * kmax) ** hv_order * dt_ref)  # damping O(1) per step at 2/3 kmax
+    p = dict(Re=Re, cfl_factor=0.5, adaptive_dt=0, dt=dt, hv_enabled=1, hv_coefficient=c, hv_order=hv_order,
+             hv_cutoff_ratio=0.0)
     if forcing_seed is not None:
         p.update(forcing_enabled=1, forcing_kmin=4.0, forcing_kmax=6.0, forcing_epsilon=epsilon,
                  forcing_seed=forcing_seed, forcing_substeps=substeps)
@@ -69,7 +72,7 @@ def fine_dt(fine_n: int, seed: int, k0: float, cfl: float = 0.4) -> float:
 
 
 def generate(seeds, fine_n=1024, coarse_n=256, ratio=8, spinup=200, snapshots=32, k0=8.0, dt_f=None,
-             forcing=False):
+             forcing=False, hv_order=4):
     """Samples (inputs [N][2][c][c], targets [N][c][c]) from seeded fine runs."""
     if dt_f is None:
         dt_f = fine_dt(fine_n, seeds[0], k0)
@@ -78,8 +81,8 @@ def generate(seeds, fine_n=1024, coarse_n=256, ratio=8, spinup=200, snapshots=32
     xs, ts = [], []
     for seed in seeds:
         fseed = (1000 + seed) if forcing else None
-        fine.set_params(**params(fine_n, dt_f, forcing_seed=fseed))
-        coarse.set_params(**params(coarse_n, ratio * dt_f, forcing_seed=fseed, substeps=ratio))
+        fine.set_params(**params(fine_n, dt_f, forcing_seed=fseed, hv_order=hv_order))
+        coarse.set_params(**params(coarse_n, ratio * dt_f, forcing_seed=fseed, substeps=ratio, hv_order=hv_order))
         fine.random_spectrum(seed, k0, 0.5)
         fine.advance(spinup)
         for _ in range(snapshots):
@@ -231,5 +234,108 @@ def main(argv=None):
     return 0
 
 
+
+
+def ensemble_spectrum_comparison(net: "nsgb.Corrector", fine_n: int, coarse_n: int, ratio: int, members: int,
+                                 fine_steps: int, spectrum_every: int, dt_f: float, k0: float = 8.0, seed: int = 0,
+                                 hv_order: int = 4, forcing: bool = True):
+    """Config-5 comparison: time-averaged energy spectrum of one fine run (spectrum
+    every `spectrum_every` fine steps) against that of an ensemble of `members`
+    learned-corrected coarse runs of the same statistics (own seeds, same forcing
+    parameters), and of the plain coarse ensemble; wall time of each."""
+    def prm(n, dt, fseed, sub):
+        return params(n, dt, forcing_seed=fseed if forcing else None, substeps=sub, hv_order=hv_order)
+
+    fine = nsgb.Gpu(fine_n, fine_n, L, L, nsgb.FP32)
+    fine.set_params(**prm(fine_n, dt_f, 5000 + seed, 1))
+    fine.random_spectrum(seed, k0, 0.5)
+    nb = coarse_n // 2
+    e_fine = np.zeros(nb)
+    t0 = time.perf_counter()
+    nspec = 0
+    for _ in range(fine_steps // spectrum_every):
+        fine.advance(spectrum_every)
+        e_fine += fine.energy_spectrum(nb)[1]
+        nspec += 1
+    fine.sync()
+    t_fine = time.perf_counter() - t0
+    e_fine /= max(nspec, 1)
+    fine.close()
+
+    coarse_steps = fine_steps // ratio
+    every_c = max(1, spectrum_every // ratio)
+    out = {}
+    for mode in ("plain", "learned"):
+        acc = np.zeros(nb)
+        cnt = 0
+        t_run = 0.0
+        g = nsgb.Gpu(coarse_n, coarse_n, L, L, nsgb.FP32)
+        for m in range(members):
+            g.set_params(**prm(coarse_n, ratio * dt_f, 7000 + m, ratio))
+            g.random_spectrum(100 + m, k0, 0.5)
+            g.sync()
+            t0 = time.perf_counter()
+            for _ in range(coarse_steps // every_c):
+                if mode == "plain":
+                    g.advance(every_c)
+                else:
+                    net.correct_step(g, every_c)
+                acc += g.energy_spectrum(nb)[1]
+                cnt += 1
+            g.sync()
+            t_run += time.perf_counter() - t0
+        g.close()
+        acc /= max(cnt, 1)
+        band = slice(1, coarse_n // 3)
+        err = float(np.mean(np.abs(np.log(np.maximum(acc[band], 1e-300) / np.maximum(e_fine[band], 1e-300)))))
+        out[mode] = {"log_spectrum_error": err, "wall_s": t_run, "spectrum": acc.tolist()}
+    return {"fine": {"n": fine_n, "steps": fine_steps, "wall_s": t_fine, "spectrum": e_fine.tolist()},
+            "coarse": {"n": coarse_n, "members": members, "steps_per_member": coarse_steps}, **out}
+
+
+def config5(argv=None):
+    """Train a fine -> coarse corrector (default 4096^2 -> 512^2) and compare the
+    time-averaged E(k) of the fine run with learned and plain coarse ensembles."""
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--fine", type=int, default=4096)
+    ap.add_argument("--coarse", type=int, default=512)
+    ap.add_argument("--ratio", type=int, default=8)
+    ap.add_argument("--train-seeds", type=int, default=8)
+    ap.add_argument("--snapshots", type=int, default=16)
+    ap.add_argument("--iters", type=int, default=1000)
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--members", type=int, default=64)
+    ap.add_argument("--fine-steps", type=int, default=10000)
+    ap.add_argument("--spectrum-every", type=int, default=100)
+    ap.add_argument("--hv-order", type=int, default=8, help="hyperviscosity order (p = 4 -> 8)")
+    a = ap.parse_args(argv)
+    t0 = time.time()
+    x, t, dt_f = generate(list(range(a.train_seeds)), a.fine, a.coarse, a.ratio, 200, a.snapshots, forcing=True,
+                          hv_order=a.hv_order)
+    t_gen = time.time() - t0
+    s0, s1, so = normalisation(x, t)
+    net = nsgb.Corrector(a.coarse, a.coarse, max_batch=a.batch, seed=1)
+    net.set_normalization(s0, s1, so)
+    net.set_dataset(x, t)
+    t0 = time.time()
+    hist = net.train(a.iters, a.batch, 1e-3, 1e-4, seed=11)
+    t_train = time.time() - t0
+    res = ensemble_spectrum_comparison(net, a.fine, a.coarse, a.ratio, a.members, a.fine_steps, a.spectrum_every,
+                                       dt_f, hv_order=a.hv_order)
+    net.close()
+    res["training"] = {"samples": int(x.shape[0]), "iters": a.iters, "batch": a.batch, "generate_s": t_gen,
+                       "train_s": t_train, "loss_first": float(hist[:10].mean()), "loss_last": float(hist[-50:].mean())}
+    res["dt_fine"] = dt_f
+    print(json.dumps(res))
+    return 0
+
+
 if __name__ == "__main__":
+    import sys
+
+    if len(sys.argv) > 1 and sys.argv[1] == "config5":
+        raise SystemExit(config5(sys.argv[2:]))
     raise SystemExit(main())
