@@ -165,6 +165,20 @@ template <typename T> static int stage_row(ns_gpu* g, int stage) {
     a.dx[0] = 1; a.dx[1] = 0; a.dx[2] = 1; a.dx[3] = 0;  // psi_x, psi_y, omega_x, omega_y
     a.cfl = (stage == 1 && g->p.adaptive_dt) ? 1 : 0;
     a.marker = (stage == 1) ? 1 : (stage == 2 ? 2 : 0);
+    if constexpr (sizeof(T) == 4 && NSG_ROW_TMEM) {
+        if (g->fast_row) {
+            // FP32: Jacobian operands in tensor memory, inboxes filled by cp.async
+            auto kern = k_row_t<NSG_RT_NW, NSG_RT_GW, NSG_RT_NB>;
+            const size_t smem = rt_smem_bytes<NSG_RT_NW, NSG_RT_NB>();
+            NSG_TRY(set_smem(g, kern, smem));
+            int grid = g->g.ny / NSG_RT_NW;
+            if (grid > g->num_sms) grid = g->num_sms;
+            const cudaError_t e = launch_stage(kern, grid, 32 * NSG_RT_NW, smem, g->st, g->g, a);
+            if (e != cudaSuccess) NSG_FAIL(g, NS_GPU_ERR_CUDA, "k_row_t launch: %s", cudaGetErrorString(e));
+            NSG_LAUNCHED(g);
+            return NS_GPU_OK;
+        }
+    }
     if (g->fast_row) {
         const size_t smem = rw_smem_bytes<T>();
         NSG_TRY(set_smem(g, k_row_w<T>, smem));

@@ -720,4 +720,351 @@ __global__ void __launch_bounds__(64 * cw_teams<T>(), 1) k_col_w(Geo g, ColArgs<
     if (STAGE == 4 && blockIdx.x == 0 && threadIdx.x == 0) a.ds->t = a.ds->t + dt;
 }
 
+// ============================================================ k_row_t
+// FP32 row pass at nx = 2048 with the Jacobian operands in tensor memory.
+// Same transforms and row ownership as k_row_w (groups of GW warps own GW
+// consecutive rows; every transform of a row stays inside its warp), with two
+// changes to where data waits:
+//  * the next field of the group's rows streams into per-warp inboxes with
+//    cp.async (no register staging), so its global latency overlaps the
+//    current field's transform whatever the register allocator does;
+//  * psi_x (then psi_x omega_y) and psi_y live in the warp's 128 columns of
+//    tensor memory (tcgen05.st / tcgen05.ld, 32x32b shape: lane = thread),
+//    which frees the 16 KB per row that they took in shared memory and moves
+//    their traffic off the shared-memory pipe.
+// NB inboxes per warp: 2 lets the copy of field q + 1 start as soon as field q
+// has landed (one group barrier per field); 1 waits until every warp of the
+// group has packed field q (two barriers per field).
+// dynamic smem (float2): tw [32][33] | twh [1024] | per warp: S [32][33], IN [NB][712]
+//                        | kx [704] float | tensor-memory address
+#define NSG_RT_IN 712
+#ifndef NSG_ROW_TMEM
+#define NSG_ROW_TMEM 1   // 0: the FP32 row pass runs k_row_w
+#endif
+#ifndef NSG_RT_NW
+#define NSG_RT_NW 8
+#endif
+#ifndef NSG_RT_GW
+#define NSG_RT_GW 8     // the whole CTA reads 8 consecutive rows: 64-byte runs per kx column
+#endif
+#ifndef NSG_RT_NB
+#define NSG_RT_NB 1
+#endif
+#ifndef NSG_RT_TWTM
+#define NSG_RT_TWTM 1   // per-lane twiddles of the transforms and the inverse pack in tensor memory
+#endif
+template <int NB> __host__ __device__ constexpr int rt_wstride() {
+    // 16-byte aligned blocks whose bases differ by 4 float2 modulo 16 between
+    // neighbouring warps (group-wide deposits and unpack reads hit distinct banks)
+    return ((1056 + NB * NSG_RT_IN + 15) / 16) * 16 + 4;
+}
+template <int NW, int NB> __host__ __device__ constexpr size_t rt_smem_bytes() {
+    return (size_t)(32 * 33 + 1024 + NW * rt_wstride<NB>()) * sizeof(float2) + (size_t)NSG_RW_KXMAX * sizeof(float) + 16;
+}
+template <int NW> __host__ __device__ constexpr unsigned rt_tmem_cols() {
+    // 128 columns per warp (warps w and w + 4 share lanes) + 128 twiddle columns
+    return 128 * ((NW + 3) / 4) + (NSG_RT_TWTM ? 128 : 0) <= 256 ? 256u : 512u;
+}
+
+__device__ __forceinline__ void tm_st16(unsigned ta, const float2 (&v)[32], int c) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16};" ::"r"(ta),
+        "f"(v[8 * c + 0].x), "f"(v[8 * c + 0].y), "f"(v[8 * c + 1].x), "f"(v[8 * c + 1].y), "f"(v[8 * c + 2].x), "f"(v[8 * c + 2].y),
+        "f"(v[8 * c + 3].x), "f"(v[8 * c + 3].y), "f"(v[8 * c + 4].x), "f"(v[8 * c + 4].y), "f"(v[8 * c + 5].x), "f"(v[8 * c + 5].y),
+        "f"(v[8 * c + 6].x), "f"(v[8 * c + 6].y), "f"(v[8 * c + 7].x), "f"(v[8 * c + 7].y)
+        : "memory");
+}
+__device__ __forceinline__ void tm_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+// issue a 16-column load (8 complex) into r without waiting
+__device__ __forceinline__ void tm_ld16_issue(unsigned ta, float (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+        : "=f"(r[0]), "=f"(r[1]), "=f"(r[2]), "=f"(r[3]), "=f"(r[4]), "=f"(r[5]), "=f"(r[6]), "=f"(r[7]), "=f"(r[8]), "=f"(r[9]),
+          "=f"(r[10]), "=f"(r[11]), "=f"(r[12]), "=f"(r[13]), "=f"(r[14]), "=f"(r[15])
+        : "r"(ta)
+        : "memory");
+}
+// wait for the outstanding loads; the registers pass through the wait so that
+// no use of them can be scheduled before it
+__device__ __forceinline__ void tm_wait_ld(float (&r)[16]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+f"(r[0]), "+f"(r[1]), "+f"(r[2]), "+f"(r[3]), "+f"(r[4]), "+f"(r[5]), "+f"(r[6]), "+f"(r[7]), "+f"(r[8]),
+                   "+f"(r[9]), "+f"(r[10]), "+f"(r[11]), "+f"(r[12]), "+f"(r[13]), "+f"(r[14]), "+f"(r[15])
+                 :
+                 : "memory");
+}
+__device__ __forceinline__ void tm_wait_ld2(float (&r)[16], float (&s)[16]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+f"(r[0]), "+f"(r[1]), "+f"(r[2]), "+f"(r[3]), "+f"(r[4]), "+f"(r[5]), "+f"(r[6]), "+f"(r[7]), "+f"(r[8]),
+                   "+f"(r[9]), "+f"(r[10]), "+f"(r[11]), "+f"(r[12]), "+f"(r[13]), "+f"(r[14]), "+f"(r[15]), "+f"(s[0]),
+                   "+f"(s[1]), "+f"(s[2]), "+f"(s[3]), "+f"(s[4]), "+f"(s[5]), "+f"(s[6]), "+f"(s[7]), "+f"(s[8]), "+f"(s[9]),
+                   "+f"(s[10]), "+f"(s[11]), "+f"(s[12]), "+f"(s[13]), "+f"(s[14]), "+f"(s[15])
+                 :
+                 : "memory");
+}
+
+// the 1024-point transform of warp_fft1024 with the per-lane twiddles
+// W_1024^{lane k1} (k1 < 32) read from tensor memory columns ttw .. ttw + 63
+__device__ __forceinline__ void warp_fft1024_tm(float2 (&a)[32], float2* S, unsigned ttw, int lane) {
+    dft32<false>(a);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        float r[16];
+        tm_ld16_issue(ttw + 16u * c, r);
+        tm_wait_ld(r);
+#pragma unroll
+        for (int m = 0; m < 8; ++m) {
+            const int k1 = 8 * c + m;
+            if (k1 > 0) a[k1] = cmul(a[k1], make_float2(r[2 * m], r[2 * m + 1]));
+        }
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < 32; ++k1) S[k1 * 33 + lane] = a[k1];
+    __syncwarp();
+#pragma unroll
+    for (int n2 = 0; n2 < 32; ++n2) a[n2] = S[lane * 33 + n2];
+    __syncwarp();
+    dft32<false>(a);
+}
+
+// copy X_f[k] of row y, k = kb + 32 i < NSG_RW_KX, into the inbox IN (at sx(k)); always commits a group
+__device__ __forceinline__ void rt_issue(float2* IN, const float2* __restrict__ src, int ny, int y, bool ok, int kb) {
+    if (ok) {
+#pragma unroll
+        for (int i = 0; i < NSG_RW_KXMAX / 32; ++i) {
+            const int k = kb + 32 * i;
+            if (k < NSG_RW_KX) cp_async(&IN[33 * i + kb], &src[(size_t)k * ny + y]);
+        }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+// row_pack from an inbox, with the i kx factor of the x-derivative fields applied on the way
+// (twh: the shared table exp(-2 pi i k/nx); with TW the pack twiddles of this
+// lane, k = lane + 32 n1, come from tensor memory columns ttwh + 2 n1, + 1)
+template <bool DX, bool TW>
+__device__ __forceinline__ void rt_pack(float2 (&a)[32], const float2* IN, const float* kxs, const float2* twh, unsigned ttwh,
+                                        int lane) {
+    const int ob = lane ? 32 - lane : 33;
+    const float2 zero = make_float2(0.f, 0.f);
+    float r[16];
+#pragma unroll
+    for (int n1 = 0; n1 < 32; ++n1) {
+        if (TW && (n1 & 7) == 0) {
+            tm_ld16_issue(ttwh + 2u * n1, r);
+            tm_wait_ld(r);
+        }
+        const int k = lane + 32 * n1;
+        float2 xa = (k < NSG_RW_KX) ? IN[33 * n1 + lane] : zero;
+        float2 xb = (k > 0 && 1024 - k < NSG_RW_KX) ? IN[33 * (31 - n1) + ob] : zero;
+        if (DX) {
+            const float ka = (k < NSG_RW_KX) ? kxs[k] : 0.f;
+            const float kb = (k > 0 && 1024 - k < NSG_RW_KX) ? kxs[1024 - k] : 0.f;
+            xa = make_float2(-ka * xa.y, ka * xa.x);
+            xb = make_float2(-kb * xb.y, kb * xb.x);
+        }
+        if (n1 == 0 && lane == 0) {
+            a[n1] = make_float2(xa.x, -xa.x);
+        } else {
+            const float2 e = TW ? make_float2(r[2 * (n1 & 7)], r[2 * (n1 & 7) + 1]) : twh[k];
+            const float2 A = cadd(xa, cconj(xb));
+            const float2 dd = csub(xa, cconj(xb));
+            const float Dx = dd.x * e.x + dd.y * e.y;
+            const float Dy = dd.y * e.x - dd.x * e.y;
+            a[n1] = make_float2(A.x - Dy, -(A.y + Dx));
+        }
+    }
+}
+
+template <int NW, int GW, int NB>
+__global__ void __launch_bounds__(32 * NW, 1) k_row_t(Geo g, RowArgs<float> a) {
+    static_assert(NW % GW == 0 && NB >= 1 && NB <= 2, "row tiling");
+    static_assert(128 * ((NW + 3) / 4) + (NSG_RT_TWTM ? 128 : 0) <= 512, "tensor-memory columns");
+    constexpr int WS = rt_wstride<NB>();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* tw = reinterpret_cast<float2*>(smem_raw);
+    float2* twh_s = tw + 32 * 33;
+    float2* S0 = twh_s + 1024;
+    float* kx_s = reinterpret_cast<float*>(S0 + NW * WS);
+    unsigned* tslot = reinterpret_cast<unsigned*>(kx_s + NSG_RW_KXMAX);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float2* S = S0 + warp * WS;
+    const int ny = g.ny;
+    const int grp = warp / GW;
+    const int tg = threadIdx.x - grp * 32 * GW;
+    const int kb = tg / GW, wme = tg - kb * GW;
+    float2* Sg = S0 + grp * GW * WS;
+    float2* INme = Sg + wme * WS + 1056;   // inbox 0 of the warp whose row this thread copies
+    const float2* INw = S + 1056;          // this warp's inbox 0
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         (unsigned)__cvta_generic_to_shared(tslot)),
+                     "r"(rt_tmem_cols<NW>()));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    for (int i = threadIdx.x; i < 1024; i += blockDim.x) {
+        const int k1 = i >> 5, t = i & 31;
+        tw[k1 * 33 + t] = a.twr[t * k1];
+        twh_s[i] = a.twh[i];
+    }
+    for (int i = threadIdx.x; i < NSG_RW_KXMAX; i += blockDim.x) kx_s[i] = (i < NSG_RW_KX) ? a.kxv[i] : 0.f;
+    wait_previous_kernel();
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (a.marker == 1) {
+            a.ds->step_cur = a.ds->step_next;
+            a.ds->step_next = a.ds->step_next + (a.ds->fsub ? a.ds->fsub : 1ULL);
+        } else if (a.marker == 2) {
+            a.ds->maxvel2 = 0ULL;
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();  // tables and the tensor-memory address
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // this warp's 128 columns: R (psi_x, then psi_x omega_y) at +0, Q (psi_y) at +64
+    const unsigned tR = *tslot + ((unsigned)(32 * (warp & 3)) << 16) + 128u * (unsigned)(warp >> 2);
+    const unsigned tQ = tR + 64u;
+    // per-lane twiddles after the warps' R and Q columns, one copy per lane
+    // quarter (written by warps 0-3, read by every warp of the quarter):
+    // tTW + 2 k1 (+1) = W_1024^{lane k1}, tTWH + 2 n1 (+1) = exp(-2 pi i (lane + 32 n1)/nx)
+    const unsigned tTW = *tslot + ((unsigned)(32 * (warp & 3)) << 16) + 128u * (unsigned)((NW + 3) / 4);
+    const unsigned tTWH = tTW + 64u;
+    if (NSG_RT_TWTM) {
+        if (warp < 4) {
+            float2 t[32];
+#pragma unroll
+            for (int k1 = 0; k1 < 32; ++k1) t[k1] = tw[k1 * 33 + lane];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) tm_st16(tTW + 16u * c, t, c);
+#pragma unroll
+            for (int n1 = 0; n1 < 32; ++n1) t[n1] = twh_s[lane + 32 * n1];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) tm_st16(tTWH + 16u * c, t, c);
+            tm_wait_st();
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    }
+
+    float vmax2 = 0.f;
+    float2 v[32];
+    const int ystep = gridDim.x * NW;
+    int y0 = blockIdx.x * NW + grp * GW;
+    int buf = 0;
+    rt_issue(INme, a.F[0], ny, y0 + wme, y0 + wme < ny, kb);
+    for (; y0 < ny; y0 += ystep) {
+        const int y = y0 + (warp - grp * GW);
+        // q = 0..3: inverse transforms of psi_x (F0, d/dx), psi_y (F1), omega_y (F3),
+        // omega_x (F2, d/dx); q = 4: forward transform of the packed Jacobian
+#pragma unroll 1
+        for (int q = 0; q < 5; ++q) {
+            if (q < 4) {
+                asm volatile("cp.async.wait_all;" ::: "memory");  // field q (the only copies in flight)
+                group_sync<GW, NW>(grp);                           // ... from every thread; the other inbox is free
+                const int yn = (q < 3) ? y0 + wme : y0 + ystep + wme;
+                const float2* src = a.F[(q < 3) ? ((q + 1 < 2) ? q + 1 : 4 - q) : 0];
+                if (NB == 2) rt_issue(INme + (buf ^ 1) * NSG_RT_IN, src, ny, yn, yn < ny, kb);
+                if (y < ny) {
+                    const float2* IN = INw + buf * NSG_RT_IN;
+                    if (q == 0 || q == 3) rt_pack<true, NSG_RT_TWTM>(v, IN, kx_s, twh_s, tTWH, lane);
+                    else rt_pack<false, NSG_RT_TWTM>(v, IN, kx_s, twh_s, tTWH, lane);
+                }
+                if (NB == 1) {
+                    group_sync<GW, NW>(grp);  // every warp has packed field q
+                    rt_issue(INme, src, ny, yn, yn < ny, kb);
+                }
+                buf ^= (NB - 1);
+            }
+            if (y >= ny) continue;
+            if (NSG_RT_TWTM) warp_fft1024_tm(v, S, tTW, lane);
+            else warp_fft1024<false>(v, S, tw, lane);
+            if (q == 4) break;
+#pragma unroll
+            for (int k = 0; k < 32; ++k) v[k].y = -v[k].y;
+            if (q == 0) {
+#pragma unroll
+                for (int c = 0; c < 4; ++c) tm_st16(tR + 16u * c, v, c);
+            } else if (q == 1) {
+                if (a.cfl) {
+                    tm_wait_st();
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        float r[16];
+                        tm_ld16_issue(tR + 16u * c, r);
+                        tm_wait_ld(r);
+#pragma unroll
+                        for (int m = 0; m < 8; ++m) {
+                            const float2 p = v[8 * c + m];
+                            vmax2 = fmaxf(vmax2, fmaxf(r[2 * m] * r[2 * m] + p.x * p.x, r[2 * m + 1] * r[2 * m + 1] + p.y * p.y));
+                        }
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < 4; ++c) tm_st16(tQ + 16u * c, v, c);
+            } else if (q == 2) {
+                tm_wait_st();
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    float r[16];
+                    tm_ld16_issue(tR + 16u * c, r);
+                    tm_wait_ld(r);
+                    float2 pr[32];
+#pragma unroll
+                    for (int m = 0; m < 8; ++m) pr[8 * c + m] = make_float2(r[2 * m] * v[8 * c + m].x, r[2 * m + 1] * v[8 * c + m].y);
+                    tm_st16(tR + 16u * c, pr, c);
+                }
+            } else {
+                // J = psi_x omega_y - psi_y omega_x, packed as w[m] = J[2m] + i J[2m+1]
+                tm_wait_st();
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    float r[16], s[16];
+                    tm_ld16_issue(tR + 16u * c, r);
+                    tm_ld16_issue(tQ + 16u * c, s);
+                    tm_wait_ld2(r, s);
+#pragma unroll
+                    for (int m = 0; m < 8; ++m) {
+                        const float2 w = v[8 * c + m];
+                        v[8 * c + m] = make_float2(r[2 * m] - s[2 * m] * w.x, r[2 * m + 1] - s[2 * m + 1] * w.y);
+                    }
+                }
+            }
+        }
+        if (y < ny) {
+#pragma unroll
+            for (int k = 0; k < 32; ++k) S[k * 33 + lane] = v[k];
+        }
+        group_sync<GW, NW>(grp);
+        const float half = 0.5f;
+        const int nrows = (ny - y0 < GW) ? ny - y0 : GW;
+        for (int e = tg; e < NSG_RW_KX * GW; e += 32 * GW) {
+            const int k = e / GW, w = e - k * GW;
+            if (w >= nrows) continue;
+            const float2* Sw = Sg + w * WS;
+            const float2 wa = Sw[sx(k)];
+            const float2 wb = Sw[sx((1024 - k) & 1023)];
+            float2 ev, od;
+            ev.x = half * (wa.x + wb.x);
+            ev.y = half * (wa.y - wb.y);
+            od.x = half * (wa.y + wb.y);
+            od.y = -half * (wa.x - wb.x);
+            a.G[(size_t)k * ny + y0 + w] = cadd(ev, cmul(od, twh_s[k]));
+        }
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    tm_wait_st();
+    if (a.cfl) {
+        const double vm = warp_max((double)vmax2);
+        if (lane == 0) atomicMax(&a.ds->maxvel2, (unsigned long long)__double_as_longlong(vm));
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(*tslot), "r"(rt_tmem_cols<NW>()));
+    }
+}
+
 }  // namespace nsg

@@ -46,11 +46,15 @@ def test_fast_kernels_fp64_match_oracle(nsgb, port, nx, ny, steps):
     assert rel_l2(g.real("omega"), o.real("omega")) <= TOL
 
 
-def test_fast_fp32_vs_fp64_2048(nsgb):
-    a = _gpu_run(nsgb, 2048, 2048, 10, nsgb.FP64)
-    b = _gpu_run(nsgb, 2048, 2048, 10, nsgb.FP32)
+@pytest.mark.parametrize("nx,ny,steps", [(2048, 2048, 10), (2048, 128, 10)])
+def test_fast_fp32_vs_fp64_2048(nsgb, nx, ny, steps):
+    # the FP32 row pass (tensor-memory operands) against the FP64 path
+    a = _gpu_run(nsgb, nx, ny, steps, nsgb.FP64)
+    b = _gpu_run(nsgb, nx, ny, steps, nsgb.FP32)
     err = rel_l2(b.cplx("omega_hat"), a.cplx("omega_hat"))
     assert err <= 1e-5, err
+    assert rel_l2(b.real("u"), a.real("u")) <= 1e-5
+    assert abs(b.d.t - a.d.t) <= 1e-6 * a.d.t
     ea, za = a.diagnostics()
     eb, zb = b.diagnostics()
     assert abs(eb - ea) <= 1e-6 * ea
