@@ -195,6 +195,20 @@ template <typename T> static int stage_row(ns_gpu* g, int stage) {
 
 template <typename T, int STAGE> static int stage_col(ns_gpu* g, const ColArgs<T>& a) {
     ProfScope ps(g, 1);
+    if constexpr (sizeof(T) == 4 && NSG_COL_Q) {
+        if (g->fast_col) {
+            // FP32: four warps per column (k_col_q)
+            const size_t smem = cq_smem_bytes(g->g.Ky);
+            auto kern = a.sp.ifrk ? k_col_q<STAGE, true> : k_col_q<STAGE, false>;
+            NSG_TRY(set_smem(g, kern, smem));
+            int grid = g->num_sms;
+            if (grid > g->g.Kx) grid = g->g.Kx;
+            const cudaError_t e = launch_stage(kern, grid, 128 * NSG_CQ_TEAMS, smem, g->st, g->g, a);
+            if (e != cudaSuccess) NSG_FAIL(g, NS_GPU_ERR_CUDA, "k_col_q launch: %s", cudaGetErrorString(e));
+            NSG_LAUNCHED(g);
+            return NS_GPU_OK;
+        }
+    }
     if (g->fast_col) {
         const size_t smem = cw_smem_bytes<T>(g->g.Ky);
         auto kern = a.sp.ifrk ? k_col_w<T, STAGE, true> : k_col_w<T, STAGE, false>;

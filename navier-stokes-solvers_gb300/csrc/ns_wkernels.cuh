@@ -25,6 +25,9 @@
 #ifndef NSG_FFT_ONEDFT
 #define NSG_FFT_ONEDFT 0   // FP32 stage transforms: both DFT32 passes through one loop body (measured no faster)
 #endif
+#ifndef NSG_RT_SPREAD
+#define NSG_RT_SPREAD 1   // FP32 row pass: equal contiguous row ranges per CTA (measured neutral at 2048^2)
+#endif
 #ifndef NSG_RT_ROLL
 #define NSG_RT_ROLL 0   // FP32 row pass: inverse pack eight elements at a time through tensor memory (measured slower)
 #endif
@@ -914,6 +917,326 @@ __global__ void __launch_bounds__(64 * cw_teams<T>(), 1) k_col_w(Geo g, ColArgs<
     }
 }
 
+// ============================================================ k_col_q
+// FP32 column pass at ny = 2048 with four warps per kept kx column.  Every SM
+// holds all of its columns at once (684 columns, 5 per SM), so the pass takes
+// as long as one column's chain of five transforms and the RK algebra; 128
+// threads with 16 points each run that chain with half the serial work per
+// thread of the two-warp teams (k_col_w), in the same shared memory per column.
+//
+// 2048-point transform, 2048 = 16 x 16 x 8 (thread t < 128, k1 = t & 15):
+//   pass A   t holds x[128 n1 + t] (n1 < 16): DFT16 over n1, times W_2048^{t k1}
+//   pass B1  thread (k1, m2 = t >> 4) takes z[8 m1 + m2] of column k1 (m1 < 16):
+//            DFT16 over m1, times W_128^{m2 q1}
+//   pass B2  thread (k1, qp = t >> 4) takes the eight m2 values of q1 = 2 qp + r
+//            (r < 2): DFT8 -> X[k1 + 16 q1 + 256 q2] in a[8 r + q2]
+// The exchange buffer holds [16][129] values; a pitch of 129 makes every
+// exchange store and load conflict-free (16 banks pairs, two wavefronts).
+#ifndef NSG_COL_Q
+#define NSG_COL_Q 1   // 0: the FP32 column pass runs k_col_w
+#endif
+#ifndef NSG_CQ_TEAMS
+#define NSG_CQ_TEAMS 5
+#endif
+#define NSG_CQ_EX 2064
+__host__ __device__ constexpr int cq_xl(int Ky) { return 2 * cw_kyp(Ky) > NSG_CQ_EX ? 2 * cw_kyp(Ky) : NSG_CQ_EX; }
+__host__ __device__ constexpr size_t cq_smem_bytes(int Ky) {
+    return (size_t)(2048 + NSG_CQ_TEAMS * (cq_xl(Ky) + cw_kyp(Ky))) * sizeof(float2) +
+           (size_t)(NSG_CQ_TEAMS + 1) * cw_kyp(Ky) * sizeof(float);
+}
+// barrier over one 128-thread team (named barrier bid, 1 <= bid <= 15)
+__device__ __forceinline__ void quad_sync(int bid) { asm volatile("bar.sync %0, 128;" ::"r"(bid) : "memory"); }
+
+// forward 2048-point transform of a team: a[n1] = x[128 n1 + t] on entry,
+// a[8 r + q2] = X[k1 + 16 (2 qp + r) + 256 q2] on exit; E is the team's exchange
+// buffer (free again on return), TW1[k1 * 128 + t] = W_2048^{t k1}
+__device__ __forceinline__ void col_fwd2048_q(float2 (&a)[16], float2* E, const float2* TW1, int t, int bid) {
+    const int k1 = t & 15, hi = t >> 4;
+    dft16<false>(a);
+#pragma unroll
+    for (int c = 1; c < 16; ++c) a[c] = cmul(a[c], TW1[c * 128 + t]);
+#pragma unroll
+    for (int c = 0; c < 16; ++c) E[c * 129 + t] = a[c];
+    quad_sync(bid);
+#pragma unroll
+    for (int m1 = 0; m1 < 16; ++m1) a[m1] = E[k1 * 129 + 8 * m1 + hi];
+    quad_sync(bid);
+    dft16<false>(a);
+#pragma unroll
+    for (int q1 = 1; q1 < 16; ++q1) a[q1] = cmul(a[q1], TW1[q1 * 128 + 16 * hi]);  // W_128^{m2 q1}
+#pragma unroll
+    for (int q1 = 0; q1 < 16; ++q1) E[k1 * 129 + q1 * 8 + hi] = a[q1];
+    quad_sync(bid);
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+#pragma unroll
+        for (int m2 = 0; m2 < 8; ++m2) a[8 * r + m2] = E[k1 * 129 + (2 * hi + r) * 8 + m2];
+    }
+    quad_sync(bid);
+    dft8<false>(a);
+    dft8<false>(a + 8);
+}
+
+// output mode of a[e] (e = 8 r + q2) in thread t
+__device__ __forceinline__ int cq_mode(int t, int e) { return (t & 15) + 16 * (2 * (t >> 4) + (e >> 3)) + 256 * (e & 7); }
+
+// Persistent column pass (FP32): one CTA per SM, NSG_CQ_TEAMS teams of 128
+// threads, team q of CTA b takes the kept columns b + gridDim.x (q + NT r).
+// Staging, tables and stage algebra follow k_col_w; only the thread <-> mode
+// maps differ (build: j = 128 n1 + t; stage algebra: j = cq_mode(t, e)).
+// dynamic smem: TW1 [16][128] | per team: X [XL] (exchange, then WS | ACC), NS [Kyp]
+//               | per team SHV [Kyp] float | KYS [Kyp] float
+template <int STAGE, bool IFRK>
+__global__ void __launch_bounds__(128 * NSG_CQ_TEAMS, 1) k_col_q(Geo g, ColArgs<float> a) {
+    typedef float T;
+    typedef float2 C;
+    constexpr int NT = NSG_CQ_TEAMS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int Ky = g.Ky, Kyp = cw_kyp(Ky), XL = cq_xl(Ky), Kx = g.Kx;
+    const int team = threadIdx.x >> 7, t = threadIdx.x & 127;
+    const int bid = 1 + team;
+    C* TW1 = reinterpret_cast<C*>(smem_raw);
+    C* X = TW1 + 2048 + team * (XL + Kyp);
+    C* NS = X + XL;
+    T* SHV = reinterpret_cast<T*>(TW1 + 2048 + NT * (XL + Kyp)) + team * Kyp;
+    T* KYS = reinterpret_cast<T*>(TW1 + 2048 + NT * (XL + Kyp)) + NT * Kyp;
+    const int hv = a.sp.hv, sfd = a.sp.sfd;
+    __shared__ double s_dt;
+
+    for (int m = threadIdx.x; m < 2048; m += blockDim.x) TW1[m] = a.twc[((m & 127) * (m >> 7)) & 2047];
+    for (int jj = threadIdx.x; jj < Ky; jj += blockDim.x) KYS[jj] = a.kyv[jj];
+    const int cstride = gridDim.x * NT;
+    int i = blockIdx.x + gridDim.x * team;
+    if (i < Kx) {
+        const size_t base = (size_t)i * Ky;
+        for (int jj = t; jj < Ky; jj += 128) {
+            cp_async(&NS[jj], &a.W0[base + jj]);
+            if (hv) cp_async(&SHV[jj], &a.hvw[base + jj]);
+        }
+    }
+    wait_previous_kernel();
+    if (threadIdx.x == 0) {
+        double dt;
+        if (STAGE == 1) {
+            if (a.sp.adaptive) {
+                // spectral_time_integration.c:9-31 on max|u| of the stage-1 fields
+                const double vmax = sqrt(__longlong_as_double((long long)a.ds->maxvel2));
+                const double dt_cfl = a.sp.cfl * a.sp.dxmin / (vmax + 1e-12);
+                const double dt_visc = 0.5 * a.sp.Re * a.sp.dxmin * a.sp.dxmin;
+                dt = fmin(dt_cfl, dt_visc);
+                dt = fmax(dt, 1e-8);
+                dt = fmin(dt, 0.1);
+            } else {
+                dt = a.ds->dt_fixed;
+            }
+            if (blockIdx.x == 0) a.ds->dt = dt;
+        } else {
+            dt = a.ds->dt;
+        }
+        s_dt = dt;
+    }
+    __syncthreads();  // tables and dt
+
+    const double dt = s_dt;
+    const T inv_re = (T)a.sp.inv_re;
+    const T sc = (T)a.sp.scale;
+    const T cst = (STAGE == 1 || STAGE == 2) ? (T)(0.5 * dt) : (STAGE == 3 ? (T)dt : (T)(dt / 6.0));
+    const T ch = (T)(0.5 * dt), cf = (T)dt, c6 = (T)(dt / 6.0);
+    C* __restrict__ W0 = a.W0;
+    C* __restrict__ WS = a.WS;
+    C* __restrict__ ACC = a.ACC;
+    const C zero = make_float2(0.f, 0.f);
+
+    for (bool first = true; i < Kx; i += cstride, first = false) {
+        if (!first) {
+            const size_t base = (size_t)i * Ky;
+            for (int jj = t; jj < Ky; jj += 128) {
+                cp_async(&NS[jj], &a.W0[base + jj]);
+                if (hv) cp_async(&SHV[jj], &a.hvw[base + jj]);
+            }
+        }
+        const T kx = __ldg(&a.kxv[i]);
+        const size_t cbase = (size_t)i * Ky;
+        C v[16];
+        // q = -1: forward transform of the Jacobian column and the RK stage;
+        // q = 0..3: inverse transforms of Omega, Omega_y, Psi, Psi_y
+#pragma unroll 1
+        for (int q = -1; q < 4; ++q) {
+            const int f = (q + 2) & 3;
+            if (q < 0) {
+                const C* __restrict__ Gc = a.G + (size_t)i * 2048;
+#pragma unroll
+                for (int n1 = 0; n1 < 16; ++n1) v[n1] = ld_stream(&Gc[128 * n1 + t]);
+            } else {
+                // thread t builds modes j = 128 n1 + t; Psi = -w/k^2 is formed once
+                // (written back to NS) and reused for Psi_y by the same thread
+#pragma unroll
+                for (int n1 = 0; n1 < 16; ++n1) {
+                    const int j = 128 * n1 + t;
+                    const int jj = kept_jj(g, j);
+                    C x = zero;
+                    if (jj >= 0) {
+                        const T ky = KYS[jj];
+                        C w = NS[jj];
+                        if (f == 0) {
+                            w = field_value<T, C>(0, w, kx, ky);
+                            NS[jj] = w;
+                        }
+                        if (f == 1 || f == 3) {
+                            x.x = -ky * w.y;
+                            x.y = ky * w.x;
+                        } else {
+                            x = w;
+                        }
+                    }
+                    v[n1] = cconj(x);
+                }
+            }
+            col_fwd2048_q(v, X, TW1, t, bid);  // ends with a team barrier: X is free
+            if (q >= 0) {
+                C* __restrict__ Fc = a.F[f] + (size_t)i * 2048;
+#pragma unroll
+                for (int e = 0; e < 16; ++e) Fc[cq_mode(t, e)] = cconj(v[e]);
+                continue;
+            }
+            if (STAGE != 1) {
+                for (int jj = t; jj < Ky; jj += 128) {
+                    cp_async(&X[jj], &WS[cbase + jj]);
+                    cp_async(&X[Kyp + jj], &ACC[cbase + jj]);
+                }
+            }
+            cp_async_wait_all();
+            quad_sync(bid);  // the team's staged omega_hat, weights, WS and ACC
+
+            // RK stage algebra (spectral_time_integration.c:50-100) on this
+            // thread's forward outputs, modes j = cq_mode(t, e)
+#pragma unroll
+            for (int e = 0; e < 16; ++e) {
+                const int j = cq_mode(t, e);
+                const int jj = kept_jj(g, j);
+                if (jj < 0) continue;
+                const size_t s = cbase + jj;
+                const C jh = v[e];
+                const C w0 = NS[jj];
+                const C ws = (STAGE == 1) ? w0 : X[jj];
+                const C acc0 = (STAGE == 1) ? zero : X[Kyp + jj];
+                const T hw = hv ? SHV[jj] : (T)0;
+                T sw = (T)0;
+                C fb = zero;
+                if (sfd) {
+                    sw = a.sfdw[s];
+                    fb = a.SFD[s];
+                }
+                const T k2v = k2sum(kx, KYS[jj]);
+                C wn;
+                if (IFRK) {
+                    // integrating-factor RK4: explicit part N - SFD relaxation, exact
+                    // decay by E1 = exp(-(k^2/Re + w) dt/2), E2 = E1^2
+                    C k;
+                    k.x = -(jh.x * sc);
+                    k.y = -(jh.y * sc);
+                    if (sfd && sw > (T)0) {
+                        k.x -= sw * (ws.x - fb.x);
+                        k.y -= sw * (ws.y - fb.y);
+                    }
+                    const T lam = k2v * inv_re + hw;
+                    const T e1 = exp(-lam * ch), e2 = e1 * e1;
+                    if (STAGE == 1) {
+                        ACC[s] = make_float2(e2 * k.x, e2 * k.y);
+                        wn.x = e1 * (w0.x + ch * k.x); wn.y = e1 * (w0.y + ch * k.y);
+                        WS[s] = wn;
+                    } else if (STAGE == 2 || STAGE == 3) {
+                        C acc = acc0;
+                        acc.x = acc.x + (T)2 * (e1 * k.x);
+                        acc.y = acc.y + (T)2 * (e1 * k.y);
+                        ACC[s] = acc;
+                        if (STAGE == 2) { wn.x = e1 * w0.x + ch * k.x; wn.y = e1 * w0.y + ch * k.y; }
+                        else { wn.x = e2 * w0.x + cf * (e1 * k.x); wn.y = e2 * w0.y + cf * (e1 * k.y); }
+                        WS[s] = wn;
+                    } else {
+                        wn.x = e2 * w0.x + c6 * (acc0.x + k.x);
+                        wn.y = e2 * w0.y + c6 * (acc0.y + k.y);
+                        W0[s] = wn;
+                    }
+                } else {
+                    C k;
+                    k.x = -(jh.x * sc) - k2v * ws.x * inv_re;
+                    k.y = -(jh.y * sc) - k2v * ws.y * inv_re;
+                    if (hv || sfd) {
+                        C damp = zero;
+                        if (hv) { damp.x += hw * ws.x; damp.y += hw * ws.y; }
+                        if (sfd && sw > (T)0) {
+                            damp.x += sw * (ws.x - fb.x);
+                            damp.y += sw * (ws.y - fb.y);
+                        }
+                        k.x -= damp.x;
+                        k.y -= damp.y;
+                    }
+                    if (STAGE == 1) {
+                        ACC[s] = k;
+                        wn.x = w0.x + cst * k.x; wn.y = w0.y + cst * k.y;
+                        WS[s] = wn;
+                    } else if (STAGE == 2 || STAGE == 3) {
+                        C acc = acc0;
+                        acc.x = acc.x + (T)2 * k.x;
+                        acc.y = acc.y + (T)2 * k.y;
+                        ACC[s] = acc;
+                        wn.x = w0.x + cst * k.x; wn.y = w0.y + cst * k.y;
+                        WS[s] = wn;
+                    } else {
+                        wn.x = w0.x + cst * (acc0.x + k.x);
+                        wn.y = w0.y + cst * (acc0.y + k.y);
+                        W0[s] = wn;
+                    }
+                }
+                NS[jj] = wn;
+            }
+            if (STAGE == 4 && (a.sp.forcing || sfd)) {
+                // forcing increment (few low-|k| modes), then the SFD post-step, on omega_hat^{n+1}
+                const double f_amp = a.sp.forcing ? a.sp.f_sigma * sqrt(dt / a.sp.fsub) : 0.0;
+                double sa = 0.0;
+                if (sfd) {
+                    sa = dt / a.sp.sfd_tau;
+                    sa = sa > 1.0 ? 1.0 : (sa < 0.0 ? 0.0 : sa);
+                }
+                const bool force_col = a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9;
+                // |k|^2 window, widened far beyond FP32 rounding, that screens modes before the exact FP64 shell test
+                const T k2lo = (T)(a.sp.f_kmin * a.sp.f_kmin * (1.0 - 1e-3));
+                const T k2hi = (T)(a.sp.f_kmax * a.sp.f_kmax * (1.0 + 1e-3));
+#pragma unroll 1
+                for (int e = 0; e < 16 && (force_col || sfd); ++e) {
+                    const int j = cq_mode(t, e);
+                    const int jj = kept_jj(g, j);
+                    if (jj < 0) continue;
+                    const size_t s = cbase + jj;
+                    C wn = NS[jj];
+                    const T ky = KYS[jj];
+                    const T k2f = kx * kx + ky * ky;
+                    if (force_col && k2f >= k2lo && k2f <= k2hi) {
+                        const double2 df =
+                            forcing_increment(g, i, j, a.ds->step_cur, a.sp.fsub, a.sp.f_seed, a.sp.f_kmin, a.sp.f_kmax, f_amp);
+                        if (df.x != 0.0 || df.y != 0.0) {
+                            wn.x = (T)((double)wn.x + df.x);
+                            wn.y = (T)((double)wn.y + df.y);
+                            W0[s] = wn;
+                            NS[jj] = wn;
+                        }
+                    }
+                    if (sfd) {
+                        C fb = a.SFD[s];
+                        const T al = (T)sa, om = (T)(1.0 - sa);
+                        fb.x = om * fb.x + al * wn.x;
+                        fb.y = om * fb.y + al * wn.y;
+                        a.SFD[s] = fb;
+                    }
+                }
+            }
+            quad_sync(bid);  // NS complete for the inverse transforms; X is free again
+        }
+    }
+    if (STAGE == 4 && blockIdx.x == 0 && threadIdx.x == 0) a.ds->t = a.ds->t + dt;
+}
+
 // ============================================================ k_row_t
 // FP32 row pass at nx = 2048 with the Jacobian operands in tensor memory.
 // Same transforms and row ownership as k_row_w (groups of GW warps own GW
@@ -1165,11 +1488,17 @@ __global__ void __launch_bounds__(32 * NW, 1) k_row_t(Geo g, RowArgs<float> a) {
 
     float vmax2 = 0.f;
     float2 v[32];
-    const int ystep = gridDim.x * NW;
-    int y0 = blockIdx.x * NW + grp * GW;
+    // rows of this CTA: [r0, yend), in rounds of NW.  NSG_RT_SPREAD gives every
+    // CTA an equal contiguous share (13-14 rows at 2048 over 152 CTAs), so the
+    // last round is short on every SM instead of full on some and absent on others
+    // (the rounds are latency-bound, so at 2048^2 this measured the same as round-robin).
+    const int r0 = NSG_RT_SPREAD ? (int)(((long long)ny * blockIdx.x) / gridDim.x) : blockIdx.x * NW;
+    const int yend = NSG_RT_SPREAD ? (int)(((long long)ny * (blockIdx.x + 1)) / gridDim.x) : ny;
+    const int ystep = NSG_RT_SPREAD ? NW : gridDim.x * NW;
+    int y0 = r0 + grp * GW;
     int buf = 0;
-    rt_issue(INme, a.F[0], ny, y0 + wme, y0 + wme < ny, kb);
-    for (; y0 < ny; y0 += ystep) {
+    rt_issue(INme, a.F[0], ny, y0 + wme, y0 + wme < yend, kb);
+    for (; y0 < yend; y0 += ystep) {
         const int y = y0 + (warp - grp * GW);
         // q = 0..3: inverse transforms of psi_x (F0, d/dx), psi_y (F1), omega_y (F3),
         // omega_x (F2, d/dx); q = 4: forward transform of the packed Jacobian
@@ -1180,8 +1509,8 @@ __global__ void __launch_bounds__(32 * NW, 1) k_row_t(Geo g, RowArgs<float> a) {
                 group_sync<GW, NW>(grp);                           // ... from every thread; the other inbox is free
                 const int yn = (q < 3) ? y0 + wme : y0 + ystep + wme;
                 const float2* src = a.F[(q < 3) ? ((q + 1 < 2) ? q + 1 : 4 - q) : 0];
-                if (NB == 2) rt_issue(INme + (buf ^ 1) * NSG_RT_IN, src, ny, yn, yn < ny, kb);
-                if (y < ny) {
+                if (NB == 2) rt_issue(INme + (buf ^ 1) * NSG_RT_IN, src, ny, yn, yn < yend, kb);
+                if (y < yend) {
                     const float2* IN = INw + buf * NSG_RT_IN;
                     if (NSG_RT_ROLL) {
                         if (q == 0 || q == 3) rt_pack_roll<true>(v, IN, kx_s, tTWH, tP, lane);
@@ -1194,11 +1523,11 @@ __global__ void __launch_bounds__(32 * NW, 1) k_row_t(Geo g, RowArgs<float> a) {
                 }
                 if (NB == 1) {
                     group_sync<GW, NW>(grp);  // every warp has packed field q
-                    rt_issue(INme, src, ny, yn, yn < ny, kb);
+                    rt_issue(INme, src, ny, yn, yn < yend, kb);
                 }
                 buf ^= (NB - 1);
             }
-            if (y >= ny) continue;
+            if (y >= yend) continue;
             if (NSG_RT_TWTM) warp_fft1024_tm(v, S, tTW, lane);
             else warp_fft1024<false>(v, S, tw, lane);
             if (q == 4) break;
@@ -1253,13 +1582,13 @@ __global__ void __launch_bounds__(32 * NW, 1) k_row_t(Geo g, RowArgs<float> a) {
                 }
             }
         }
-        if (y < ny) {
+        if (y < yend) {
 #pragma unroll
             for (int k = 0; k < 32; ++k) S[k * 33 + lane] = v[k];
         }
         group_sync<GW, NW>(grp);
         const float half = 0.5f;
-        const int nrows = (ny - y0 < GW) ? ny - y0 : GW;
+        const int nrows = (yend - y0 < GW) ? yend - y0 : GW;
         for (int e = tg; e < NSG_RW_KX * GW; e += 32 * GW) {
             const int k = e / GW, w = e - k * GW;
             if (w >= nrows) continue;
