@@ -168,6 +168,10 @@ def ncu_traffic(kind: str, n: int, prec: str):
     return None
 
 
+# the FP32 stage kernels at 2048^2: x-pass (row) and y-pass (column)
+STAGE_KERNELS = {"row": "k_row_t", "col": "k_col_q"}
+
+
 def model_bytes(n: int, elem: int):
     """Algorithmic HBM bytes per launch: row kernel 5A, column kernel 5A + 11C/4
     (A = Kx*ny, C = Kx*Ky complex values; 40A + 11C per RK4 step)."""
@@ -499,7 +503,7 @@ def main():
     peak, peak_src = hbm_peak()
     achieved = mb[dom] / (dom_ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": ncu_traffic(dom, n, "fp32"), "kernel": f"k_{dom} (FP32, {n}^2)",
+                "traffic": ncu_traffic(dom, n, "fp32"), "kernel": f"{STAGE_KERNELS[dom]} (FP32, {n}^2)",
                 "peak_source": peak_src,
                 "algorithmic_bytes_per_launch": mb[dom], "mean_launch_ms": dom_ms,
                 "kernels": {"row": {"mean_ms": row_ms, "launches": kcnt[0], "bytes": mb["row"],
