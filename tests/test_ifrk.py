@@ -83,10 +83,10 @@ def _oracle_run(port, nx, ny, steps, sfd=False, Re=1e3, hv=2.0, seed=5):
     return s
 
 
-def _gpu_run(nsgb, nx, ny, steps, prec, sfd=False, Re=1e3, hv=2.0, seed=5):
+def _gpu_run(nsgb, nx, ny, steps, prec, sfd=False, Re=1e3, hv=2.0, seed=5, scheme=1):
     s = nsgb.Solver(nx, ny, Re=Re, precision=prec).setup(ic=None)
     s.set_forcing(4.0, 6.0, 1e-3, 11)
-    s.set_scheme(1)
+    s.set_scheme(scheme)
     s.d.cfl_factor = 0.5
     s.random_spectrum(seed, 4.0, 0.5)
     kw = dict(enabled=1, coefficient=hv, order=4, cutoff_ratio=0.0)
@@ -114,6 +114,18 @@ def test_gpu_ifrk4_fp32_2048_tracks_fp64(nsgb):
     a = _gpu_run(nsgb, 2048, 2048, 5, nsgb.FP64)
     b = _gpu_run(nsgb, 2048, 2048, 5, nsgb.FP32)
     assert rel_l2(b.cplx("omega_hat"), a.cplx("omega_hat")) <= 1e-5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nx,ny,scheme", [(128, 2048, 0), (128, 2048, 1), (2048, 2048, 0)])
+def test_gpu_fp32_column_pass_with_sfd_tracks_fp64(nsgb, nx, ny, scheme):
+    # the FP32 2048-point column pass with every term of its stage algebra on:
+    # hyperviscosity, SFD relaxation and post-step, forcing (explicit RK4 and IF-RK4)
+    a = _gpu_run(nsgb, nx, ny, 5, nsgb.FP64, sfd=True, scheme=scheme)
+    b = _gpu_run(nsgb, nx, ny, 5, nsgb.FP32, sfd=True, scheme=scheme)
+    assert rel_l2(b.cplx("omega_hat"), a.cplx("omega_hat")) <= 1e-5
+    assert rel_l2(b.cplx("sfd_hat"), a.cplx("sfd_hat")) <= 1e-5
+    assert abs(b.d.t - a.d.t) <= 1e-6 * a.d.t
 
 
 @pytest.mark.gpu
