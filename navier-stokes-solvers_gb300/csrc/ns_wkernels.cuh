@@ -22,20 +22,11 @@
 #pragma once
 #include "ns_kernels.cuh"
 
-#ifndef NSG_FFT_ONEDFT
-#define NSG_FFT_ONEDFT 0   // FP32 stage transforms: both DFT32 passes through one loop body (measured no faster)
-#endif
 #ifndef NSG_RT_SPREAD
 #define NSG_RT_SPREAD 1   // FP32 row pass: equal contiguous row ranges per CTA (measured neutral at 2048^2)
 #endif
-#ifndef NSG_RT_ROLL
-#define NSG_RT_ROLL 0   // FP32 row pass: inverse pack eight elements at a time through tensor memory (measured slower)
-#endif
 
 namespace nsg {
-
-// unroll factor of the two DFT32 passes of the FP32 stage transforms
-constexpr int kDftPassUnroll = NSG_FFT_ONEDFT ? 1 : 2;
 
 // ------------------------------------------------------------ streamed loads
 // Global loads that do not allocate in L1: the column pass streams ~50 KB per
@@ -496,54 +487,6 @@ __device__ __forceinline__ void tm_wait_ld2(float (&r)[16], float (&s)[16]) {
 }
 
 
-// col_fwd2048 with the per-thread twiddles W_2048^{t k1} (k1 < 32) read from
-// tensor memory columns ttw .. ttw + 63 (FP32)
-template <bool TWT>
-__device__ __forceinline__ void col_fwd2048_tm(float2 (&a)[32], float2* col, const float2* tw, unsigned ttw, int t, int lane,
-                                               int h, int bid) {
-    // the two DFT32 passes share one body (NSG_FFT_ONEDFT): a smaller kernel
-#pragma unroll(kDftPassUnroll)
-    for (int pass = 0; pass < 2; ++pass) {
-        dft32<false>(a);
-        if (pass == 1) break;
-        if (TWT) {
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                float r[16];
-                tm_ld16_issue(ttw + 16u * c, r);
-                tm_wait_ld(r);
-#pragma unroll
-                for (int m = 0; m < 8; ++m) {
-                    const int k1 = 8 * c + m;
-                    if (k1 > 0) a[k1] = cmul(a[k1], make_float2(r[2 * m], r[2 * m + 1]));
-                }
-            }
-        } else {
-#pragma unroll
-            for (int k1 = 1; k1 < 32; ++k1) a[k1] = cmul(a[k1], tw[k1 * 65 + t]);
-        }
-#pragma unroll
-        for (int k1 = 0; k1 < 32; ++k1) col[k1 * 65 + t] = a[k1];
-        team_sync(bid);
-#pragma unroll
-        for (int m = 0; m < 32; ++m) a[m] = col[lane * 65 + 2 * m + h];
-        team_sync(bid);
-    }
-    if (h) {
-#pragma unroll
-        for (int k2 = 1; k2 < 32; ++k2) a[k2] = cmul(a[k2], tw[k2 * 65 + 32]);
-    }
-#pragma unroll
-    for (int k2 = 0; k2 < 32; ++k2) col[h * 1056 + k2 * 33 + lane] = a[k2];
-    team_sync(bid);
-#pragma unroll
-    for (int k2 = 0; k2 < 32; ++k2) {
-        const float2 b = col[(1 - h) * 1056 + k2 * 33 + lane];
-        a[k2] = h ? csub(b, a[k2]) : cadd(a[k2], b);
-    }
-    team_sync(bid);
-}
-
 // Persistent column pass: one CTA per SM, NT teams of 64 threads, team q of
 // CTA b takes the kept columns i = b + gridDim.x (q + NT r).  The CTA keeps the
 // twiddle table W_2048^m and the kept ky values in shared memory (every
@@ -558,12 +501,6 @@ __device__ __forceinline__ void col_fwd2048_tm(float2 (&a)[32], float2* col, con
 // dynamic smem: TW [32][65] C | per team: X [XL] C (FFT exchange, then WS | ACC),
 // NS [Kyp] C (omega_hat at the step start, then the next stage's state) |
 // per team SHV [Kyp] T | KYS [Kyp] T   (Kyp = Ky rounded up to a multiple of 4)
-#ifndef NSG_CW_ROLL
-#define NSG_CW_ROLL 1   // FP32 column pass: RK algebra and field build eight modes at a time
-#endif
-#ifndef NSG_CW_TWTM
-#define NSG_CW_TWTM 0   // FP32 column pass: transform twiddles in tensor memory (columns 0-63; measured no faster)
-#endif
 #define NSG_CW_EX 2112
 #define NSG_CW_TW (32 * 65)
 __host__ __device__ constexpr int cw_kyp(int Ky) { return (Ky + 3) & ~3; }
@@ -589,24 +526,6 @@ __global__ void __launch_bounds__(64 * cw_teams<T>(), 1) k_col_w(Geo g, ColArgs<
     T* KYS = reinterpret_cast<T*>(TW + NSG_CW_TW + NT * (XL + Kyp)) + NT * Kyp;
     const int hv = a.sp.hv, sfd = a.sp.sfd;
     __shared__ double s_dt;
-    __shared__ unsigned s_tmem;
-    // FP32: the per-thread transform twiddles W_2048^{t k1} live in tensor
-    // memory (64 columns; the 32 lanes of quarter w mod 4 are threads
-    // t = 32 (w mod 2) + lane of every team, so one copy per quarter serves all)
-    // With ROLL the RK algebra and the field build run over eight modes at a
-    // time, through 64 more columns per warp (the kernel body shrinks by two
-    // 32-mode unrolled blocks).
-    constexpr bool ROLL = sizeof(T) == 4 && NSG_CW_ROLL;
-    constexpr bool TWT = sizeof(T) == 4 && NSG_CW_TWTM;
-    constexpr bool TM = ROLL || TWT;
-    constexpr unsigned TMC = ROLL ? 256u : 64u;
-    static_assert(!ROLL || 64 * (1 + (cw_teams<T>() * 2 + 3) / 4) <= 256, "tensor-memory columns");
-    const int warp = threadIdx.x >> 5;
-    if (TM && warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-            (unsigned)__cvta_generic_to_shared(&s_tmem)), "r"(TMC));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-    }
 
     // constant tables, and the first column's omega_hat / weights: these were
     // written before the previous kernel (the row pass, which waited for them)
@@ -645,28 +564,7 @@ __global__ void __launch_bounds__(64 * cw_teams<T>(), 1) k_col_w(Geo g, ColArgs<
         }
         s_dt = dt;
     }
-    if (TM) asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();  // tables, dt and the tensor-memory address
-    unsigned ttw = 0, tV = 0;
-    if (TM) {
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        ttw = s_tmem + ((unsigned)(32 * (warp & 3)) << 16);
-        tV = ttw + 64u * (unsigned)(1 + (warp >> 2));
-        if (TWT && warp < 4) {
-            float2 tt[32];
-#pragma unroll
-            for (int k1 = 0; k1 < 32; ++k1) {
-                const C w = TW[k1 * 65 + t];
-                tt[k1] = make_float2((float)w.x, (float)w.y);
-            }
-#pragma unroll
-            for (int c = 0; c < 4; ++c) tm_st16(ttw + 16u * c, tt, c);
-            tm_wait_st();
-        }
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    }
+    __syncthreads();  // tables and dt
 
     const double dt = s_dt;
     const T inv_re = (T)a.sp.inv_re;
@@ -701,7 +599,8 @@ __global__ void __launch_bounds__(64 * cw_teams<T>(), 1) k_col_w(Geo g, ColArgs<
             } else {
                 // thread t builds modes j = 64 n1 + t; Psi = -w/k^2 is formed once
                 // (written back to NS) and reused for Psi_y by the same thread
-                auto build = [&](int n1) -> C {
+#pragma unroll
+                for (int n1 = 0; n1 < 32; ++n1) {
                     const int j = 64 * n1 + t;
                     const int jj = kept_jj(g, j);
                     C x = zero;
@@ -719,38 +618,10 @@ __global__ void __launch_bounds__(64 * cw_teams<T>(), 1) k_col_w(Geo g, ColArgs<
                             x = w;
                         }
                     }
-                    return cconj(x);
-                };
-                if constexpr (ROLL) {
-                    // eight modes per pass through tensor memory: a compact loop body
-#pragma unroll 1
-                    for (int c = 0; c < 4; ++c) {
-                        float2 tb[32];
-#pragma unroll
-                        for (int m = 0; m < 8; ++m) tb[m] = build(8 * c + m);
-                        tm_st16(tV + 16u * c, tb, 0);
-                    }
-                    tm_wait_st();
-#pragma unroll
-                    for (int c = 0; c < 4; c += 2) {
-                        float r[16], s2[16];
-                        tm_ld16_issue(tV + 16u * c, r);
-                        tm_ld16_issue(tV + 16u * (c + 1), s2);
-                        tm_wait_ld2(r, s2);
-#pragma unroll
-                        for (int m = 0; m < 8; ++m) {
-                            v[8 * c + m] = cmake<C>(r[2 * m], r[2 * m + 1]);
-                            v[8 * c + 8 + m] = cmake<C>(s2[2 * m], s2[2 * m + 1]);
-                        }
-                    }
-                } else {
-#pragma unroll
-                    for (int n1 = 0; n1 < 32; ++n1) v[n1] = build(n1);
+                    v[n1] = cconj(x);
                 }
             }
-            // (ends with a team barrier: X is free)
-            if constexpr (TM) col_fwd2048_tm<TWT>(v, X, TW, ttw, t, lane, h, bid);
-            else col_fwd2048(v, X, TW, t, lane, h, bid);
+            col_fwd2048(v, X, TW, t, lane, h, bid);  // ends with a team barrier: X is free
             if (q >= 0) {
                 C* __restrict__ Fc = a.F[f] + (size_t)i * 2048;
 #pragma unroll
@@ -768,11 +639,13 @@ __global__ void __launch_bounds__(64 * cw_teams<T>(), 1) k_col_w(Geo g, ColArgs<
 
             // RK stage algebra (spectral_time_integration.c:50-100) on this
             // thread's forward outputs, modes j = lane + 32 k2 + 1024 h
-            auto rk = [&](int k2, C jh) {
+#pragma unroll
+            for (int k2 = 0; k2 < 32; ++k2) {
                 const int j = lane + 32 * k2 + 1024 * h;
                 const int jj = kept_jj(g, j);
-                if (jj < 0) return;
+                if (jj < 0) continue;
                 const size_t s = cbase + jj;
+                const C jh = v[k2];
                 const C w0 = NS[jj];
                 const C ws = (STAGE == 1) ? w0 : X[jj];
                 const C acc0 = (STAGE == 1) ? zero : X[Kyp + jj];
@@ -846,22 +719,6 @@ __global__ void __launch_bounds__(64 * cw_teams<T>(), 1) k_col_w(Geo g, ColArgs<
                     }
                 }
                 NS[jj] = wn;
-            };
-            if constexpr (ROLL) {
-#pragma unroll
-                for (int c = 0; c < 4; ++c) tm_st16(tV + 16u * c, v, c);
-                tm_wait_st();
-#pragma unroll 1
-                for (int c = 0; c < 4; ++c) {
-                    float r[16];
-                    tm_ld16_issue(tV + 16u * c, r);
-                    tm_wait_ld(r);
-#pragma unroll
-                    for (int m = 0; m < 8; ++m) rk(8 * c + m, cmake<C>(r[2 * m], r[2 * m + 1]));
-                }
-            } else {
-#pragma unroll
-                for (int k2 = 0; k2 < 32; ++k2) rk(k2, v[k2]);
             }
             if (STAGE == 4 && (a.sp.forcing || sfd)) {
                 // forcing increment (few low-|k| modes), then the SFD post-step, on omega_hat^{n+1}
@@ -907,14 +764,6 @@ __global__ void __launch_bounds__(64 * cw_teams<T>(), 1) k_col_w(Geo g, ColArgs<
         }
     }
     if (STAGE == 4 && blockIdx.x == 0 && threadIdx.x == 0) a.ds->t = a.ds->t + dt;
-    if (TM) {
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
-        if (warp == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(s_tmem), "r"(TMC));
-        }
-    }
 }
 
 // ============================================================ k_col_q
@@ -1279,38 +1128,33 @@ template <int NW, int NB> __host__ __device__ constexpr size_t rt_smem_bytes() {
     return (size_t)(32 * 33 + 1024 + NW * rt_wstride<NB>()) * sizeof(float2) + (size_t)NSG_RW_KXMAX * sizeof(float) + 16;
 }
 template <int NW> __host__ __device__ constexpr int rt_tmem_need() {
-    // 128 columns per warp (warps w and w + 4 share lanes), 128 twiddle columns,
-    // 64 staging columns per warp for the rolled pack
-    return 128 * ((NW + 3) / 4) + (NSG_RT_TWTM || NSG_RT_ROLL ? 128 : 0) + (NSG_RT_ROLL ? 64 * ((NW + 3) / 4) : 0);
+    // 128 columns per warp (warps w and w + 4 share lanes) + 128 twiddle columns
+    return 128 * ((NW + 3) / 4) + (NSG_RT_TWTM ? 128 : 0);
 }
 template <int NW> __host__ __device__ constexpr unsigned rt_tmem_cols() { return rt_tmem_need<NW>() <= 256 ? 256u : 512u; }
 
 // the 1024-point transform of warp_fft1024 with the per-lane twiddles
 // W_1024^{lane k1} (k1 < 32) read from tensor memory columns ttw .. ttw + 63
 __device__ __forceinline__ void warp_fft1024_tm(float2 (&a)[32], float2* S, unsigned ttw, int lane) {
-    // the two DFT32 passes share one body (NSG_FFT_ONEDFT): a smaller kernel
-#pragma unroll(kDftPassUnroll)
-    for (int pass = 0; pass < 2; ++pass) {
-        dft32<false>(a);
-        if (pass == 1) break;
+    dft32<false>(a);
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            float r[16];
-            tm_ld16_issue(ttw + 16u * c, r);
-            tm_wait_ld(r);
+    for (int c = 0; c < 4; ++c) {
+        float r[16];
+        tm_ld16_issue(ttw + 16u * c, r);
+        tm_wait_ld(r);
 #pragma unroll
-            for (int m = 0; m < 8; ++m) {
-                const int k1 = 8 * c + m;
-                if (k1 > 0) a[k1] = cmul(a[k1], make_float2(r[2 * m], r[2 * m + 1]));
-            }
+        for (int m = 0; m < 8; ++m) {
+            const int k1 = 8 * c + m;
+            if (k1 > 0) a[k1] = cmul(a[k1], make_float2(r[2 * m], r[2 * m + 1]));
         }
-#pragma unroll
-        for (int k1 = 0; k1 < 32; ++k1) S[k1 * 33 + lane] = a[k1];
-        __syncwarp();
-#pragma unroll
-        for (int n2 = 0; n2 < 32; ++n2) a[n2] = S[lane * 33 + n2];
-        __syncwarp();
     }
+#pragma unroll
+    for (int k1 = 0; k1 < 32; ++k1) S[k1 * 33 + lane] = a[k1];
+    __syncwarp();
+#pragma unroll
+    for (int n2 = 0; n2 < 32; ++n2) a[n2] = S[lane * 33 + n2];
+    __syncwarp();
+    dft32<false>(a);
 }
 
 // copy X_f[k] of row y, k = kb + 32 i < NSG_RW_KX, into the inbox IN (at sx(k)); always commits a group
@@ -1362,61 +1206,10 @@ __device__ __forceinline__ void rt_pack(float2 (&a)[32], const float2* IN, const
     }
 }
 
-// rt_pack (tensor-memory twiddles) as a loop over four chunks of eight
-// elements that passes each chunk through tensor memory columns tP + 16 c: the
-// same arithmetic with an eighth of the unrolled code
-template <bool DX>
-__device__ __forceinline__ void rt_pack_roll(float2 (&a)[32], const float2* IN, const float* kxs, unsigned ttwh, unsigned tP,
-                                             int lane) {
-    const int ob = lane ? 32 - lane : 33;
-    const float2 zero = make_float2(0.f, 0.f);
-#pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
-        float r[16];
-        tm_ld16_issue(ttwh + 16u * c, r);
-        tm_wait_ld(r);
-        float2 tb[32];
-#pragma unroll
-        for (int m = 0; m < 8; ++m) {
-            const int n1 = 8 * c + m;
-            const int k = lane + 32 * n1;
-            float2 xa = (k < NSG_RW_KX) ? IN[33 * n1 + lane] : zero;
-            float2 xb = (k > 0 && 1024 - k < NSG_RW_KX) ? IN[33 * (31 - n1) + ob] : zero;
-            if (DX) {
-                const float ka = (k < NSG_RW_KX) ? kxs[k] : 0.f;
-                const float kb = (k > 0 && 1024 - k < NSG_RW_KX) ? kxs[1024 - k] : 0.f;
-                xa = make_float2(-ka * xa.y, ka * xa.x);
-                xb = make_float2(-kb * xb.y, kb * xb.x);
-            }
-            const float2 e = make_float2(r[2 * m], r[2 * m + 1]);
-            const float2 A = cadd(xa, cconj(xb));
-            const float2 dd = csub(xa, cconj(xb));
-            const float Dx = dd.x * e.x + dd.y * e.y;
-            const float Dy = dd.y * e.x - dd.x * e.y;
-            tb[m] = (k == 0) ? make_float2(xa.x, -xa.x) : make_float2(A.x - Dy, -(A.y + Dx));
-        }
-        tm_st16(tP + 16u * c, tb, 0);
-    }
-    tm_wait_st();
-#pragma unroll
-    for (int c = 0; c < 4; c += 2) {
-        float r[16], s2[16];
-        tm_ld16_issue(tP + 16u * c, r);
-        tm_ld16_issue(tP + 16u * (c + 1), s2);
-        tm_wait_ld2(r, s2);
-#pragma unroll
-        for (int m = 0; m < 8; ++m) {
-            a[8 * c + m] = make_float2(r[2 * m], r[2 * m + 1]);
-            a[8 * c + 8 + m] = make_float2(s2[2 * m], s2[2 * m + 1]);
-        }
-    }
-}
-
 template <int NW, int GW, int NB>
 __global__ void __launch_bounds__(32 * NW, 1) k_row_t(Geo g, RowArgs<float> a) {
     static_assert(NW % GW == 0 && NB >= 1 && NB <= 2, "row tiling");
     static_assert(rt_tmem_need<NW>() <= 512, "tensor-memory columns");
-    static_assert(!NSG_RT_ROLL || NSG_RT_TWTM, "the rolled pack reads its twiddles from tensor memory");
     constexpr int WS = rt_wstride<NB>();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* tw = reinterpret_cast<float2*>(smem_raw);
@@ -1466,8 +1259,6 @@ __global__ void __launch_bounds__(32 * NW, 1) k_row_t(Geo g, RowArgs<float> a) {
     // tTW + 2 k1 (+1) = W_1024^{lane k1}, tTWH + 2 n1 (+1) = exp(-2 pi i (lane + 32 n1)/nx)
     const unsigned tTW = *tslot + ((unsigned)(32 * (warp & 3)) << 16) + 128u * (unsigned)((NW + 3) / 4);
     const unsigned tTWH = tTW + 64u;
-    // the rolled pack's staging: 64 columns per warp after the twiddles
-    const unsigned tP = tTW + 128u + 64u * (unsigned)(warp >> 2);
     if (NSG_RT_TWTM) {
         if (warp < 4) {
             float2 t[32];
@@ -1512,14 +1303,8 @@ __global__ void __launch_bounds__(32 * NW, 1) k_row_t(Geo g, RowArgs<float> a) {
                 if (NB == 2) rt_issue(INme + (buf ^ 1) * NSG_RT_IN, src, ny, yn, yn < yend, kb);
                 if (y < yend) {
                     const float2* IN = INw + buf * NSG_RT_IN;
-                    if (NSG_RT_ROLL) {
-                        if (q == 0 || q == 3) rt_pack_roll<true>(v, IN, kx_s, tTWH, tP, lane);
-                        else rt_pack_roll<false>(v, IN, kx_s, tTWH, tP, lane);
-                    } else if (q == 0 || q == 3) {
-                        rt_pack<true, NSG_RT_TWTM>(v, IN, kx_s, twh_s, tTWH, lane);
-                    } else {
-                        rt_pack<false, NSG_RT_TWTM>(v, IN, kx_s, twh_s, tTWH, lane);
-                    }
+                    if (q == 0 || q == 3) rt_pack<true, NSG_RT_TWTM>(v, IN, kx_s, twh_s, tTWH, lane);
+                    else rt_pack<false, NSG_RT_TWTM>(v, IN, kx_s, twh_s, tTWH, lane);
                 }
                 if (NB == 1) {
                     group_sync<GW, NW>(grp);  // every warp has packed field q
