@@ -1,24 +1,22 @@
-// Register-resident radix-32 stage kernels (the hot path at nx = 2048 / ny = 2048).
+// Register-resident stage kernels (the hot path at nx = 2048 / ny = 2048).
 //
-// Four-step FFT with 32 points per thread (N = N1 * N2, N1 = 32):
-//   forward   X[k1 + 32 k2] = sum_n2 W_N^{n2 k1} W_N2^{n2 k2} sum_n1 x[N2 n1 + n2] W_32^{n1 k1}
-//   pass A    thread n2 holds x[N2 n1 + n2] (n1 < 32), DFT32 over n1, times W_N^{n2 k1}
-//   exchange  shared-memory transpose (rows padded to 33 / 65 elements: conflict-free)
-//   pass B    DFT over n2 for each k1
-// The inverse runs the same steps in reverse order (decimation in frequency),
-// so it takes the forward's output layout and returns the forward's input
-// layout: no reordering pass exists anywhere.
+// Each RK stage is one row pass (x direction) and one column pass (y
+// direction).  Both keep each transform's points in registers and exchange
+// them through padded shared-memory buffers (conflict-free pitches).  Every
+// transform runs through one forward body: an inverse is conj(DFT(conj x)).
 //
-// k_row_w  (nx = 2048, H = 1024 = 32 x 32): one warp per row, persistent over
-//          rows.  All five transforms of a row stay inside one warp, so the only
-//          synchronisation is __syncwarp.  The inverse outputs land in exactly
-//          the layout the forward transform reads, so the Jacobian is formed in
-//          registers between them.
-// k_col_w  (ny = 2048 = 32 x 64): two warps per kept kx column (N2 = 64 is
-//          split into even/odd halves, one per warp, joined by one radix-2
-//          exchange), two columns per CTA.  The RK stage algebra runs on the
-//          forward's output registers and the four inverse transforms start
-//          from registers.
+//   k_row_t  FP32 row pass: one warp per row, 1024-point half-length transform
+//            as a 32 x 32 four-step FFT (32 points per thread).  Inboxes filled
+//            by cp.async; Jacobian operands and per-lane twiddles in tensor memory.
+//   k_row_w  FP64 row pass: the same transform with the Jacobian operands in
+//            shared memory and the next field staged in registers.
+//   k_col_q  FP32 column pass: four warps per kept kx column, 2048-point transform
+//            as 16 x 16 x 8 (16 points per thread), all columns in flight at once.
+//   k_col_w  FP64 column pass: two warps per column, 32 x 64 four-step FFT.
+// The forward's output layout equals its input layout for the 32 x 32 row
+// transform, so the row pass forms the Jacobian in registers between the
+// inverse and forward transforms; the column pass runs its RK stage algebra on
+// the forward's output and builds the inverse inputs per mode.
 #pragma once
 #include "ns_kernels.cuh"
 

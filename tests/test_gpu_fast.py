@@ -1,4 +1,4 @@
-"""The radix-32 stage kernels (k_row_w for nx = 2048, k_col_w for ny = 2048).
+"""The 2048-point stage kernels (row pass for nx = 2048, column pass for ny = 2048).
 
 FP64 runs of the benchmark physics (random-phase IC, hyperviscosity, Philox
 forcing, device CFL dt) against the oracle restatement at <= 1e-12 relative L2,
