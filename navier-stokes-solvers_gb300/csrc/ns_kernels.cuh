@@ -413,6 +413,136 @@ __device__ __forceinline__ C field_value(int f, C w, T kx, T ky) {
     return v;
 }
 
+// white-in-time forcing increment of one kept mode: amp times the mode's noise
+// (forcing_xi_sum) when kmin <= |k| <= kmax (FP64 shell test as the reference's k2)
+static __device__ __noinline__ double2 forcing_increment(const Geo& g, int i, int j, unsigned long long step, int M,
+                                                         unsigned long long seed, double kmin, double kmax, double amp) {
+    const double kxd = 2.0 * 3.141592653589793 * i / g.Lx;
+    const double kyd = (j <= g.ny / 2) ? 2.0 * 3.141592653589793 * j / g.Ly : 2.0 * 3.141592653589793 * (j - g.ny) / g.Ly;
+    const double k2d = kxd * kxd + kyd * kyd;
+    const double km = sqrt(k2d);
+    if (!(k2d > 1e-12 && km >= kmin && km <= kmax)) return make_double2(0.0, 0.0);
+    const double2 xi = forcing_xi_sum(i, j, g.ny, step, M, seed);
+    return make_double2(amp * xi.x, amp * xi.y);
+}
+
+// constants of one RK4 stage (spectral_time_integration.c:50-100)
+template <typename T> struct StageCoef {
+    T inv_re, sc, ch, cf, c6;  // 1/Re, N scale, dt/2, dt, dt/6
+    int hv, sfd;
+};
+template <typename T> __device__ __forceinline__ StageCoef<T> stage_coef(const StepParams& sp, double dt) {
+    StageCoef<T> q;
+    q.inv_re = (T)sp.inv_re;
+    q.sc = (T)sp.scale;
+    q.ch = (T)(0.5 * dt);
+    q.cf = (T)dt;
+    q.c6 = (T)(dt / 6.0);
+    q.hv = sp.hv;
+    q.sfd = sp.sfd;
+    return q;
+}
+
+// RK stage STAGE on one kept mode (spectral_time_integration.c:50-100 with
+// hyperviscosity.c:104-150): jh = r2c(J) of the mode (N = -sc jh), w0 = omega_hat
+// at the step start, ws = stage state, acc0 = accumulator (stages 2-4), hw the
+// hyperviscosity weight (0 when off), sw / fb the SFD ramp and filtered state
+// (read only when SFD is on), k2 = |k|^2.  Stores ACC and WS at s for stages 1-3
+// and returns the next stage state (stage 4: omega_hat^{n+1} before forcing).
+// IFRK: integrating-factor RK4, explicit part N - SFD relaxation, exact decay by
+// E1 = exp(-(k^2/Re + w) dt/2), E2 = E1^2.
+template <typename T, int STAGE, bool IFRK, typename C>
+__device__ __forceinline__ C rk_stage_mode(const StageCoef<T>& q, C jh, C w0, C ws, C acc0, T hw, T sw, C fb, T k2,
+                                           C* __restrict__ ACC, C* __restrict__ WS, size_t s) {
+    C wn;
+    if (IFRK) {
+        C k;
+        k.x = -(jh.x * q.sc);
+        k.y = -(jh.y * q.sc);
+        if (q.sfd && sw > (T)0) {
+            k.x -= sw * (ws.x - fb.x);
+            k.y -= sw * (ws.y - fb.y);
+        }
+        const T lam = k2 * q.inv_re + hw;
+        const T e1 = exp(-lam * q.ch), e2 = e1 * e1;
+        if (STAGE == 1) {
+            ACC[s] = cmake<C>(e2 * k.x, e2 * k.y);
+            wn.x = e1 * (w0.x + q.ch * k.x); wn.y = e1 * (w0.y + q.ch * k.y);
+            WS[s] = wn;
+        } else if (STAGE == 2 || STAGE == 3) {
+            C acc = acc0;
+            acc.x = acc.x + (T)2 * (e1 * k.x);
+            acc.y = acc.y + (T)2 * (e1 * k.y);
+            ACC[s] = acc;
+            if (STAGE == 2) { wn.x = e1 * w0.x + q.ch * k.x; wn.y = e1 * w0.y + q.ch * k.y; }
+            else { wn.x = e2 * w0.x + q.cf * (e1 * k.x); wn.y = e2 * w0.y + q.cf * (e1 * k.y); }
+            WS[s] = wn;
+        } else {
+            wn.x = e2 * w0.x + q.c6 * (acc0.x + k.x);
+            wn.y = e2 * w0.y + q.c6 * (acc0.y + k.y);
+        }
+    } else {
+        C k;  // k = N - k^2 omega / Re - damping (spectral_time_integration.c:50-54)
+        k.x = -(jh.x * q.sc) - k2 * ws.x * q.inv_re;
+        k.y = -(jh.y * q.sc) - k2 * ws.y * q.inv_re;
+        if (q.hv || q.sfd) {
+            C damp = cmake<C>(0.0, 0.0);
+            if (q.hv) { damp.x += hw * ws.x; damp.y += hw * ws.y; }
+            if (q.sfd && sw > (T)0) {
+                damp.x += sw * (ws.x - fb.x);
+                damp.y += sw * (ws.y - fb.y);
+            }
+            k.x -= damp.x;
+            k.y -= damp.y;
+        }
+        if (STAGE == 1) {
+            ACC[s] = k;
+            wn.x = w0.x + q.ch * k.x; wn.y = w0.y + q.ch * k.y;
+            WS[s] = wn;
+        } else if (STAGE == 2 || STAGE == 3) {
+            C acc = acc0;
+            acc.x = acc.x + (T)2 * k.x;
+            acc.y = acc.y + (T)2 * k.y;
+            ACC[s] = acc;
+            const T cc = (STAGE == 2) ? q.ch : q.cf;
+            wn.x = w0.x + cc * k.x; wn.y = w0.y + cc * k.y;
+            WS[s] = wn;
+        } else {
+            wn.x = w0.x + q.c6 * (acc0.x + k.x);
+            wn.y = w0.y + q.c6 * (acc0.y + k.y);
+        }
+    }
+    return wn;
+}
+
+// stage-4 forcing increment and SFD post-step (hyperviscosity.c:152-178) of kept
+// mode (i, j) at s: adds the forcing to wn when its |k| lies in the shell (an
+// FP32/FP64 |k|^2 screen, margin far beyond rounding, before the exact FP64
+// test), then relaxes the SFD filter toward it; sets forced when wn changed
+template <typename T, typename C>
+__device__ __forceinline__ C post_step_mode(const Geo& g, const ColArgs<T>& a, int i, int j, size_t s, C wn, T kx, T ky,
+                                            double f_amp, double sfd_a, bool& forced) {
+    forced = false;
+    const T k2f = kx * kx + ky * ky;
+    if (a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9 && k2f >= (T)(a.sp.f_kmin * a.sp.f_kmin * (1.0 - 1e-3)) &&
+        k2f <= (T)(a.sp.f_kmax * a.sp.f_kmax * (1.0 + 1e-3))) {
+        const double2 df = forcing_increment(g, i, j, a.ds->step_cur, a.sp.fsub, a.sp.f_seed, a.sp.f_kmin, a.sp.f_kmax, f_amp);
+        if (df.x != 0.0 || df.y != 0.0) {
+            wn.x = (T)((double)wn.x + df.x);
+            wn.y = (T)((double)wn.y + df.y);
+            forced = true;
+        }
+    }
+    if (a.sp.sfd) {
+        C fb = a.SFD[s];
+        const T al = (T)sfd_a, om = (T)(1.0 - sfd_a);
+        fb.x = om * fb.x + al * wn.x;
+        fb.y = om * fb.y + al * wn.y;
+        a.SFD[s] = fb;
+    }
+    return wn;
+}
+
 // grid = Kxp / CW, block = CW * (ny / E), dynamic smem = CW * spad_len(ny) * sizeof(C)
 // body of the column pass for column block bx (kept columns bx*CW .. bx*CW + CW - 1);
 // the block must have exactly CW * (ny / E) threads
@@ -475,9 +605,7 @@ __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, cons
             return;
         } else {
             const double dt = s_dt;
-            const T inv_re = (T)a.sp.inv_re;
-            const T sc = (T)a.sp.scale;
-            const T ch = (T)(0.5 * dt), cf = (T)dt, c6 = (T)(dt / 6.0);
+            const StageCoef<T> q = stage_coef<T>(a.sp, dt);
             double f_amp = 0.0;
             double sfd_a = 0.0;
             if (STAGE == 4) {
@@ -492,108 +620,24 @@ __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, cons
                 if (i >= Kx) continue;
                 const int j = kept_j(g, jj);
                 const C gh = sm[c * LP + spad(j)];
-                C nl;  // N = -(r2c(J) / (nx ny))
-                nl.x = -(gh.x * sc);
-                nl.y = -(gh.y * sc);
                 const size_t s = (size_t)i * Ky + jj;
                 const C w0 = a.W0[s];
                 const C ws = (STAGE == 1) ? w0 : a.WS[s];
+                const C acc0 = (STAGE == 1) ? cmake<C>(0.0, 0.0) : a.ACC[s];
                 const T kx = a.kxv[i], ky = a.kyv[jj];
-                const T k2 = k2sum(kx, ky);
-                C wn;
-                if (a.sp.ifrk) {
-                    // integrating-factor RK4: explicit part N - SFD relaxation, decay
-                    // lam = k^2/Re + w integrated by E1 = exp(-lam dt/2), E2 = E1^2
-                    C k = nl;
-                    if (a.sp.sfd) {
-                        const T sw = a.sfdw[s];
-                        if (sw > (T)0) {
-                            const C fb = a.SFD[s];
-                            k.x -= sw * (ws.x - fb.x);
-                            k.y -= sw * (ws.y - fb.y);
-                        }
-                    }
-                    const T lam = k2 * inv_re + (a.sp.hv ? a.hvw[s] : (T)0);
-                    const T e1 = exp(-lam * ch), e2 = e1 * e1;
-                    if (STAGE == 1) {
-                        a.ACC[s] = cmake<C>(e2 * k.x, e2 * k.y);
-                        wn.x = e1 * (w0.x + ch * k.x); wn.y = e1 * (w0.y + ch * k.y);
-                        a.WS[s] = wn;
-                    } else if (STAGE == 2 || STAGE == 3) {
-                        C acc = a.ACC[s];
-                        acc.x = acc.x + (T)2 * (e1 * k.x);
-                        acc.y = acc.y + (T)2 * (e1 * k.y);
-                        a.ACC[s] = acc;
-                        if (STAGE == 2) { wn.x = e1 * w0.x + ch * k.x; wn.y = e1 * w0.y + ch * k.y; }
-                        else { wn.x = e2 * w0.x + cf * (e1 * k.x); wn.y = e2 * w0.y + cf * (e1 * k.y); }
-                        a.WS[s] = wn;
-                    } else {
-                        const C acc = a.ACC[s];
-                        wn.x = e2 * w0.x + c6 * (acc.x + k.x);
-                        wn.y = e2 * w0.y + c6 * (acc.y + k.y);
-                    }
-                } else {
-                    C k;  // k = N - k^2 omega / Re - damping (spectral_time_integration.c:50-54)
-                    k.x = nl.x - k2 * ws.x * inv_re;
-                    k.y = nl.y - k2 * ws.y * inv_re;
-                    if (a.sp.hv || a.sp.sfd) {
-                        C damp = cmake<C>(0.0, 0.0);
-                        if (a.sp.hv) { const T w = a.hvw[s]; damp.x += w * ws.x; damp.y += w * ws.y; }
-                        if (a.sp.sfd) {
-                            const T sw = a.sfdw[s];
-                            if (sw > (T)0) {
-                                const C fb = a.SFD[s];
-                                damp.x += sw * (ws.x - fb.x);
-                                damp.y += sw * (ws.y - fb.y);
-                            }
-                        }
-                        k.x -= damp.x;
-                        k.y -= damp.y;
-                    }
-                    if (STAGE == 1) {
-                        a.ACC[s] = k;
-                        wn.x = w0.x + ch * k.x; wn.y = w0.y + ch * k.y;
-                        a.WS[s] = wn;
-                    } else if (STAGE == 2 || STAGE == 3) {
-                        C acc = a.ACC[s];
-                        acc.x = acc.x + (T)2 * k.x;
-                        acc.y = acc.y + (T)2 * k.y;
-                        a.ACC[s] = acc;
-                        const T cc = (STAGE == 2) ? ch : cf;
-                        wn.x = w0.x + cc * k.x; wn.y = w0.y + cc * k.y;
-                        a.WS[s] = wn;
-                    } else {
-                        const C acc = a.ACC[s];
-                        wn.x = w0.x + c6 * (acc.x + k.x);
-                        wn.y = w0.y + c6 * (acc.y + k.y);
-                    }
+                const T hw = a.sp.hv ? a.hvw[s] : (T)0;
+                T sw = (T)0;
+                C fb = cmake<C>(0.0, 0.0);
+                if (a.sp.sfd) {
+                    sw = a.sfdw[s];
+                    fb = a.SFD[s];
                 }
+                const T k2 = k2sum(kx, ky);
+                C wn = a.sp.ifrk ? rk_stage_mode<T, STAGE, true>(q, gh, w0, ws, acc0, hw, sw, fb, k2, a.ACC, a.WS, s)
+                                 : rk_stage_mode<T, STAGE, false>(q, gh, w0, ws, acc0, hw, sw, fb, k2, a.ACC, a.WS, s);
                 if (STAGE == 4) {
-                    // FP32/FP64 |k|^2 screen (margin far beyond rounding) before the exact FP64 shell test
-                    const T k2s = kx * kx + ky * ky;
-                    if (a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9 &&
-                        k2s >= (T)(a.sp.f_kmin * a.sp.f_kmin * (1.0 - 1e-3)) &&
-                        k2s <= (T)(a.sp.f_kmax * a.sp.f_kmax * (1.0 + 1e-3))) {
-                        // white-in-time forcing increment sigma sqrt(dt) xi (Euler-Maruyama)
-                        const double kxd = 2.0 * 3.141592653589793 * i / g.Lx;
-                        const double kyd = (j <= g.ny / 2) ? 2.0 * 3.141592653589793 * j / g.Ly
-                                                           : 2.0 * 3.141592653589793 * (j - g.ny) / g.Ly;
-                        const double k2d = kxd * kxd + kyd * kyd;
-                        const double km = sqrt(k2d);
-                        if (k2d > 1e-12 && km >= a.sp.f_kmin && km <= a.sp.f_kmax) {
-                            const double2 xi = forcing_xi_sum(i, j, g.ny, a.ds->step_cur, a.sp.fsub, a.sp.f_seed);
-                            const double xr = xi.x, xi_im = xi.y;
-                            wn.x = (T)((double)wn.x + f_amp * xr);
-                            wn.y = (T)((double)wn.y + f_amp * xi_im);
-                        }
-                    }
-                    if (a.sp.sfd) {
-                        C fb = a.SFD[s];
-                        const T al = (T)sfd_a, om = (T)(1.0 - sfd_a);
-                        fb.x = om * fb.x + al * wn.x;
-                        fb.y = om * fb.y + al * wn.y;
-                        a.SFD[s] = fb;
-                    }
+                    bool forced;
+                    wn = post_step_mode(g, a, i, j, s, wn, kx, ky, f_amp, sfd_a, forced);
                     a.W0[s] = wn;
                 }
             }

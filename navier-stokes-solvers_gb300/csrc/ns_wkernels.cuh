@@ -409,19 +409,6 @@ __device__ __forceinline__ void col_fwd2048(C (&a)[32], C* col, const C* tw, int
     team_sync(bid);
 }
 
-// white-in-time forcing increment of one kept mode: amp times the mode's noise
-// (forcing_xi_sum) when kmin <= |k| <= kmax (FP64 shell test as the reference's k2)
-__device__ __noinline__ double2 forcing_increment(const Geo& g, int i, int j, unsigned long long step, int M,
-                                                  unsigned long long seed, double kmin, double kmax, double amp) {
-    const double kxd = 2.0 * 3.141592653589793 * i / g.Lx;
-    const double kyd = (j <= g.ny / 2) ? 2.0 * 3.141592653589793 * j / g.Ly : 2.0 * 3.141592653589793 * (j - g.ny) / g.Ly;
-    const double k2d = kxd * kxd + kyd * kyd;
-    const double km = sqrt(k2d);
-    if (!(k2d > 1e-12 && km >= kmin && km <= kmax)) return make_double2(0.0, 0.0);
-    const double2 xi = forcing_xi_sum(i, j, g.ny, step, M, seed);
-    return make_double2(amp * xi.x, amp * xi.y);
-}
-
 // ------------------------------------------------------------ cp.async staging
 // Asynchronous global -> shared copies (no register staging); each thread
 // waits for its own copies with cp_async_wait_all, a barrier publishes them.
@@ -565,10 +552,7 @@ __global__ void __launch_bounds__(64 * cw_teams<T>(), 1) k_col_w(Geo g, ColArgs<
     __syncthreads();  // tables and dt
 
     const double dt = s_dt;
-    const T inv_re = (T)a.sp.inv_re;
-    const T sc = (T)a.sp.scale;
-    const T cst = (STAGE == 1 || STAGE == 2) ? (T)(0.5 * dt) : (STAGE == 3 ? (T)dt : (T)(dt / 6.0));
-    const T ch = (T)(0.5 * dt), cf = (T)dt, c6 = (T)(dt / 6.0);
+    const StageCoef<T> sq = stage_coef<T>(a.sp, dt);
     C* __restrict__ W0 = a.W0;
     C* __restrict__ WS = a.WS;
     C* __restrict__ ACC = a.ACC;
@@ -654,68 +638,8 @@ __global__ void __launch_bounds__(64 * cw_teams<T>(), 1) k_col_w(Geo g, ColArgs<
                     sw = a.sfdw[s];
                     fb = a.SFD[s];
                 }
-                const T k2v = k2sum(kx, KYS[jj]);
-                C wn;
-                if (IFRK) {
-                    // integrating-factor RK4: explicit part N - SFD relaxation, exact
-                    // decay by E1 = exp(-(k^2/Re + w) dt/2), E2 = E1^2
-                    C k;
-                    k.x = -(jh.x * sc);
-                    k.y = -(jh.y * sc);
-                    if (sfd && sw > (T)0) {
-                        k.x -= sw * (ws.x - fb.x);
-                        k.y -= sw * (ws.y - fb.y);
-                    }
-                    const T lam = k2v * inv_re + hw;
-                    const T e1 = exp(-lam * ch), e2 = e1 * e1;
-                    if (STAGE == 1) {
-                        ACC[s] = cmake<C>(e2 * k.x, e2 * k.y);
-                        wn.x = e1 * (w0.x + ch * k.x); wn.y = e1 * (w0.y + ch * k.y);
-                        WS[s] = wn;
-                    } else if (STAGE == 2 || STAGE == 3) {
-                        C acc = acc0;
-                        acc.x = acc.x + (T)2 * (e1 * k.x);
-                        acc.y = acc.y + (T)2 * (e1 * k.y);
-                        ACC[s] = acc;
-                        if (STAGE == 2) { wn.x = e1 * w0.x + ch * k.x; wn.y = e1 * w0.y + ch * k.y; }
-                        else { wn.x = e2 * w0.x + cf * (e1 * k.x); wn.y = e2 * w0.y + cf * (e1 * k.y); }
-                        WS[s] = wn;
-                    } else {
-                        wn.x = e2 * w0.x + c6 * (acc0.x + k.x);
-                        wn.y = e2 * w0.y + c6 * (acc0.y + k.y);
-                        W0[s] = wn;
-                    }
-                } else {
-                    C k;
-                    k.x = -(jh.x * sc) - k2v * ws.x * inv_re;
-                    k.y = -(jh.y * sc) - k2v * ws.y * inv_re;
-                    if (hv || sfd) {
-                        C damp = zero;
-                        if (hv) { damp.x += hw * ws.x; damp.y += hw * ws.y; }
-                        if (sfd && sw > (T)0) {
-                            damp.x += sw * (ws.x - fb.x);
-                            damp.y += sw * (ws.y - fb.y);
-                        }
-                        k.x -= damp.x;
-                        k.y -= damp.y;
-                    }
-                    if (STAGE == 1) {
-                        ACC[s] = k;
-                        wn.x = w0.x + cst * k.x; wn.y = w0.y + cst * k.y;
-                        WS[s] = wn;
-                    } else if (STAGE == 2 || STAGE == 3) {
-                        C acc = acc0;
-                        acc.x = acc.x + (T)2 * k.x;
-                        acc.y = acc.y + (T)2 * k.y;
-                        ACC[s] = acc;
-                        wn.x = w0.x + cst * k.x; wn.y = w0.y + cst * k.y;
-                        WS[s] = wn;
-                    } else {
-                        wn.x = w0.x + cst * (acc0.x + k.x);
-                        wn.y = w0.y + cst * (acc0.y + k.y);
-                        W0[s] = wn;
-                    }
-                }
+                const C wn = rk_stage_mode<T, STAGE, IFRK>(sq, jh, w0, ws, acc0, hw, sw, fb, k2sum(kx, KYS[jj]), ACC, WS, s);
+                if (STAGE == 4) W0[s] = wn;
                 NS[jj] = wn;
             }
             if (STAGE == 4 && (a.sp.forcing || sfd)) {
@@ -726,35 +650,19 @@ __global__ void __launch_bounds__(64 * cw_teams<T>(), 1) k_col_w(Geo g, ColArgs<
                     sa = dt / a.sp.sfd_tau;
                     sa = sa > 1.0 ? 1.0 : (sa < 0.0 ? 0.0 : sa);
                 }
+                // columns beyond the shell only relax the SFD filter
                 const bool force_col = a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9;
-                // |k|^2 window, widened far beyond FP32 rounding, that screens modes before the exact FP64 shell test
-                const T k2lo = (T)(a.sp.f_kmin * a.sp.f_kmin * (1.0 - 1e-3));
-                const T k2hi = (T)(a.sp.f_kmax * a.sp.f_kmax * (1.0 + 1e-3));
 #pragma unroll 1
                 for (int k2 = 0; k2 < 32 && (force_col || sfd); ++k2) {
                     const int j = lane + 32 * k2 + 1024 * h;
                     const int jj = kept_jj(g, j);
                     if (jj < 0) continue;
                     const size_t s = cbase + jj;
-                    C wn = NS[jj];
-                    const T ky = KYS[jj];
-                    const T k2f = kx * kx + ky * ky;
-                    if (force_col && k2f >= k2lo && k2f <= k2hi) {
-                        const double2 df =
-                            forcing_increment(g, i, j, a.ds->step_cur, a.sp.fsub, a.sp.f_seed, a.sp.f_kmin, a.sp.f_kmax, f_amp);
-                        if (df.x != 0.0 || df.y != 0.0) {
-                            wn.x = (T)((double)wn.x + df.x);
-                            wn.y = (T)((double)wn.y + df.y);
-                            W0[s] = wn;
-                            NS[jj] = wn;
-                        }
-                    }
-                    if (sfd) {
-                        C fb = a.SFD[s];
-                        const T al = (T)sa, om = (T)(1.0 - sa);
-                        fb.x = om * fb.x + al * wn.x;
-                        fb.y = om * fb.y + al * wn.y;
-                        a.SFD[s] = fb;
+                    bool forced;
+                    const C wn = post_step_mode(g, a, i, j, s, NS[jj], kx, KYS[jj], f_amp, sa, forced);
+                    if (forced) {
+                        W0[s] = wn;
+                        NS[jj] = wn;
                     }
                 }
             }
@@ -885,10 +793,7 @@ __global__ void __launch_bounds__(128 * NSG_CQ_TEAMS, 1) k_col_q(Geo g, ColArgs<
     __syncthreads();  // tables and dt
 
     const double dt = s_dt;
-    const T inv_re = (T)a.sp.inv_re;
-    const T sc = (T)a.sp.scale;
-    const T cst = (STAGE == 1 || STAGE == 2) ? (T)(0.5 * dt) : (STAGE == 3 ? (T)dt : (T)(dt / 6.0));
-    const T ch = (T)(0.5 * dt), cf = (T)dt, c6 = (T)(dt / 6.0);
+    const StageCoef<T> sq = stage_coef<T>(a.sp, dt);
     C* __restrict__ W0 = a.W0;
     C* __restrict__ WS = a.WS;
     C* __restrict__ ACC = a.ACC;
@@ -974,68 +879,8 @@ __global__ void __launch_bounds__(128 * NSG_CQ_TEAMS, 1) k_col_q(Geo g, ColArgs<
                     sw = a.sfdw[s];
                     fb = a.SFD[s];
                 }
-                const T k2v = k2sum(kx, KYS[jj]);
-                C wn;
-                if (IFRK) {
-                    // integrating-factor RK4: explicit part N - SFD relaxation, exact
-                    // decay by E1 = exp(-(k^2/Re + w) dt/2), E2 = E1^2
-                    C k;
-                    k.x = -(jh.x * sc);
-                    k.y = -(jh.y * sc);
-                    if (sfd && sw > (T)0) {
-                        k.x -= sw * (ws.x - fb.x);
-                        k.y -= sw * (ws.y - fb.y);
-                    }
-                    const T lam = k2v * inv_re + hw;
-                    const T e1 = exp(-lam * ch), e2 = e1 * e1;
-                    if (STAGE == 1) {
-                        ACC[s] = make_float2(e2 * k.x, e2 * k.y);
-                        wn.x = e1 * (w0.x + ch * k.x); wn.y = e1 * (w0.y + ch * k.y);
-                        WS[s] = wn;
-                    } else if (STAGE == 2 || STAGE == 3) {
-                        C acc = acc0;
-                        acc.x = acc.x + (T)2 * (e1 * k.x);
-                        acc.y = acc.y + (T)2 * (e1 * k.y);
-                        ACC[s] = acc;
-                        if (STAGE == 2) { wn.x = e1 * w0.x + ch * k.x; wn.y = e1 * w0.y + ch * k.y; }
-                        else { wn.x = e2 * w0.x + cf * (e1 * k.x); wn.y = e2 * w0.y + cf * (e1 * k.y); }
-                        WS[s] = wn;
-                    } else {
-                        wn.x = e2 * w0.x + c6 * (acc0.x + k.x);
-                        wn.y = e2 * w0.y + c6 * (acc0.y + k.y);
-                        W0[s] = wn;
-                    }
-                } else {
-                    C k;
-                    k.x = -(jh.x * sc) - k2v * ws.x * inv_re;
-                    k.y = -(jh.y * sc) - k2v * ws.y * inv_re;
-                    if (hv || sfd) {
-                        C damp = zero;
-                        if (hv) { damp.x += hw * ws.x; damp.y += hw * ws.y; }
-                        if (sfd && sw > (T)0) {
-                            damp.x += sw * (ws.x - fb.x);
-                            damp.y += sw * (ws.y - fb.y);
-                        }
-                        k.x -= damp.x;
-                        k.y -= damp.y;
-                    }
-                    if (STAGE == 1) {
-                        ACC[s] = k;
-                        wn.x = w0.x + cst * k.x; wn.y = w0.y + cst * k.y;
-                        WS[s] = wn;
-                    } else if (STAGE == 2 || STAGE == 3) {
-                        C acc = acc0;
-                        acc.x = acc.x + (T)2 * k.x;
-                        acc.y = acc.y + (T)2 * k.y;
-                        ACC[s] = acc;
-                        wn.x = w0.x + cst * k.x; wn.y = w0.y + cst * k.y;
-                        WS[s] = wn;
-                    } else {
-                        wn.x = w0.x + cst * (acc0.x + k.x);
-                        wn.y = w0.y + cst * (acc0.y + k.y);
-                        W0[s] = wn;
-                    }
-                }
+                const C wn = rk_stage_mode<T, STAGE, IFRK>(sq, jh, w0, ws, acc0, hw, sw, fb, k2sum(kx, KYS[jj]), ACC, WS, s);
+                if (STAGE == 4) W0[s] = wn;
                 NS[jj] = wn;
             }
             if (STAGE == 4 && (a.sp.forcing || sfd)) {
@@ -1046,35 +891,19 @@ __global__ void __launch_bounds__(128 * NSG_CQ_TEAMS, 1) k_col_q(Geo g, ColArgs<
                     sa = dt / a.sp.sfd_tau;
                     sa = sa > 1.0 ? 1.0 : (sa < 0.0 ? 0.0 : sa);
                 }
+                // columns beyond the shell only relax the SFD filter
                 const bool force_col = a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9;
-                // |k|^2 window, widened far beyond FP32 rounding, that screens modes before the exact FP64 shell test
-                const T k2lo = (T)(a.sp.f_kmin * a.sp.f_kmin * (1.0 - 1e-3));
-                const T k2hi = (T)(a.sp.f_kmax * a.sp.f_kmax * (1.0 + 1e-3));
 #pragma unroll 1
                 for (int e = 0; e < 16 && (force_col || sfd); ++e) {
                     const int j = cq_mode(t, e);
                     const int jj = kept_jj(g, j);
                     if (jj < 0) continue;
                     const size_t s = cbase + jj;
-                    C wn = NS[jj];
-                    const T ky = KYS[jj];
-                    const T k2f = kx * kx + ky * ky;
-                    if (force_col && k2f >= k2lo && k2f <= k2hi) {
-                        const double2 df =
-                            forcing_increment(g, i, j, a.ds->step_cur, a.sp.fsub, a.sp.f_seed, a.sp.f_kmin, a.sp.f_kmax, f_amp);
-                        if (df.x != 0.0 || df.y != 0.0) {
-                            wn.x = (T)((double)wn.x + df.x);
-                            wn.y = (T)((double)wn.y + df.y);
-                            W0[s] = wn;
-                            NS[jj] = wn;
-                        }
-                    }
-                    if (sfd) {
-                        C fb = a.SFD[s];
-                        const T al = (T)sa, om = (T)(1.0 - sa);
-                        fb.x = om * fb.x + al * wn.x;
-                        fb.y = om * fb.y + al * wn.y;
-                        a.SFD[s] = fb;
+                    bool forced;
+                    const C wn = post_step_mode(g, a, i, j, s, NS[jj], kx, KYS[jj], f_amp, sa, forced);
+                    if (forced) {
+                        W0[s] = wn;
+                        NS[jj] = wn;
                     }
                 }
             }
