@@ -193,21 +193,24 @@ template <typename T> static int stage_row(ns_gpu* g, int stage) {
     return row_launch<T, ROW_STAGE>(g, a);
 }
 
+// FP32 column pass k_col_q for ny = 2^NL (NL = 11, 12)
+template <int NL, int STAGE> static int launch_col_q(ns_gpu* g, const ColArgs<float>& a) {
+    const size_t smem = cq_smem_bytes<NL>(g->g.Ky);
+    auto kern = a.sp.ifrk ? k_col_q<NL, STAGE, true> : k_col_q<NL, STAGE, false>;
+    NSG_TRY(set_smem(g, kern, smem));
+    int grid = g->num_sms;
+    if (grid > g->g.Kx) grid = g->g.Kx;
+    const cudaError_t e = launch_stage(kern, grid, CQ<NL>::TT * CQ<NL>::NT, smem, g->st, g->g, a);
+    if (e != cudaSuccess) NSG_FAIL(g, NS_GPU_ERR_CUDA, "k_col_q launch: %s", cudaGetErrorString(e));
+    NSG_LAUNCHED(g);
+    return NS_GPU_OK;
+}
+
 template <typename T, int STAGE> static int stage_col(ns_gpu* g, const ColArgs<T>& a) {
     ProfScope ps(g, 1);
     if constexpr (sizeof(T) == 4 && NSG_COL_Q) {
-        if (g->fast_col) {
-            // FP32: four warps per column (k_col_q)
-            const size_t smem = cq_smem_bytes(g->g.Ky);
-            auto kern = a.sp.ifrk ? k_col_q<STAGE, true> : k_col_q<STAGE, false>;
-            NSG_TRY(set_smem(g, kern, smem));
-            int grid = g->num_sms;
-            if (grid > g->g.Kx) grid = g->g.Kx;
-            const cudaError_t e = launch_stage(kern, grid, 128 * NSG_CQ_TEAMS, smem, g->st, g->g, a);
-            if (e != cudaSuccess) NSG_FAIL(g, NS_GPU_ERR_CUDA, "k_col_q launch: %s", cudaGetErrorString(e));
-            NSG_LAUNCHED(g);
-            return NS_GPU_OK;
-        }
+        // FP32: N/128 warps per column (k_col_q)
+        if (g->fast_col) return g->g.ny == 4096 ? launch_col_q<12, STAGE>(g, a) : launch_col_q<11, STAGE>(g, a);
     }
     if (g->fast_col) {
         const size_t smem = cw_smem_bytes<T>(g->g.Ky);
@@ -469,7 +472,8 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
         const char* gen = getenv("NS_GB300_GENERIC_KERNELS");
         const int generic = (gen && gen[0] == '1') || (kc && (kc->er || kc->ec));
         g->fast_row = (!generic && nx == 2048) ? 1 : 0;
-        g->fast_col = (!generic && ny == 2048) ? 1 : 0;
+        // the column pass also has an FP32 kernel for ny = 4096
+        g->fast_col = (!generic && (ny == 2048 || (ny == 4096 && precision == NS_GPU_FP32 && NSG_COL_Q))) ? 1 : 0;
     }
     if (cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking) != cudaSuccess) {
         delete g;

@@ -673,98 +673,115 @@ __global__ void __launch_bounds__(64 * cw_teams<T>(), 1) k_col_w(Geo g, ColArgs<
 }
 
 // ============================================================ k_col_q
-// FP32 column pass at ny = 2048 with four warps per kept kx column.  Every SM
-// holds all of its columns at once (684 columns, 5 per SM), so the pass takes
-// as long as one column's chain of five transforms and the RK algebra; 128
-// threads with 16 points each run that chain with half the serial work per
-// thread of the two-warp teams (k_col_w), in the same shared memory per column.
+// FP32 column pass at ny = 2048 or 4096 with N/128 warps (N/16 threads, 16
+// points each) per kept kx column.  At 2048 every SM holds all of its columns at
+// once (684 columns, 5 per SM), so the pass takes as long as one column's chain
+// of five transforms and the RK algebra; four warps per column run that chain
+// with half the serial work per thread of the two-warp teams (k_col_w), in the
+// same shared memory per column.  At 4096 two columns of eight warps share an SM.
 //
-// 2048-point transform, 2048 = 16 x 16 x 8 (thread t < 128, k1 = t & 15):
-//   pass A   t holds x[128 n1 + t] (n1 < 16): DFT16 over n1, times W_2048^{t k1}
-//   pass B1  thread (k1, m2 = t >> 4) takes z[8 m1 + m2] of column k1 (m1 < 16):
-//            DFT16 over m1, times W_128^{m2 q1}
-//   pass B2  thread (k1, qp = t >> 4) takes the eight m2 values of q1 = 2 qp + r
-//            (r < 2): DFT8 -> X[k1 + 16 q1 + 256 q2] in a[8 r + q2]
-// The exchange buffer holds [16][129] values; a pitch of 129 makes every
-// exchange store and load conflict-free (16 banks pairs, two wavefronts).
+// N-point transform, N = 16 x 16 x M2 with TT = N/16 threads, M2 = TT/16
+// (2048: 16 x 16 x 8; 4096: 16 x 16 x 16), thread t < TT, k1 = t & 15, hi = t >> 4:
+//   pass A   t holds x[TT n1 + t] (n1 < 16): DFT16 over n1, times W_N^{t k1}
+//   pass B1  thread (k1, m2 = hi) takes z[M2 m1 + m2] of column k1 (m1 < 16):
+//            DFT16 over m1, times W_TT^{m2 q1}
+//   pass B2  thread (k1, hi) takes the M2 values m2 of q1 = R hi + r (r < R = 16/M2):
+//            DFT_M2 -> X[k1 + 16 q1 + 256 q2] in a[M2 r + q2]
+// The exchange buffer holds [16][TT + 1] values; a pitch of TT + 1 makes every
+// exchange store and load conflict-free (16 bank pairs, two wavefronts).
 #ifndef NSG_COL_Q
-#define NSG_COL_Q 1   // 0: the FP32 column pass runs k_col_w
+#define NSG_COL_Q 1   // 0: the FP32 column pass at 2048 runs k_col_w
 #endif
-#ifndef NSG_CQ_TEAMS
-#define NSG_CQ_TEAMS 5
-#endif
-#define NSG_CQ_EX 2064
-__host__ __device__ constexpr int cq_xl(int Ky) { return 2 * cw_kyp(Ky) > NSG_CQ_EX ? 2 * cw_kyp(Ky) : NSG_CQ_EX; }
-__host__ __device__ constexpr size_t cq_smem_bytes(int Ky) {
-    return (size_t)(2048 + NSG_CQ_TEAMS * (cq_xl(Ky) + cw_kyp(Ky))) * sizeof(float2) +
-           (size_t)(NSG_CQ_TEAMS + 1) * cw_kyp(Ky) * sizeof(float);
+template <int NL> struct CQ {
+    static constexpr int N = 1 << NL, TT = N / 16, M2 = TT / 16, R = 16 / M2, P = TT + 1;
+    static constexpr int NT = NL == 11 ? 5 : 2;  // teams per CTA (shared memory: ~38 / 77 KB per column)
+    static constexpr int EX = 16 * P;            // exchange buffer extent
+};
+template <int NL> __host__ __device__ constexpr int cq_xl(int Ky) {
+    return 2 * cw_kyp(Ky) > CQ<NL>::EX ? 2 * cw_kyp(Ky) : CQ<NL>::EX;
 }
-// barrier over one 128-thread team (named barrier bid, 1 <= bid <= 15)
-__device__ __forceinline__ void quad_sync(int bid) { asm volatile("bar.sync %0, 128;" ::"r"(bid) : "memory"); }
+template <int NL> __host__ __device__ constexpr size_t cq_smem_bytes(int Ky) {
+    return (size_t)(CQ<NL>::N + CQ<NL>::NT * (cq_xl<NL>(Ky) + cw_kyp(Ky))) * sizeof(float2) +
+           (size_t)(CQ<NL>::NT + 1) * cw_kyp(Ky) * sizeof(float);
+}
+// barrier over one team of TT threads (named barrier bid, 1 <= bid <= 15)
+template <int TT> __device__ __forceinline__ void team_bar(int bid) {
+    asm volatile("bar.sync %0, %1;" ::"r"(bid), "n"(TT) : "memory");
+}
 
-// forward 2048-point transform of a team: a[n1] = x[128 n1 + t] on entry,
-// a[8 r + q2] = X[k1 + 16 (2 qp + r) + 256 q2] on exit; E is the team's exchange
-// buffer (free again on return), TW1[k1 * 128 + t] = W_2048^{t k1}
-__device__ __forceinline__ void col_fwd2048_q(float2 (&a)[16], float2* E, const float2* TW1, int t, int bid) {
+// forward N-point transform of a team: a[n1] = x[TT n1 + t] on entry,
+// a[M2 r + q2] = X[k1 + 16 (R hi + r) + 256 q2] on exit; E is the team's exchange
+// buffer (free again on return), TW1[k1 * TT + t] = W_N^{t k1}
+template <int NL>
+__device__ __forceinline__ void col_fwd_q(float2 (&a)[16], float2* E, const float2* TW1, int t, int bid) {
+    typedef CQ<NL> Q;
     const int k1 = t & 15, hi = t >> 4;
     dft16<false>(a);
 #pragma unroll
-    for (int c = 1; c < 16; ++c) a[c] = cmul(a[c], TW1[c * 128 + t]);
+    for (int c = 1; c < 16; ++c) a[c] = cmul(a[c], TW1[c * Q::TT + t]);
 #pragma unroll
-    for (int c = 0; c < 16; ++c) E[c * 129 + t] = a[c];
-    quad_sync(bid);
+    for (int c = 0; c < 16; ++c) E[c * Q::P + t] = a[c];
+    team_bar<Q::TT>(bid);
 #pragma unroll
-    for (int m1 = 0; m1 < 16; ++m1) a[m1] = E[k1 * 129 + 8 * m1 + hi];
-    quad_sync(bid);
+    for (int m1 = 0; m1 < 16; ++m1) a[m1] = E[k1 * Q::P + Q::M2 * m1 + hi];
+    team_bar<Q::TT>(bid);
     dft16<false>(a);
 #pragma unroll
-    for (int q1 = 1; q1 < 16; ++q1) a[q1] = cmul(a[q1], TW1[q1 * 128 + 16 * hi]);  // W_128^{m2 q1}
+    for (int q1 = 1; q1 < 16; ++q1) a[q1] = cmul(a[q1], TW1[q1 * Q::TT + 16 * hi]);  // W_TT^{m2 q1}
 #pragma unroll
-    for (int q1 = 0; q1 < 16; ++q1) E[k1 * 129 + q1 * 8 + hi] = a[q1];
-    quad_sync(bid);
+    for (int q1 = 0; q1 < 16; ++q1) E[k1 * Q::P + q1 * Q::M2 + hi] = a[q1];
+    team_bar<Q::TT>(bid);
 #pragma unroll
-    for (int r = 0; r < 2; ++r) {
+    for (int r = 0; r < Q::R; ++r) {
 #pragma unroll
-        for (int m2 = 0; m2 < 8; ++m2) a[8 * r + m2] = E[k1 * 129 + (2 * hi + r) * 8 + m2];
+        for (int m2 = 0; m2 < Q::M2; ++m2) a[Q::M2 * r + m2] = E[k1 * Q::P + (Q::R * hi + r) * Q::M2 + m2];
     }
-    quad_sync(bid);
-    dft8<false>(a);
-    dft8<false>(a + 8);
+    team_bar<Q::TT>(bid);
+    if constexpr (Q::M2 == 8) {
+        dft8<false>(a);
+        dft8<false>(a + 8);
+    } else {
+        dft16<false>(a);
+    }
 }
 
-// output mode of a[e] (e = 8 r + q2) in thread t
-__device__ __forceinline__ int cq_mode(int t, int e) { return (t & 15) + 16 * (2 * (t >> 4) + (e >> 3)) + 256 * (e & 7); }
+// output mode of a[e] (e = M2 r + q2) in thread t
+template <int NL> __device__ __forceinline__ int cq_mode(int t, int e) {
+    typedef CQ<NL> Q;
+    return (t & 15) + 16 * (Q::R * (t >> 4) + e / Q::M2) + 256 * (e % Q::M2);
+}
 
-// Persistent column pass (FP32): one CTA per SM, NSG_CQ_TEAMS teams of 128
-// threads, team q of CTA b takes the kept columns b + gridDim.x (q + NT r).
-// Staging, tables and stage algebra follow k_col_w; only the thread <-> mode
-// maps differ (build: j = 128 n1 + t; stage algebra: j = cq_mode(t, e)).
-// dynamic smem: TW1 [16][128] | per team: X [XL] (exchange, then WS | ACC), NS [Kyp]
+// Persistent column pass (FP32): one CTA per SM, NT teams of TT threads,
+// team q of CTA b takes the kept columns b + gridDim.x (q + NT r).  Staging,
+// tables and stage algebra follow k_col_w; only the thread <-> mode maps differ
+// (build: j = TT n1 + t; stage algebra: j = cq_mode<NL>(t, e)).
+// dynamic smem: TW1 [16][TT] | per team: X [XL] (exchange, then WS | ACC), NS [Kyp]
 //               | per team SHV [Kyp] float | KYS [Kyp] float
-template <int STAGE, bool IFRK>
-__global__ void __launch_bounds__(128 * NSG_CQ_TEAMS, 1) k_col_q(Geo g, ColArgs<float> a) {
+template <int NL, int STAGE, bool IFRK>
+__global__ void __launch_bounds__(CQ<NL>::TT * CQ<NL>::NT, 1) k_col_q(Geo g, ColArgs<float> a) {
     typedef float T;
     typedef float2 C;
-    constexpr int NT = NSG_CQ_TEAMS;
+    typedef CQ<NL> Q;
+    constexpr int NT = Q::NT, TT = Q::TT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int Ky = g.Ky, Kyp = cw_kyp(Ky), XL = cq_xl(Ky), Kx = g.Kx;
-    const int team = threadIdx.x >> 7, t = threadIdx.x & 127;
+    const int Ky = g.Ky, Kyp = cw_kyp(Ky), XL = cq_xl<NL>(Ky), Kx = g.Kx;
+    const int team = threadIdx.x / TT, t = threadIdx.x % TT;
     const int bid = 1 + team;
     C* TW1 = reinterpret_cast<C*>(smem_raw);
-    C* X = TW1 + 2048 + team * (XL + Kyp);
+    C* X = TW1 + Q::N + team * (XL + Kyp);
     C* NS = X + XL;
-    T* SHV = reinterpret_cast<T*>(TW1 + 2048 + NT * (XL + Kyp)) + team * Kyp;
-    T* KYS = reinterpret_cast<T*>(TW1 + 2048 + NT * (XL + Kyp)) + NT * Kyp;
+    T* SHV = reinterpret_cast<T*>(TW1 + Q::N + NT * (XL + Kyp)) + team * Kyp;
+    T* KYS = reinterpret_cast<T*>(TW1 + Q::N + NT * (XL + Kyp)) + NT * Kyp;
     const int hv = a.sp.hv, sfd = a.sp.sfd;
     __shared__ double s_dt;
 
-    for (int m = threadIdx.x; m < 2048; m += blockDim.x) TW1[m] = a.twc[((m & 127) * (m >> 7)) & 2047];
+    for (int m = threadIdx.x; m < Q::N; m += blockDim.x) TW1[m] = a.twc[((m % TT) * (m / TT)) & (Q::N - 1)];
     for (int jj = threadIdx.x; jj < Ky; jj += blockDim.x) KYS[jj] = a.kyv[jj];
     const int cstride = gridDim.x * NT;
     int i = blockIdx.x + gridDim.x * team;
     if (i < Kx) {
         const size_t base = (size_t)i * Ky;
-        for (int jj = t; jj < Ky; jj += 128) {
+        for (int jj = t; jj < Ky; jj += TT) {
             cp_async(&NS[jj], &a.W0[base + jj]);
             if (hv) cp_async(&SHV[jj], &a.hvw[base + jj]);
         }
@@ -802,7 +819,7 @@ __global__ void __launch_bounds__(128 * NSG_CQ_TEAMS, 1) k_col_q(Geo g, ColArgs<
     for (bool first = true; i < Kx; i += cstride, first = false) {
         if (!first) {
             const size_t base = (size_t)i * Ky;
-            for (int jj = t; jj < Ky; jj += 128) {
+            for (int jj = t; jj < Ky; jj += TT) {
                 cp_async(&NS[jj], &a.W0[base + jj]);
                 if (hv) cp_async(&SHV[jj], &a.hvw[base + jj]);
             }
@@ -816,15 +833,15 @@ __global__ void __launch_bounds__(128 * NSG_CQ_TEAMS, 1) k_col_q(Geo g, ColArgs<
         for (int q = -1; q < 4; ++q) {
             const int f = (q + 2) & 3;
             if (q < 0) {
-                const C* __restrict__ Gc = a.G + (size_t)i * 2048;
+                const C* __restrict__ Gc = a.G + (size_t)i * Q::N;
 #pragma unroll
-                for (int n1 = 0; n1 < 16; ++n1) v[n1] = ld_stream(&Gc[128 * n1 + t]);
+                for (int n1 = 0; n1 < 16; ++n1) v[n1] = ld_stream(&Gc[TT * n1 + t]);
             } else {
-                // thread t builds modes j = 128 n1 + t; Psi = -w/k^2 is formed once
+                // thread t builds modes j = TT n1 + t; Psi = -w/k^2 is formed once
                 // (written back to NS) and reused for Psi_y by the same thread
 #pragma unroll
                 for (int n1 = 0; n1 < 16; ++n1) {
-                    const int j = 128 * n1 + t;
+                    const int j = TT * n1 + t;
                     const int jj = kept_jj(g, j);
                     C x = zero;
                     if (jj >= 0) {
@@ -844,27 +861,27 @@ __global__ void __launch_bounds__(128 * NSG_CQ_TEAMS, 1) k_col_q(Geo g, ColArgs<
                     v[n1] = cconj(x);
                 }
             }
-            col_fwd2048_q(v, X, TW1, t, bid);  // ends with a team barrier: X is free
+            col_fwd_q<NL>(v, X, TW1, t, bid);  // ends with a team barrier: X is free
             if (q >= 0) {
-                C* __restrict__ Fc = a.F[f] + (size_t)i * 2048;
+                C* __restrict__ Fc = a.F[f] + (size_t)i * Q::N;
 #pragma unroll
-                for (int e = 0; e < 16; ++e) Fc[cq_mode(t, e)] = cconj(v[e]);
+                for (int e = 0; e < 16; ++e) Fc[cq_mode<NL>(t, e)] = cconj(v[e]);
                 continue;
             }
             if (STAGE != 1) {
-                for (int jj = t; jj < Ky; jj += 128) {
+                for (int jj = t; jj < Ky; jj += TT) {
                     cp_async(&X[jj], &WS[cbase + jj]);
                     cp_async(&X[Kyp + jj], &ACC[cbase + jj]);
                 }
             }
             cp_async_wait_all();
-            quad_sync(bid);  // the team's staged omega_hat, weights, WS and ACC
+            team_bar<TT>(bid);  // the team's staged omega_hat, weights, WS and ACC
 
             // RK stage algebra (spectral_time_integration.c:50-100) on this
-            // thread's forward outputs, modes j = cq_mode(t, e)
+            // thread's forward outputs, modes j = cq_mode<NL>(t, e)
 #pragma unroll
             for (int e = 0; e < 16; ++e) {
-                const int j = cq_mode(t, e);
+                const int j = cq_mode<NL>(t, e);
                 const int jj = kept_jj(g, j);
                 if (jj < 0) continue;
                 const size_t s = cbase + jj;
@@ -895,7 +912,7 @@ __global__ void __launch_bounds__(128 * NSG_CQ_TEAMS, 1) k_col_q(Geo g, ColArgs<
                 const bool force_col = a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9;
 #pragma unroll 1
                 for (int e = 0; e < 16 && (force_col || sfd); ++e) {
-                    const int j = cq_mode(t, e);
+                    const int j = cq_mode<NL>(t, e);
                     const int jj = kept_jj(g, j);
                     if (jj < 0) continue;
                     const size_t s = cbase + jj;
@@ -907,7 +924,7 @@ __global__ void __launch_bounds__(128 * NSG_CQ_TEAMS, 1) k_col_q(Geo g, ColArgs<
                     }
                 }
             }
-            quad_sync(bid);  // NS complete for the inverse transforms; X is free again
+            team_bar<TT>(bid);  // NS complete for the inverse transforms; X is free again
         }
     }
     if (STAGE == 4 && blockIdx.x == 0 && threadIdx.x == 0) a.ds->t = a.ds->t + dt;
