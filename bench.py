@@ -313,8 +313,8 @@ def corrector_leg(steps: int = 20, batch: int = 32) -> dict:
 
 
 def config5_leg(steps: int = 10) -> dict:
-    """4096^2 forced run (FP32 bulk, p=4 hyperviscosity, CFL 0.4): generic row
-    pass, k_col_q column pass, with the energy spectrum of the device state."""
+    """4096^2 forced run (FP32 bulk, p=4 hyperviscosity, CFL 0.4) on the 4096-point row
+    (k_row_4k) and column (k_col_q) passes, with the energy spectrum of the device state."""
     import nsgb
 
     n = 4096
@@ -336,7 +336,7 @@ def config5_leg(steps: int = 10) -> dict:
     t_spec = time.perf_counter() - t0
     d = g.diagnostics()
     g.close()
-    return {"workload": "forced 4096^2, FP32, RK4, hyperviscosity p=4 (order 8), CFL 0.4, generic row pass, k_col_q column pass",
+    return {"workload": "forced 4096^2, FP32, RK4, hyperviscosity p=4 (order 8), CFL 0.4, stage kernels k_row_4k / k_col_q",
             "value": n * n * steps / (total.value * 1e-3), "unit": UNIT, "ms_per_step": total.value / steps,
             "spectrum_ms": t_spec * 1e3, "spectrum_bins": int(len(es)), "energy": d["energy"],
             "l2": "working set above L2; no flush"}

@@ -165,6 +165,19 @@ template <typename T> static int stage_row(ns_gpu* g, int stage) {
     a.dx[0] = 1; a.dx[1] = 0; a.dx[2] = 1; a.dx[3] = 0;  // psi_x, psi_y, omega_x, omega_y
     a.cfl = (stage == 1 && g->p.adaptive_dt) ? 1 : 0;
     a.marker = (stage == 1) ? 1 : (stage == 2 ? 2 : 0);
+    if constexpr (sizeof(T) == 4) {
+        if (g->fast_row && g->g.nx == 4096) {
+            // FP32, nx = 4096: two warps per row
+            const size_t smem = r4_smem_bytes();
+            NSG_TRY(set_smem(g, k_row_4k, smem));
+            int grid = g->g.ny / NSG_R4_ROWS;
+            if (grid > g->num_sms) grid = g->num_sms;
+            const cudaError_t e = launch_stage(k_row_4k, grid, 64 * NSG_R4_ROWS, smem, g->st, g->g, a);
+            if (e != cudaSuccess) NSG_FAIL(g, NS_GPU_ERR_CUDA, "k_row_4k launch: %s", cudaGetErrorString(e));
+            NSG_LAUNCHED(g);
+            return NS_GPU_OK;
+        }
+    }
     if constexpr (sizeof(T) == 4 && NSG_ROW_TMEM) {
         if (g->fast_row) {
             // FP32: Jacobian operands in tensor memory, inboxes filled by cp.async
@@ -471,8 +484,8 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
         // NS_GB300_GENERIC_KERNELS=1 selects the generic Stockham stage kernels at every size
         const char* gen = getenv("NS_GB300_GENERIC_KERNELS");
         const int generic = (gen && gen[0] == '1') || (kc && (kc->er || kc->ec));
-        g->fast_row = (!generic && nx == 2048) ? 1 : 0;
-        // the column pass also has an FP32 kernel for ny = 4096
+        // FP32 also has register-resident row and column passes at 4096
+        g->fast_row = (!generic && (nx == 2048 || (nx == 4096 && precision == NS_GPU_FP32))) ? 1 : 0;
         g->fast_col = (!generic && (ny == 2048 || (ny == 4096 && precision == NS_GPU_FP32 && NSG_COL_Q))) ? 1 : 0;
     }
     if (cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking) != cudaSuccess) {

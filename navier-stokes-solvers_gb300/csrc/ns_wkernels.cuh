@@ -1246,4 +1246,236 @@ __global__ void __launch_bounds__(32 * NW, 1) k_row_t(Geo g, RowArgs<float> a) {
     }
 }
 
+// ============================================================ k_row_4k
+// FP32 row pass at nx = 4096 (H = 2048, 1367 kept kx): two warps (64 threads,
+// 32 points each) per row, four rows per CTA, each CTA owning an equal
+// contiguous range of rows.  The half-length transforms are the two-warp
+// 2048-point transform of the column pass (col_fwd2048: input x[64 n1 + t],
+// output X[lane + 32 k2 + 1024 h]); inverses run as conj(DFT(conj z)).  The
+// inverse outputs are spatial samples z[m] in the output layout, where the
+// Jacobian is formed (psi_x and psi_y in tensor memory, 128 columns per warp);
+// J then passes once through the row's exchange buffer (dense, conflict-free
+// both ways) into the input layout of its forward transform.
+// dynamic smem (float2): tw [32][65] (W_2048^{t k1}) | twh [2048] | per row: IN [1368],
+//                        X [2112] (block pitch 3480 = 8 mod 16) | kx [1368] float | tensor-memory address
+#define NSG_R4_ROWS 4
+#define NSG_R4_KX 1367
+#define NSG_R4_IN 1368
+#define NSG_R4_BLK (NSG_R4_IN + NSG_CW_EX)
+__host__ __device__ constexpr size_t r4_smem_bytes() {
+    return (size_t)(32 * 65 + 2048 + NSG_R4_ROWS * NSG_R4_BLK) * sizeof(float2) + (size_t)NSG_R4_IN * sizeof(float) + 16;
+}
+
+// the CTA's rows y0 + w (w = tid & 3, valid while < yend) of field src into the
+// inboxes: thread tid copies k = (tid >> 2) + 64 i, so the four rows of one kx
+// column are one 32-byte run
+__device__ __forceinline__ void r4_issue(float2* IN0, const float2* __restrict__ src, int ny, int y0, int yend, int tid) {
+    const int w = tid & 3, kb = tid >> 2;
+    if (y0 + w < yend) {
+#pragma unroll
+        for (int i = 0; i < 22; ++i) {
+            const int k = kb + 64 * i;
+            if (k < NSG_R4_KX) cp_async(&IN0[w * NSG_R4_BLK + k], &src[(size_t)k * ny + y0 + w]);
+        }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+// conj of the half-length inverse input Z[k] (k = 64 n1 + t) from the inbox IN
+// (half spectrum X[k], k < 1367), with the i kx factor of the x-derivative fields:
+// Z[k] = (X[k] + conj X[H-k]) + i e^{+2 pi i k/nx} (X[k] - conj X[H-k])
+template <bool DX>
+__device__ __forceinline__ void r4_pack(float2 (&a)[32], const float2* IN, const float* kxs, const float2* twh, int t) {
+    const float2 zero = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int n1 = 0; n1 < 32; ++n1) {
+        const int k = 64 * n1 + t;
+        const bool ka_ok = k < NSG_R4_KX, kb_ok = k > 0 && 2048 - k < NSG_R4_KX;
+        float2 xa = ka_ok ? IN[k] : zero;
+        float2 xb = kb_ok ? IN[2048 - k] : zero;
+        if (DX) {
+            const float ka = ka_ok ? kxs[k] : 0.f;
+            const float kb = kb_ok ? kxs[2048 - k] : 0.f;
+            xa = make_float2(-ka * xa.y, ka * xa.x);
+            xb = make_float2(-kb * xb.y, kb * xb.x);
+        }
+        if (k == 0) {
+            a[n1] = make_float2(xa.x, -xa.x);  // conj of Re X[0] (1 + i); the Nyquist bin is masked
+        } else {
+            const float2 e = twh[k];  // exp(-2 pi i k/nx)
+            const float2 A = cadd(xa, cconj(xb));
+            const float2 dd = csub(xa, cconj(xb));
+            const float Dx = dd.x * e.x + dd.y * e.y;
+            const float Dy = dd.y * e.x - dd.x * e.y;
+            a[n1] = make_float2(A.x - Dy, -(A.y + Dx));
+        }
+    }
+}
+
+__global__ void __launch_bounds__(64 * NSG_R4_ROWS, 1) k_row_4k(Geo g, RowArgs<float> a) {
+    constexpr int NR = NSG_R4_ROWS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* tw = reinterpret_cast<float2*>(smem_raw);
+    float2* twh_s = tw + 32 * 65;
+    float2* B0 = twh_s + 2048;  // row r's block: IN at B0 + r * BLK, X at + NSG_R4_IN
+    float* kx_s = reinterpret_cast<float*>(B0 + NR * NSG_R4_BLK);
+    unsigned* tslot = reinterpret_cast<unsigned*>(kx_s + NSG_R4_IN);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int rr = warp >> 1, t = tid & 63, h = t >> 5, bid = 1 + rr;
+    const float2* INr = B0 + rr * NSG_R4_BLK;
+    float2* Xr = B0 + rr * NSG_R4_BLK + NSG_R4_IN;
+    const int ny = g.ny;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(
+            (unsigned)__cvta_generic_to_shared(tslot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    for (int i = tid; i < 32 * 65; i += blockDim.x) {
+        const int k1 = i / 65, tt = i - 65 * k1;
+        tw[i] = (tt < 64) ? a.twr[(tt * k1) & 2047] : make_float2(0.f, 0.f);
+    }
+    for (int i = tid; i < 2048; i += blockDim.x) twh_s[i] = a.twh[i];
+    for (int i = tid; i < NSG_R4_IN; i += blockDim.x) kx_s[i] = (i < NSG_R4_KX) ? a.kxv[i] : 0.f;
+    wait_previous_kernel();
+    if (blockIdx.x == 0 && tid == 0) {
+        if (a.marker == 1) {
+            a.ds->step_cur = a.ds->step_next;
+            a.ds->step_next = a.ds->step_next + (a.ds->fsub ? a.ds->fsub : 1ULL);
+        } else if (a.marker == 2) {
+            a.ds->maxvel2 = 0ULL;
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // this warp's 128 columns: R (psi_x, then psi_x omega_y) at +0, Q (psi_y) at +64
+    const unsigned tR = *tslot + ((unsigned)(32 * (warp & 3)) << 16) + 128u * (unsigned)(warp >> 2);
+    const unsigned tQ = tR + 64u;
+
+    const int r0 = (int)(((long long)ny * blockIdx.x) / gridDim.x);
+    const int yend = (int)(((long long)ny * (blockIdx.x + 1)) / gridDim.x);
+    float vmax2 = 0.f;
+    float2 v[32];
+    r4_issue(B0, a.F[0], ny, r0, yend, tid);
+    for (int y0 = r0; y0 < yend; y0 += NR) {
+        const int y = y0 + rr;
+        // q = 0..3: inverse transforms of psi_x (F0, d/dx), psi_y (F1), omega_y (F3),
+        // omega_x (F2, d/dx); q = 4: forward transform of the packed Jacobian
+#pragma unroll 1
+        for (int q = 0; q < 5; ++q) {
+            if (q < 4) {
+                asm volatile("cp.async.wait_all;" ::: "memory");
+                __syncthreads();  // field q of every row has landed
+                if (y < yend) {
+                    if (q == 0 || q == 3) r4_pack<true>(v, INr, kx_s, twh_s, t);
+                    else r4_pack<false>(v, INr, kx_s, twh_s, t);
+                }
+                __syncthreads();  // every row has packed field q: the inboxes take the next field
+                const int yn = (q < 3) ? y0 : y0 + NR;
+                r4_issue(B0, a.F[(q < 3) ? ((q + 1 < 2) ? q + 1 : 4 - q) : 0], ny, yn, yend, tid);
+            }
+            if (y >= yend) continue;
+            if (q == 4) {
+                // J from the output layout (m = lane + 32 k2 + 1024 h) to the input layout (64 n1 + t)
+#pragma unroll
+                for (int k2 = 0; k2 < 32; ++k2) Xr[lane + 32 * k2 + 1024 * h] = v[k2];
+                team_sync(bid);
+#pragma unroll
+                for (int n1 = 0; n1 < 32; ++n1) v[n1] = Xr[64 * n1 + t];
+                team_sync(bid);
+                col_fwd2048(v, Xr, tw, t, lane, h, bid);
+                break;
+            }
+            col_fwd2048(v, Xr, tw, t, lane, h, bid);
+#pragma unroll
+            for (int k = 0; k < 32; ++k) v[k].y = -v[k].y;
+            if (q == 0) {
+#pragma unroll
+                for (int c = 0; c < 4; ++c) tm_st16(tR + 16u * c, v, c);
+            } else if (q == 1) {
+                if (a.cfl) {
+                    tm_wait_st();
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        float r[16];
+                        tm_ld16_issue(tR + 16u * c, r);
+                        tm_wait_ld(r);
+#pragma unroll
+                        for (int m = 0; m < 8; ++m) {
+                            const float2 p = v[8 * c + m];
+                            vmax2 = fmaxf(vmax2, fmaxf(r[2 * m] * r[2 * m] + p.x * p.x, r[2 * m + 1] * r[2 * m + 1] + p.y * p.y));
+                        }
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < 4; ++c) tm_st16(tQ + 16u * c, v, c);
+            } else if (q == 2) {
+                tm_wait_st();
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    float r[16];
+                    tm_ld16_issue(tR + 16u * c, r);
+                    tm_wait_ld(r);
+                    float2 pr[32];
+#pragma unroll
+                    for (int m = 0; m < 8; ++m) pr[m] = make_float2(r[2 * m] * v[8 * c + m].x, r[2 * m + 1] * v[8 * c + m].y);
+                    tm_st16(tR + 16u * c, pr, 0);
+                }
+            } else {
+                // J = psi_x omega_y - psi_y omega_x, packed as w[m] = J[2m] + i J[2m+1]
+                tm_wait_st();
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    float r[16], s2[16];
+                    tm_ld16_issue(tR + 16u * c, r);
+                    tm_ld16_issue(tQ + 16u * c, s2);
+                    tm_wait_ld2(r, s2);
+#pragma unroll
+                    for (int m = 0; m < 8; ++m) {
+                        const float2 w = v[8 * c + m];
+                        v[8 * c + m] = make_float2(r[2 * m] - s2[2 * m] * w.x, r[2 * m + 1] - s2[2 * m + 1] * w.y);
+                    }
+                }
+            }
+        }
+        // the row's half-length spectrum W into its exchange buffer, by frequency
+        if (y < yend) {
+#pragma unroll
+            for (int k2 = 0; k2 < 32; ++k2) Xr[lane + 32 * k2 + 1024 * h] = v[k2];
+        }
+        __syncthreads();
+        // unpack the kept kx < Kx of the CTA's rows together: element e is
+        // (k = e / 4, row y0 + e % 4), so four consecutive threads write one
+        // 32-byte run of a G column
+        const float half = 0.5f;
+        const int nrows = (yend - y0 < NR) ? yend - y0 : NR;
+        for (int e = tid; e < NSG_R4_KX * NR; e += blockDim.x) {
+            const int k = e >> 2, w = e & 3;
+            if (w >= nrows) continue;
+            const float2* Sw = B0 + w * NSG_R4_BLK + NSG_R4_IN;
+            const float2 wa = Sw[k];
+            const float2 wb = Sw[(2048 - k) & 2047];
+            float2 ev, od;
+            ev.x = half * (wa.x + wb.x);
+            ev.y = half * (wa.y - wb.y);
+            od.x = half * (wa.y + wb.y);
+            od.y = -half * (wa.x - wb.x);
+            a.G[(size_t)k * ny + y0 + w] = cadd(ev, cmul(od, twh_s[k]));
+        }
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    tm_wait_st();
+    if (a.cfl) {
+        const double vm = warp_max((double)vmax2);
+        if (lane == 0) atomicMax(&a.ds->maxvel2, (unsigned long long)__double_as_longlong(vm));
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(*tslot));
+    }
+}
+
 }  // namespace nsg

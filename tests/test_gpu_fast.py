@@ -47,9 +47,9 @@ def test_fast_kernels_fp64_match_oracle(nsgb, port, nx, ny, steps):
 
 
 @pytest.mark.parametrize("nx,ny,steps", [(2048, 2048, 10), (2048, 128, 10), (128, 2048, 10), (128, 4096, 10),
-                                         (4096, 4096, 3)])
+                                         (4096, 128, 10), (4096, 4096, 3)])
 def test_fast_fp32_vs_fp64_2048(nsgb, nx, ny, steps):
-    # the FP32 stage kernels (k_row_t, k_col_q at ny = 2048 and 4096; alone on the non-square grids) against FP64
+    # the FP32 stage kernels (k_row_t / k_row_4k, k_col_q at 2048 and 4096; alone on the non-square grids) against FP64
     a = _gpu_run(nsgb, nx, ny, steps, nsgb.FP64)
     b = _gpu_run(nsgb, nx, ny, steps, nsgb.FP32)
     err = rel_l2(b.cplx("omega_hat"), a.cplx("omega_hat"))
