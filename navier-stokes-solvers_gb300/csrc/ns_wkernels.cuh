@@ -1248,8 +1248,8 @@ __global__ void __launch_bounds__(32 * NW, 1) k_row_t(Geo g, RowArgs<float> a) {
 
 // ============================================================ k_row_4k
 // FP32 row pass at nx = 4096 (H = 2048, 1367 kept kx): two warps (64 threads,
-// 32 points each) per row, four rows per CTA, each CTA owning an equal
-// contiguous range of rows.  The half-length transforms are the two-warp
+// 32 points each) per row, four rows per CTA, rows assigned to the CTAs
+// round-robin in groups of four.  The half-length transforms are the two-warp
 // 2048-point transform of the column pass (col_fwd2048: input x[64 n1 + t],
 // output X[lane + 32 k2 + 1024 h]); inverses run as conj(DFT(conj z)).  The
 // inverse outputs are spatial samples z[m] in the output layout, where the
@@ -1353,12 +1353,14 @@ __global__ void __launch_bounds__(64 * NSG_R4_ROWS, 1) k_row_4k(Geo g, RowArgs<f
     const unsigned tR = *tslot + ((unsigned)(32 * (warp & 3)) << 16) + 128u * (unsigned)(warp >> 2);
     const unsigned tQ = tR + 64u;
 
-    const int r0 = (int)(((long long)ny * blockIdx.x) / gridDim.x);
-    const int yend = (int)(((long long)ny * (blockIdx.x + 1)) / gridDim.x);
+    // rows round-robin: in one round CTAs b .. b + 3 read rows 16 c .. 16 c + 15, so
+    // the four 32-byte sectors of each 128-byte line of F are read together (the
+    // fields exceed L2 at 4096^2, so a line split over rounds is fetched again)
+    const int yend = ny, ystep = gridDim.x * NR;
     float vmax2 = 0.f;
     float2 v[32];
-    r4_issue(B0, a.F[0], ny, r0, yend, tid);
-    for (int y0 = r0; y0 < yend; y0 += NR) {
+    r4_issue(B0, a.F[0], ny, blockIdx.x * NR, yend, tid);
+    for (int y0 = blockIdx.x * NR; y0 < yend; y0 += ystep) {
         const int y = y0 + rr;
         // q = 0..3: inverse transforms of psi_x (F0, d/dx), psi_y (F1), omega_y (F3),
         // omega_x (F2, d/dx); q = 4: forward transform of the packed Jacobian
@@ -1372,7 +1374,7 @@ __global__ void __launch_bounds__(64 * NSG_R4_ROWS, 1) k_row_4k(Geo g, RowArgs<f
                     else r4_pack<false>(v, INr, kx_s, twh_s, t);
                 }
                 __syncthreads();  // every row has packed field q: the inboxes take the next field
-                const int yn = (q < 3) ? y0 : y0 + NR;
+                const int yn = (q < 3) ? y0 : y0 + ystep;
                 r4_issue(B0, a.F[(q < 3) ? ((q + 1 < 2) ? q + 1 : 4 - q) : 0], ny, yn, yend, tid);
             }
             if (y >= yend) continue;
