@@ -76,9 +76,16 @@ __global__ void __launch_bounds__(TP*(COUT / CPT)) k_conv3x3(const float* __rest
             sx[q * CP + c] = inb[((size_t)wrapi(y0 + hy - 1, H) * W + wrapi(x0 + hx - 1, W)) * CIN + c];
         }
         __syncthreads();
-        float acc[CPT];
+        // NA independent partial sums per output (over ci mod NA) when a thread has
+        // fewer than four outputs, so the FMA chain is not one long dependency
+        constexpr int NA = (CPT >= 4 || CIN % 4 != 0) ? 1 : 4;
+        float acc[NA][CPT];
 #pragma unroll
-        for (int k = 0; k < CPT; ++k) acc[k] = bias ? bias[g * CPT + k] : 0.0f;
+        for (int k = 0; k < CPT; ++k) {
+            acc[0][k] = bias ? bias[g * CPT + k] : 0.0f;
+#pragma unroll
+            for (int u = 1; u < NA; ++u) acc[u][k] = 0.0f;
+        }
 #pragma unroll 1
         for (int tap = 0; tap < 9; ++tap) {
             const int dy = tap / 3, dx = tap - 3 * dy;
@@ -89,14 +96,19 @@ __global__ void __launch_bounds__(TP*(COUT / CPT)) k_conv3x3(const float* __rest
                 const float xv = xs[ci];
                 const float* wr = ws + ci * COUT;
 #pragma unroll
-                for (int k = 0; k < CPT; ++k) acc[k] = fmaf(xv, wr[k], acc[k]);
+                for (int k = 0; k < CPT; ++k) acc[ci % NA][k] = fmaf(xv, wr[k], acc[ci % NA][k]);
             }
+        }
+#pragma unroll
+        for (int u = 1; u < NA; ++u) {
+#pragma unroll
+            for (int k = 0; k < CPT; ++k) acc[0][k] += acc[u][k];
         }
         const size_t o = (((size_t)b * H + y0 + py) * W + x0 + px) * COUT + g * CPT;
 #pragma unroll
         for (int k = 0; k < CPT; ++k) {
-            pre[o + k] = acc[k];
-            if (act) act[o + k] = GELU ? gelu(acc[k]) : acc[k];
+            pre[o + k] = acc[0][k];
+            if (act) act[o + k] = GELU ? gelu(acc[0][k]) : acc[0][k];
         }
     }
 }
@@ -546,7 +558,9 @@ static int conv(ns_cnn* c, cudaStream_t st, const float* in, const __nv_bfloat16
     auto k = k_conv3x3<CIN, COUT, CPT, GELU>;
     if (sm > 48 * 1024) CNN_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     const int tiles = B * (c->H / TH) * (c->W / TW);
-    k<<<grid_of(tiles, 1, c->num_sms), TP * (COUT / CPT), sm, st>>>(in, w, bias, pre, act, B, c->H, c->W);
+    // up to eight CTAs per SM: one 8 x 16 tile each at the corrector's sizes, so the
+    // halo loads of several tiles overlap
+    k<<<grid_of(tiles, 1, 8 * c->num_sms), TP * (COUT / CPT), sm, st>>>(in, w, bias, pre, act, B, c->H, c->W);
     CNN_LAUNCHED(c);
     return NS_GPU_OK;
 }
