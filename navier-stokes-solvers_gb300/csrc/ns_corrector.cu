@@ -316,6 +316,42 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __nv_bfloat16* __restr
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(taddr));
 }
 
+// inference first layer (2 -> 64, GELU) straight to the BF16 activations that the
+// tensor-core layers read: lane l of a warp computes channels 2l and 2l + 1 of one
+// pixel in the arithmetic order of k_conv3x3<2, 64, 32, true> (bias, then taps,
+// then input channels), so each pixel's 64 outputs leave as one 128-byte store and
+// no FP32 activation or separate conversion pass is written
+__global__ void __launch_bounds__(256) k_conv_in_bf16(const float* __restrict__ in, const __nv_bfloat16* __restrict__ w,
+                                                      const float* __restrict__ bias, __nv_bfloat16* __restrict__ out, int B,
+                                                      int H, int W) {
+    __shared__ float sw[9 * 2 * 64];  // [tap][ci][co]
+    for (int i = threadIdx.x; i < 9 * 2 * 64; i += blockDim.x) sw[i] = __bfloat162float(w[i]);
+    __syncthreads();
+    const int co = 2 * (threadIdx.x & 31);
+    const float b0 = bias ? bias[co] : 0.0f, b1 = bias ? bias[co + 1] : 0.0f;
+    const long long npix = (long long)B * H * W, hw = (long long)H * W;
+    for (long long p = blockIdx.x * 8LL + (threadIdx.x >> 5); p < npix; p += gridDim.x * 8LL) {
+        const int b = (int)(p / hw), r = (int)(p - b * hw);
+        const int y = r / W, x = r - y * W;
+        float a0 = b0, a1 = b1;
+#pragma unroll
+        for (int tap = 0; tap < 9; ++tap) {
+            const int dy = tap / 3, dx = tap - 3 * dy;
+            const float* ip = in + (((size_t)b * H + wrapi(y + dy - 1, H)) * W + wrapi(x + dx - 1, W)) * 2;
+#pragma unroll
+            for (int ci = 0; ci < 2; ++ci) {
+                const float xv = ip[ci];
+                a0 = fmaf(xv, sw[(tap * 2 + ci) * 64 + co], a0);
+                a1 = fmaf(xv, sw[(tap * 2 + ci) * 64 + co + 1], a1);
+            }
+        }
+        __nv_bfloat162 o;
+        o.x = __float2bfloat16_rn(gelu(a0));
+        o.y = __float2bfloat16_rn(gelu(a1));
+        *reinterpret_cast<__nv_bfloat162*>(out + p * 64 + co) = o;
+    }
+}
+
 __global__ void k_to_bf16(const float* __restrict__ a, __nv_bfloat16* __restrict__ b, long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         b[i] = __float2bfloat16_rn(a[i]);
@@ -599,11 +635,20 @@ static int conv_tc(ns_cnn* c, cudaStream_t st, const __nv_bfloat16* in, const __
 // activation for the backward pass, otherwise only what the next layer reads.
 static int forward(ns_cnn* c, cudaStream_t st, int B, bool training = true) {
     const float* x = c->x0;
-    CNN_TRY((conv<2, HID, 32, true>(c, st, x, c->wb[0], c->p + c->boff[0], c->pre[0], c->act[0], B)));
-    if (c->tc) {
-        const long long n = (long long)B * c->H * c->W * HID;
-        k_to_bf16<<<grid_of(n, 256, 8 * c->num_sms), 256, 0, st>>>(c->act[0], c->ab0, n);
+    if (c->tc && !training) {
+        const long long npix = (long long)B * c->H * c->W;
+        k_conv_in_bf16<<<grid_of(npix, 8, 8 * c->num_sms), 256, 0, st>>>(x, c->wb[0], c->p + c->boff[0], c->ab0, B, c->H,
+                                                                          c->W);
         CNN_LAUNCHED(c);
+    } else {
+        CNN_TRY((conv<2, HID, 32, true>(c, st, x, c->wb[0], c->p + c->boff[0], c->pre[0], c->act[0], B)));
+    }
+    if (c->tc) {
+        if (training) {
+            const long long n = (long long)B * c->H * c->W * HID;
+            k_to_bf16<<<grid_of(n, 256, 8 * c->num_sms), 256, 0, st>>>(c->act[0], c->ab0, n);
+            CNN_LAUNCHED(c);
+        }
         __nv_bfloat16* ain = c->ab0;
         __nv_bfloat16* aout = c->ab1;
         for (int l = 1; l < NL - 1; ++l) {
@@ -879,7 +924,7 @@ int ns_cnn_forward_host(ns_cnn* c, const float* inputs, int B, float* out) {
         k_gather<<<grid_of((long long)B * hw, 256, 1024), 256, 0, st>>>(din, nullptr, c->didx, B, c->H, c->W, c->s0, c->s1,
                                                                          c->so, c->x0, nullptr);
         c->launches++;
-        s = forward(c, st, B);
+        s = forward(c, st, B, false);  // the inference path of correct_step
     }
     if (s == NS_GPU_OK) {
         k_scale<<<grid_of((long long)B * hw, 256, 1024), 256, 0, st>>>(c->pre[NL - 1], (long long)B * hw, 1.0f / c->so);

@@ -91,7 +91,8 @@ def test_training_reduces_the_loss_on_a_learnable_map(nsgb):
 @pytest.mark.gpu
 def test_tensor_core_layers_match_oracle_with_bf16_activations(nsgb):
     """W = 128: the four 64 -> 64 layers run on tcgen05 (BF16 operands, FP32
-    accumulation in tensor memory); the oracle rounds the same activations to BF16."""
+    accumulation in tensor memory); the oracle rounds the same activations to BF16.
+    forward() runs the inference path of correct_step (first layer straight to BF16)."""
     H, W, B = 8, 128, 2
     net = nsgb.Corrector(H, W, max_batch=2, seed=4)
     p = rand_params(21).astype(np.float32)
