@@ -193,21 +193,26 @@ def ensemble_member_params(n: int, seed: int) -> dict:
                 forcing_epsilon=F_EPS, forcing_seed=F_SEED + 7919 * seed)
 
 
-def ensemble_leg(steps: int, seq_steps: int = 10) -> dict:
+def ensemble_leg(steps: int, seq_steps: int = 10, tiling=None) -> dict:
     """Config-3 ensemble: one persistent launch (CUDA graph) per `steps` steps versus
-    every member advanced alone, one member after another, with the same tiling."""
+    every member advanced alone, one member after another, with the same tiling.
+    tiling (threads, row radix, column radix, cluster) skips the autotuner, so the
+    first ensemble launch is the untimed warm-up of that tiling (ncu captures)."""
     import nsgb
 
     sizes = [n for n, cnt in ENS_MIX for _ in range(cnt)]
-    ens = nsgb.Ensemble(sizes, 2 * math.pi, config=(128, 16, 16, 1))
+    ens = nsgb.Ensemble(sizes, 2 * math.pi, config=tuple(tiling) if tiling else (128, 16, 16, 1))
     cache = os.path.join(ROOT, "navier-stokes-solvers_gb300", "_build", "ensemble_tune.jsonl")
     os.makedirs(os.path.dirname(cache), exist_ok=True)
     for i, (m, n) in enumerate(zip(ens.members, sizes)):
         m.set_params(**ensemble_member_params(n, i))
         m.random_spectrum(IC_SEED + i, ENS_K0, E0)
-    best, tune_ms = ens.autotune(steps=2, cache_path=cache)
-    for i, (m, n) in enumerate(zip(ens.members, sizes)):  # tuning advanced the members: restart
-        m.random_spectrum(IC_SEED + i, ENS_K0, E0)
+    if tiling:
+        best, tune_ms = tuple(tiling), None
+    else:
+        best, tune_ms = ens.autotune(steps=2, cache_path=cache)
+        for i, (m, n) in enumerate(zip(ens.members, sizes)):  # tuning advanced the members: restart
+            m.random_spectrum(IC_SEED + i, ENS_K0, E0)
     ens.advance(3)
     ms = ens.advance_timed(steps, 1)
     points = sum(n * n for n in sizes)
@@ -309,7 +314,8 @@ def corrector_leg(steps: int = 20, batch: int = 32) -> dict:
                                 "achieved": tflops, "peak": peak, "unit": "TFLOP/s", "frac": tflops / peak,
                                 "peak_source": peak_src},
             "simt_same_layer_ms": ms_simt,
-            "accuracy": "profiles/corrector_config4.md (trained by navier-stokes-solvers_gb300/corrector.py)"}
+            "accuracy": "not measured in this leg: the trained network's error against the filtered 1024^2 run "
+                        "comes from navier-stokes-solvers_gb300/corrector.py on held-out seeds"}
 
 
 def config5_leg(steps: int = 10) -> dict:
@@ -430,6 +436,8 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--ensemble-steps", type=int, default=100, help="steps of the timed ensemble launch (0: skip)")
     ap.add_argument("--ensemble-only", action="store_true", help="run only the ensemble leg and print its JSON")
+    ap.add_argument("--ensemble-tiling", default="",
+                    help="threads,row_radix,col_radix,cluster for the ensemble leg instead of the autotuner")
     ap.add_argument("--no-extra", action="store_true", help="skip the corrector and 4096^2 legs")
     ap.add_argument("--extra-only", action="store_true", help="run only the corrector and 4096^2 legs")
     args = ap.parse_args()
@@ -452,8 +460,9 @@ def main():
     import numpy as np
     import nsgb
 
+    ens_tiling = tuple(int(x) for x in args.ensemble_tiling.split(",")) if args.ensemble_tiling else None
     if args.ensemble_only:
-        print(json.dumps(ensemble_leg(max(1, args.ensemble_steps))), flush=True)
+        print(json.dumps(ensemble_leg(max(1, args.ensemble_steps), tiling=ens_tiling)), flush=True)
         return 0
     if args.extra_only:
         print(json.dumps({"corrector": corrector_leg(), "config5_4096": config5_leg()}), flush=True)
@@ -555,7 +564,7 @@ def main():
     ens = corr = c5 = None
     if rank == 0:
         if args.ensemble_steps > 0:
-            ens = ensemble_leg(args.ensemble_steps)
+            ens = ensemble_leg(args.ensemble_steps, tiling=ens_tiling)
         if not args.no_extra:
             corr = corrector_leg()
             c5 = config5_leg()

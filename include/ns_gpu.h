@@ -210,8 +210,8 @@ int ns_gpu_forcing_generate(ns_gpu *g, int n, const double *weights, int active,
 /* ------------------------------------------- device-resident access */
 
 /* Allocation-free forward transform, for callers that cannot allocate device
- * memory (no counterpart in the reference; it has the effect of
- * ns_spectral_physical_to_spectral, spectral_transforms.c:9-22, on device data).
+ * memory (no counterpart in the reference): r2c of a real field, scaled by
+ * 1/(nx*ny), with every mode outside the 2/3 mask set to zero.
  * Frameworks that own every device allocation through their own pool,
  * real-time loops that may not allocate, and processes whose device memory is
  * already fully reserved pass their own input and output and get the transform
@@ -344,6 +344,17 @@ int ns_cnn_train(ns_cnn *c, int iterations, int batch, float lr, float weight_de
  * weights, FP32 accumulation in tensor memory) when W is a multiple of 128 (the
  * default there); 0 selects the FP32 SIMT kernels for every layer. */
 int ns_cnn_set_tensor_cores(ns_cnn *c, int enable);
+/* Failure-detection self-test of the tensor-core layer (W a multiple of 128):
+ * every completion wait of that kernel is bounded, and on expiry the kernel
+ * records an error, frees its tensor memory and returns instead of waiting
+ * forever.  This launch issues no MMA, so each wait runs out after wait_cycles
+ * clock cycles (1 .. about 2 s worth); *timed_out receives 1 when the expiry
+ * was recorded.  With no tensor-core work in flight the network stays usable.
+ * A timeout reported by a real launch (training or inference) instead marks the
+ * network unusable: its MMAs may still have been running when the kernel
+ * returned, so later tensor-core launches fail until the network is destroyed
+ * and recreated. */
+int ns_cnn_probe_wait_timeout(ns_cnn *c, long long wait_cycles, int *timed_out);
 /* Mean CUDA-event time of one 64 -> 64 hidden layer (the network's dominant
  * kernel) on batch samples, over reps launches after one untimed launch. */
 int ns_cnn_time_hidden_layer(ns_cnn *c, int batch, int reps, double *ms_per_launch);

@@ -134,7 +134,7 @@ constexpr int TC_WB_BYTES = 9 * 8 * 64 * 16;               // 73,728
 constexpr int TC_HX_BYTES = 3 * 8 * TC_HP * 16;            // 49,920 per halo buffer
 constexpr int TC_ST = 65;                                  // staged output row pitch (floats)
 constexpr int TC_SMEM = TC_WB_BYTES + 2 * TC_HX_BYTES + 64;  // + mbarrier and tmem address
-constexpr long long TC_WAIT_CYCLES = 4000000000LL;         // about 2 s
+constexpr long long TC_WAIT_CYCLES = 4000000000LL;         // default wait limit: about 2 s
 static_assert(TC_W * TC_ST * 4 <= TC_HX_BYTES, "output staging must fit in a halo buffer");
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -159,7 +159,7 @@ __device__ __forceinline__ void tc_mma(unsigned taddr, unsigned long long a, uns
         "l"(a), "l"(b), "r"(TC_IDESC), "r"(accum));
 }
 
-__device__ __forceinline__ bool mbar_wait(unsigned mbar, unsigned parity) {
+__device__ __forceinline__ bool mbar_wait(unsigned mbar, unsigned parity, long long limit) {
     const long long t0 = clock64();
     for (;;) {
         unsigned done;
@@ -169,7 +169,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned mbar, unsigned parity) {
             : "r"(mbar), "r"(parity)
             : "memory");
         if (done) return true;
-        if (clock64() - t0 > TC_WAIT_CYCLES) return false;
+        if (clock64() - t0 > limit) return false;
     }
 }
 
@@ -227,11 +227,15 @@ __device__ __forceinline__ void tc_issue(unsigned taddr, unsigned hx, unsigned w
 // current tile's MMAs and epilogue run; the epilogue stages the accumulator
 // through the current tile's (consumed) halo buffer so that every output of a
 // tile leaves as one contiguous, coalesced block.
+// wait_cycles bounds each MMA-completion wait (clock64 cycles).  probe != 0 is
+// the self-test of that bound: no MMA is issued, so the first wait (on an
+// mbarrier nothing arrives on) runs out, the kernel records the expiry in err,
+// frees its tensor memory and returns with no tensor-core work in flight.
 template <bool GELU>
 __global__ void __launch_bounds__(128, 1) k_conv_tc(const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ w,
                                                     const float* __restrict__ bias, float* __restrict__ pre,
                                                     float* __restrict__ actf, __nv_bfloat16* __restrict__ actb, int B, int H,
-                                                    int W, int* __restrict__ err) {
+                                                    int W, int* __restrict__ err, long long wait_cycles, int probe) {
     extern __shared__ __align__(128) unsigned char tsm[];
     unsigned char* WB = tsm;                            // [9][8][64][8] bf16
     unsigned char* HXB = tsm + TC_WB_BYTES;             // 2 x [3][8][130][8] bf16
@@ -263,7 +267,7 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __nv_bfloat16* __restr
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const unsigned taddr = *tslot;
-    if (tile < ntiles && tid == 0) tc_issue(taddr, hxb, wbs, mb);
+    if (tile < ntiles && tid == 0 && !probe) tc_issue(taddr, hxb, wbs, mb);
     unsigned phase = 0;
     int buf = 0;
     for (; tile < ntiles; tile += gridDim.x, buf ^= 1) {
@@ -272,7 +276,7 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __nv_bfloat16* __restr
         if (next < ntiles) tc_load_halo(in, hx_next, next, H, W, ntx, tid);  // overlaps this tile's MMAs and epilogue
         // every thread must take the same branch (barriers follow): the tile
         // succeeds only if every thread saw the MMAs complete in time
-        const bool ok = __syncthreads_and(mbar_wait(mb, phase) ? 1 : 0) != 0;
+        const bool ok = __syncthreads_and(mbar_wait(mb, phase, wait_cycles) ? 1 : 0) != 0;
         phase ^= 1u;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         if (!ok) {
@@ -564,6 +568,11 @@ struct ns_cnn {
     __nv_bfloat16 *ab0 = nullptr, *ab1 = nullptr;  // BF16 activations of the tensor-core layers
     int tc = 0;                    // 64 -> 64 layers on tcgen05 (W % 128 == 0)
     int* derr = nullptr;           // device error flag of the tensor-core kernel
+    long long tc_wait_cycles = TC_WAIT_CYCLES;  // limit of each MMA-completion wait
+    // set when a tensor-core launch reported an expired wait: its MMAs may still
+    // have been running when the CTA freed its tensor memory and exited, so the
+    // instance refuses further tensor-core launches until it is recreated
+    int tc_broken = 0;
     unsigned long long launches = 0;
     std::string err;
 };
@@ -621,10 +630,15 @@ static int conv_dw(ns_cnn* c, cudaStream_t st, const float* in, const float* dpr
 template <bool GELU>
 static int conv_tc(ns_cnn* c, cudaStream_t st, const __nv_bfloat16* in, const __nv_bfloat16* w, const float* bias, float* pre,
                    float* actf, __nv_bfloat16* actb, int B) {
+    if (c->tc_broken)
+        CNN_FAIL(c, NS_GPU_ERR_CUDA,
+                 "tensor-core convolution refused: an earlier launch timed out waiting for its MMAs; destroy and "
+                 "recreate the network");
     auto k = k_conv_tc<GELU>;
     CNN_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
     const int tiles = B * c->H * (c->W / TC_W);
-    k<<<grid_of(tiles, 1, c->num_sms), 128, TC_SMEM, st>>>(in, w, bias, pre, actf, actb, B, c->H, c->W, c->derr);
+    k<<<grid_of(tiles, 1, c->num_sms), 128, TC_SMEM, st>>>(in, w, bias, pre, actf, actb, B, c->H, c->W, c->derr,
+                                                           c->tc_wait_cycles, 0);
     CNN_LAUNCHED(c);
     return NS_GPU_OK;
 }
@@ -672,7 +686,12 @@ static int check_tc(ns_cnn* c) {
     if (!c->tc) return NS_GPU_OK;
     int e = 0;
     CNN_CUDA(c, cudaMemcpy(&e, c->derr, sizeof(int), cudaMemcpyDeviceToHost));
-    if (e) CNN_FAIL(c, NS_GPU_ERR_CUDA, "tensor-core convolution: an MMA completion wait timed out");
+    if (e) {
+        c->tc_broken = 1;
+        CNN_FAIL(c, NS_GPU_ERR_CUDA,
+                 "tensor-core convolution: an MMA completion wait timed out; the network refuses further "
+                 "tensor-core launches until it is destroyed and recreated");
+    }
     return NS_GPU_OK;
 }
 
@@ -1020,6 +1039,33 @@ int ns_cnn_set_tensor_cores(ns_cnn* c, int enable) {
     if (!c) return NS_GPU_ERR_INVALID;
     if (enable && (c->W % TC_W != 0 || !c->ab0)) CNN_FAIL(c, NS_GPU_ERR_INVALID, "tensor cores need W %% %d == 0", TC_W);
     c->tc = enable ? 1 : 0;
+    return NS_GPU_OK;
+}
+
+// Self-test of the tensor-core kernel's bounded wait: one launch over one
+// sample in which no MMA is issued, so each CTA's first completion wait (on an
+// mbarrier nothing arrives on) runs out after wait_cycles clock cycles; every
+// CTA then records the expiry, frees its tensor memory and returns.
+// *timed_out receives the kernel's error flag.  No tensor-core work was in
+// flight, so the network stays usable and its flag is cleared afterwards.
+int ns_cnn_probe_wait_timeout(ns_cnn* c, long long wait_cycles, int* timed_out) {
+    if (!c || !timed_out || wait_cycles < 1 || wait_cycles > TC_WAIT_CYCLES) return NS_GPU_ERR_INVALID;
+    if (!c->tc) CNN_FAIL(c, NS_GPU_ERR_INVALID, "the wait probe needs the tensor-core layers (W %% %d == 0)", TC_W);
+    if (c->tc_broken) CNN_FAIL(c, NS_GPU_ERR_CUDA, "the network must be recreated after a tensor-core timeout");
+    cudaStream_t st = c->st;
+    CNN_CUDA(c, cudaMemsetAsync(c->derr, 0, sizeof(int), st));
+    auto k = k_conv_tc<true>;
+    CNN_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+    const int tiles = c->H * (c->W / TC_W);
+    k<<<grid_of(tiles, 1, c->num_sms), 128, TC_SMEM, st>>>(c->ab0, c->wb[1], nullptr, nullptr, nullptr, nullptr, 1, c->H,
+                                                           c->W, c->derr, wait_cycles, 1);
+    CNN_LAUNCHED(c);
+    int e = 0;
+    CNN_CUDA(c, cudaMemcpyAsync(&e, c->derr, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CNN_CUDA(c, cudaStreamSynchronize(st));
+    CNN_CUDA(c, cudaMemsetAsync(c->derr, 0, sizeof(int), st));
+    CNN_CUDA(c, cudaStreamSynchronize(st));
+    *timed_out = e;
     return NS_GPU_OK;
 }
 

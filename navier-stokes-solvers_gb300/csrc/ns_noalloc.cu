@@ -51,6 +51,7 @@ static size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 // geometry of the instance path (ns_gpu_create) for a grid, FP64
 static void noalloc_geo(int nx, int ny, Geo& G, int& ER, int& EC) {
+    memset(&G, 0, sizeof(G));
     G.nx = nx;
     G.ny = ny;
     G.nkx = nx / 2 + 1;
@@ -107,19 +108,39 @@ static int noalloc_setup(void** base) {
             return NS_GPU_ERR_CUDA;
         }
         const int smem = 100 * 1024 + 4096;
-        cudaFuncSetAttribute(k_row<double, 16, ROW_FWD1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        cudaFuncSetAttribute(k_row<double, 4, ROW_FWD1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        cudaFuncSetAttribute(k_col<double, 16, COL_FWD_EXPORT, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        cudaFuncSetAttribute(k_col<double, 4, COL_FWD_EXPORT, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        e = cudaGetLastError();
-        if (e != cudaSuccess) {
-            fprintf(stderr, "ns_gpu_forward_noalloc: cudaFuncSetAttribute: %s\n", cudaGetErrorString(e));
-            return NS_GPU_ERR_CUDA;
+        const void* kerns[] = {(const void*)k_row<double, 16, ROW_FWD1>, (const void*)k_row<double, 4, ROW_FWD1>,
+                               (const void*)k_col<double, 16, COL_FWD_EXPORT, 0>,
+                               (const void*)k_col<double, 4, COL_FWD_EXPORT, 0>};
+        for (const void* k : kerns) {
+            e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e != cudaSuccess) {
+                fprintf(stderr, "ns_gpu_forward_noalloc: cudaFuncSetAttribute: %s\n", cudaGetErrorString(e));
+                return NS_GPU_ERR_CUDA;
+            }
         }
         g_noalloc_addr[dev] = p;
     }
     *base = g_noalloc_addr[dev];
     return NS_GPU_OK;
+}
+
+// one launch; the returned status is this launch's own (a <<<>>> launch is only
+// checked through cudaGetLastError, which would also report and clear an
+// unrelated earlier error of the caller)
+template <typename... KArgs, typename... Args>
+static cudaError_t noalloc_launch(void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t st,
+                                  Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
+static int noalloc_fail(const char* what, cudaError_t e) {
+    fprintf(stderr, "ns_gpu_forward_noalloc: %s: %s\n", what, cudaGetErrorString(e));
+    return NS_GPU_ERR_CUDA;
 }
 
 template <int ER, int EC>
@@ -128,9 +149,12 @@ static int noalloc_run(const Geo& G, unsigned char* base, const double* field, d
     double2* twr = (double2*)(base + round256((size_t)G.ny * sizeof(double2)));
     double2* twh = (double2*)((unsigned char*)twr + round256((size_t)G.H * sizeof(double2)));
     double2* Gbuf = (double2*)((unsigned char*)twh + round256((size_t)G.H * sizeof(double2)));
-    k_twiddles<<<(G.ny + 255) / 256, 256, 0, st>>>(twc, G.ny, G.ny);
-    k_twiddles<<<(G.H + 255) / 256, 256, 0, st>>>(twr, G.H, G.H);
-    k_twiddles<<<(G.H + 255) / 256, 256, 0, st>>>(twh, G.H, G.nx);
+    cudaError_t e = noalloc_launch(k_twiddles<double2>, (G.ny + 255) / 256, 256, 0, st, twc, G.ny, G.ny);
+    if (e != cudaSuccess) return noalloc_fail("twiddle launch", e);
+    e = noalloc_launch(k_twiddles<double2>, (G.H + 255) / 256, 256, 0, st, twr, G.H, G.H);
+    if (e != cudaSuccess) return noalloc_fail("twiddle launch", e);
+    e = noalloc_launch(k_twiddles<double2>, (G.H + 255) / 256, 256, 0, st, twh, G.H, G.nx);
+    if (e != cudaSuccess) return noalloc_fail("twiddle launch", e);
     RowArgs<double> ra;
     memset(&ra, 0, sizeof(ra));
     ra.G = Gbuf;
@@ -139,12 +163,10 @@ static int noalloc_run(const Geo& G, unsigned char* base, const double* field, d
     ra.twh = twh;
     const int TT = G.H / ER;
     const size_t rsm = (size_t)G.RPC * spad_len(G.H) * sizeof(double2);
-    k_row<double, ER, ROW_FWD1><<<G.ny / G.RPC, G.RPC * TT, rsm, st>>>(G, ra);
-    cudaError_t e = cudaMemsetAsync(field_hat, 0, (size_t)G.nkx * G.nky * sizeof(double2), st);
-    if (e != cudaSuccess) {
-        fprintf(stderr, "ns_gpu_forward_noalloc: %s\n", cudaGetErrorString(e));
-        return NS_GPU_ERR_CUDA;
-    }
+    e = noalloc_launch(k_row<double, ER, ROW_FWD1>, G.ny / G.RPC, G.RPC * TT, rsm, st, G, ra);
+    if (e != cudaSuccess) return noalloc_fail("row-pass launch", e);
+    e = cudaMemsetAsync(field_hat, 0, (size_t)G.nkx * G.nky * sizeof(double2), st);
+    if (e != cudaSuccess) return noalloc_fail("cudaMemsetAsync", e);
     ColArgs<double> ca;
     memset(&ca, 0, sizeof(ca));
     ca.G = Gbuf;
@@ -153,12 +175,8 @@ static int noalloc_run(const Geo& G, unsigned char* base, const double* field, d
     ca.out_scale = 1.0 / ((double)G.nx * (double)G.ny);
     const int TC = G.ny / EC;
     const size_t csm = (size_t)G.CW * spad_len(G.ny) * sizeof(double2);
-    k_col<double, EC, COL_FWD_EXPORT, 0><<<G.Kxp / G.CW, G.CW * TC, csm, st>>>(G, ca);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) {
-        fprintf(stderr, "ns_gpu_forward_noalloc: kernel launch: %s\n", cudaGetErrorString(e));
-        return NS_GPU_ERR_CUDA;
-    }
+    e = noalloc_launch(k_col<double, EC, COL_FWD_EXPORT, 0>, G.Kxp / G.CW, G.CW * TC, csm, st, G, ca);
+    if (e != cudaSuccess) return noalloc_fail("column-pass launch", e);
     return NS_GPU_OK;
 }
 

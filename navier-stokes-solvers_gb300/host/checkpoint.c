@@ -226,7 +226,7 @@ static int npy_read(const unsigned char *p, size_t size, const char *descr, size
     snprintf(want, sizeof(want), "'descr': '%s'", descr);
     if (!strstr(dict, want) || strstr(dict, "'fortran_order': True")) return -1;
     if (size - off - hl != count * elem) return -1;
-    memcpy(out, p + off + hl, count * elem);
+    if (out) memcpy(out, p + off + hl, count * elem); /* out == NULL: check only */
     return 0;
 }
 
@@ -326,12 +326,24 @@ int ns_checkpoint_read_spectral(const char *filename, NSSpectralData *state) {
         free(r.buf);
         return -1;
     }
+    const size_t nr = (size_t)d->nx * d->ny, nc = (size_t)d->nkx * d->nky;
+    /* every required dataset is checked (name, type, element count) before the
+     * first one is copied, so a bad file leaves the state untouched */
+    static const char *const req_real[] = {"fields/u.npy", "fields/v.npy", "fields/omega.npy", "fields/psi.npy"};
+    static const char *const req_cplx[] = {"fields/u_hat.npy", "fields/v_hat.npy", "fields/omega_hat.npy"};
+    for (size_t i = 0; i < sizeof(req_real) / sizeof(req_real[0]); ++i)
+        st |= npz_get(&r, req_real[i], "<f8", nr, sizeof(double), NULL);
+    for (size_t i = 0; i < sizeof(req_cplx) / sizeof(req_cplx[0]); ++i)
+        st |= npz_get(&r, req_cplx[i], "<c16", nc, sizeof(fftw_complex), NULL);
+    if (st) {
+        free(r.buf);
+        return -1;
+    }
     /* newer device-resident steps must not overwrite what is read below */
     if (d->gpu && ns_spectral_gpu_sync_host(d) != SOLVER_SUCCESS) {
         free(r.buf);
         return -1;
     }
-    const size_t nr = (size_t)d->nx * d->ny, nc = (size_t)d->nkx * d->nky;
     st |= npz_get(&r, "fields/u.npy", "<f8", nr, sizeof(double), d->u);
     st |= npz_get(&r, "fields/v.npy", "<f8", nr, sizeof(double), d->v);
     st |= npz_get(&r, "fields/omega.npy", "<f8", nr, sizeof(double), d->omega);

@@ -185,6 +185,7 @@ def load(build: bool = True) -> C.CDLL:
     proto("ns_cnn_correct_step", C.c_int, vp, vp, C.c_int)
     proto("ns_cnn_set_tensor_cores", C.c_int, vp, C.c_int)
     proto("ns_cnn_time_hidden_layer", C.c_int, vp, C.c_int, C.c_int, _DP)
+    proto("ns_cnn_probe_wait_timeout", C.c_int, vp, C.c_longlong, C.POINTER(C.c_int))
     ecp = C.POINTER(EnsembleConfig)
     proto("ns_gpu_create_for_ensemble", C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, ecp, C.POINTER(vp))
     proto("ns_gpu_ensemble_create", C.c_int, C.c_int, C.POINTER(C.c_int), C.c_double, ecp, C.POINTER(vp))
@@ -562,6 +563,13 @@ class Corrector:
         ms = C.c_double()
         self.check(self.lib.ns_cnn_time_hidden_layer(self.h, batch, reps, C.byref(ms)), "time_hidden_layer")
         return ms.value
+
+    def probe_wait_timeout(self, wait_cycles: int) -> int:
+        """Failure-detection self-test: a tensor-core launch whose waits run out
+        with no MMA issued; returns the kernel's error flag (1 = expiry recorded)."""
+        out = C.c_int(-1)
+        self.check(self.lib.ns_cnn_probe_wait_timeout(self.h, int(wait_cycles), C.byref(out)), "probe_wait_timeout")
+        return out.value
 
     def set_tensor_cores(self, enable: bool):
         self.check(self.lib.ns_cnn_set_tensor_cores(self.h, 1 if enable else 0), "set_tensor_cores")

@@ -22,7 +22,15 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libns_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libns_ref.so")
-REF_TREE = "/root/reference"
+# The reference tree is named by the environment (NS_REFERENCE_TREE); without
+# it the Makefile's own default location is tried by its ``ref-if-present``
+# target, and the reference build is skipped where no tree exists.
+REF_TREE = os.environ.get("NS_REFERENCE_TREE") or None
+
+
+def have_ref() -> bool:
+    """True when the reference build (oracle/_ref/libns_ref.so) exists."""
+    return os.path.exists(REF_SO)
 
 
 class HVConfig(C.Structure):
@@ -89,8 +97,13 @@ class ForcingState(C.Structure):
 def build(ref: bool = True) -> None:
     """Compile the restatement (and the reference build when its tree exists)."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
-    if ref and os.path.isdir(REF_TREE):
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_TREE}"], check=True)
+    if not ref:
+        return
+    if REF_TREE:
+        if os.path.isdir(REF_TREE):
+            subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_TREE}"], check=True)
+    else:
+        subprocess.run(["make", "-s", "-C", HERE, "ref-if-present"], check=True)
 
 
 _LIBS: dict = {}

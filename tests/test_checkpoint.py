@@ -82,6 +82,26 @@ def test_read_rejects_mismatched_grid_and_garbage(nsgb, tmp_path):
     assert lib.ns_checkpoint_read_spectral(str(tmp_path / "missing.npz").encode(), C.byref(a)) == -1
 
 
+def test_failed_read_leaves_state_untouched(nsgb, tmp_path):
+    """A file whose omega_hat entry is missing is refused before any array of the
+    state is overwritten (u, v, omega, psi come earlier in the file)."""
+    lib = nsgb.load(build=False)
+    a, _ = host_state(nsgb, 32, 16, 6)
+    path = tmp_path / "ck.npz"
+    assert lib.ns_checkpoint_write_spectral(str(path).encode(), C.byref(a)) == 0
+    bad = tmp_path / "no_omega_hat.npz"
+    raw = path.read_bytes()
+    assert raw.count(b"fields/omega_hat.npy") == 2  # local header + central directory
+    bad.write_bytes(raw.replace(b"fields/omega_hat.npy", b"fields/omegX_hat.npy"))
+    b, brr = host_state(nsgb, 32, 16, 7)
+    before = {k: v.copy() for k, v in brr.items()}
+    t0, dt0 = b.t, b.dt
+    assert lib.ns_checkpoint_read_spectral(str(bad).encode(), C.byref(b)) == -1
+    for name, v in before.items():
+        assert np.array_equal(brr[name], v), name
+    assert (b.t, b.dt) == (t0, dt0)
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("device_resident", [False, True])
 def test_resume_continues_exactly(nsgb, tmp_path, device_resident):

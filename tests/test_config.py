@@ -190,7 +190,7 @@ def test_missing_file_reports_error(product, tmp_path):
     assert st == -1 and "Failed to open" in err
 
 
-@pytest.mark.skipif(not os.path.isdir(O.REF_TREE), reason="reference build needs the reference tree")
+@pytest.mark.skipif(not O.have_ref(), reason="reference build not present")
 def test_matches_reference_parser(product, files, tmp_path):
     O.build(ref=True)
     ref = _bind(C.CDLL(O.REF_SO))

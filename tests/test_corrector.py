@@ -148,3 +148,22 @@ def test_tensor_core_gradients_track_the_oracle(nsgb):
             assert np.linalg.norm(a - b) / np.linalg.norm(b) <= tol, (tc, ci, co)
             off += n + co
     net.close()
+
+
+@pytest.mark.gpu
+def test_tensor_core_wait_limit_reports_and_recovers(nsgb):
+    """The bounded MMA-completion wait of the tensor-core layer: a probe launch that
+    issues no MMA makes every CTA's wait run out after ~1 ms of clock cycles; the
+    kernel reports the expiry, frees its tensor memory and returns (no GPU fault,
+    no hang).  A normal forward afterwards allocates tensor memory on the same SMs
+    and reproduces the output taken before the probe."""
+    H, W, B = 8, 128, 2
+    net = nsgb.Corrector(H, W, max_batch=2, seed=5)
+    net.set_params(rand_params(41).astype(np.float32))
+    x = np.random.default_rng(23).standard_normal((B, 2, H, W)).astype(np.float32)
+    before = net.forward(x)
+    assert net.probe_wait_timeout(2_000_000) == 1
+    assert net.probe_wait_timeout(2_000_000) == 1  # repeatable: the flag is cleared after each probe
+    after = net.forward(x)
+    assert np.array_equal(before, after)
+    net.close()

@@ -144,7 +144,7 @@ def test_taylor_green_decay_on_oracle(port):
     assert rel_l2(g["omega_hat"], w0 * decay) < 1e-9
 
 
-@pytest.mark.skipif(not os.path.isdir(O.REF_TREE), reason="reference tree not present (bit-exact check runs where it is)")
+@pytest.mark.skipif(not O.have_ref(), reason="reference build not present (bit-exact check runs where it is)")
 def test_restatement_bit_exact_vs_reference_build(port):
     ref = O.load("ref")
     os.environ["OMP_NUM_THREADS"] = "1"

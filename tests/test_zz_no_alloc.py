@@ -41,7 +41,10 @@ def _instance_forward(nsgb, field):
     return out
 
 
-@pytest.mark.parametrize("shape_seq", [((64, 128), (256, 32))])
+# (ny, nx) pairs, two calls in a row per case: the second grid differs from the
+# first.  (8, 16) runs the radix-4 branches of both passes (a row transform of 8
+# points, a column of 8); (1024, 1024) is the largest grid the 8 MiB array admits.
+@pytest.mark.parametrize("shape_seq", [((64, 128), (256, 32)), ((8, 16), (1024, 1024))])
 def test_forward_noalloc_matches_instance_path(nsgb, shape_seq):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
