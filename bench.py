@@ -182,6 +182,66 @@ def model_bytes(n: int, elem: int):
     return {"row": 5 * A * elem, "col": (5 * A + 11 * Cc / 4) * elem, "step": (40 * A + 11 * Cc) * elem}
 
 
+# ------------------------------------------------------- FP64 and horizon legs
+def fp64_leg(n: int, steps: int, warmup: int = 3) -> dict:
+    """The same 2048^2 workload on the FP64 path (every operation in double, the
+    precision of the reference's own solver), timed like the headline: CUDA events
+    per step on the library stream with the L2 flush between steps."""
+    import ctypes as C
+
+    import nsgb
+
+    g = nsgb.Gpu(n, n, precision=nsgb.FP64)
+    g.set_params(**gpu_params(nsgb, n))
+    g.random_spectrum(IC_SEED, K0, E0)
+    g.advance(warmup)
+    g.sync()
+    total = C.c_double()
+    g.check(g.lib.ns_gpu_advance_timed(g.h, steps, C.c_size_t(FLUSH_BYTES), C.byref(total), None), "advance_timed")
+    g.close()
+    ms = total.value / steps
+    mb = model_bytes(n, 16)
+    return {"workload": f"{n}^2, the headline workload in FP64", "dtype": "f64", "steps": steps,
+            "ms_per_step": ms, "value": n * n / (ms * 1e-3), "unit": UNIT,
+            "step_model_bytes": mb["step"], "step_GBps": mb["step"] / (ms * 1e-3) / 1e9}
+
+
+def horizon_leg(n: int, steps: int, every: int) -> dict:
+    """FP32 bulk against the FP64 path over the full config-2 horizon: the same
+    initial spectrum, forcing stream and adaptive-dt rule, sampled every `every`
+    steps (relative L2 of the vorticity spectrum, energy and enstrophy error).
+    The two runs choose their own dt from their own velocity, so their times are
+    reported beside the errors."""
+    import nsgb
+    import numpy as np
+
+    g64 = nsgb.Gpu(n, n, precision=nsgb.FP64)
+    g32 = nsgb.Gpu(n, n, precision=nsgb.FP32)
+    for x in (g64, g32):
+        x.set_params(**gpu_params(nsgb, n))
+        x.random_spectrum(IC_SEED, K0, E0)
+    samples = []
+    t0 = time.perf_counter()
+    done = 0
+    while done < steps:
+        k = min(every, steps - done)
+        g64.advance(k)
+        g32.advance(k)
+        done += k
+        a = g32.download(("omega_hat",))["omega_hat"]
+        b = g64.download(("omega_hat",))["omega_hat"]
+        d32, d64 = g32.diagnostics(), g64.diagnostics()
+        samples.append({"step": done, "rel_l2_vorticity": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
+                        "energy_rel_err": abs(d32["energy"] - d64["energy"]) / abs(d64["energy"]),
+                        "enstrophy_rel_err": abs(d32["enstrophy"] - d64["enstrophy"]) / abs(d64["enstrophy"]),
+                        "t_fp32": d32["t"], "t_fp64": d64["t"], "energy_fp64": d64["energy"],
+                        "enstrophy_fp64": d64["enstrophy"]})
+    g64.close()
+    g32.close()
+    return {"workload": f"{n}^2 config-2 physics, FP32 bulk vs FP64, {steps} steps", "every": every,
+            "samples": samples, "wall_s": time.perf_counter() - t0}
+
+
 # ------------------------------------------------------------ ensemble leg
 ENS_MIX = ((64, 128), (128, 96), (256, 32))   # (side, members): 4,194,304 points = 2048^2
 ENS_K0 = 4.0
@@ -439,6 +499,10 @@ def main():
     ap.add_argument("--ensemble-tiling", default="",
                     help="threads,row_radix,col_radix,cluster for the ensemble leg instead of the autotuner")
     ap.add_argument("--no-extra", action="store_true", help="skip the corrector and 4096^2 legs")
+    ap.add_argument("--fp64-steps", type=int, default=20, help="timed steps of the FP64 leg (0: skip)")
+    ap.add_argument("--horizon-steps", type=int, default=5000,
+                    help="steps of the FP32-vs-FP64 horizon comparison (config 2: 5000; 0: skip)")
+    ap.add_argument("--horizon-every", type=int, default=500)
     ap.add_argument("--extra-only", action="store_true", help="run only the corrector and 4096^2 legs")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -561,8 +625,12 @@ def main():
         s.close()
 
     # the secondary workloads run once, on rank 0 (replicas add nothing to them)
-    ens = corr = c5 = None
+    ens = corr = c5 = f64 = horizon = None
     if rank == 0:
+        if args.fp64_steps > 0:
+            f64 = fp64_leg(n, args.fp64_steps)
+        if args.horizon_steps > 0:
+            horizon = horizon_leg(n, args.horizon_steps, max(1, args.horizon_every))
         if args.ensemble_steps > 0:
             ens = ensemble_leg(args.ensemble_steps, tiling=ens_tiling)
         if not args.no_extra:
@@ -580,6 +648,8 @@ def main():
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
         "gpu_launches": launches, "wall_s_timed_region": t_wall,
         "fp32_vs_fp64": fp32_cmp,
+        "fp64": f64,
+        "fp32_vs_fp64_horizon": horizon,
         "ensemble": ens,
         "corrector": corr,
         "config5_4096": c5,

@@ -82,8 +82,15 @@ enum { NS_GPU_RK4 = 0, NS_GPU_IFRK4 = 1 };
 /* ----------------------------------------------------------- lifetime */
 
 /* Replaces the device side of ns_spectral_allocate / initialize_fft_plans
- * (spectral_memory.c:6-68, spectral_initialization.c:57-69).  nx, ny must be
- * powers of two in [8, 4096]; precision is NS_GPU_FP64 or NS_GPU_FP32. */
+ * (spectral_memory.c:6-68, spectral_initialization.c:57-69).  The reference's
+ * FFTW takes any size; here nx and ny lie in [8, 4096] and each transform
+ * length (nx/2 for even nx, nx for odd nx; ny) has no prime factor above 31
+ * (every 2^a 3^b 5^c 7^d grid qualifies; a prime factor p costs a direct
+ * p-point pass).  Power-of-two sides run the radix-16/8/4 kernels, other sides
+ * the mixed-radix ones.  Any other size returns NS_GPU_ERR_INVALID with the
+ * reason on stderr, as does a grid whose stage kernels would need more shared
+ * memory than one CTA has (odd nx above about 2700 in FP64).  precision is
+ * NS_GPU_FP64 or NS_GPU_FP32. */
 int ns_gpu_create(int nx, int ny, double Lx, double Ly, int precision, ns_gpu **out);
 /* Per-instance teardown (spectral_memory.c:71-104 without the global fftw_cleanup). */
 void ns_gpu_destroy(ns_gpu *g);

@@ -95,7 +95,10 @@ typedef struct {
 } NSSpectralData;
 
 /* Memory management (spectral_memory.c:6-104).  allocate returns NULL on any
- * failure, including the absence of a CUDA device; free is per instance. */
+ * failure, including the absence of a CUDA device and a size outside what the
+ * device transforms take (nx, ny in [8, 4096], transform lengths nx/2 or odd nx,
+ * and ny, free of prime factors above 31; the reason goes to stderr); free is
+ * per instance. */
 NSSpectralData *ns_spectral_allocate(int nx, int ny, double Lx, double Ly, double Re);
 void ns_spectral_free(NSSpectralData *data);
 

@@ -212,4 +212,143 @@ __device__ void fft_smem(C* sb, int L, int logL, int t, int TT, const C* __restr
     }
 }
 
+// ------------------------------------------------ mixed-radix lengths
+// Lengths that are not powers of two (any L whose prime factors are all small:
+// the reference's FFTW accepts every length) use the same Stockham recurrence
+// with a per-length list of radices, packed one per byte (pass p in byte p of
+// ra for p < 8, of rb for p >= 8; at most 16 passes).  Radices 2, 3, 4, 5, 7 and
+// 8 run from registers; any other (prime) radix R runs as a direct R-point sum.
+// Each pass reads one buffer and writes the other (sb and a scratch sequence sc
+// of the same padded length), so a thread's butterflies need not fit a fixed
+// register budget: thread t of TT takes butterflies t, t + TT, ...  The result
+// ends in sb.  The roots of unity of the odd radices are entries of the same
+// FP64-generated twiddle table, W_R^m = tw[m L / R].
+
+__device__ __forceinline__ int mr_radix(unsigned long long ra, unsigned long long rb, int p) {
+    return (int)(((p < 8) ? (ra >> (8 * p)) : (rb >> (8 * (p - 8)))) & 0xffULL);
+}
+
+template <int R, bool INV, typename C>
+__device__ __forceinline__ void dft_odd(C* a, const C* __restrict__ tw, int L) {
+    const int s = L / R;
+    C y[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+        C acc = a[0];
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+            C w = __ldg(&tw[((q * r) % R) * s]);
+            if (INV) w.y = -w.y;
+            acc = cadd(acc, cmul(a[r], w));
+        }
+        y[q] = acc;
+    }
+#pragma unroll
+    for (int q = 0; q < R; ++q) a[q] = y[q];
+}
+
+template <int R, bool INV, typename C>
+__device__ __forceinline__ void mr_pass(const C* src, C* dst, int L, int Ns, int t, int TT, const C* __restrict__ tw) {
+    const int LR = L / R;
+    const int tstep = L / (Ns * R);
+    for (int j = t; j < LR; j += TT) {
+        const int k = j % Ns;
+        C a[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) a[r] = src[spad(j + r * LR)];
+        if (Ns > 1) {
+#pragma unroll
+            for (int r = 1; r < R; ++r) {
+                C w = __ldg(&tw[tstep * k * r]);
+                if (INV) w.y = -w.y;
+                a[r] = cmul(a[r], w);
+            }
+        }
+        if constexpr (R == 3 || R == 5 || R == 7) dft_odd<R, INV>(a, tw, L);
+        else dftR<R, INV>(a);
+        const int base = (j - k) * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) dst[spad(base + r * Ns)] = a[r];
+    }
+}
+
+// any radix R as the direct sum y_q = sum_r W_R^{qr} W_{Ns R}^{kr} x_r
+template <bool INV, typename C>
+__device__ void mr_pass_direct(const C* src, C* dst, int L, int R, int Ns, int t, int TT, const C* __restrict__ tw) {
+    const int LR = L / R;
+    const int tstep = L / (Ns * R);
+    for (int j = t; j < LR; j += TT) {
+        const int k = j % Ns;
+        const int base = (j - k) * R + k;
+        for (int q = 0; q < R; ++q) {
+            C acc = src[spad(j)];
+            for (int r = 1; r < R; ++r) {
+                C x = src[spad(j + r * LR)];
+                C w = __ldg(&tw[(tstep * k * r) % L]);
+                C v = __ldg(&tw[((q * r) % R) * LR]);
+                if (INV) { w.y = -w.y; v.y = -v.y; }
+                acc = cadd(acc, cmul(cmul(x, w), v));
+            }
+            dst[spad(base + q * Ns)] = acc;
+        }
+    }
+}
+
+// In-place (through sc) FFT of the sequence at sb; all threads of the CTA call
+// it (it synchronises), thread t < TT of this sequence.
+template <bool INV, typename C>
+__device__ void fft_smem_mr(C* sb, C* sc, int L, unsigned long long ra, unsigned long long rb, int np, int t, int TT,
+                            const C* __restrict__ tw) {
+    C* src = sb;
+    C* dst = sc;
+    int Ns = 1;
+    for (int p = 0; p < np; ++p) {
+        const int R = mr_radix(ra, rb, p);
+        switch (R) {
+            case 2: mr_pass<2, INV>(src, dst, L, Ns, t, TT, tw); break;
+            case 3: mr_pass<3, INV>(src, dst, L, Ns, t, TT, tw); break;
+            case 4: mr_pass<4, INV>(src, dst, L, Ns, t, TT, tw); break;
+            case 5: mr_pass<5, INV>(src, dst, L, Ns, t, TT, tw); break;
+            case 7: mr_pass<7, INV>(src, dst, L, Ns, t, TT, tw); break;
+            case 8: mr_pass<8, INV>(src, dst, L, Ns, t, TT, tw); break;
+            default: mr_pass_direct<INV>(src, dst, L, R, Ns, t, TT, tw); break;
+        }
+        __syncthreads();
+        C* x = src;
+        src = dst;
+        dst = x;
+        Ns *= R;
+    }
+    if (src != sb) {
+        for (int i = t; i < L; i += TT) sb[spad(i)] = src[spad(i)];
+        __syncthreads();
+    }
+}
+
+// Radix list of a length for fft_smem_mr: 8s, then 4, 2, 3, 5, 7, then the
+// remaining prime factors in increasing order.  Returns the number of passes,
+// or -1 when a prime factor exceeds max_prime or more than 16 passes are needed.
+static inline int mr_plan(int L, int max_prime, unsigned long long* ra, unsigned long long* rb) {
+    int rad[64];
+    int n = 0, m = L;
+    while (m % 8 == 0 && n < 64) { rad[n++] = 8; m /= 8; }
+    while (m % 4 == 0 && n < 64) { rad[n++] = 4; m /= 4; }
+    while (m % 2 == 0 && n < 64) { rad[n++] = 2; m /= 2; }
+    for (int p = 3; p <= m && n < 64; p += 2) {
+        while (m % p == 0 && n < 64) {
+            if (p > max_prime) return -1;
+            rad[n++] = p;
+            m /= p;
+        }
+    }
+    if (m != 1 || n > 16) return -1;
+    *ra = 0;
+    *rb = 0;
+    for (int p = 0; p < n; ++p) {
+        if (p < 8) *ra |= (unsigned long long)rad[p] << (8 * p);
+        else *rb |= (unsigned long long)rad[p] << (8 * (p - 8));
+    }
+    return n;
+}
+
 }  // namespace nsg

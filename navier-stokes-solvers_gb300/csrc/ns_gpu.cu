@@ -7,6 +7,7 @@
 // entry points synchronise that stream before returning.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -29,6 +30,9 @@ static int ilog2(int n) {
     return l;
 }
 static int is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+// largest prime factor a transform length may have (one direct p-point pass)
+#define NSG_MAX_PRIME 31
 
 static int grid_for(long long n, int threads = 256, int cap = 2048) {
     long long b = (n + threads - 1) / threads;
@@ -71,26 +75,29 @@ template <typename K> static int set_smem(ns_gpu* g, K kernel, size_t bytes) {
 
 template <typename T, int E, int MODE> static int row_launch_e(ns_gpu* g, const RowArgs<T>& a) {
     const int NF = RowNF<MODE>::v;
-    const int TT = g->g.H / E;
-    const size_t smem = (size_t)NF * g->g.RPC * spad_len(g->g.H) * sizeof(Cx<T>);
+    const int TT = E ? g->g.H / E : g->g.TTr;
+    // E = 0 (mixed radix): one scratch sequence per row after the NF field buffers
+    const size_t smem = (size_t)(NF + (E ? 0 : 1)) * g->g.RPC * spad_len(g->g.H) * sizeof(Cx<T>);
     NSG_TRY(set_smem(g, k_row<T, E, MODE>, smem));
     k_row<T, E, MODE><<<g->g.ny / g->g.RPC, g->g.RPC * TT, smem, g->st>>>(g->g, a);
     NSG_LAUNCHED(g);
     return NS_GPU_OK;
 }
 template <typename T, int MODE> static int row_launch(ns_gpu* g, const RowArgs<T>& a) {
+    if (g->ER == 0) return row_launch_e<T, 0, MODE>(g, a);
     return g->ER == 16 ? row_launch_e<T, 16, MODE>(g, a) : row_launch_e<T, 4, MODE>(g, a);
 }
 
 template <typename T, int E, int MODE, int STAGE> static int col_launch_e(ns_gpu* g, const ColArgs<T>& a) {
-    const int TC = g->g.ny / E;
-    const size_t smem = (size_t)g->g.CW * spad_len(g->g.ny) * sizeof(Cx<T>);
+    const int TC = E ? g->g.ny / E : g->g.TTc;
+    const size_t smem = (size_t)(E ? 1 : 2) * g->g.CW * spad_len(g->g.ny) * sizeof(Cx<T>);
     NSG_TRY(set_smem(g, k_col<T, E, MODE, STAGE>, smem));
     k_col<T, E, MODE, STAGE><<<g->g.Kxp / g->g.CW, g->g.CW * TC, smem, g->st>>>(g->g, a);
     NSG_LAUNCHED(g);
     return NS_GPU_OK;
 }
 template <typename T, int MODE, int STAGE> static int col_launch(ns_gpu* g, const ColArgs<T>& a) {
+    if (g->EC == 0) return col_launch_e<T, 0, MODE, STAGE>(g, a);
     return g->EC == 16 ? col_launch_e<T, 16, MODE, STAGE>(g, a) : col_launch_e<T, 4, MODE, STAGE>(g, a);
 }
 
@@ -443,10 +450,23 @@ void ns_gpu_destroy(ns_gpu* g) {
 int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTiling* kc, ns_gpu** out) {
     if (!out) return NS_GPU_ERR_INVALID;
     *out = nullptr;
-    if (!is_pow2(nx) || !is_pow2(ny) || nx < 8 || ny < 8 || nx > 4096 || ny > 4096) {
-        fprintf(stderr, "ns_gpu_create: nx=%d ny=%d must be powers of two in [8, 4096]\n", nx, ny);
+    // Any side in [8, 4096] whose transform lengths (nx/2 for even nx, nx for odd
+    // nx; ny) factor into primes up to NSG_MAX_PRIME: a prime factor p is one
+    // direct p-point pass, p operations per output, so large primes are refused
+    // rather than run at quadratic cost.
+    unsigned long long rxa = 0, rxb = 0, rya = 0, ryb = 0;
+    const int oddx = (nx & 1);
+    const int Hlen = oddx ? nx : nx / 2;
+    const int nrx = (nx >= 8 && nx <= 4096) ? mr_plan(Hlen, NSG_MAX_PRIME, &rxa, &rxb) : -1;
+    const int nry = (ny >= 8 && ny <= 4096) ? mr_plan(ny, NSG_MAX_PRIME, &rya, &ryb) : -1;
+    if (nrx < 0 || nry < 0) {
+        fprintf(stderr,
+                "ns_gpu_create: nx=%d ny=%d: each side must lie in [8, 4096] and its transform length (nx/2 for even "
+                "nx, nx for odd nx; ny) have no prime factor above %d\n",
+                nx, ny, NSG_MAX_PRIME);
         return NS_GPU_ERR_INVALID;
     }
+    const int pow2_grid = is_pow2(nx) && is_pow2(ny);
     if (!(Lx > 0.0) || !(Ly > 0.0) || (precision != NS_GPU_FP64 && precision != NS_GPU_FP32)) return NS_GPU_ERR_INVALID;
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
@@ -485,8 +505,11 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
         const char* gen = getenv("NS_GB300_GENERIC_KERNELS");
         const int generic = (gen && gen[0] == '1') || (kc && (kc->er || kc->ec));
         // FP32 also has register-resident row and column passes at 4096
-        g->fast_row = (!generic && (nx == 2048 || (nx == 4096 && precision == NS_GPU_FP32))) ? 1 : 0;
-        g->fast_col = (!generic && (ny == 2048 || (ny == 4096 && precision == NS_GPU_FP32 && NSG_COL_Q))) ? 1 : 0;
+        // (their F/G layouts assume a power-of-two ny)
+        g->fast_row = (!generic && pow2_grid && (nx == 2048 || (nx == 4096 && precision == NS_GPU_FP32))) ? 1 : 0;
+        g->fast_col = (!generic && pow2_grid && (ny == 2048 || (ny == 4096 && precision == NS_GPU_FP32 && NSG_COL_Q)))
+                          ? 1
+                          : 0;
     }
     if (cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking) != cudaSuccess) {
         delete g;
@@ -497,12 +520,22 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
     G.ny = ny;
     G.nkx = nx / 2 + 1;
     G.nky = ny;
-    G.H = nx / 2;
+    G.H = Hlen;
     G.Kx = (2 * G.nkx) / 3 + 1;
     G.Kyh = (2 * ny) / 6;
     G.Ky = 2 * G.Kyh + 1;
     G.logny = ilog2(ny);
     G.logH = ilog2(G.H);
+    G.rxa = rxa;
+    G.rxb = rxb;
+    G.rya = rya;
+    G.ryb = ryb;
+    G.nrx = nrx;
+    G.nry = nry;
+    G.oddx = oddx;
+    // mixed-radix threads per sequence: about one per eight points, whole warps, at most 256
+    G.TTr = std::min(256, std::max(32, ((G.H + 7) / 8 + 31) / 32 * 32));
+    G.TTc = std::min(256, std::max(32, ((ny + 7) / 8 + 31) / 32 * 32));
     G.Lx = Lx;
     G.Ly = Ly;
     // With the register-resident stage kernels F and G are both kx-column-contiguous
@@ -514,14 +547,17 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
     // automatic tiling: 16 values per thread from 512-point transforms up (a
     // row or column keeps at least 32 threads), 4 values per thread below, so
     // that small grids still fill warps and spread over the SMs
-    g->ER = (kc && kc->er) ? kc->er : (G.H >= 512 ? 16 : 4);
-    g->EC = (kc && kc->ec) ? kc->ec : (ny >= 512 ? 16 : 4);
+    // (E = 0: the mixed-radix bodies, for lengths that are not powers of two)
+    const int mr_row = oddx || !is_pow2(G.H), mr_col = !is_pow2(ny);
+    g->ER = mr_row ? 0 : (kc && kc->er) ? kc->er : (G.H >= 512 ? 16 : 4);
+    g->EC = mr_col ? 0 : (kc && kc->ec) ? kc->ec : (ny >= 512 ? 16 : 4);
     const size_t cs = (precision == NS_GPU_FP64) ? sizeof(double2) : sizeof(float2);
     // column tile width: up to 16 columns, <= 512 threads, <= ~100 KB shared memory
     {
-        const int TC = ny / g->EC;
+        const int TC = g->EC ? ny / g->EC : G.TTc;
+        const int nbuf = g->EC ? 1 : 2;
         int CW = 1;
-        while (CW < 16 && 2 * CW * TC <= 512 && (size_t)2 * CW * spad_len(ny) * cs <= 100 * 1024 && CW < G.Kx &&
+        while (CW < 16 && 2 * CW * TC <= 512 && (size_t)nbuf * 2 * CW * spad_len(ny) * cs <= 100 * 1024 && CW < G.Kx &&
                G.Kx / (2 * CW) >= g->num_sms)
             CW *= 2;
         if (kc && kc->cw) CW = kc->cw;
@@ -532,13 +568,31 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
     }
     // rows per CTA: up to 128 threads, <= ~100 KB shared memory for four fields
     {
-        const int TT = G.H / g->ER;
+        const int TT = g->ER ? G.H / g->ER : G.TTr;
+        const int nbuf = g->ER ? 4 : 5;  // four field buffers (+ the mixed-radix scratch)
         int RPC = 1;
-        while (2 * RPC * TT <= 128 && 2 * RPC <= ny && (size_t)4 * 2 * RPC * spad_len(G.H) * cs <= 100 * 1024 &&
-               ny / (2 * RPC) >= g->num_sms)
+        while (2 * RPC * TT <= 128 && 2 * RPC <= ny && ny % (2 * RPC) == 0 &&
+               (size_t)nbuf * 2 * RPC * spad_len(G.H) * cs <= 100 * 1024 && ny / (2 * RPC) >= g->num_sms)
             RPC *= 2;
         if (kc && kc->rpc) RPC = kc->rpc;
         G.RPC = RPC;
+    }
+    // the stage kernels' shared memory must fit one CTA (odd nx near the upper
+    // bound needs the full length-nx row in five buffers)
+    {
+        int optin = 0;
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, g->device);
+        const size_t row_sm = (size_t)(g->ER ? 4 : 5) * G.RPC * spad_len(G.H) * cs;
+        const size_t col_sm = (size_t)(g->EC ? 1 : 2) * G.CW * spad_len(ny) * cs;
+        if (optin > 0 && (row_sm > (size_t)optin || col_sm > (size_t)optin)) {
+            fprintf(stderr,
+                    "ns_gpu_create: nx=%d ny=%d: the stage kernels need %zu / %zu bytes of shared memory per CTA, above "
+                    "the device's %d\n",
+                    nx, ny, row_sm, col_sm, optin);
+            cudaStreamDestroy(g->st);
+            delete g;
+            return NS_GPU_ERR_INVALID;
+        }
     }
     const size_t A = (size_t)ny * G.Kxp * cs;
     const size_t Cb = (size_t)G.Kxp * G.Ky * cs;

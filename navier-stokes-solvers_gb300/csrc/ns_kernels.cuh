@@ -37,7 +37,23 @@ struct Geo {
     int RPC;        // rows per row-kernel CTA
     int fLB;        // F stored in blocks of 2^fLB rows: [ny >> fLB][Kxp][1 << fLB]
     int fTG;        // G stored kx-column-contiguous
+    // mixed-radix transforms (lengths that are not powers of two; the stage
+    // bodies instantiated with E = 0): radix lists of the row (length H) and
+    // column (length ny) transforms, their pass counts and threads per sequence.
+    // oddx: nx is odd, so the row transform is the full complex length nx
+    // (H = nx) with Hermitian-extended input instead of the half-length packing.
+    unsigned long long rxa, rxb, rya, ryb;
+    int nrx, nry, TTr, TTc, oddx;
 };
+
+// one transform of a row or column buffer b: the power-of-two engine for E > 0,
+// the mixed-radix engine (through the scratch sequence sc) for E == 0
+template <int E, bool INV, typename C>
+__device__ __forceinline__ void fft_any(C* b, C* sc, int L, int logL, unsigned long long ra, unsigned long long rb, int np,
+                                        int t, int TT, const C* __restrict__ tw) {
+    if constexpr (E == 0) fft_smem_mr<INV>(b, sc, L, ra, rb, np, t, TT, tw);
+    else fft_smem<E, INV>(b, L, logL, t, TT, tw);
+}
 
 // element (row y, kept column c) of an F buffer / of the G buffer
 __device__ __forceinline__ size_t fidx(const Geo& g, int y, int c) {
@@ -199,19 +215,23 @@ template <typename T> struct RowArgs {
 
 template <int MODE> struct RowNF { static const int v = (MODE == ROW_STAGE || MODE == ROW_DUMP) ? 4 : (MODE == ROW_UVW ? 3 : 1); };
 
-// grid = ny / RPC, block = RPC * (H / E), dynamic smem = NF * RPC * spad_len(H) * sizeof(C)
+// grid = ny / RPC, block = RPC * TT with TT = H / E (E > 0) or g.TTr (E = 0),
+// dynamic smem = NF * RPC * spad_len(H) * sizeof(C), plus RPC * spad_len(H) *
+// sizeof(C) of mixed-radix scratch when E = 0
 // body of the row pass for row block bx (rows bx*RPC .. bx*RPC + RPC - 1); the
-// block must have exactly RPC * (H / E) threads
+// block must have exactly RPC * TT threads
 template <typename T, int E, int MODE>
 __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, const int bx) {
     typedef typename CT<T>::C C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* sm = reinterpret_cast<C*>(smem_raw);
     constexpr int NF = RowNF<MODE>::v;
-    const int H = g.H, TT = H / E, LP = spad_len(H);
+    const int H = g.H, TT = (E == 0) ? g.TTr : H / E, LP = spad_len(H);
     const int r = threadIdx.x / TT, t = threadIdx.x - r * TT;
     const int y = bx * g.RPC + r;
     const int nx = g.nx, Kx = g.Kx;
+    C* scr = sm + (NF * g.RPC + r) * LP;  // mixed-radix scratch of this row (E = 0 only)
+    const bool oddx = (E == 0) && g.oddx;
 
     if (MODE == ROW_STAGE && bx == 0 && threadIdx.x == 0) {
         if (a.marker == 1) {
@@ -227,29 +247,38 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
         const double* src = a.in_real + (size_t)y * nx;
         for (int m = t; m < H; m += TT) {
             C z;
-            z.x = (T)src[2 * m];
-            z.y = (T)src[2 * m + 1];
+            if (oddx) {
+                z.x = (T)src[m];
+                z.y = (T)0;
+            } else {
+                z.x = (T)src[2 * m];
+                z.y = (T)src[2 * m + 1];
+            }
             b[spad(m)] = z;
         }
         __syncthreads();
-        fft_smem<E, false>(b, H, g.logH, t, TT, a.twr);
+        fft_any<E, false>(b, scr, H, g.logH, g.rxa, g.rxb, g.nrx, t, TT, a.twr);
     } else {
-        // half spectra X_f[k], k < Kx (zero above)
+        // half spectra X_f[k], k < Kx (zero above); odd nx: the full Hermitian
+        // spectrum X[k], X[nx - k] = conj X[k], of the length-nx transform
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
             C* b = sm + (f * g.RPC + r) * LP;
             const C* src = a.F[f];
             for (int k = t; k < H; k += TT) {
+                const bool mirror = oddx && k >= g.nkx;
+                const int kk = mirror ? nx - k : k;
                 C x = cmake<C>(0.0, 0.0);
-                if (k < Kx) {
-                    x = src[fidx(g, y, k)];
+                if (kk < Kx) {
+                    x = src[fidx(g, y, kk)];
                     if (a.dx[f]) {
-                        const T kx = a.kxv[k];
+                        const T kx = a.kxv[kk];
                         C d;
                         d.x = -kx * x.y;
                         d.y = kx * x.x;
                         x = d;
                     }
+                    if (mirror) x.y = -x.y;
                 }
                 b[spad(k)] = x;
             }
@@ -259,7 +288,7 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
         // Z[k] = (X[k] + conj X[H-k]) + i exp(+2 pi i k/nx) (X[k] - conj X[H-k]);
         // the imaginary parts of X[0] and the Nyquist bin (zero here) are ignored.
 #pragma unroll
-        for (int f = 0; f < NF; ++f) {
+        for (int f = 0; f < NF && !oddx; ++f) {
             C* b = sm + (f * g.RPC + r) * LP;
             for (int k = t; 2 * k <= H; k += TT) {
                 if (k == 0) {
@@ -282,9 +311,10 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
                 }
             }
         }
-        __syncthreads();
+        if (!oddx) __syncthreads();
 #pragma unroll
-        for (int f = 0; f < NF; ++f) fft_smem<E, true>(sm + (f * g.RPC + r) * LP, H, g.logH, t, TT, a.twr);
+        for (int f = 0; f < NF; ++f)
+            fft_any<E, true>(sm + (f * g.RPC + r) * LP, scr, H, g.logH, g.rxa, g.rxb, g.nrx, t, TT, a.twr);
 
         if constexpr (MODE == ROW_STAGE || MODE == ROW_DUMP) {
             C* b0 = sm + (0 * g.RPC + r) * LP;
@@ -292,7 +322,24 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
             const C* b2 = sm + (2 * g.RPC + r) * LP;
             const C* b3 = sm + (3 * g.RPC + r) * LP;
             T vmax2 = (T)0;
-            for (int m = t; m < H; m += TT) {
+            if (oddx) {
+                // one grid point per element (the real parts of the length-nx inverse)
+                for (int m = t; m < H; m += TT) {
+                    const T p0 = b0[spad(m)].x, p1 = b1[spad(m)].x, p2 = b2[spad(m)].x, p3 = b3[spad(m)].x;
+                    const T jv = p0 * p3 - p1 * p2;
+                    if (a.cfl) vmax2 = fmax(vmax2, p0 * p0 + p1 * p1);
+                    if constexpr (MODE == ROW_DUMP) {
+                        const size_t o = (size_t)y * nx + m;
+                        a.out_real[0][o] = p0;
+                        a.out_real[1][o] = p1;
+                        a.out_real[2][o] = p2;
+                        a.out_real[3][o] = p3;
+                        a.out_real[4][o] = jv;
+                    }
+                    b0[spad(m)] = cmake<C>(jv, 0.0);
+                }
+            }
+            for (int m = oddx ? H : t; m < H; m += TT) {
                 const C z0 = b0[spad(m)], z1 = b1[spad(m)], z2 = b2[spad(m)], z3 = b3[spad(m)];
                 // z0 = psi_x, z1 = psi_y, z2 = omega_x, z3 = omega_y at points 2m (re) and 2m+1 (im)
                 const T je = z0.x * z3.x - z1.x * z2.x;
@@ -321,9 +368,23 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
                 }
             }
             __syncthreads();
-            fft_smem<E, false>(b0, H, g.logH, t, TT, a.twr);
+            fft_any<E, false>(b0, scr, H, g.logH, g.rxa, g.rxb, g.nrx, t, TT, a.twr);
         } else {
             const C* b0 = sm + (0 * g.RPC + r) * LP;
+            if (oddx) {
+                for (int m = t; m < H; m += TT) {
+                    const size_t o = (size_t)y * nx + m;
+                    const T p0 = b0[spad(m)].x;
+                    if constexpr (MODE == ROW_UVW) {
+                        a.out_real[0][o] = p0;                                 // u = psi_y
+                        a.out_real[1][o] = -sm[(1 * g.RPC + r) * LP + spad(m)].x;  // v = -psi_x
+                        a.out_real[2][o] = sm[(2 * g.RPC + r) * LP + spad(m)].x;   // omega
+                    } else {
+                        a.out_real[0][o] = p0;
+                    }
+                }
+                return;
+            }
             for (int m = t; m < H; m += TT) {
                 const size_t o = (size_t)y * nx + 2 * m;
                 const C z0 = b0[spad(m)];
@@ -346,10 +407,14 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
     {
         const C* b0 = sm + r * LP;
         C* dst = a.G;
+        if (oddx) {  // the length-nx transform of the real row: X[k] directly
+            for (int k = t; k < Kx; k += TT) dst[gidx(g, y, k)] = b0[spad(k)];
+            return;
+        }
         const T half = (T)0.5;
         for (int k = t; k < Kx; k += TT) {
             const C wa = b0[spad(k)];
-            const C wb = b0[spad((H - k) & (H - 1))];
+            const C wb = b0[spad(k == 0 ? 0 : H - k)];
             C ev, od;
             ev.x = half * (wa.x + wb.x);
             ev.y = half * (wa.y - wb.y);
@@ -543,20 +608,23 @@ __device__ __forceinline__ C post_step_mode(const Geo& g, const ColArgs<T>& a, i
     return wn;
 }
 
-// grid = Kxp / CW, block = CW * (ny / E), dynamic smem = CW * spad_len(ny) * sizeof(C)
+// grid = Kxp / CW, block = CW * TC with TC = ny / E (E > 0) or g.TTc (E = 0),
+// dynamic smem = CW * spad_len(ny) * sizeof(C), twice that when E = 0 (the
+// mixed-radix scratch)
 // body of the column pass for column block bx (kept columns bx*CW .. bx*CW + CW - 1);
-// the block must have exactly CW * (ny / E) threads
+// the block must have exactly CW * TC threads
 template <typename T, int E, int MODE, int STAGE>
 __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, const int bx) {
     typedef typename CT<T>::C C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* sm = reinterpret_cast<C*>(smem_raw);
-    const int ny = g.ny, TC = ny / E, LP = spad_len(ny), CW = g.CW;
+    const int ny = g.ny, TC = (E == 0) ? g.TTc : ny / E, LP = spad_len(ny), CW = g.CW;
     const int b = threadIdx.x / TC, t = threadIdx.x - b * TC;
     const int c0 = bx * CW;
     const int Kx = g.Kx, Ky = g.Ky;
     const int nthr = blockDim.x;
     C* mybuf = sm + b * LP;
+    C* myscr = sm + (CW + b) * LP;  // mixed-radix scratch (E = 0 only)
     __shared__ double s_dt;
 
     if (MODE == COL_STAGE) {
@@ -591,7 +659,7 @@ __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, cons
             sm[c * LP + spad(y)] = v;
         }
         __syncthreads();
-        fft_smem<E, false>(mybuf, ny, g.logny, t, TC, a.twc);
+        fft_any<E, false>(mybuf, myscr, ny, g.logny, g.rya, g.ryb, g.nry, t, TC, a.twc);
 
         if constexpr (MODE == COL_FWD_EXPORT || MODE == COL_NL_EXPORT) {
             const T sc = (T)a.out_scale;
@@ -671,7 +739,7 @@ __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, cons
             sm[c * LP + spad(j)] = v;
         }
         __syncthreads();
-        fft_smem<E, true>(mybuf, ny, g.logny, t, TC, a.twc);
+        fft_any<E, true>(mybuf, myscr, ny, g.logny, g.rya, g.ryb, g.nry, t, TC, a.twc);
         C* dstF = a.F[f];
         for (int idx = threadIdx.x; idx < ny * CW; idx += nthr) {
             int y, c;

@@ -13,8 +13,8 @@
  *   x[n] = sum_k X[k] exp(+2 pi i k n / N)         (backward, unnormalised)
  *
  * Power-of-two lengths use an iterative radix-2 decimation-in-time
- * Cooley-Tukey transform (Cooley & Tukey 1965); other lengths use the direct
- * O(N^2) sum.  Column transforms run on blocks of columns interleaved so the
+ * Cooley-Tukey transform (Cooley & Tukey 1965); other lengths a mixed-radix
+ * Stockham transform over their prime factors (each pass a direct p-point sum).  Column transforms run on blocks of columns interleaved so the
  * innermost loop is unit-stride across the block.  The real transforms of
  * length N (even) use the standard half-length packing z[m] = x[2m] + i x[2m+1]
  * with the even/odd split X[k] = E[k] + W^k O[k].  OpenMP threads follow
@@ -68,6 +68,8 @@ static void shim_cossin(long k, long n, double *c, double *s) {
 typedef struct {
     int n;
     int pow2;
+    int nfac;     /* prime-factor radices of a non-power-of-two length */
+    int fac[32];
     int *bitrev;
     double *wr; /* cos(2 pi k/n), k < n */
     double *wi; /* -sin(2 pi k/n): forward twiddle exp(-2 pi i k/n) */
@@ -87,6 +89,13 @@ static int shim_cfft_init(shim_cfft *f, int n) {
         shim_cossin(k, n, &c, &s);
         f->wr[k] = c;
         f->wi[k] = -s;
+    }
+    if (!f->pow2) {
+        int m = n;
+        while (m % 4 == 0) { f->fac[f->nfac++] = 4; m /= 4; }
+        while (m % 2 == 0) { f->fac[f->nfac++] = 2; m /= 2; }
+        for (int p = 3; m > 1; p += 2)
+            while (m % p == 0) { f->fac[f->nfac++] = p; m /= p; }
     }
     if (f->pow2) {
         f->bitrev = (int *)malloc(sizeof(int) * (size_t)n);
@@ -154,26 +163,48 @@ static void shim_cfft_batch(const shim_cfft *f, double *re, double *im, int B, i
         }
         return;
     }
-    /* direct DFT for other lengths */
-    double *orr = scratch;
-    double *oii = scratch + (size_t)n * B;
-    for (int k = 0; k < n; ++k) {
-        for (int b = 0; b < B; ++b) {
-            double sr = 0.0, si = 0.0;
-            for (int t = 0; t < n; ++t) {
-                const long idx = ((long)k * t) % n;
-                const double wr = f->wr[idx];
-                const double wi = (sign < 0) ? f->wi[idx] : -f->wi[idx];
-                const double xr = re[t * B + b], xi = im[t * B + b];
-                sr += xr * wr - xi * wi;
-                si += xr * wi + xi * wr;
+    /* other lengths: mixed-radix Stockham autosort (Cooley-Tukey over the prime
+     * factors of n, each pass a direct p-point DFT of the twiddled inputs):
+     *   butterfly j in [0, n/p), k = j mod Ns:
+     *     Y[(j - k) p + k + q Ns] = sum_r X[j + r n/p] W_n^{(k r n/(Ns p)) + (q r mod p) n/p}
+     * ping-ponging between the data and the scratch arrays */
+    double *sr = re, *si = im;
+    double *dr = scratch, *di = scratch + (size_t)n * B;
+    int Ns = 1;
+    for (int pi = 0; pi < f->nfac; ++pi) {
+        const int R = f->fac[pi];
+        const int LR = n / R, tstep = n / (Ns * R);
+        for (int j = 0; j < LR; ++j) {
+            const int k = j % Ns;
+            const int base = (j - k) * R + k;
+            for (int q = 0; q < R; ++q) {
+                double *yr = dr + (size_t)(base + q * Ns) * B;
+                double *yi = di + (size_t)(base + q * Ns) * B;
+                for (int b = 0; b < B; ++b) {
+                    yr[b] = 0.0;
+                    yi[b] = 0.0;
+                }
+                for (int r = 0; r < R; ++r) {
+                    const long idx = ((long)tstep * k * r + (long)LR * ((q * r) % R)) % n;
+                    const double wr = f->wr[idx];
+                    const double wi = (sign < 0) ? f->wi[idx] : -f->wi[idx];
+                    const double *xr = sr + (size_t)(j + r * LR) * B;
+                    const double *xi = si + (size_t)(j + r * LR) * B;
+                    for (int b = 0; b < B; ++b) {
+                        yr[b] += xr[b] * wr - xi[b] * wi;
+                        yi[b] += xr[b] * wi + xi[b] * wr;
+                    }
+                }
             }
-            orr[k * B + b] = sr;
-            oii[k * B + b] = si;
         }
+        double *t = sr; sr = dr; dr = t;
+        t = si; si = di; di = t;
+        Ns *= R;
     }
-    memcpy(re, orr, sizeof(double) * (size_t)n * B);
-    memcpy(im, oii, sizeof(double) * (size_t)n * B);
+    if (sr != re) {
+        memcpy(re, sr, sizeof(double) * (size_t)n * B);
+        memcpy(im, si, sizeof(double) * (size_t)n * B);
+    }
 }
 
 struct fftw_plan_s {

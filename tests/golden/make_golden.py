@@ -45,6 +45,11 @@ def random_field(nx, ny, seed):
     return np.fft.irfft2(fh, s=(ny, nx))
 
 
+HV_SFD = dict(enabled=1, coefficient=0.5, order=4, cutoff_ratio=0.5, sfd_enabled=1, sfd_strength=0.2,
+              sfd_timescale=0.3)
+HV_ONLY = dict(enabled=1, coefficient=0.3, order=8, cutoff_ratio=0.65)
+
+
 def config1(ref, n, steps):
     """Config 1: omega0 = 2 sin x sin y written into omega, physical_to_spectral,
     compute_derivatives (as performance_benchmark.c:63), nu = 0.01, dt = 1e-3."""
@@ -61,13 +66,22 @@ def config1(ref, n, steps):
     return out
 
 
-def random_hv(ref, n, steps, seed=1):
-    s = O.Solver(ref, n, n, Re=1000.0).setup(ic=None)
-    w = random_field(n, n, seed)
+def config1_benchmark_case(ref, n, steps):
+    """Config-1 physics on the reference benchmark's non-power-of-two grid
+    (performance_benchmark.c:103 runs 192^2 for 150 steps): omega_hat, time,
+    energy and enstrophy only (the spectrum of this run is a few modes plus
+    round-off, so one array is the whole check)."""
+    out = config1(ref, n, steps)
+    return {k: out[k] for k in ("omega_hat", "t", "energy", "enstrophy", "omega_row")}
+
+
+def random_hv(ref, n, steps, seed=1, ny=None, hv=None):
+    ny = n if ny is None else ny
+    s = O.Solver(ref, n, ny, Re=1000.0).setup(ic=None)
+    w = random_field(n, ny, seed)
     s.set_vorticity(w)
     s.derivatives()
-    s.set_hyperviscosity(enabled=1, coefficient=0.5, order=4, cutoff_ratio=0.5, sfd_enabled=1, sfd_strength=0.2,
-                         sfd_timescale=0.3)
+    s.set_hyperviscosity(**(hv or HV_SFD))
     s.d.cfl_factor = 0.5
     omega0 = w.copy()
     dts = []
@@ -149,6 +163,10 @@ def main():
     np.savez_compressed(os.path.join(HERE, "config1_tg32.npz"), **config1(ref, 32, 100))
     np.savez_compressed(os.path.join(HERE, "config1_tg128.npz"), **config1(ref, 128, 1000))
     np.savez_compressed(os.path.join(HERE, "random64_hv_sfd.npz"), **random_hv(ref, 64, 20))
+    # grids that are not powers of two (FFTW, and so the reference, takes any size)
+    np.savez_compressed(os.path.join(HERE, "config1_tg192.npz"), **config1_benchmark_case(ref, 192, 150))
+    np.savez_compressed(os.path.join(HERE, "random96x64_hv_sfd.npz"), **random_hv(ref, 96, 20, seed=2, ny=64))
+    np.savez_compressed(os.path.join(HERE, "random45x30_hv.npz"), **random_hv(ref, 45, 10, seed=4, ny=30, hv=HV_ONLY))
     np.savez_compressed(os.path.join(HERE, "nonlinear_32x16.npz"), **nonlinear(ref, 32, 16))
     np.savez_compressed(os.path.join(HERE, "forcing_toy.npz"), **forcing_case(ref))
     np.savez_compressed(os.path.join(HERE, "analysis64.npz"), **analysis(ref))

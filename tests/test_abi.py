@@ -75,9 +75,27 @@ def test_no_cpu_fallback_without_gpu(nsgb):
         nsgb.Solver(64, 64)
 
 
+def test_non_pow2_sizes_accepted(nsgb):
+    """Sizes the reference's FFTW takes (192^2, 96 x 64, odd 45 x 30, a factor 31)
+    pass validation and reach the device check (here: no device)."""
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present: this checks validation on a host without one")
+    except ImportError:
+        pass
+    lib = nsgb.load()
+    h = C.c_void_p()
+    for nx, ny in [(192, 192), (96, 64), (45, 30), (62, 31), (4095, 8), (8, 3000)]:
+        assert lib.ns_gpu_create(nx, ny, 1.0, 1.0, 0, C.byref(h)) == 2  # NS_GPU_ERR_NO_DEVICE, not INVALID
+
+
 def test_invalid_sizes_rejected_before_any_device_call(nsgb):
     lib = nsgb.load()
     h = C.c_void_p()
-    for nx, ny in [(96, 64), (64, 4), (8192, 64), (0, 64)]:
+    # out of [8, 4096], or a transform length with a prime factor above 31
+    # (74: row length 37; 37 and 2 * 41 * 3: column lengths)
+    for nx, ny in [(64, 4), (8192, 64), (0, 64), (74, 64), (64, 37), (64, 246)]:
         assert lib.ns_gpu_create(nx, ny, 1.0, 1.0, 0, C.byref(h)) == 1  # NS_GPU_ERR_INVALID
     assert lib.ns_gpu_create(64, 64, 1.0, 1.0, 7, C.byref(h)) == 1

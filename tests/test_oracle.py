@@ -23,7 +23,10 @@ def _solver(port, nx, ny, Re=100.0):
     return O.Solver(port, nx, ny, Re=Re).setup(ic=None)
 
 
-@pytest.mark.parametrize("nx,ny", [(32, 32), (64, 16), (128, 64), (12, 10), (8, 8)])
+SHIM_SIZES_MIXED = [(12, 10), (192, 192), (96, 64), (45, 30), (98, 21), (62, 31)]
+
+
+@pytest.mark.parametrize("nx,ny", [(32, 32), (64, 16), (128, 64), (8, 8)] + SHIM_SIZES_MIXED)
 def test_shim_r2c_matches_numpy(port, nx, ny):
     s = _solver(port, nx, ny)
     f = np.random.default_rng(0).standard_normal((ny, nx))
@@ -33,7 +36,7 @@ def test_shim_r2c_matches_numpy(port, nx, ny):
     assert np.abs(s.cplx("u_hat") - ref).max() <= 1e-14 * np.abs(ref).max()
 
 
-@pytest.mark.parametrize("nx,ny", [(32, 32), (64, 16), (128, 64)])
+@pytest.mark.parametrize("nx,ny", [(32, 32), (64, 16), (128, 64)] + SHIM_SIZES_MIXED)
 def test_shim_c2r_matches_numpy(port, nx, ny):
     s = _solver(port, nx, ny)
     f = np.random.default_rng(1).standard_normal((ny, nx))
@@ -80,6 +83,41 @@ def test_random_hv_sfd_matches_reference_fixture(port):
     assert np.allclose(dts, g["dts"], rtol=1e-14, atol=0)
     assert rel_l2(s.cplx("omega_hat"), g["omega_hat"]) <= 1e-14
     assert rel_l2(s.cplx("sfd_hat"), g["sfd_hat"]) <= 1e-14
+
+
+# grids that are not powers of two: the reference (FFTW) accepts any size; its
+# benchmark runs config-1 physics at 192^2 (performance_benchmark.c:103)
+HV_SFD = dict(enabled=1, coefficient=0.5, order=4, cutoff_ratio=0.5, sfd_enabled=1, sfd_strength=0.2,
+              sfd_timescale=0.3)
+HV_ONLY = dict(enabled=1, coefficient=0.3, order=8, cutoff_ratio=0.65)
+
+
+def test_config1_tg192_matches_reference_fixture(port):
+    g = golden("config1_tg192.npz")
+    s = _solver(port, 192, 192)
+    s.set_vorticity(tg_vorticity(192, 192))
+    s.derivatives()
+    s.d.dt = 1e-3
+    s.advance(150)
+    assert rel_l2(s.cplx("omega_hat"), g["omega_hat"]) <= 1e-14
+    assert s.d.t == float(g["t"])
+    assert abs(s.energy() - float(g["energy"])) <= 1e-15
+
+
+@pytest.mark.parametrize("name,nx,ny,hv", [("random96x64_hv_sfd.npz", 96, 64, HV_SFD),
+                                           ("random45x30_hv.npz", 45, 30, HV_ONLY)])
+def test_random_non_pow2_matches_reference_fixture(port, name, nx, ny, hv):
+    g = golden(name)
+    s = _solver(port, nx, ny, Re=1000.0)
+    s.set_vorticity(g["omega0"])
+    s.derivatives()
+    s.set_hyperviscosity(**hv)
+    s.d.cfl_factor = 0.5
+    for dt in g["dts"]:
+        s.d.dt = s.cfl()
+        assert s.d.dt == dt
+        s.advance(1)
+    assert rel_l2(s.cplx("omega_hat"), g["omega_hat"]) <= 1e-14
 
 
 def test_nonlinear_matches_reference_fixture(port):
@@ -145,12 +183,13 @@ def test_taylor_green_decay_on_oracle(port):
 
 
 @pytest.mark.skipif(not O.have_ref(), reason="reference build not present (bit-exact check runs where it is)")
-def test_restatement_bit_exact_vs_reference_build(port):
+@pytest.mark.parametrize("nx,ny", [(32, 32), (96, 64), (45, 30)])
+def test_restatement_bit_exact_vs_reference_build(port, nx, ny):
     ref = O.load("ref")
     os.environ["OMP_NUM_THREADS"] = "1"
-    w = random_field(32, 32, 9)
-    a = O.Solver(port, 32, 32, Re=800.0).setup(ic=None)
-    b = O.Solver(ref, 32, 32, Re=800.0).setup(ic=None)
+    w = random_field(nx, ny, 9)
+    a = O.Solver(port, nx, ny, Re=800.0).setup(ic=None)
+    b = O.Solver(ref, nx, ny, Re=800.0).setup(ic=None)
     for s in (a, b):
         s.set_vorticity(w)
         s.derivatives()
