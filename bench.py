@@ -253,32 +253,45 @@ def ensemble_member_params(n: int, seed: int) -> dict:
                 forcing_epsilon=F_EPS, forcing_seed=F_SEED + 7919 * seed)
 
 
-def ensemble_leg(steps: int, seq_steps: int = 10, tiling=None) -> dict:
+def ensemble_leg(steps: int, seq_steps: int = 10, tiling=None, ws: int = 1, rank: int = 0) -> dict:
     """Config-3 ensemble: one persistent launch (CUDA graph) per `steps` steps versus
     every member advanced alone, one member after another, with the same tiling.
     tiling (threads, row radix, column radix, cluster) skips the autotuner, so the
-    first ensemble launch is the untimed warm-up of that tiling (ncu captures)."""
+    first ensemble launch is the untimed warm-up of that tiling (ncu captures).
+    With ws > 1 ranks, each rank runs the members ns_ensemble_partition gives it
+    (member seeds stay the global member index) and the value is all members'
+    points over the slowest rank's time."""
     import nsgb
 
-    sizes = [n for n, cnt in ENS_MIX for _ in range(cnt)]
+    all_sizes = [n for n, cnt in ENS_MIX for _ in range(cnt)]
+    rank_of, rank_cost = nsgb.ensemble_partition(all_sizes, ws)
+    mine = [i for i in range(len(all_sizes)) if rank_of[i] == rank]
+    sizes = [all_sizes[i] for i in mine]
     ens = nsgb.Ensemble(sizes, 2 * math.pi, config=tuple(tiling) if tiling else (128, 16, 16, 1))
     cache = os.path.join(ROOT, "navier-stokes-solvers_gb300", "_build", "ensemble_tune.jsonl")
     os.makedirs(os.path.dirname(cache), exist_ok=True)
-    for i, (m, n) in enumerate(zip(ens.members, sizes)):
+    for i, m, n in zip(mine, ens.members, sizes):
         m.set_params(**ensemble_member_params(n, i))
         m.random_spectrum(IC_SEED + i, ENS_K0, E0)
     if tiling:
         best, tune_ms = tuple(tiling), None
     else:
         best, tune_ms = ens.autotune(steps=2, cache_path=cache)
-        for i, (m, n) in enumerate(zip(ens.members, sizes)):  # tuning advanced the members: restart
+        for i, m in zip(mine, ens.members):  # tuning advanced the members: restart
             m.random_spectrum(IC_SEED + i, ENS_K0, E0)
     ens.advance(3)
-    ms = ens.advance_timed(steps, 1)
-    points = sum(n * n for n in sizes)
+    barrier(ws)
+    ms = reduce_max(ens.advance_timed(steps, 1), ws)
+    points = sum(n * n for n in all_sizes)
     energies = [m.diagnostics()["energy"] for m in ens.members]
     info = ens.info()
     ens.close()
+    if ws > 1:
+        value = points * steps / (ms * 1e-3)
+        return {"workload": "config-3 ensemble over ranks (256 members: 128 x 64^2, 96 x 128^2, 32 x 256^2)",
+                "metric": "aggregate grid-pt*steps/s", "value": value, "steps": steps, "ms_per_step": ms / steps,
+                "ranks": ws, "members_on_rank0": len(mine), "partition": "ns_ensemble_partition (LPT on n^2 log n^2)",
+                "rank_cost": rank_cost, "scaling": "strong (fixed member set split over ranks)"}
 
     # the same members one after another through the single-instance path
     cfg = nsgb.EnsembleConfig(*best)
@@ -624,15 +637,16 @@ def main():
                "path": "ns_spectral_compute_cfl_timestep + ns_spectral_advance_rk4 per step (FP32 instance)"}
         s.close()
 
-    # the secondary workloads run once, on rank 0 (replicas add nothing to them)
+    # the ensemble members are split over the ranks (ns_ensemble_partition); the
+    # other secondary workloads run once, on rank 0 (replicas add nothing to them)
     ens = corr = c5 = f64 = horizon = None
+    if args.ensemble_steps > 0:
+        ens = ensemble_leg(args.ensemble_steps, tiling=ens_tiling, ws=ws, rank=rank)
     if rank == 0:
         if args.fp64_steps > 0:
             f64 = fp64_leg(n, args.fp64_steps)
         if args.horizon_steps > 0:
             horizon = horizon_leg(n, args.horizon_steps, max(1, args.horizon_every))
-        if args.ensemble_steps > 0:
-            ens = ensemble_leg(args.ensemble_steps, tiling=ens_tiling)
         if not args.no_extra:
             corr = corrector_leg()
             c5 = config5_leg()

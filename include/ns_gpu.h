@@ -284,6 +284,15 @@ typedef struct {
     int cluster;    /* CTAs of a thread-block cluster that share one large member: 1, 2, 4 or 8 */
 } ns_gpu_ensemble_config;
 
+/* Members over ranks (one GPU per rank; no reference counterpart): longest
+ * processing time first on the cost n^2 log2(n^2) of member m's side n[m],
+ * deterministic, so every rank computes the same split with no exchange.
+ * rank_of_member[m] receives the rank of member m; rank_cost (nranks entries,
+ * may be NULL) the summed cost per rank.  Host-only: needs no device. */
+int ns_ensemble_partition(int nmembers, const int *n, int nranks, int *rank_of_member, double *rank_cost);
+/* the cost a member of side n counts for in that partition */
+double ns_ensemble_member_cost(int n);
+
 /* A standalone instance whose stage kernels use an ensemble tiling: the
  * sequential reference run of one ensemble member.  nx == ny. */
 int ns_gpu_create_for_ensemble(int nx, int ny, double Lx, double Ly, int precision,

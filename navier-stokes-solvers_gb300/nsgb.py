@@ -170,6 +170,8 @@ def load(build: bool = True) -> C.CDLL:
     proto("ns_gpu_vorticity_device", C.c_int, vp, vp)
     proto("ns_gpu_add_vorticity_device", C.c_int, vp, vp)
     proto("ns_gpu_filter_state", C.c_int, vp, vp)
+    proto("ns_ensemble_partition", C.c_int, C.c_int, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_int), _DP)
+    proto("ns_ensemble_member_cost", C.c_double, C.c_int)
     proto("ns_cnn_create", C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64, C.POINTER(vp))
     proto("ns_cnn_destroy", None, vp)
     proto("ns_cnn_last_error", C.c_char_p, vp)
@@ -321,6 +323,18 @@ class Solver:
 
     def launches(self) -> int:
         return int(self.lib.ns_gpu_launch_count(self.lib.ns_spectral_gpu_handle(self.ptr)))
+
+
+def ensemble_partition(sizes, nranks: int):
+    """rank of every member (ns_ensemble_partition) and the summed cost per rank"""
+    lib = load()
+    n = (C.c_int * max(1, len(sizes)))(*sizes)
+    out = (C.c_int * max(1, len(sizes)))()
+    cost = (C.c_double * nranks)()
+    st = lib.ns_ensemble_partition(len(sizes), n, nranks, out, cost)
+    if st != 0:
+        raise RuntimeError(f"ns_ensemble_partition failed: {lib.ns_gpu_status_string(st).decode()}")
+    return [int(out[i]) for i in range(len(sizes))], [float(cost[r]) for r in range(nranks)]
 
 
 class Gpu:
