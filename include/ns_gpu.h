@@ -172,6 +172,22 @@ int ns_gpu_advance(ns_gpu *g, int nsteps);
  * u, v, omega are the masked inverse transforms. */
 int ns_gpu_download_state(ns_gpu *g, double *omega_hat, double *psi_hat, double *u_hat, double *v_hat,
                           double *sfd_hat, double *u, double *v, double *omega, double *t, double *dt);
+/* One classical RK4 step over host arrays: ns_gpu_upload_state(omega_hat,
+ * psi_hat, sfd_hat, t, dt, step0), ns_gpu_advance(g, 1) and
+ * ns_gpu_download_state(omega_hat, psi_hat, u_hat, v_hat, sfd_hat, u, v, omega)
+ * in one call (the data movement of ns_spectral_advance_rk4,
+ * spectral_time_integration.c:34-106), with the copies overlapped: psi_hat and
+ * sfd_hat upload on a second stream beside omega_hat, and the output spectra
+ * leave on that stream while the instance stream computes and copies out the
+ * physical fields.  Modes outside the 2/3 mask that were zero in the caller's
+ * omega_hat and psi_hat are zero after the step, so those two arrays only take
+ * their kept modes back (the rest of each array is left as it is, equal to what
+ * a full copy would write).  sfd_hat may be NULL (SFD off); u_hat, v_hat, u, v,
+ * omega may be NULL.  t_out, dt_out (may be NULL) receive the new time and the
+ * step's dt. */
+int ns_gpu_step_host(ns_gpu *g, double *omega_hat, double *psi_hat, double *u_hat, double *v_hat, double *sfd_hat,
+                     double *u, double *v, double *omega, double t, double dt, uint64_t step0, double *t_out,
+                     double *dt_out);
 /* Advance nsteps, timing each step with CUDA events on the instance stream.
  * When flush_bytes > 0 a device buffer of that size is overwritten between
  * steps, outside the timed events, so no timed step starts with the previous

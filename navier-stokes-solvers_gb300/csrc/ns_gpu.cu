@@ -439,6 +439,9 @@ void ns_gpu_destroy(ns_gpu* g) {
         if (g->spec[i]) cudaFree(g->spec[i]);
         if (g->real[i]) cudaFree(g->real[i]);
     }
+    if (g->st2) cudaStreamDestroy(g->st2);
+    if (g->ev_a) cudaEventDestroy(g->ev_a);
+    if (g->ev_b) cudaEventDestroy(g->ev_b);
     if (g->st) cudaStreamDestroy(g->st);
     delete g;
 }
@@ -687,10 +690,9 @@ int ns_gpu_set_params(ns_gpu* g, const ns_gpu_params* p) {
     g->params_set = 1;
     if (hv_changed) NSG_TRY(compute_hv(g));
     if (f_changed) NSG_TRY(compute_sigma(g));
-    if (dt_changed) {
-        double dt = p->dt;
-        NSG_TRY(h2d(g, &g->ds->dt_fixed, &dt, sizeof(double)));
-        NSG_TRY(sync(g));
+    if (dt_changed) {  // a kernel parameter, ordered on the stream: no host copy, no sync
+        k_set_dt_fixed<<<1, 1, 0, g->st>>>(g->ds, p->dt);
+        NSG_LAUNCHED(g);
     }
     if (fsub_changed) {
         unsigned long long m = p->forcing_substeps > 1 ? (unsigned long long)p->forcing_substeps : 1ULL;
@@ -1112,6 +1114,122 @@ int ns_gpu_download_state(ns_gpu* g, double* omega_hat, double* psi_hat, double*
     if (t) *t = h.t;
     if (dt) *dt = h.dt;
     return NS_GPU_OK;
+}
+
+// --------------------------------------------- one step over host arrays
+static int ensure_aux_stream(ns_gpu* g) {
+    if (g->st2) return NS_GPU_OK;
+    NSG_CUDA(g, cudaStreamCreateWithFlags(&g->st2, cudaStreamNonBlocking));
+    NSG_CUDA(g, cudaEventCreateWithFlags(&g->ev_a, cudaEventDisableTiming));
+    NSG_CUDA(g, cudaEventCreateWithFlags(&g->ev_b, cudaEventDisableTiming));
+    return NS_GPU_OK;
+}
+
+// kept modes of a host-layout spectrum [nky][nkx]: the kx < Kx columns of the
+// rows |band| <= Kyh, two row ranges
+static int d2h_kept(ns_gpu* g, double* dst, const double2* src, cudaStream_t st) {
+    const Geo& G = g->g;
+    const size_t pitch = (size_t)G.nkx * sizeof(double2), width = (size_t)G.Kx * sizeof(double2);
+    NSG_CUDA(g, cudaMemcpy2DAsync(dst, pitch, src, pitch, width, (size_t)G.Kyh + 1, cudaMemcpyDeviceToHost, st));
+    const size_t r0 = (size_t)(G.ny - G.Kyh);
+    NSG_CUDA(g, cudaMemcpy2DAsync(dst + 2 * r0 * G.nkx, pitch, src + r0 * G.nkx, pitch, width, (size_t)G.Kyh,
+                                  cudaMemcpyDeviceToHost, st));
+    return NS_GPU_OK;
+}
+
+template <typename T>
+static int step_host_t(ns_gpu* g, double* wh, double* ph, double* uh, double* vh, double* sh, double* u, double* v,
+                       double* w, double t, double dt, uint64_t step0, double* t_out, double* dt_out) {
+    const size_t sb = spec_bytes(g), rb = real_bytes(g);
+    // inputs: omega_hat on the instance stream, psi_hat (and the SFD state) on the
+    // second stream, after everything already queued on the instance stream
+    NSG_CUDA(g, cudaEventRecord(g->ev_a, g->st));
+    NSG_CUDA(g, cudaStreamWaitEvent(g->st2, g->ev_a, 0));
+    NSG_TRY(h2d(g, g->spec[0], wh, sb));
+    NSG_CUDA(g, cudaMemcpyAsync(g->spec[1], ph, sb, cudaMemcpyHostToDevice, g->st2));
+    if (sh) NSG_CUDA(g, cudaMemcpyAsync(g->spec[2], sh, sb, cudaMemcpyHostToDevice, g->st2));
+    NSG_CUDA(g, cudaEventRecord(g->ev_b, g->st2));
+    NSG_CUDA(g, cudaStreamWaitEvent(g->st, g->ev_b, 0));
+    NSG_TRY(ensure_outside(g));
+    NSG_CUDA(g, cudaMemsetAsync(g->dflag, 0, sizeof(int), g->st));
+    const long long n = (long long)g->g.nkx * g->g.nky;
+    k_import<T><<<grid_for(n), 256, 0, g->st>>>(g->g, g->spec[0], g->spec[1], sh ? g->spec[2] : nullptr, (Cx<T>*)g->W0,
+                                                (Cx<T>*)g->PSI0, sh ? (Cx<T>*)g->SFD : nullptr, g->out, g->outsfd,
+                                                g->dflag);
+    NSG_LAUNCHED(g);
+    DevScalars h;
+    memset(&h, 0, sizeof(h));
+    h.t = t;
+    h.dt = dt;
+    h.dt_fixed = dt;
+    h.step_next = step0;
+    h.step_cur = step0;
+    h.fsub = g->p.forcing_substeps > 1 ? (unsigned long long)g->p.forcing_substeps : 1ULL;
+    k_set_scalars<<<1, 1, 0, g->st>>>(g->ds, h);
+    NSG_LAUNCHED(g);
+    int flag = 0;
+    NSG_TRY(d2h(g, &flag, g->dflag, sizeof(int)));
+    NSG_TRY(sync(g));
+    g->p.dt = dt;
+    g->outside_active = (flag & 1) ? 1 : 0;
+    g->fields_valid = 0;
+    g->psi0_valid = 1;
+    NSG_TRY(advance_t<T>(g, 1));
+    // outputs: the spectra leave on the second stream while the instance stream
+    // computes u, v, omega and copies them out
+    const int sfd_on = (g->p.sfd_enabled && g->p.sfd_strength > 0.0);
+    k_export<T><<<grid_for(n), 256, 0, g->st>>>(g->g, (const Cx<T>*)g->W0, sfd_on ? (const Cx<T>*)g->SFD : nullptr,
+                                                g->outside_active ? g->out : nullptr,
+                                                (g->outside_active && sfd_on) ? g->outsfd : nullptr, g->spec[0],
+                                                g->spec[1], g->spec[2], g->spec[3], g->spec[4]);
+    NSG_LAUNCHED(g);
+    NSG_CUDA(g, cudaEventRecord(g->ev_a, g->st));
+    NSG_CUDA(g, cudaStreamWaitEvent(g->st2, g->ev_a, 0));
+    // modes outside the mask that were zero in the caller's omega_hat (bit 0) and
+    // psi_hat (bit 1) stay zero after the step: those arrays only take their
+    // kept modes back
+    if (flag & 1) NSG_CUDA(g, cudaMemcpyAsync(wh, g->spec[0], sb, cudaMemcpyDeviceToHost, g->st2));
+    else NSG_TRY(d2h_kept(g, wh, g->spec[0], g->st2));
+    if (flag & 3) NSG_CUDA(g, cudaMemcpyAsync(ph, g->spec[1], sb, cudaMemcpyDeviceToHost, g->st2));
+    else NSG_TRY(d2h_kept(g, ph, g->spec[1], g->st2));
+    if (uh) NSG_CUDA(g, cudaMemcpyAsync(uh, g->spec[2], sb, cudaMemcpyDeviceToHost, g->st2));
+    if (vh) NSG_CUDA(g, cudaMemcpyAsync(vh, g->spec[3], sb, cudaMemcpyDeviceToHost, g->st2));
+    if (sh) NSG_CUDA(g, cudaMemcpyAsync(sh, g->spec[4], sb, cudaMemcpyDeviceToHost, g->st2));
+    NSG_CUDA(g, cudaEventRecord(g->ev_b, g->st2));
+    if (u || v || w) {
+        RowArgs<T> a = row_args<T>(g);
+        a.F[0] = (const Cx<T>*)g->F[1];
+        a.F[1] = (const Cx<T>*)g->F[0];
+        a.F[2] = (const Cx<T>*)g->F[2];
+        a.dx[0] = 0; a.dx[1] = 1; a.dx[2] = 0;
+        a.out_real[0] = g->real[0];
+        a.out_real[1] = g->real[1];
+        a.out_real[2] = g->real[2];
+        NSG_TRY(row_launch<T, ROW_UVW>(g, a));
+        if (u) NSG_TRY(d2h(g, u, g->real[0], rb));
+        if (v) NSG_TRY(d2h(g, v, g->real[1], rb));
+        if (w) NSG_TRY(d2h(g, w, g->real[2], rb));
+    }
+    NSG_CUDA(g, cudaStreamWaitEvent(g->st, g->ev_b, 0));
+    DevScalars hs;
+    NSG_TRY(d2h(g, &hs, g->ds, sizeof(hs)));
+    NSG_TRY(sync(g));
+    if (t_out) *t_out = hs.t;
+    if (dt_out) *dt_out = hs.dt;
+    return NS_GPU_OK;
+}
+
+int ns_gpu_step_host(ns_gpu* g, double* omega_hat, double* psi_hat, double* u_hat, double* v_hat, double* sfd_hat,
+                     double* u, double* v, double* omega, double t, double dt, uint64_t step0, double* t_out,
+                     double* dt_out) {
+    if (!g || !omega_hat || !psi_hat) return NS_GPU_ERR_INVALID;
+    NSG_TRY(ensure_staging(g));
+    NSG_TRY(ensure_aux_stream(g));
+    return g->prec == NS_GPU_FP64
+               ? step_host_t<double>(g, omega_hat, psi_hat, u_hat, v_hat, sfd_hat, u, v, omega, t, dt, step0, t_out,
+                                     dt_out)
+               : step_host_t<float>(g, omega_hat, psi_hat, u_hat, v_hat, sfd_hat, u, v, omega, t, dt, step0, t_out,
+                                    dt_out);
 }
 
 static int flush_l2(ns_gpu* g, size_t bytes, int salt) {

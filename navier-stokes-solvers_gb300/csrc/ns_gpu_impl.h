@@ -22,6 +22,8 @@ struct ns_gpu {
     int fast_row;       // radix-32 warp row kernel (nx = 2048)
     int fast_col;       // radix-32 column kernel (ny = 2048)
     cudaStream_t st;
+    cudaStream_t st2;              // copies that overlap the instance stream (ns_gpu_step_host)
+    cudaEvent_t ev_a, ev_b;        // ordering between st and st2
     std::string err;
     unsigned long long launches;
     ns_gpu_params p;

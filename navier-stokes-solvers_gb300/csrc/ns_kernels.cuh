@@ -881,6 +881,10 @@ __global__ void k_import(Geo g, const double2* wh, const double2* ph, const doub
             if (out) out[idx] = w;
             if (outsfd) outsfd[idx] = sh ? sh[idx] : make_double2(0.0, 0.0);
             if (flag && (w.x != 0.0 || w.y != 0.0)) atomicOr(flag, 1);
+            if (flag && ph) {  // bit 2: the stream function has a non-zero mode outside the mask
+                const double2 p = ph[idx];
+                if (p.x != 0.0 || p.y != 0.0) atomicOr(flag, 2);
+            }
         }
     }
 }
@@ -971,6 +975,10 @@ __global__ void k_hv_apply(Geo g, const double* w_full, int visc, int sfd, doubl
         rhs[idx] = r;
     }
 }
+
+// device scalars from kernel parameters: ordered on the stream, no host copy or sync
+__global__ void k_set_scalars(DevScalars* ds, DevScalars h) { *ds = h; }
+__global__ void k_set_dt_fixed(DevScalars* ds, double dt) { ds->dt_fixed = dt; }
 
 __global__ void k_hv_post(Geo g, double alpha, const double2* st, double2* sf) {
     const long long n = (long long)g.nkx * g.nky;

@@ -266,16 +266,12 @@ void ns_spectral_advance_rk4(NSSpectralData *d) {
     NS_CALL(d, "advance_rk4", ns_enter(d));
     NS_CALL(d, "advance_rk4", ns_sync_params(d, 0));
     const int sfd = ns_sfd_on(d);
-    ns_gpu *g = d->gpu->dev;
-    NS_CALL(d, "advance_rk4",
-            ns_gpu_upload_state(g, (const double *)d->omega_hat, (const double *)d->psi_hat,
-                                sfd ? (const double *)d->sfd_hat : NULL, d->t, d->dt, d->gpu->step));
-    NS_CALL(d, "advance_rk4", ns_gpu_advance(g, 1));
     double t = d->t, dt = d->dt;
+    /* upload, one device step and download in one call with overlapped copies */
     NS_CALL(d, "advance_rk4",
-            ns_gpu_download_state(g, (double *)d->omega_hat, (double *)d->psi_hat, (double *)d->u_hat,
-                                  (double *)d->v_hat, sfd ? (double *)d->sfd_hat : NULL, d->u, d->v, d->omega, &t,
-                                  &dt));
+            ns_gpu_step_host(d->gpu->dev, (double *)d->omega_hat, (double *)d->psi_hat, (double *)d->u_hat,
+                             (double *)d->v_hat, sfd ? (double *)d->sfd_hat : NULL, d->u, d->v, d->omega, d->t, d->dt,
+                             d->gpu->step, &t, &dt));
     d->t = t;
     d->gpu->step += 1;
 }

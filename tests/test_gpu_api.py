@@ -279,3 +279,32 @@ def test_2048_fp32_properties(nsgb):
     ky = np.ctypeslib.as_array(s.d.ky, shape=(s.d.nky,))[:, None]
     div = kx * s.cplx("u_hat") + ky * s.cplx("v_hat")
     assert np.abs(div).max() <= 1e-12 * np.abs(kx * s.cplx("u_hat")).max()
+
+
+def test_host_step_rewrites_what_the_reference_rewrites(nsgb, port):
+    """ns_spectral_advance_rk4 moves its arrays with ns_gpu_step_host: omega_hat and
+    psi_hat come back as kept modes only when the call itself saw zeros outside the
+    mask.  A caller that scribbled on psi_hat outside the mask and on u_hat, v_hat
+    gets every array back as the reference writes it (psi_hat = -omega_hat/k^2 on
+    all modes, spectral_core.c:17-31)."""
+    n = 32
+    w = random_field(n, n, 5)
+    gpu = nsgb.Solver(n, n, Re=300.0).setup(ic=None)
+    ora = O.Solver(port, n, n, Re=300.0).setup(ic=None)
+    out = gpu.mask() == 0
+    junk = np.random.default_rng(3).standard_normal(int(out.sum()))
+    for x in (gpu, ora):
+        x.set_vorticity(w)
+        x.derivatives()
+        x.d.dt = 1e-3
+        x.cplx("psi_hat")[out] = junk
+        x.cplx("u_hat")[:] = 7.0
+        x.cplx("v_hat")[:] = -3.0
+    gpu.advance(2)
+    ora.advance(2)
+    for name in ("omega_hat", "psi_hat", "u_hat", "v_hat"):
+        assert rel_l2(gpu.cplx(name), ora.cplx(name)) <= 1e-12, name
+    assert np.all(gpu.cplx("psi_hat")[out] == 0)
+    for name in ("u", "v", "omega"):
+        assert rel_l2(gpu.real(name), ora.real(name)) <= 1e-12, name
+    assert gpu.d.t == ora.d.t
