@@ -124,18 +124,23 @@ __global__ void __launch_bounds__(TP*(COUT / CPT)) k_conv3x3(const float* __rest
 // 128 B apart, K chunks 2080 B apart); the operand of tap (dy, dx) therefore
 // starts dx x 16 B and dy rows into the halo, with no im2col copy.  The weights
 // (B operand) stay in shared memory as [tap][chunk][64 co][8 ci].  One thread
-// issues the MMAs and commits them to an mbarrier; all four warps then read
-// their 32 rows of the accumulator with tcgen05.ld and run the epilogue (bias,
-// GELU, FP32 and BF16 stores).  Every wait is bounded by a clock budget: on
-// expiry the kernel records an error, frees its tensor memory and returns.
+// issues the MMAs and commits them to an mbarrier.  Two accumulators (128
+// tensor-memory columns) let the MMAs of the next tile run while eight warps
+// drain the current one: warps w and w + 4 read lane quarter w % 4 of the
+// accumulator (pixels), columns 32 (w / 4) .. + 31 (output channels), with
+// tcgen05.ld, add the bias and stage the tile in shared memory, from where all
+// warps apply GELU and store the tile's outputs as contiguous, coalesced runs.
+// Every wait is bounded by a clock budget: on expiry the kernel records an
+// error, frees its tensor memory and returns.
 constexpr int TC_W = 128;                                  // pixels per tile
 constexpr int TC_HP = TC_W + 2;                            // halo pixels per row
 constexpr int TC_WB_BYTES = 9 * 8 * 64 * 16;               // 73,728
 constexpr int TC_HX_BYTES = 3 * 8 * TC_HP * 16;            // 49,920 per halo buffer
 constexpr int TC_ST = 65;                                  // staged output row pitch (floats)
-constexpr int TC_SMEM = TC_WB_BYTES + 2 * TC_HX_BYTES + 64;  // + mbarrier and tmem address
+constexpr int TC_STG_BYTES = TC_W * TC_ST * 4;             // 33,280
+constexpr int TC_THREADS = 256;                            // eight warps: two per accumulator lane quarter
+constexpr int TC_SMEM = TC_WB_BYTES + 2 * TC_HX_BYTES + TC_STG_BYTES + 64;  // + mbarriers and tmem address
 constexpr long long TC_WAIT_CYCLES = 4000000000LL;         // default wait limit: about 2 s
-static_assert(TC_W * TC_ST * 4 <= TC_HX_BYTES, "output staging must fit in a halo buffer");
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -194,7 +199,7 @@ __device__ __forceinline__ void tc_load_halo(const __nv_bfloat16* __restrict__ i
                                              int ntx, int tid) {
     const int b = tile / (H * ntx), r = tile - b * H * ntx;
     const int y = r / ntx, x0 = (r - y * ntx) * TC_W;
-    for (int i = tid; i < 3 * TC_HP * 8; i += 128) {
+    for (int i = tid; i < 3 * TC_HP * 8; i += TC_THREADS) {
         const int row = i / (TC_HP * 8), q = i - row * TC_HP * 8;
         const int px = q >> 3, kc = q & 7;
         const int gy = wrapi(y + row - 1, H), gx = wrapi(x0 + px - 1, W);
@@ -223,101 +228,123 @@ __device__ __forceinline__ void tc_issue(unsigned taddr, unsigned hx, unsigned w
 
 // in: BF16 activations [B][H][W][64]; w: BF16 weights [9][64 ci][64 co]; bias
 // may be null; outputs (each may be null): pre FP32, actf FP32, actb BF16, all
-// [B][H][W][64].  Two halo buffers: the next tile's halo loads while the
-// current tile's MMAs and epilogue run; the epilogue stages the accumulator
-// through the current tile's (consumed) halo buffer so that every output of a
-// tile leaves as one contiguous, coalesced block.
+// [B][H][W][64].  Pipeline per CTA (tiles t = blockIdx.x, + gridDim.x, ...;
+// iteration i uses halo buffer, accumulator and mbarrier i % 2): the MMAs of
+// iteration i + 1 were issued before iteration i's epilogue starts; once
+// iteration i's MMAs are complete its halo buffer takes the halo of iteration
+// i + 2 (cp.async), and after the epilogue has drained accumulator i % 2 the
+// MMAs of iteration i + 2 go into it.
 // wait_cycles bounds each MMA-completion wait (clock64 cycles).  probe != 0 is
 // the self-test of that bound: no MMA is issued, so the first wait (on an
 // mbarrier nothing arrives on) runs out, the kernel records the expiry in err,
 // frees its tensor memory and returns with no tensor-core work in flight.
 template <bool GELU>
-__global__ void __launch_bounds__(128, 1) k_conv_tc(const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ w,
-                                                    const float* __restrict__ bias, float* __restrict__ pre,
-                                                    float* __restrict__ actf, __nv_bfloat16* __restrict__ actb, int B, int H,
-                                                    int W, int* __restrict__ err, long long wait_cycles, int probe) {
+__global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __nv_bfloat16* __restrict__ in,
+                                                           const __nv_bfloat16* __restrict__ w,
+                                                           const float* __restrict__ bias, float* __restrict__ pre,
+                                                           float* __restrict__ actf, __nv_bfloat16* __restrict__ actb,
+                                                           int B, int H, int W, int* __restrict__ err, long long wait_cycles,
+                                                           int probe) {
     extern __shared__ __align__(128) unsigned char tsm[];
     unsigned char* WB = tsm;                            // [9][8][64][8] bf16
     unsigned char* HXB = tsm + TC_WB_BYTES;             // 2 x [3][8][130][8] bf16
-    unsigned long long* mbar = reinterpret_cast<unsigned long long*>(tsm + TC_WB_BYTES + 2 * TC_HX_BYTES);
-    unsigned* tslot = reinterpret_cast<unsigned*>(tsm + TC_WB_BYTES + 2 * TC_HX_BYTES + 16);
+    float* stg = reinterpret_cast<float*>(tsm + TC_WB_BYTES + 2 * TC_HX_BYTES);  // [128][65] fp32
+    unsigned long long* mbar = reinterpret_cast<unsigned long long*>(tsm + TC_WB_BYTES + 2 * TC_HX_BYTES + TC_STG_BYTES);
+    unsigned* tslot = reinterpret_cast<unsigned*>(mbar + 2);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int ntx = W / TC_W;
     const int ntiles = B * H * ntx;
+    const int gstride = gridDim.x;
 
     // weights into the B-operand layout: WB[tap][kc][co][j] = w[tap][8 kc + j][co]
-    for (int i = tid; i < 9 * 64 * 64; i += 128) {
+    for (int i = tid; i < 9 * 64 * 64; i += TC_THREADS) {
         const int tap = i >> 12, r = i & 4095, ci = r >> 6, co = r & 63;
         reinterpret_cast<__nv_bfloat16*>(WB)[((tap * 8 + (ci >> 3)) * 64 + co) * 8 + (ci & 7)] = w[i];
     }
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(smem_u32(tslot)));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(smem_u32(tslot)));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar + 1)));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    const unsigned hxb = smem_u32(HXB), wbs = smem_u32(WB), mb = smem_u32(mbar);
+    const unsigned hxb = smem_u32(HXB), wbs = smem_u32(WB), mb0 = smem_u32(mbar);
     int tile = blockIdx.x;
     if (tile < ntiles) tc_load_halo(in, hxb, tile, H, W, ntx, tid);
+    if (tile + gstride < ntiles) tc_load_halo(in, hxb + TC_HX_BYTES, tile + gstride, H, W, ntx, tid);
     asm volatile("cp.async.wait_all;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic-proxy writes -> tensor-core reads
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const unsigned taddr = *tslot;
-    if (tile < ntiles && tid == 0 && !probe) tc_issue(taddr, hxb, wbs, mb);
-    unsigned phase = 0;
-    int buf = 0;
-    for (; tile < ntiles; tile += gridDim.x, buf ^= 1) {
-        const int next = tile + gridDim.x;
-        const unsigned hx_next = hxb + (unsigned)((buf ^ 1) * TC_HX_BYTES);
-        if (next < ntiles) tc_load_halo(in, hx_next, next, H, W, ntx, tid);  // overlaps this tile's MMAs and epilogue
+    if (tid == 0 && !probe) {
+        if (tile < ntiles) tc_issue(taddr, hxb, wbs, mb0);
+        if (tile + gstride < ntiles) tc_issue(taddr + 64u, hxb + TC_HX_BYTES, wbs, mb0 + 8u);
+    }
+    const int q = warp & 3, h = warp >> 2;
+    const bool bf16_only = !pre && !actf && actb;
+    for (int it = 0; tile < ntiles; tile += gstride, ++it) {
+        const int buf = it & 1;
+        const unsigned mb = mb0 + 8u * (unsigned)buf;
+        const unsigned hx = hxb + (unsigned)(buf * TC_HX_BYTES);
         // every thread must take the same branch (barriers follow): the tile
-        // succeeds only if every thread saw the MMAs complete in time
-        const bool ok = __syncthreads_and(mbar_wait(mb, phase, wait_cycles) ? 1 : 0) != 0;
-        phase ^= 1u;
+        // succeeds only if every thread saw its MMAs complete in time
+        const bool ok = __syncthreads_and(mbar_wait(mb, (unsigned)((it >> 1) & 1), wait_cycles) ? 1 : 0) != 0;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         if (!ok) {
             if (tid == 0) atomicExch(err, 1);
             break;
         }
-        // epilogue: accumulator row of this thread = pixel warp*32 + lane of the tile
-        const int b = tile / (H * ntx), r = tile - b * H * ntx;
-        const int y = r / ntx, x0 = (r - y * ntx) * TC_W;
-        const size_t obase = (((size_t)b * H + y) * W + x0) * 64;  // the tile's 128 x 64 outputs are contiguous
-        float* stg = reinterpret_cast<float*>(HXB + buf * TC_HX_BYTES);  // this tile's halo is consumed
-        const int prow = warp * 32 + lane;
-#pragma unroll
-        for (int half = 0; half < 2; ++half) {
+        // this tile's MMAs are complete: its halo buffer takes the tile two iterations on
+        const int t2 = tile + 2 * gstride;
+        if (t2 < ntiles) tc_load_halo(in, hx, t2, H, W, ntx, tid);
+        // accumulator rows 32 q .. 32 q + 31 (pixels), columns 32 h .. 32 h + 31 (channels)
+        {
             float v[32];
-            tc_ld32(taddr + ((unsigned)(warp * 32) << 16) + (unsigned)(half * 32), v);
+            tc_ld32(taddr + ((unsigned)(32 * q) << 16) + (unsigned)(buf * 64 + h * 32), v);
+            const int prow = 32 * q + lane;
 #pragma unroll
             for (int k = 0; k < 32; ++k) {
-                const int co = half * 32 + k;
+                const int co = 32 * h + k;
                 stg[prow * TC_ST + co] = bias ? v[k] + bias[co] : v[k];
             }
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();  // staged; the accumulator may be overwritten
-        for (int i = tid; i < TC_W * 64; i += 128) {
-            const float pv = stg[(i >> 6) * TC_ST + (i & 63)];
-            const float av = GELU ? gelu(pv) : pv;
-            if (pre) pre[obase + i] = pv;
-            if (actf) actf[obase + i] = av;
-            if (actb) actb[obase + i] = __float2bfloat16_rn(av);
+        __syncthreads();  // staged; accumulator buf is drained
+        const int b = tile / (H * ntx), r = tile - b * H * ntx;
+        const int y = r / ntx, x0 = (r - y * ntx) * TC_W;
+        const size_t obase = (((size_t)b * H + y) * W + x0) * 64;  // the tile's 128 x 64 outputs are contiguous
+        if (bf16_only) {
+            for (int i = 2 * tid; i < TC_W * 64; i += 2 * TC_THREADS) {
+                const float* sp = stg + (i >> 6) * TC_ST + (i & 63);
+                const float a0 = GELU ? gelu(sp[0]) : sp[0], a1 = GELU ? gelu(sp[1]) : sp[1];
+                *reinterpret_cast<__nv_bfloat162*>(actb + obase + i) = __floats2bfloat162_rn(a0, a1);
+            }
+        } else {
+            for (int i = tid; i < TC_W * 64; i += TC_THREADS) {
+                const float pv = stg[(i >> 6) * TC_ST + (i & 63)];
+                const float av = GELU ? gelu(pv) : pv;
+                if (pre) pre[obase + i] = pv;
+                if (actf) actf[obase + i] = av;
+                if (actb) actb[obase + i] = __float2bfloat16_rn(av);
+            }
         }
-        // the next tile's halo must have landed before its MMAs start
+        // the halo two iterations on must have landed before its MMAs start
         asm volatile("cp.async.wait_all;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();  // staging read done (the buffer takes a halo again), next halo visible
-        if (next < ntiles && tid == 0) tc_issue(taddr, hx_next, wbs, mb);
+        __syncthreads();  // staging read done, that halo visible
+        if (tid == 0 && t2 < ntiles) tc_issue(taddr + (unsigned)(buf * 64), hx, wbs, mb);
     }
     asm volatile("cp.async.wait_all;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(taddr));
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(taddr));
+    }
 }
 
 // inference first layer (2 -> 64, GELU) straight to the BF16 activations that the
@@ -637,8 +664,8 @@ static int conv_tc(ns_cnn* c, cudaStream_t st, const __nv_bfloat16* in, const __
     auto k = k_conv_tc<GELU>;
     CNN_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
     const int tiles = B * c->H * (c->W / TC_W);
-    k<<<grid_of(tiles, 1, c->num_sms), 128, TC_SMEM, st>>>(in, w, bias, pre, actf, actb, B, c->H, c->W, c->derr,
-                                                           c->tc_wait_cycles, 0);
+    k<<<grid_of(tiles, 1, c->num_sms), TC_THREADS, TC_SMEM, st>>>(in, w, bias, pre, actf, actb, B, c->H, c->W, c->derr,
+                                                                  c->tc_wait_cycles, 0);
     CNN_LAUNCHED(c);
     return NS_GPU_OK;
 }
@@ -1057,8 +1084,8 @@ int ns_cnn_probe_wait_timeout(ns_cnn* c, long long wait_cycles, int* timed_out) 
     auto k = k_conv_tc<true>;
     CNN_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
     const int tiles = c->H * (c->W / TC_W);
-    k<<<grid_of(tiles, 1, c->num_sms), 128, TC_SMEM, st>>>(c->ab0, c->wb[1], nullptr, nullptr, nullptr, nullptr, 1, c->H,
-                                                           c->W, c->derr, wait_cycles, 1);
+    k<<<grid_of(tiles, 1, c->num_sms), TC_THREADS, TC_SMEM, st>>>(c->ab0, c->wb[1], nullptr, nullptr, nullptr, nullptr, 1,
+                                                                  c->H, c->W, c->derr, wait_cycles, 1);
     CNN_LAUNCHED(c);
     int e = 0;
     CNN_CUDA(c, cudaMemcpyAsync(&e, c->derr, sizeof(int), cudaMemcpyDeviceToHost, st));
