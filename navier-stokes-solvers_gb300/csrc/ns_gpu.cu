@@ -151,6 +151,11 @@ template <typename T> static ColArgs<T> col_args(ns_gpu* g) {
     a.twc = (const Cx<T>*)g->twc;
     a.ds = g->ds;
     a.sp = step_params<T>(g);
+    if (a.sp.forcing && g->fM > 0) {
+        a.fnoise = g->fnoise;
+        a.fkxr = g->fkxr;
+        a.fkyr = g->fkyr;
+    }
     a.nfields = 4;
     return a;
 }
@@ -246,7 +251,44 @@ template <typename T, int STAGE> static int stage_col(ns_gpu* g, const ColArgs<T
     return col_launch<T, COL_STAGE, STAGE>(g, a);
 }
 
+static int dalloc(ns_gpu* g, void** p, size_t bytes);
+
+// The per-step forcing-noise table: every (kept mode with |kx|, |ky| <= kmax,
+// draw) pair gets one thread of k_forcing_noise before the step's first stage,
+// instead of one thread per mode drawing them in sequence at stage 4.
+static int ensure_noise(ns_gpu* g) {
+    g->fM = 0;
+    const StepParams sp = step_params<double>(g);
+    if (!sp.forcing) return NS_GPU_OK;
+    const double two_pi = 2.0 * 3.14159265358979323846;
+    const int kxr = std::min((int)floor(sp.f_kmax * g->g.Lx / two_pi + 1e-9), g->g.Kx - 1);
+    const int kyr = std::min((int)floor(sp.f_kmax * g->g.Ly / two_pi + 1e-9), g->g.Kyh);
+    if (kxr < 0 || kyr < 0) return NS_GPU_OK;
+    const size_t need = (size_t)(kxr + 1) * (2 * kyr + 1) * sp.fsub;
+    if (need > g->fnoise_cap) {
+        if (g->fnoise) cudaFree(g->fnoise);
+        g->fnoise = nullptr;
+        g->fnoise_cap = 0;
+        NSG_TRY(dalloc(g, (void**)&g->fnoise, need * sizeof(double2)));
+        g->fnoise_cap = need;
+    }
+    g->fkxr = kxr;
+    g->fkyr = kyr;
+    g->fM = sp.fsub;
+    return NS_GPU_OK;
+}
+
+static int launch_noise(ns_gpu* g) {
+    const StepParams sp = step_params<double>(g);
+    const int n = (g->fkxr + 1) * (2 * g->fkyr + 1) * g->fM;
+    k_forcing_noise<<<(n + 127) / 128, 128, 0, g->st>>>(g->g.ny, g->g.Lx, g->g.Ly, &g->ds->step_next, g->fM, sp.f_seed,
+                                                        sp.f_kmin, sp.f_kmax, g->fkxr, g->fkyr, g->fnoise);
+    NSG_LAUNCHED(g);
+    return NS_GPU_OK;
+}
+
 template <typename T> static int advance_t(ns_gpu* g, int nsteps) {
+    NSG_TRY(ensure_noise(g));
     if (!g->fields_valid) {
         NSG_TRY(prologue<T>(g, g->W0, g->PSI0, g->psi0_valid ? 0 : 1, 4));
         g->fields_valid = 1;
@@ -254,6 +296,7 @@ template <typename T> static int advance_t(ns_gpu* g, int nsteps) {
     }
     ColArgs<T> a = col_args<T>(g);
     for (int n = 0; n < nsteps; ++n) {
+        if (g->fM > 0) NSG_TRY(launch_noise(g));
         NSG_TRY(stage_row<T>(g, 1));
         NSG_TRY((stage_col<T, 1>(g, a)));
         NSG_TRY(stage_row<T>(g, 2));
@@ -288,6 +331,7 @@ void nsg_stage_args(ns_gpu* g, RowArgs<float>* ra, ColArgs<float>* ca) {
     for (int f = 0; f < 4; ++f) ra->F[f] = (const float2*)g->F[f];
     ra->dx[0] = 1; ra->dx[1] = 0; ra->dx[2] = 1; ra->dx[3] = 0;  // psi_x, psi_y, omega_x, omega_y
     *ca = col_args<float>(g);
+    ca->fnoise = nullptr;  // the ensemble kernel draws its members' forcing itself
 }
 
 // ------------------------------------------------------------ allocation
@@ -439,6 +483,7 @@ void ns_gpu_destroy(ns_gpu* g) {
         if (g->spec[i]) cudaFree(g->spec[i]);
         if (g->real[i]) cudaFree(g->real[i]);
     }
+    if (g->fnoise) cudaFree(g->fnoise);
     if (g->st2) cudaStreamDestroy(g->st2);
     if (g->ev_a) cudaEventDestroy(g->ev_a);
     if (g->ev_b) cudaEventDestroy(g->ev_b);

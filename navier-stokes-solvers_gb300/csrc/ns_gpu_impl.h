@@ -45,6 +45,9 @@ struct ns_gpu {
     double2* spec[5];
     double* real[5];
     double2 *out, *outsfd;  // masked-out modes of the state (FP64)
+    double2* fnoise;        // this step's forcing draws (k_forcing_noise), [entries][draws]
+    size_t fnoise_cap;      // entries x draws allocated
+    int fkxr, fkyr, fM;     // table extent (kx index, |ky|) and draws per step; fM = 0: no table
     int outside_active;
     int fields_valid;   // F holds the stage-1 fields of the current state
     int psi0_valid;     // PSI0 holds the caller's psi_hat for the next prologue

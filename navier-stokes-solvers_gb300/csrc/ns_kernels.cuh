@@ -140,8 +140,8 @@ __device__ __forceinline__ double2 forcing_xi_sum(int i, int j, int ny, unsigned
         const double rad = sqrt(-2.0 * log(u1)) * 0.70710678118654752440;
         double sn, cs;
         sincos(2.0 * 3.141592653589793 * u2, &sn, &cs);
-        sx += rad * cs;
-        sy += rad * sn;
+        sx = __dadd_rn(sx, __dmul_rn(rad, cs));
+        sy = __dadd_rn(sy, __dmul_rn(rad, sn));
     }
     return make_double2(sx, flip ? -sy : sy);
 }
@@ -453,6 +453,10 @@ template <typename T> struct ColArgs {
     double out_scale;           // export scale (1/(nx ny) forward, -1/(nx ny) nonlinear)
     int psi_from_w;             // prologue: Psi = -W0/k^2 instead of PSI0
     int nfields;                // prologue: number of fields (4 for a stage, 3 = Psi,Psi_y,Omega)
+    // this step's forcing noise, one term per (mode, draw) (k_forcing_noise), or null:
+    // entry e = i (2 fkyr + 1) + ky + fkyr for kx index i <= fkxr and |ky| <= fkyr
+    const double2* fnoise;
+    int fkxr, fkyr;
 };
 
 // x / k2 for the Poisson solve: IEEE division in FP64 (as the reference), the
@@ -478,16 +482,36 @@ __device__ __forceinline__ C field_value(int f, C w, T kx, T ky) {
     return v;
 }
 
-// white-in-time forcing increment of one kept mode: amp times the mode's noise
-// (forcing_xi_sum) when kmin <= |k| <= kmax (FP64 shell test as the reference's k2)
-static __device__ __noinline__ double2 forcing_increment(const Geo& g, int i, int j, unsigned long long step, int M,
-                                                         unsigned long long seed, double kmin, double kmax, double amp) {
+// FP64 shell test of mode (i, j): kmin <= |k| <= kmax, |k| > 0 (as the reference's k2)
+__device__ __forceinline__ bool forcing_in_shell(const Geo& g, int i, int j, double kmin, double kmax) {
     const double kxd = 2.0 * 3.141592653589793 * i / g.Lx;
     const double kyd = (j <= g.ny / 2) ? 2.0 * 3.141592653589793 * j / g.Ly : 2.0 * 3.141592653589793 * (j - g.ny) / g.Ly;
     const double k2d = kxd * kxd + kyd * kyd;
     const double km = sqrt(k2d);
-    if (!(k2d > 1e-12 && km >= kmin && km <= kmax)) return make_double2(0.0, 0.0);
-    const double2 xi = forcing_xi_sum(i, j, g.ny, step, M, seed);
+    return k2d > 1e-12 && km >= kmin && km <= kmax;
+}
+
+// white-in-time forcing increment of one kept mode: amp times the mode's noise
+// (the sum over this step's draws) when kmin <= |k| <= kmax.  With a noise table
+// the draws were made for the step by k_forcing_noise (in parallel, before the
+// step's first stage); otherwise they are drawn here (forcing_xi_sum).
+static __device__ __noinline__ double2 forcing_increment(const Geo& g, int i, int j, unsigned long long step, int M,
+                                                         unsigned long long seed, double kmin, double kmax, double amp,
+                                                         const double2* fnoise, int fkxr, int fkyr) {
+    if (!forcing_in_shell(g, i, j, kmin, kmax)) return make_double2(0.0, 0.0);
+    double2 xi;
+    const int ky = (j <= g.ny / 2) ? j : j - g.ny;
+    if (fnoise && i <= fkxr && ky >= -fkyr && ky <= fkyr) {
+        const double2* t = fnoise + ((size_t)i * (2 * fkyr + 1) + (ky + fkyr)) * M;
+        double sx = 0.0, sy = 0.0;
+        for (int s = 0; s < M; ++s) {
+            sx = __dadd_rn(sx, t[s].x);
+            sy = __dadd_rn(sy, t[s].y);
+        }
+        xi = make_double2(sx, sy);
+    } else {
+        xi = forcing_xi_sum(i, j, g.ny, step, M, seed);
+    }
     return make_double2(amp * xi.x, amp * xi.y);
 }
 
@@ -591,7 +615,8 @@ __device__ __forceinline__ C post_step_mode(const Geo& g, const ColArgs<T>& a, i
     const T k2f = kx * kx + ky * ky;
     if (a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9 && k2f >= (T)(a.sp.f_kmin * a.sp.f_kmin * (1.0 - 1e-3)) &&
         k2f <= (T)(a.sp.f_kmax * a.sp.f_kmax * (1.0 + 1e-3))) {
-        const double2 df = forcing_increment(g, i, j, a.ds->step_cur, a.sp.fsub, a.sp.f_seed, a.sp.f_kmin, a.sp.f_kmax, f_amp);
+        const double2 df = forcing_increment(g, i, j, a.ds->step_cur, a.sp.fsub, a.sp.f_seed, a.sp.f_kmin, a.sp.f_kmax, f_amp,
+                                             a.fnoise, a.fkxr, a.fkyr);
         if (df.x != 0.0 || df.y != 0.0) {
             wn.x = (T)((double)wn.x + df.x);
             wn.y = (T)((double)wn.y + df.y);
@@ -973,6 +998,41 @@ __global__ void k_hv_apply(Geo g, const double* w_full, int visc, int sfd, doubl
         r.x -= dr;
         r.y -= di;
         rhs[idx] = r;
+    }
+}
+
+// This step's forcing draws, one thread per (mode entry, draw s): entry e is
+// kx index i = e / (2 kyr + 1), ky = e % (2 kyr + 1) - kyr; the draw uses the
+// counter the stage-4 kernel would use, step_next + s (read before the step's
+// first stage advances the counters).  Terms are stored as forcing_xi_sum forms
+// them (the conjugate row of kx = 0, ky < 0 negated), modes outside the shell
+// as zeros.
+__global__ void k_forcing_noise(int ny, double Lx, double Ly, const unsigned long long* step_next, int M,
+                                unsigned long long seed, double kmin, double kmax, int kxr, int kyr, double2* out) {
+    const int n = (kxr + 1) * (2 * kyr + 1) * M;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int e = t / M, s = t - e * M;
+        const int i = e / (2 * kyr + 1);
+        int ky = e - i * (2 * kyr + 1) - kyr;
+        const double kxd = 2.0 * 3.141592653589793 * i / Lx;
+        const double kyd = 2.0 * 3.141592653589793 * ky / Ly;
+        const double k2d = kxd * kxd + kyd * kyd;
+        const double km = sqrt(k2d);
+        double2 v = make_double2(0.0, 0.0);
+        if (k2d > 1e-12 && km >= kmin && km <= kmax) {
+            int flip = 0;
+            if (i == 0 && ky < 0) { ky = -ky; flip = 1; }
+            const unsigned long long id = ((unsigned long long)(unsigned int)ky << 32) | (unsigned int)i;
+            unsigned long long ctr[4] = {id, *step_next + (unsigned long long)s, NSG_TAG_FORCE, 0ULL};
+            philox4x64(ctr, seed, 0ULL);
+            const double u1 = fmax(u53(ctr[0]), 2.2250738585072014e-308);
+            const double u2 = u53(ctr[1]);
+            const double rad = sqrt(-2.0 * log(u1)) * 0.70710678118654752440;
+            double sn, cs;
+            sincos(2.0 * 3.141592653589793 * u2, &sn, &cs);
+            v = make_double2(__dmul_rn(rad, cs), flip ? -__dmul_rn(rad, sn) : __dmul_rn(rad, sn));
+        }
+        out[t] = v;
     }
 }
 
