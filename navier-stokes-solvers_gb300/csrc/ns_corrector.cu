@@ -383,6 +383,113 @@ __global__ void __launch_bounds__(256) k_conv_in_bf16(const float* __restrict__ 
     }
 }
 
+// ---------------------------------------------- tiled inference first / last layers
+// 8 x 32 pixel tiles (W % 32 == 0, H % 8 == 0) with the periodic halo (10 x 34
+// pixels) in shared memory; 256 threads per CTA.
+constexpr int IT_H = 8, IT_W = 32, IT_HALO = (IT_H + 2) * (IT_W + 2);
+
+// first layer (2 -> 64, GELU) to the BF16 activations of the tensor-core layers:
+// thread = (pixel column, eight consecutive output channels), eight lanes write
+// one pixel's 128 bytes; the arithmetic order of k_conv_in_bf16 (bias, then taps,
+// then input channels), so the outputs are the same bits
+__global__ void __launch_bounds__(256) k_conv_in_tile(const float* __restrict__ in, const __nv_bfloat16* __restrict__ w,
+                                                      const float* __restrict__ bias, __nv_bfloat16* __restrict__ out,
+                                                      int B, int H, int W) {
+    __shared__ __align__(16) float sw[9 * 2 * 64];  // [tap][ci][co]
+    __shared__ float sb[64];
+    __shared__ float2 sx[IT_HALO];
+    for (int i = threadIdx.x; i < 9 * 2 * 64; i += blockDim.x) sw[i] = __bfloat162float(w[i]);
+    if (threadIdx.x < 64) sb[threadIdx.x] = bias ? bias[threadIdx.x] : 0.0f;
+    const int g = threadIdx.x & 7, pl = threadIdx.x >> 3;
+    const int ntx = W / IT_W, nty = H / IT_H, ntiles = B * nty * ntx;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int b = tile / (nty * ntx), r = tile - b * nty * ntx;
+        const int y0 = (r / ntx) * IT_H, x0 = (r % ntx) * IT_W;
+        __syncthreads();  // previous tile done with sx (and the weights written)
+        for (int i = threadIdx.x; i < IT_HALO; i += blockDim.x) {
+            const int hy = i / (IT_W + 2), hx = i - hy * (IT_W + 2);
+            sx[i] = *reinterpret_cast<const float2*>(in + (((size_t)b * H + wrapi(y0 + hy - 1, H)) * W + wrapi(x0 + hx - 1, W)) * 2);
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int py = 0; py < IT_H; ++py) {
+            float a[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) a[k] = sb[8 * g + k];
+#pragma unroll 1
+            for (int tap = 0; tap < 9; ++tap) {
+                const int dy = tap / 3, dx = tap - 3 * dy;
+                const float2 xv = sx[(py + dy) * (IT_W + 2) + pl + dx];
+                const float* w0 = sw + (tap * 2) * 64 + 8 * g;
+#pragma unroll
+                for (int k = 0; k < 8; ++k) a[k] = fmaf(xv.x, w0[k], a[k]);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) a[k] = fmaf(xv.y, w0[64 + k], a[k]);
+            }
+            uint4 pk;
+            unsigned* pw = reinterpret_cast<unsigned*>(&pk);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                __nv_bfloat162 h2;
+                h2.x = __float2bfloat16_rn(gelu(a[2 * k]));
+                h2.y = __float2bfloat16_rn(gelu(a[2 * k + 1]));
+                pw[k] = *reinterpret_cast<unsigned*>(&h2);
+            }
+            *reinterpret_cast<uint4*>(out + (((size_t)b * H + y0 + py) * W + x0 + pl) * 64 + 8 * g) = pk;
+        }
+    }
+}
+
+// output layer (64 -> 1, no activation): every pixel of the tile and its halo is
+// projected once onto the nine taps, P[p][t] = sum_ci act[p][ci] w[t][ci], and
+// out[p] = bias + sum_t P[p + offset(t)][t]; each activation is read once rather
+// than once per tap.  act FP32 [B][H][W][64], w [9][64][1], out [B][H][W].
+__global__ void __launch_bounds__(256) k_conv_out_tile(const float* __restrict__ act, const __nv_bfloat16* __restrict__ w,
+                                                       const float* __restrict__ bias, float* __restrict__ out, int B, int H,
+                                                       int W) {
+    __shared__ __align__(16) float sw[9 * 64];  // [tap][ci]
+    __shared__ float sp[IT_HALO * 9];
+    for (int i = threadIdx.x; i < 9 * 64; i += blockDim.x) sw[i] = __bfloat162float(w[i]);
+    const float b0 = bias ? bias[0] : 0.0f;
+    const int ntx = W / IT_W, nty = H / IT_H, ntiles = B * nty * ntx;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int b = tile / (nty * ntx), r = tile - b * nty * ntx;
+        const int y0 = (r / ntx) * IT_H, x0 = (r % ntx) * IT_W;
+        __syncthreads();  // previous tile done with sp (and the weights written)
+        for (int i = threadIdx.x; i < IT_HALO; i += blockDim.x) {
+            const int hy = i / (IT_W + 2), hx = i - hy * (IT_W + 2);
+            const float4* ap = reinterpret_cast<const float4*>(
+                act + (((size_t)b * H + wrapi(y0 + hy - 1, H)) * W + wrapi(x0 + hx - 1, W)) * 64);
+            float acc[9];
+#pragma unroll
+            for (int t = 0; t < 9; ++t) acc[t] = 0.0f;
+#pragma unroll 4
+            for (int c4 = 0; c4 < 16; ++c4) {
+                const float4 v = ap[c4];
+#pragma unroll
+                for (int t = 0; t < 9; ++t) {
+                    const float4 wv = reinterpret_cast<const float4*>(sw)[t * 16 + c4];
+                    acc[t] = fmaf(v.x, wv.x, acc[t]);
+                    acc[t] = fmaf(v.y, wv.y, acc[t]);
+                    acc[t] = fmaf(v.z, wv.z, acc[t]);
+                    acc[t] = fmaf(v.w, wv.w, acc[t]);
+                }
+            }
+#pragma unroll
+            for (int t = 0; t < 9; ++t) sp[i * 9 + t] = acc[t];
+        }
+        __syncthreads();
+        const int py = threadIdx.x / IT_W, px = threadIdx.x - py * IT_W;
+        float o = b0;
+#pragma unroll
+        for (int t = 0; t < 9; ++t) {
+            const int dy = t / 3, dx = t - 3 * dy;
+            o += sp[((py + dy) * (IT_W + 2) + px + dx) * 9 + t];
+        }
+        out[((size_t)b * H + y0 + py) * W + x0 + px] = o;
+    }
+}
+
 __global__ void k_to_bf16(const float* __restrict__ a, __nv_bfloat16* __restrict__ b, long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         b[i] = __float2bfloat16_rn(a[i]);
@@ -676,10 +783,17 @@ static int conv_tc(ns_cnn* c, cudaStream_t st, const __nv_bfloat16* in, const __
 // activation for the backward pass, otherwise only what the next layer reads.
 static int forward(ns_cnn* c, cudaStream_t st, int B, bool training = true) {
     const float* x = c->x0;
+    const bool tiles32 = (c->W % IT_W == 0) && (c->H % IT_H == 0);
     if (c->tc && !training) {
-        const long long npix = (long long)B * c->H * c->W;
-        k_conv_in_bf16<<<grid_of(npix, 8, 8 * c->num_sms), 256, 0, st>>>(x, c->wb[0], c->p + c->boff[0], c->ab0, B, c->H,
-                                                                          c->W);
+        if (tiles32) {
+            const long long tiles = (long long)B * (c->H / IT_H) * (c->W / IT_W);
+            k_conv_in_tile<<<grid_of(tiles, 1, 8 * c->num_sms), 256, 0, st>>>(x, c->wb[0], c->p + c->boff[0], c->ab0, B,
+                                                                             c->H, c->W);
+        } else {
+            const long long npix = (long long)B * c->H * c->W;
+            k_conv_in_bf16<<<grid_of(npix, 8, 8 * c->num_sms), 256, 0, st>>>(x, c->wb[0], c->p + c->boff[0], c->ab0, B,
+                                                                              c->H, c->W);
+        }
         CNN_LAUNCHED(c);
     } else {
         CNN_TRY((conv<2, HID, 32, true>(c, st, x, c->wb[0], c->p + c->boff[0], c->pre[0], c->act[0], B)));
@@ -704,7 +818,16 @@ static int forward(ns_cnn* c, cudaStream_t st, int B, bool training = true) {
         for (int l = 1; l < NL - 1; ++l)
             CNN_TRY((conv<HID, HID, 32, true>(c, st, c->act[l - 1], c->wb[l], c->p + c->boff[l], c->pre[l], c->act[l], B)));
     }
-    CNN_TRY((conv<HID, 1, 1, false>(c, st, c->act[NL - 2], c->wb[NL - 1], c->p + c->boff[NL - 1], c->pre[NL - 1], nullptr, B)));
+    if (!training && tiles32) {  // inference: the projected output layer
+        const long long tiles = (long long)B * (c->H / IT_H) * (c->W / IT_W);
+        k_conv_out_tile<<<grid_of(tiles, 1, 8 * c->num_sms), 256, 0, st>>>(c->act[NL - 2], c->wb[NL - 1],
+                                                                          c->p + c->boff[NL - 1], c->pre[NL - 1], B, c->H,
+                                                                          c->W);
+        CNN_LAUNCHED(c);
+    } else {
+        CNN_TRY((conv<HID, 1, 1, false>(c, st, c->act[NL - 2], c->wb[NL - 1], c->p + c->boff[NL - 1], c->pre[NL - 1],
+                                        nullptr, B)));
+    }
     return NS_GPU_OK;
 }
 
