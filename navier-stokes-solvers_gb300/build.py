@@ -24,9 +24,7 @@ LIB = os.path.join(PKG, "libns_gb300.so")
 RUNNER = os.path.join(PKG, "ns_run")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-# --split-compile=0: the optimiser and ptxas of one translation unit run on all
-# host cores (the instance engine instantiates many stage kernels)
-NVFLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "--split-compile=0", "-Xcompiler", "-fPIC", "-I", INCLUDE]
+NVFLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE]
 CFLAGS = ["-O2", "-std=gnu11", "-fPIC", "-ffp-contract=off", "-Wall", "-I", INCLUDE]
 
 

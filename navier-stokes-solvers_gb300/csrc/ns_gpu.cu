@@ -18,7 +18,6 @@
 
 #include "ns_gpu.h"
 #include "ns_kernels.cuh"
-#include "ns_wkernels.cuh"
 
 using namespace nsg;
 
@@ -43,35 +42,6 @@ static int grid_for(long long n, int threads = 256, int cap = 2048) {
 
 template <typename T> using Cx = typename CT<T>::C;
 
-
-// ------------------------------------------------------------- launchers
-// Launch a stage kernel with programmatic stream serialization: it may be
-// scheduled while the previous kernel on the stream drains, runs its
-// independent prologue, and waits (griddepcontrol.wait) before it touches
-// anything the previous kernel wrote.
-#ifndef NSG_PDL
-#define NSG_PDL 1
-#endif
-template <typename... KArgs, typename... Args>
-static cudaError_t launch_stage(void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t st,
-                                Args&&... args) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(block);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = NSG_PDL;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
-}
-
-template <typename K> static int set_smem(ns_gpu* g, K kernel, size_t bytes) {
-    if (bytes > 48 * 1024) NSG_CUDA(g, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    return NS_GPU_OK;
-}
 
 template <typename T, int E, int MODE> static int row_launch_e(ns_gpu* g, const RowArgs<T>& a) {
     const int NF = RowNF<MODE>::v;
@@ -177,89 +147,35 @@ template <typename T> static int stage_row(ns_gpu* g, int stage) {
     a.dx[0] = 1; a.dx[1] = 0; a.dx[2] = 1; a.dx[3] = 0;  // psi_x, psi_y, omega_x, omega_y
     a.cfl = (stage == 1 && g->p.adaptive_dt) ? 1 : 0;
     a.marker = (stage == 1) ? 1 : (stage == 2 ? 2 : 0);
-    if constexpr (sizeof(T) == 4) {
-        if (g->fast_row && g->g.nx == 4096) {
-            // FP32, nx = 4096: two warps per row
-            const size_t smem = r4_smem_bytes();
-            NSG_TRY(set_smem(g, k_row_4k, smem));
-            int grid = g->g.ny / NSG_R4_ROWS;
-            if (grid > g->num_sms) grid = g->num_sms;
-            const cudaError_t e = launch_stage(k_row_4k, grid, 64 * NSG_R4_ROWS, smem, g->st, g->g, a);
-            if (e != cudaSuccess) NSG_FAIL(g, NS_GPU_ERR_CUDA, "k_row_4k launch: %s", cudaGetErrorString(e));
-            NSG_LAUNCHED(g);
-            return NS_GPU_OK;
-        }
-    }
-    if constexpr (sizeof(T) == 4 && NSG_ROW_TMEM) {
-        if (g->fast_row) {
-            // FP32: Jacobian operands in tensor memory, inboxes filled by cp.async
-            auto kern = k_row_t<NSG_RT_NW, NSG_RT_GW, NSG_RT_NB>;
-            const size_t smem = rt_smem_bytes<NSG_RT_NW, NSG_RT_NB>();
-            NSG_TRY(set_smem(g, kern, smem));
-            int grid = g->g.ny / NSG_RT_NW;
-            if (grid > g->num_sms) grid = g->num_sms;
-            const cudaError_t e = launch_stage(kern, grid, 32 * NSG_RT_NW, smem, g->st, g->g, a);
-            if (e != cudaSuccess) NSG_FAIL(g, NS_GPU_ERR_CUDA, "k_row_t launch: %s", cudaGetErrorString(e));
-            NSG_LAUNCHED(g);
-            return NS_GPU_OK;
-        }
-    }
     if (g->fast_row) {
-        const size_t smem = rw_smem_bytes<T>();
-        NSG_TRY(set_smem(g, k_row_w<T>, smem));
-        const int nw = rw_warps<T>();
-        int grid = g->g.ny / nw;
-        if (grid > g->num_sms) grid = g->num_sms;
-        const cudaError_t e = launch_stage(k_row_w<T>, grid, 32 * nw, smem, g->st, g->g, a);
-        if (e != cudaSuccess) NSG_FAIL(g, NS_GPU_ERR_CUDA, "k_row_w launch: %s", cudaGetErrorString(e));
-        NSG_LAUNCHED(g);
-        return NS_GPU_OK;
+        if constexpr (sizeof(T) == 4) return nsg_fast_row_f32(g, a);
+        else return nsg_fast_row_f64(g, a);
     }
     return row_launch<T, ROW_STAGE>(g, a);
 }
 
-// FP32 column pass k_col_q for ny = 2^NL (NL = 11, 12)
-template <int NL, int STAGE> static int launch_col_q(ns_gpu* g, const ColArgs<float>& a) {
-    const size_t smem = cq_smem_bytes<NL>(g->g.Ky);
-    auto kern = a.sp.ifrk ? k_col_q<NL, STAGE, true> : k_col_q<NL, STAGE, false>;
-    NSG_TRY(set_smem(g, kern, smem));
-    int grid = g->num_sms;
-    if (grid > g->g.Kx) grid = g->g.Kx;
-    const cudaError_t e = launch_stage(kern, grid, CQ<NL>::TT * CQ<NL>::NT, smem, g->st, g->g, a);
-    if (e != cudaSuccess) NSG_FAIL(g, NS_GPU_ERR_CUDA, "k_col_q launch: %s", cudaGetErrorString(e));
-    NSG_LAUNCHED(g);
-    return NS_GPU_OK;
-}
-
 template <typename T, int STAGE> static int stage_col(ns_gpu* g, const ColArgs<T>& a) {
     ProfScope ps(g, 1);
-    if constexpr (sizeof(T) == 4 && NSG_COL_Q) {
-        // FP32: N/128 warps per column (k_col_q)
-        if (g->fast_col) return g->g.ny == 4096 ? launch_col_q<12, STAGE>(g, a) : launch_col_q<11, STAGE>(g, a);
-    }
     if (g->fast_col) {
-        const size_t smem = cw_smem_bytes<T>(g->g.Ky);
-        auto kern = a.sp.ifrk ? k_col_w<T, STAGE, true> : k_col_w<T, STAGE, false>;
-        NSG_TRY(set_smem(g, kern, smem));
-        int grid = g->num_sms;
-        if (grid > g->g.Kx) grid = g->g.Kx;
-        const cudaError_t e = launch_stage(kern, grid, 64 * cw_teams<T>(), smem, g->st, g->g, a);
-        if (e != cudaSuccess) NSG_FAIL(g, NS_GPU_ERR_CUDA, "k_col_w launch: %s", cudaGetErrorString(e));
-        NSG_LAUNCHED(g);
-        return NS_GPU_OK;
+        if constexpr (sizeof(T) == 4) return nsg_fast_col_f32(g, a, STAGE);
+        else return nsg_fast_col_f64(g, a, STAGE);
     }
     return col_launch<T, COL_STAGE, STAGE>(g, a);
 }
 
 static int dalloc(ns_gpu* g, void** p, size_t bytes);
 
-// The per-step forcing-noise table: every (kept mode with |kx|, |ky| <= kmax,
-// draw) pair gets one thread of k_forcing_noise before the step's first stage,
-// instead of one thread per mode drawing them in sequence at stage 4.
+// The per-step forcing-noise table of steps that take several draws: every (kept
+// mode with |kx|, |ky| <= kmax, draw) pair gets one thread of k_forcing_noise
+// before the step's first stage, instead of one thread per mode drawing them in
+// sequence at stage 4.
 static int ensure_noise(ns_gpu* g) {
     g->fM = 0;
     const StepParams sp = step_params<double>(g);
-    if (!sp.forcing) return NS_GPU_OK;
+    // one draw per step costs the stage-4 kernel less than a kernel of its own
+    // costs the step; several draws (coarse steps that sum fine-step forcing) go
+    // to the table
+    if (!sp.forcing || sp.fsub <= 1) return NS_GPU_OK;
     const double two_pi = 2.0 * 3.14159265358979323846;
     const int kxr = std::min((int)floor(sp.f_kmax * g->g.Lx / two_pi + 1e-9), g->g.Kx - 1);
     const int kyr = std::min((int)floor(sp.f_kmax * g->g.Ly / two_pi + 1e-9), g->g.Kyh);
@@ -555,7 +471,7 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
         // FP32 also has register-resident row and column passes at 4096
         // (their F/G layouts assume a power-of-two ny)
         g->fast_row = (!generic && pow2_grid && (nx == 2048 || (nx == 4096 && precision == NS_GPU_FP32))) ? 1 : 0;
-        g->fast_col = (!generic && pow2_grid && (ny == 2048 || (ny == 4096 && precision == NS_GPU_FP32 && NSG_COL_Q)))
+        g->fast_col = (!generic && pow2_grid && (ny == 2048 || (ny == 4096 && precision == NS_GPU_FP32 && nsg_fast_col_q())))
                           ? 1
                           : 0;
     }

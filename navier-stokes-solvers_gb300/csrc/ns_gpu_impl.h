@@ -5,6 +5,7 @@
 
 #include <cstdio>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "ns_gpu.h"
@@ -106,6 +107,45 @@ struct ProfScope {
         int _s = (__VA_ARGS__); \
         if (_s != NS_GPU_OK) return _s; \
     } while (0)
+
+// ------------------------------------------------------------- launchers
+// Launch a stage kernel with programmatic stream serialization: it may be
+// scheduled while the previous kernel on the stream drains, runs its
+// independent prologue, and waits (griddepcontrol.wait) before it touches
+// anything the previous kernel wrote.
+#ifndef NSG_PDL
+#define NSG_PDL 1
+#endif
+template <typename... KArgs, typename... Args>
+static inline cudaError_t launch_stage(void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t st,
+                                Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = NSG_PDL;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
+
+template <typename K> static inline int set_smem(ns_gpu* g, K kernel, size_t bytes) {
+    if (bytes > 48 * 1024) NSG_CUDA(g, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    return NS_GPU_OK;
+}
+
+
+// Register-resident stage kernels at nx or ny = 2048 (and 4096 in FP32), in
+// their own translation unit (csrc/ns_fast.cu); stage is 1..4.
+int nsg_fast_row_f32(ns_gpu* g, const nsg::RowArgs<float>& a);
+int nsg_fast_row_f64(ns_gpu* g, const nsg::RowArgs<double>& a);
+int nsg_fast_col_f32(ns_gpu* g, const nsg::ColArgs<float>& a, int stage);
+int nsg_fast_col_f64(ns_gpu* g, const nsg::ColArgs<double>& a, int stage);
+// 1 when the FP32 column pass at 2048 / 4096 is k_col_q (else k_col_w)
+int nsg_fast_col_q();
 
 // Tiling of the generic stage kernels (zero: automatic), see nsg_create.
 struct NsgTiling {
