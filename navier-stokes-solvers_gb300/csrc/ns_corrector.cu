@@ -226,8 +226,9 @@ __device__ __forceinline__ void tc_issue(unsigned taddr, unsigned hx, unsigned w
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb) : "memory");
 }
 
-// in: BF16 activations [B][H][W][64]; w: BF16 weights [9][64 ci][64 co]; bias
-// may be null; outputs (each may be null): pre FP32, actf FP32, actb BF16, all
+// in: BF16 activations [B][H][W][64]; w: BF16 weights in the B-operand layout
+// [9 taps][8 ci / 8][64 co][8 ci % 8] (k_round_weights); bias may be null;
+// outputs (each may be null): pre FP32, actf FP32, actb BF16, all
 // [B][H][W][64].  Pipeline per CTA (tiles t = blockIdx.x, + gridDim.x, ...;
 // iteration i uses halo buffer, accumulator and mbarrier i % 2): the MMAs of
 // iteration i + 1 were issued before iteration i's epilogue starts; once
@@ -256,11 +257,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __nv_bfloat16* 
     const int ntiles = B * H * ntx;
     const int gstride = gridDim.x;
 
-    // weights into the B-operand layout: WB[tap][kc][co][j] = w[tap][8 kc + j][co]
-    for (int i = tid; i < 9 * 64 * 64; i += TC_THREADS) {
-        const int tap = i >> 12, r = i & 4095, ci = r >> 6, co = r & 63;
-        reinterpret_cast<__nv_bfloat16*>(WB)[((tap * 8 + (ci >> 3)) * 64 + co) * 8 + (ci & 7)] = w[i];
-    }
+    // weights, already in the B-operand layout WB[tap][kc][co][j] = w[tap][8 kc + j][co]
+    for (int i = tid; i < TC_WB_BYTES / 16; i += TC_THREADS)
+        reinterpret_cast<uint4*>(WB)[i] = reinterpret_cast<const uint4*>(w)[i];
+    __shared__ float sbias[64];
+    if (tid < 64) sbias[tid] = bias ? bias[tid] : 0.0f;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(smem_u32(tslot)));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
@@ -309,7 +310,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __nv_bfloat16* 
 #pragma unroll
             for (int k = 0; k < 32; ++k) {
                 const int co = 32 * h + k;
-                stg[prow * TC_ST + co] = bias ? v[k] + bias[co] : v[k];
+                stg[prow * TC_ST + co] = v[k] + sbias[co];
             }
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -387,9 +388,10 @@ __global__ void __launch_bounds__(256) k_conv_in_bf16(const float* __restrict__ 
 // 8 x 32 pixel tiles (W % 32 == 0, H % 8 == 0) with the periodic halo (10 x 34
 // pixels) in shared memory; 256 threads per CTA.
 constexpr int IT_H = 8, IT_W = 32, IT_HALO = (IT_H + 2) * (IT_W + 2);
+constexpr int IN_H = 4, IN_HALO = (IN_H + 2) * (IT_W + 2);  // first layer: 4 x 32 tiles (more CTAs in flight)
 
-// first layer (2 -> 64, GELU) to the BF16 activations of the tensor-core layers:
-// thread = (pixel column, eight consecutive output channels), eight lanes write
+// first layer (2 -> 64, GELU) to the BF16 activations of the tensor-core layers,
+// over 4 x 32 tiles: thread = (pixel column, eight consecutive output channels), eight lanes write
 // one pixel's 128 bytes; the arithmetic order of k_conv_in_bf16 (bias, then taps,
 // then input channels), so the outputs are the same bits
 __global__ void __launch_bounds__(256) k_conv_in_tile(const float* __restrict__ in, const __nv_bfloat16* __restrict__ w,
@@ -397,22 +399,22 @@ __global__ void __launch_bounds__(256) k_conv_in_tile(const float* __restrict__ 
                                                       int B, int H, int W) {
     __shared__ __align__(16) float sw[9 * 2 * 64];  // [tap][ci][co]
     __shared__ float sb[64];
-    __shared__ float2 sx[IT_HALO];
+    __shared__ float2 sx[IN_HALO];
     for (int i = threadIdx.x; i < 9 * 2 * 64; i += blockDim.x) sw[i] = __bfloat162float(w[i]);
     if (threadIdx.x < 64) sb[threadIdx.x] = bias ? bias[threadIdx.x] : 0.0f;
     const int g = threadIdx.x & 7, pl = threadIdx.x >> 3;
-    const int ntx = W / IT_W, nty = H / IT_H, ntiles = B * nty * ntx;
+    const int ntx = W / IT_W, nty = H / IN_H, ntiles = B * nty * ntx;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int b = tile / (nty * ntx), r = tile - b * nty * ntx;
-        const int y0 = (r / ntx) * IT_H, x0 = (r % ntx) * IT_W;
+        const int y0 = (r / ntx) * IN_H, x0 = (r % ntx) * IT_W;
         __syncthreads();  // previous tile done with sx (and the weights written)
-        for (int i = threadIdx.x; i < IT_HALO; i += blockDim.x) {
+        for (int i = threadIdx.x; i < IN_HALO; i += blockDim.x) {
             const int hy = i / (IT_W + 2), hx = i - hy * (IT_W + 2);
             sx[i] = *reinterpret_cast<const float2*>(in + (((size_t)b * H + wrapi(y0 + hy - 1, H)) * W + wrapi(x0 + hx - 1, W)) * 2);
         }
         __syncthreads();
 #pragma unroll 1
-        for (int py = 0; py < IT_H; ++py) {
+        for (int py = 0; py < IN_H; ++py) {
             float a[8];
 #pragma unroll
             for (int k = 0; k < 8; ++k) a[k] = sb[8 * g + k];
@@ -420,11 +422,14 @@ __global__ void __launch_bounds__(256) k_conv_in_tile(const float* __restrict__ 
             for (int tap = 0; tap < 9; ++tap) {
                 const int dy = tap / 3, dx = tap - 3 * dy;
                 const float2 xv = sx[(py + dy) * (IT_W + 2) + pl + dx];
-                const float* w0 = sw + (tap * 2) * 64 + 8 * g;
+                const float4* w4 = reinterpret_cast<const float4*>(sw + (tap * 2) * 64 + 8 * g);
+                const float4 wa = w4[0], wb = w4[1], wc = w4[16], wd = w4[17];  // ci 0: k 0-7; ci 1: k 0-7
+                const float w0[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
+                const float w1[8] = {wc.x, wc.y, wc.z, wc.w, wd.x, wd.y, wd.z, wd.w};
 #pragma unroll
                 for (int k = 0; k < 8; ++k) a[k] = fmaf(xv.x, w0[k], a[k]);
 #pragma unroll
-                for (int k = 0; k < 8; ++k) a[k] = fmaf(xv.y, w0[64 + k], a[k]);
+                for (int k = 0; k < 8; ++k) a[k] = fmaf(xv.y, w1[k], a[k]);
             }
             uint4 pk;
             unsigned* pw = reinterpret_cast<unsigned*>(&pk);
@@ -621,9 +626,13 @@ __global__ void k_adamw(float* __restrict__ p, float* __restrict__ m, float* __r
     }
 }
 
-// BF16 compute copies of one layer: wb[tap][ci][co], wbT[8 - tap][co][ci]
+// BF16 compute copies of one layer: wb[tap][ci][co], wbT[8 - tap][co][ci]; for the
+// 64 -> 64 layers also both in the tensor-core B-operand layout
+// [tap][ci / 8][co][ci % 8] (wbB, wbtB; null for the other layers), which the
+// tensor-core kernel copies to shared memory as it stands
 __global__ void k_round_weights(const float* __restrict__ w, int cin, int cout, __nv_bfloat16* __restrict__ wb,
-                                __nv_bfloat16* __restrict__ wbt) {
+                                __nv_bfloat16* __restrict__ wbt, __nv_bfloat16* __restrict__ wbB,
+                                __nv_bfloat16* __restrict__ wbtB) {
     const int n = 9 * cin * cout;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int tap = i / (cin * cout), r = i - tap * cin * cout;
@@ -631,6 +640,8 @@ __global__ void k_round_weights(const float* __restrict__ w, int cin, int cout, 
         const __nv_bfloat16 h = __float2bfloat16_rn(w[i]);
         wb[i] = h;
         wbt[((8 - tap) * cout + co) * cin + ci] = h;
+        if (wbB) wbB[((tap * 8 + (ci >> 3)) * 64 + co) * 8 + (ci & 7)] = h;
+        if (wbtB) wbtB[(((8 - tap) * 8 + (co >> 3)) * 64 + ci) * 8 + (co & 7)] = h;
     }
 }
 
@@ -686,6 +697,7 @@ struct ns_cnn {
     size_t woff[NL], boff[NL];     // offsets into the flat FP32 parameter vector
     float *p = nullptr, *gp = nullptr, *m = nullptr, *v = nullptr;  // master, grad, moments
     __nv_bfloat16 *wb[NL] = {}, *wbt[NL] = {};
+    __nv_bfloat16 *wbB[NL] = {}, *wbtB[NL] = {};  // tensor-core B-operand layouts (64 -> 64 layers)
     float* x0 = nullptr;           // [B][H][W][2]
     float *pre[NL] = {}, *act[NL] = {};
     float *d0 = nullptr, *d1 = nullptr;  // gradient ping-pong [B][H][W][64]
@@ -786,7 +798,7 @@ static int forward(ns_cnn* c, cudaStream_t st, int B, bool training = true) {
     const bool tiles32 = (c->W % IT_W == 0) && (c->H % IT_H == 0);
     if (c->tc && !training) {
         if (tiles32) {
-            const long long tiles = (long long)B * (c->H / IT_H) * (c->W / IT_W);
+            const long long tiles = (long long)B * (c->H / IN_H) * (c->W / IT_W);
             k_conv_in_tile<<<grid_of(tiles, 1, 8 * c->num_sms), 256, 0, st>>>(x, c->wb[0], c->p + c->boff[0], c->ab0, B,
                                                                              c->H, c->W);
         } else {
@@ -808,7 +820,7 @@ static int forward(ns_cnn* c, cudaStream_t st, int B, bool training = true) {
         __nv_bfloat16* aout = c->ab1;
         for (int l = 1; l < NL - 1; ++l) {
             const bool last = (l == NL - 2);
-            CNN_TRY(conv_tc<true>(c, st, ain, c->wb[l], c->p + c->boff[l], training ? c->pre[l] : nullptr,
+            CNN_TRY(conv_tc<true>(c, st, ain, c->wbB[l], c->p + c->boff[l], training ? c->pre[l] : nullptr,
                                   (training || last) ? c->act[l] : nullptr, last ? nullptr : aout, B));
             __nv_bfloat16* t = ain;
             ain = aout;
@@ -872,7 +884,7 @@ static int loss_and_backward(ns_cnn* c, cudaStream_t st, int B, int slot) {
                 const long long n = npix * HID;
                 k_to_bf16<<<grid_of(n, 256, 8 * c->num_sms), 256, 0, st>>>(dcur, c->ab0, n);
                 CNN_LAUNCHED(c);
-                CNN_TRY(conv_tc<false>(c, st, c->ab0, c->wbt[l], nullptr, nullptr, dnext, nullptr, B));
+                CNN_TRY(conv_tc<false>(c, st, c->ab0, c->wbtB[l], nullptr, nullptr, dnext, nullptr, B));
             } else {
                 CNN_TRY((conv<HID, HID, 32, false>(c, st, dcur, c->wbt[l], nullptr, dnext, nullptr, B)));
             }
@@ -889,7 +901,8 @@ static int loss_and_backward(ns_cnn* c, cudaStream_t st, int B, int slot) {
 static int round_weights(ns_cnn* c, cudaStream_t st) {
     for (int l = 0; l < NL; ++l) {
         k_round_weights<<<grid_of(9 * CIN_OF[l] * COUT_OF[l], 256, 256), 256, 0, st>>>(c->p + c->woff[l], CIN_OF[l],
-                                                                                      COUT_OF[l], c->wb[l], c->wbt[l]);
+                                                                                      COUT_OF[l], c->wb[l], c->wbt[l],
+                                                                                      c->wbB[l], c->wbtB[l]);
         CNN_LAUNCHED(c);
     }
     return NS_GPU_OK;
@@ -928,6 +941,10 @@ int ns_cnn_create(int height, int width, int max_batch, uint64_t seed, ns_cnn** 
     for (int l = 0; l < NL; ++l) {
         alloc((void**)&c->wb[l], (size_t)9 * CIN_OF[l] * COUT_OF[l] * sizeof(__nv_bfloat16));
         alloc((void**)&c->wbt[l], (size_t)9 * CIN_OF[l] * COUT_OF[l] * sizeof(__nv_bfloat16));
+        if (CIN_OF[l] == HID && COUT_OF[l] == HID) {
+            alloc((void**)&c->wbB[l], (size_t)9 * HID * HID * sizeof(__nv_bfloat16));
+            alloc((void**)&c->wbtB[l], (size_t)9 * HID * HID * sizeof(__nv_bfloat16));
+        }
         alloc((void**)&c->pre[l], npix * COUT_OF[l] * sizeof(float));
         if (l < NL - 1) alloc((void**)&c->act[l], npix * COUT_OF[l] * sizeof(float));
     }
@@ -979,6 +996,8 @@ void ns_cnn_destroy(ns_cnn* c) {
     for (int l = 0; l < NL; ++l) {
         if (c->wb[l]) cudaFree(c->wb[l]);
         if (c->wbt[l]) cudaFree(c->wbt[l]);
+        if (c->wbB[l]) cudaFree(c->wbB[l]);
+        if (c->wbtB[l]) cudaFree(c->wbtB[l]);
         if (c->pre[l]) cudaFree(c->pre[l]);
         if (c->act[l]) cudaFree(c->act[l]);
     }
@@ -1207,7 +1226,7 @@ int ns_cnn_probe_wait_timeout(ns_cnn* c, long long wait_cycles, int* timed_out) 
     auto k = k_conv_tc<true>;
     CNN_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
     const int tiles = c->H * (c->W / TC_W);
-    k<<<grid_of(tiles, 1, c->num_sms), TC_THREADS, TC_SMEM, st>>>(c->ab0, c->wb[1], nullptr, nullptr, nullptr, nullptr, 1,
+    k<<<grid_of(tiles, 1, c->num_sms), TC_THREADS, TC_SMEM, st>>>(c->ab0, c->wbB[1], nullptr, nullptr, nullptr, nullptr, 1,
                                                                   c->H, c->W, c->derr, wait_cycles, 1);
     CNN_LAUNCHED(c);
     int e = 0;
@@ -1238,7 +1257,7 @@ int ns_cnn_time_hidden_layer(ns_cnn* c, int batch, int reps, double* ms_per_laun
     int s = NS_GPU_OK;
     for (int r = 0; r <= reps && s == NS_GPU_OK; ++r) {
         if (r == 1) cudaEventRecord(a, st);
-        if (c->tc) s = conv_tc<true>(c, st, c->ab0, c->wb[1], c->p + c->boff[1], c->pre[1], c->act[1], c->ab1, batch);
+        if (c->tc) s = conv_tc<true>(c, st, c->ab0, c->wbB[1], c->p + c->boff[1], c->pre[1], c->act[1], c->ab1, batch);
         else s = conv<HID, HID, 32, true>(c, st, c->act[0], c->wb[1], c->p + c->boff[1], c->pre[1], c->act[1], batch);
     }
     cudaEventRecord(b, st);

@@ -1327,11 +1327,8 @@ template <typename T> static int vorticity_t(ns_gpu* g, float* out) {
     RowArgs<T> a = row_args<T>(g);
     a.F[0] = (const Cx<T>*)g->F[2];  // Omega, no derivative
     a.dx[0] = 0;
-    a.out_real[0] = g->real[0];
+    a.out_f32 = out;  // the physical field leaves as float directly
     NSG_TRY(row_launch<T, ROW_INV1>(g, a));
-    const long long n = (long long)g->g.nx * g->g.ny;
-    k_d2f<<<grid_for(n), 256, 0, g->st>>>(g->real[0], out, n);
-    NSG_LAUNCHED(g);
     return NS_GPU_OK;
 }
 
@@ -1343,11 +1340,8 @@ int ns_gpu_vorticity_device(ns_gpu* g, float* omega_dev) {
 }
 
 template <typename T> static int add_vorticity_t(ns_gpu* g, const float* delta) {
-    const long long n = (long long)g->g.nx * g->g.ny;
-    k_f2d<<<grid_for(n), 256, 0, g->st>>>(delta, g->real[0], n);
-    NSG_LAUNCHED(g);
     RowArgs<T> a = row_args<T>(g);
-    a.in_real = g->real[0];
+    a.in_f32 = delta;  // the row pass reads the float field directly
     NSG_TRY(row_launch<T, ROW_FWD1>(g, a));
     NSG_CUDA(g, cudaMemsetAsync(g->spec[0], 0, spec_bytes(g), g->st));
     ColArgs<T> c = col_args<T>(g);

@@ -204,6 +204,8 @@ template <typename T> struct RowArgs {
     int dx[4];                // 1: multiply by i kx before the transform
     C* G;                     // C[ny][Kxp] output (ROW_STAGE, ROW_DUMP, ROW_FWD1)
     const double* in_real;    // ROW_FWD1 input double[ny][nx]
+    const float* in_f32;      // ROW_FWD1: float[ny][nx] input instead of in_real (when set)
+    float* out_f32;           // ROW_INV1: float[ny][nx] output instead of out_real[0] (when set)
     double* out_real[5];      // physical outputs double[ny][nx]
     const T* kxv;             // kx of kept columns
     const C* twr;             // exp(-2 pi i t/H), t < H
@@ -245,11 +247,15 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
     if constexpr (MODE == ROW_FWD1) {
         C* b = sm + r * LP;
         const double* src = a.in_real + (size_t)y * nx;
+        const float* srcf = a.in_f32 ? a.in_f32 + (size_t)y * nx : nullptr;
         for (int m = t; m < H; m += TT) {
             C z;
             if (oddx) {
-                z.x = (T)src[m];
+                z.x = srcf ? (T)srcf[m] : (T)src[m];
                 z.y = (T)0;
+            } else if (srcf) {
+                z.x = (T)srcf[2 * m];
+                z.y = (T)srcf[2 * m + 1];
             } else {
                 z.x = (T)src[2 * m];
                 z.y = (T)src[2 * m + 1];
@@ -379,6 +385,8 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
                         a.out_real[0][o] = p0;                                 // u = psi_y
                         a.out_real[1][o] = -sm[(1 * g.RPC + r) * LP + spad(m)].x;  // v = -psi_x
                         a.out_real[2][o] = sm[(2 * g.RPC + r) * LP + spad(m)].x;   // omega
+                    } else if (a.out_f32) {
+                        a.out_f32[o] = (float)p0;
                     } else {
                         a.out_real[0][o] = p0;
                     }
@@ -394,6 +402,9 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
                     a.out_real[0][o] = z0.x; a.out_real[0][o + 1] = z0.y;   // u = psi_y
                     a.out_real[1][o] = -z1.x; a.out_real[1][o + 1] = -z1.y; // v = -psi_x
                     a.out_real[2][o] = z2.x; a.out_real[2][o + 1] = z2.y;   // omega
+                } else if (a.out_f32) {
+                    a.out_f32[o] = (float)z0.x;
+                    a.out_f32[o + 1] = (float)z0.y;
                 } else {
                     a.out_real[0][o] = z0.x;
                     a.out_real[0][o + 1] = z0.y;
@@ -1476,12 +1487,6 @@ __global__ void k_add_kept(Geo g, const double2* spec, typename CT<T>::C* W) {
     }
 }
 
-__global__ void k_d2f(const double* a, float* b, long long n) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) b[i] = (float)a[i];
-}
-__global__ void k_f2d(const float* a, double* b, long long n) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) b[i] = (double)a[i];
-}
 
 #endif  // NSG_NO_AUX_KERNELS
 
