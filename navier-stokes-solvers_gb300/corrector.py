@@ -311,9 +311,12 @@ def config5(argv=None):
     ap.add_argument("--fine-steps", type=int, default=10000)
     ap.add_argument("--spectrum-every", type=int, default=100)
     ap.add_argument("--hv-order", type=int, default=8, help="hyperviscosity order (p = 4 -> 8)")
+    ap.add_argument("--spinup", type=int, default=3000,
+                    help="fine steps before the training snapshots: the cascade must have reached the coarse "
+                         "cutoff, or the plain coarse step is already exact and the targets are round-off")
     a = ap.parse_args(argv)
     t0 = time.time()
-    x, t, dt_f = generate(list(range(a.train_seeds)), a.fine, a.coarse, a.ratio, 200, a.snapshots, forcing=True,
+    x, t, dt_f = generate(list(range(a.train_seeds)), a.fine, a.coarse, a.ratio, a.spinup, a.snapshots, forcing=True,
                           hv_order=a.hv_order)
     t_gen = time.time() - t0
     s0, s1, so = normalisation(x, t)
@@ -326,7 +329,9 @@ def config5(argv=None):
     res = ensemble_spectrum_comparison(net, a.fine, a.coarse, a.ratio, a.members, a.fine_steps, a.spectrum_every,
                                        dt_f, hv_order=a.hv_order)
     net.close()
-    res["training"] = {"samples": int(x.shape[0]), "iters": a.iters, "batch": a.batch, "generate_s": t_gen,
+    res["training"] = {"samples": int(x.shape[0]), "iters": a.iters, "batch": a.batch, "spinup": a.spinup,
+                       "target_rms_over_input_rms": float(np.sqrt(np.mean(t ** 2)) / np.sqrt(np.mean(x[:, 0] ** 2))),
+                       "generate_s": t_gen,
                        "train_s": t_train, "loss_first": float(hist[:10].mean()), "loss_last": float(hist[-50:].mean())}
     res["dt_fine"] = dt_f
     print(json.dumps(res))

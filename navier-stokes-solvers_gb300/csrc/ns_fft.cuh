@@ -51,6 +51,14 @@ __device__ __forceinline__ int spad(int i) { return i + (i >> 4); }
 // padded shared-memory length of one transform of length L
 __host__ __device__ inline int spad_len(int L) { return L + (L >> 4) + 4; }
 
+// barrier between the passes of one transform: a warp barrier when every
+// transform of the CTA is owned by threads of a single warp (ws), else the CTA
+// barrier; ws must be the same for every thread of the CTA
+__device__ __forceinline__ void fft_sync(bool ws) {
+    if (ws) __syncwarp();
+    else __syncthreads();
+}
+
 // ---------------------------------------------------------------- DFTs
 template <bool INV, typename C> __device__ __forceinline__ void dft2(C* a) {
     C t = a[0];
@@ -174,9 +182,11 @@ template <int LOGE> struct ConstLog;
 
 // In-place FFT of the sequence at sb (padded, natural order in and out).
 // All threads of the CTA must call this (it synchronises); thread t < TT of
-// this transform, TT = L / E.
+// this transform, TT = L / E.  ws: every transform's threads lie in one warp
+// (the passes synchronise that warp only; the caller synchronises the CTA
+// before other threads read the result).
 template <int E, bool INV, typename C>
-__device__ void fft_smem(C* sb, int L, int logL, int t, int TT, const C* __restrict__ tw) {
+__device__ void fft_smem(C* sb, int L, int logL, int t, int TT, const C* __restrict__ tw, bool ws = false) {
     C v[E];
     const int logE = (E == 16) ? 4 : (E == 8) ? 3 : (E == 4) ? 2 : 1;
     int Ns = 1;
@@ -186,27 +196,27 @@ __device__ void fft_smem(C* sb, int L, int logL, int t, int TT, const C* __restr
         if (lr == 4) {
             if constexpr (E >= 16) {
                 pass_load<E, 16>(v, sb, L, t, TT);
-                __syncthreads();
+                fft_sync(ws);
                 pass_compute_store<E, 16, INV>(v, sb, L, Ns, t, TT, tw);
             }
         } else if (lr == 3) {
             if constexpr (E >= 8) {
                 pass_load<E, 8>(v, sb, L, t, TT);
-                __syncthreads();
+                fft_sync(ws);
                 pass_compute_store<E, 8, INV>(v, sb, L, Ns, t, TT, tw);
             }
         } else if (lr == 2) {
             if constexpr (E >= 4) {
                 pass_load<E, 4>(v, sb, L, t, TT);
-                __syncthreads();
+                fft_sync(ws);
                 pass_compute_store<E, 4, INV>(v, sb, L, Ns, t, TT, tw);
             }
         } else {
             pass_load<E, 2>(v, sb, L, t, TT);
-            __syncthreads();
+            fft_sync(ws);
             pass_compute_store<E, 2, INV>(v, sb, L, Ns, t, TT, tw);
         }
-        __syncthreads();
+        fft_sync(ws);
         Ns <<= lr;
         rem -= lr;
     }
@@ -298,7 +308,7 @@ __device__ void mr_pass_direct(const C* src, C* dst, int L, int R, int Ns, int t
 // it (it synchronises), thread t < TT of this sequence.
 template <bool INV, typename C>
 __device__ void fft_smem_mr(C* sb, C* sc, int L, unsigned long long ra, unsigned long long rb, int np, int t, int TT,
-                            const C* __restrict__ tw) {
+                            const C* __restrict__ tw, bool ws = false) {
     C* src = sb;
     C* dst = sc;
     int Ns = 1;
@@ -313,7 +323,7 @@ __device__ void fft_smem_mr(C* sb, C* sc, int L, unsigned long long ra, unsigned
             case 8: mr_pass<8, INV>(src, dst, L, Ns, t, TT, tw); break;
             default: mr_pass_direct<INV>(src, dst, L, R, Ns, t, TT, tw); break;
         }
-        __syncthreads();
+        fft_sync(ws);
         C* x = src;
         src = dst;
         dst = x;
@@ -321,7 +331,7 @@ __device__ void fft_smem_mr(C* sb, C* sc, int L, unsigned long long ra, unsigned
     }
     if (src != sb) {
         for (int i = t; i < L; i += TT) sb[spad(i)] = src[spad(i)];
-        __syncthreads();
+        fft_sync(ws);
     }
 }
 

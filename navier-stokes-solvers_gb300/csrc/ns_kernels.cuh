@@ -48,11 +48,14 @@ struct Geo {
 
 // one transform of a row or column buffer b: the power-of-two engine for E > 0,
 // the mixed-radix engine (through the scratch sequence sc) for E == 0
+// (the passes synchronise one warp when TT divides the warp size: then every
+// transform of the CTA lies inside a warp)
 template <int E, bool INV, typename C>
 __device__ __forceinline__ void fft_any(C* b, C* sc, int L, int logL, unsigned long long ra, unsigned long long rb, int np,
                                         int t, int TT, const C* __restrict__ tw) {
-    if constexpr (E == 0) fft_smem_mr<INV>(b, sc, L, ra, rb, np, t, TT, tw);
-    else fft_smem<E, INV>(b, L, logL, t, TT, tw);
+    const bool ws = TT <= 32 && (32 % TT) == 0;
+    if constexpr (E == 0) fft_smem_mr<INV>(b, sc, L, ra, rb, np, t, TT, tw, ws);
+    else fft_smem<E, INV>(b, L, logL, t, TT, tw, ws);
 }
 
 // element (row y, kept column c) of an F buffer / of the G buffer
@@ -144,6 +147,30 @@ __device__ __forceinline__ double2 forcing_xi_sum(int i, int j, int ny, unsigned
         sy = __dadd_rn(sy, __dmul_rn(rad, sn));
     }
     return make_double2(sx, flip ? -sy : sy);
+}
+
+// One term of the noise table of a step: draw s of mode (kx index i, ky) with
+// counter base + s, as forcing_xi_sum forms it (the conjugate row of kx = 0,
+// ky < 0 negated); zero outside the shell kmin <= |k| <= kmax.
+__device__ __forceinline__ double2 forcing_noise_term(int i, int ky, int s, unsigned long long base,
+                                                      unsigned long long seed, double Lx, double Ly, double kmin,
+                                                      double kmax) {
+    const double kxd = 2.0 * 3.141592653589793 * i / Lx;
+    const double kyd = 2.0 * 3.141592653589793 * ky / Ly;
+    const double k2d = kxd * kxd + kyd * kyd;
+    const double km = sqrt(k2d);
+    if (!(k2d > 1e-12 && km >= kmin && km <= kmax)) return make_double2(0.0, 0.0);
+    int flip = 0;
+    if (i == 0 && ky < 0) { ky = -ky; flip = 1; }
+    const unsigned long long id = ((unsigned long long)(unsigned int)ky << 32) | (unsigned int)i;
+    unsigned long long ctr[4] = {id, base + (unsigned long long)s, NSG_TAG_FORCE, 0ULL};
+    philox4x64(ctr, seed, 0ULL);
+    const double u1 = fmax(u53(ctr[0]), 2.2250738585072014e-308);
+    const double u2 = u53(ctr[1]);
+    const double rad = sqrt(-2.0 * log(u1)) * 0.70710678118654752440;
+    double sn, cs;
+    sincos(2.0 * 3.141592653589793 * u2, &sn, &cs);
+    return make_double2(__dmul_rn(rad, cs), flip ? -__dmul_rn(rad, sn) : __dmul_rn(rad, sn));
 }
 
 // ---------------------------------------------------------------- reductions
@@ -696,6 +723,7 @@ __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, cons
         }
         __syncthreads();
         fft_any<E, false>(mybuf, myscr, ny, g.logny, g.rya, g.ryb, g.nry, t, TC, a.twc);
+        __syncthreads();  // the loops below read every column of the block
 
         if constexpr (MODE == COL_FWD_EXPORT || MODE == COL_NL_EXPORT) {
             const T sc = (T)a.out_scale;
@@ -776,6 +804,7 @@ __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, cons
         }
         __syncthreads();
         fft_any<E, true>(mybuf, myscr, ny, g.logny, g.rya, g.ryb, g.nry, t, TC, a.twc);
+        __syncthreads();  // the store loop reads every column of the block
         C* dstF = a.F[f];
         for (int idx = threadIdx.x; idx < ny * CW; idx += nthr) {
             int y, c;
@@ -1024,26 +1053,8 @@ __global__ void k_forcing_noise(int ny, double Lx, double Ly, const unsigned lon
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const int e = t / M, s = t - e * M;
         const int i = e / (2 * kyr + 1);
-        int ky = e - i * (2 * kyr + 1) - kyr;
-        const double kxd = 2.0 * 3.141592653589793 * i / Lx;
-        const double kyd = 2.0 * 3.141592653589793 * ky / Ly;
-        const double k2d = kxd * kxd + kyd * kyd;
-        const double km = sqrt(k2d);
-        double2 v = make_double2(0.0, 0.0);
-        if (k2d > 1e-12 && km >= kmin && km <= kmax) {
-            int flip = 0;
-            if (i == 0 && ky < 0) { ky = -ky; flip = 1; }
-            const unsigned long long id = ((unsigned long long)(unsigned int)ky << 32) | (unsigned int)i;
-            unsigned long long ctr[4] = {id, *step_next + (unsigned long long)s, NSG_TAG_FORCE, 0ULL};
-            philox4x64(ctr, seed, 0ULL);
-            const double u1 = fmax(u53(ctr[0]), 2.2250738585072014e-308);
-            const double u2 = u53(ctr[1]);
-            const double rad = sqrt(-2.0 * log(u1)) * 0.70710678118654752440;
-            double sn, cs;
-            sincos(2.0 * 3.141592653589793 * u2, &sn, &cs);
-            v = make_double2(__dmul_rn(rad, cs), flip ? -__dmul_rn(rad, sn) : __dmul_rn(rad, sn));
-        }
-        out[t] = v;
+        const int ky = e - i * (2 * kyr + 1) - kyr;
+        out[t] = forcing_noise_term(i, ky, s, *step_next, seed, Lx, Ly, kmin, kmax);
     }
 }
 

@@ -108,15 +108,24 @@ def loss_and_grads(params, inputs, targets, s0=1.0, s1=1.0, so=1.0, bf16_weights
     return loss, flat
 
 
-def forward(params, inputs, s0=1.0, s1=1.0, so=1.0, bf16_hidden_inputs=False):
+def gelu_tanh(x):
+    """GELU in the tanh form of Hendrycks and Gimpel (2016)."""
+    return 0.5 * x * (1.0 + np.tanh(np.sqrt(2.0 / np.pi) * (x + 0.044715 * x ** 3)))
+
+
+def forward(params, inputs, s0=1.0, s1=1.0, so=1.0, bf16_hidden_inputs=False, inference=False):
     """Network output; bf16_hidden_inputs rounds the inputs of the four 64 -> 64
-    layers to bfloat16, as the library's tensor-core path stores them."""
+    layers to bfloat16, as the library's tensor-core path stores them.
+    inference: the library's tensor-core inference path, which also applies GELU
+    in its tanh form to the activations it stores as bfloat16 (the outputs of
+    layers 0-3; the last hidden layer keeps the erf form)."""
     layers = [(bf16(w), b) for w, b in unflatten(np.asarray(params, dtype=np.float64))]
     x = np.stack([inputs[:, 0] * s0, inputs[:, 1] * s1], axis=-1).astype(np.float64)
+    bf16_hidden_inputs = bf16_hidden_inputs or inference
     for l, (w, b) in enumerate(layers):
         if bf16_hidden_inputs and 1 <= l <= len(layers) - 2:
             x = bf16(x.astype(np.float32))
         x = conv(x, w, b)
         if l < len(layers) - 1:
-            x = gelu(x)
+            x = gelu_tanh(x) if (inference and l <= len(layers) - 3) else gelu(x)
     return x[..., 0] / so
