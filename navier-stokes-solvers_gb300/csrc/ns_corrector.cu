@@ -270,9 +270,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __nv_bfloat16* 
     const int ntiles = B * H * ntx;
     const int gstride = gridDim.x;
 
-    // weights, already in the B-operand layout WB[tap][kc][co][j] = w[tap][8 kc + j][co]
+    // weights, already in the B-operand layout WB[tap][kc][co][j] = w[tap][8 kc + j][co]:
+    // cp.async (all 16-byte chunks in flight at once), completed with the first halos
     for (int i = tid; i < TC_WB_BYTES / 16; i += TC_THREADS)
-        reinterpret_cast<uint4*>(WB)[i] = reinterpret_cast<const uint4*>(w)[i];
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(WB + 16 * i)),
+                     "l"(reinterpret_cast<const uint4*>(w) + i)
+                     : "memory");
+    asm volatile("cp.async.commit_group;" ::: "memory");
     __shared__ float sbias[64];
     if (tid < 64) sbias[tid] = bias ? bias[tid] : 0.0f;
     if (warp == 0) {
@@ -481,16 +485,23 @@ __global__ void __launch_bounds__(256) k_conv_out_tile(const float* __restrict__
             float acc[9];
 #pragma unroll
             for (int t = 0; t < 9; ++t) acc[t] = 0.0f;
-#pragma unroll 4
-            for (int c4 = 0; c4 < 16; ++c4) {
-                const float4 v = ap[c4];
+#pragma unroll 1
+            for (int half = 0; half < 2; ++half) {
+                float4 xv[8];  // 32 of the pixel's activations, all loads in flight before the sums
 #pragma unroll
-                for (int t = 0; t < 9; ++t) {
-                    const float4 wv = reinterpret_cast<const float4*>(sw)[t * 16 + c4];
-                    acc[t] = fmaf(v.x, wv.x, acc[t]);
-                    acc[t] = fmaf(v.y, wv.y, acc[t]);
-                    acc[t] = fmaf(v.z, wv.z, acc[t]);
-                    acc[t] = fmaf(v.w, wv.w, acc[t]);
+                for (int c = 0; c < 8; ++c) xv[c] = ap[8 * half + c];
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    const float4 v = xv[c];
+                    const int c4 = 8 * half + c;
+#pragma unroll
+                    for (int t = 0; t < 9; ++t) {
+                        const float4 wv = reinterpret_cast<const float4*>(sw)[t * 16 + c4];
+                        acc[t] = fmaf(v.x, wv.x, acc[t]);
+                        acc[t] = fmaf(v.y, wv.y, acc[t]);
+                        acc[t] = fmaf(v.z, wv.z, acc[t]);
+                        acc[t] = fmaf(v.w, wv.w, acc[t]);
+                    }
                 }
             }
 #pragma unroll

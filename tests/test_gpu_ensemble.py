@@ -126,3 +126,35 @@ def test_invalid_configurations_are_rejected(nsgb):
         nsgb.Ensemble([64], L, config=(512, 16, 16, 1))  # 16-value transforms cap a CTA at 256 threads
     with pytest.raises(RuntimeError):
         nsgb.Ensemble([32], L, config=(128, 16, 16, 1))  # a 32^2 row block would need 128 rows
+
+
+def test_config3_members_against_the_fp64_oracle(nsgb, port):
+    """One member of each config-3 size (64^2, 128^2, 256^2), FP32 inside the
+    persistent ensemble kernel, against the FP64 oracle at its own size: same
+    random-phase initial spectrum (k0 = 4), hyperviscosity p = 2, Philox forcing
+    on 4 <= |k| <= 6 with the member's own seed, CFL 0.5 adaptive dt; relative L2
+    of the vorticity spectrum <= 1e-5 after 10 steps."""
+    import oracle as O
+
+    sizes = [64, 128, 256]
+    steps = 10
+    ens = nsgb.Ensemble(sizes, L, config=(256, 4, 4, 4))
+    for i, (m, n) in enumerate(zip(ens.members, sizes)):
+        setup_member(m, n, 40 + i)
+    ens.advance(steps)
+    ens.sync()
+    for i, (m, n) in enumerate(zip(ens.members, sizes)):
+        p = member_params(n, 40 + i)
+        o = O.Solver(port, n, n, Re=p["Re"]).setup(ic=None)
+        port.nso_ext_init_random_spectrum(o.ptr, 40 + i, 4.0, 0.5)
+        o.set_hyperviscosity(enabled=1, coefficient=p["hv_coefficient"], order=4, cutoff_ratio=0.0)
+        o.d.cfl_factor = p["cfl_factor"]
+        port.nso_ext_run(o.ptr, steps, 1, 1, p["forcing_kmin"], p["forcing_kmax"], p["forcing_epsilon"],
+                         p["forcing_seed"], 0)
+        got = m.download(("omega_hat",))
+        ref = o.cplx("omega_hat")
+        err = float(np.linalg.norm(got["omega_hat"] - ref) / np.linalg.norm(ref))
+        assert err <= 1e-5, (n, err)
+        assert abs(got["t"] - o.d.t) <= 1e-6 * o.d.t, (n, got["t"], o.d.t)
+        o.close()
+    ens.close()
