@@ -54,7 +54,7 @@ def build_runner(force: bool = False) -> str:
     """The config-driven runner (driver/ns_run.c), linked against the library."""
     src = os.path.join(PKG, "driver", "ns_run.c")
     if force or _stale(RUNNER, [src, LIB] + glob.glob(os.path.join(INCLUDE, "*.h"))):
-        _run(["gcc"] + CFLAGS + [src, "-L", PKG, "-lns_gb300", "-Wl,-rpath,$ORIGIN", "-lm", "-o", RUNNER])
+        _run(["gcc"] + CFLAGS + [src, "-L", PKG, "-lns_gb300", "-Wl,-rpath,$ORIGIN", "-lpthread", "-lm", "-o", RUNNER])
     return RUNNER
 
 

@@ -22,12 +22,21 @@
  *   output.spectrum_every     energy spectrum file every N steps (0: off)
  *   output.checkpoint_every   checkpoint (.npz) every N steps (0: off)
  *   output.solution           1: write solution.dat at the end (default 1)
+ *   output.vtk_every          legacy VTK snapshot (u, v, omega) every N steps (0: off),
+ *                             in the layout of the reference's ns_vtk_write_spectral_legacy
+ *                             (src/output/vtk_writer.c:10-62, 212-227)
  *
- * The state stays on the device between outputs (ns_spectral_gpu_advance_n).
+ * The state stays on the device between outputs (ns_spectral_gpu_advance_n); t and
+ * dt are read from the device state, and the host arrays are brought up to date
+ * only where a file needs them (checkpoints, the final solution).  VTK snapshots
+ * are written asynchronously: u, v, omega of the device state are copied into one
+ * of two host buffer sets and a writer thread formats the file while the solver
+ * carries on (the next snapshot into the same set waits for that writer).
  * Diagnostics lines: "step <n> t <t> dt <dt> energy <E> enstrophy <Z>".
  * Exit status: 0 success, 2 configuration error, 3 solver failure.
  */
 #include <math.h>
+#include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -40,6 +49,66 @@
 static const char *k_prec[] = {"fp64", "fp32"};
 static const char *k_ic[] = {"taylor_green", "random"};
 static const char *k_forcing[] = {"none", "white", "colored"};
+
+/* one asynchronous VTK snapshot: host copies of the fields and the writer thread */
+typedef struct {
+    double *u, *v, *w;
+    const double *x, *y;
+    int nx, ny;
+    double t;
+    char path[1024];
+    pthread_t thread;
+    int busy;
+    int status;
+} vtk_job;
+
+/* legacy structured-grid VTK in the reference's layout: points (x, y, 0),
+ * FIELD TIME, VECTORS velocity (u, v, 0), SCALARS vorticity */
+static void *vtk_write(void *arg) {
+    vtk_job *j = (vtk_job *)arg;
+    j->status = -1;
+    FILE *fp = fopen(j->path, "w");
+    if (!fp) return NULL;
+    const int points = j->nx * j->ny;
+    fprintf(fp, "# vtk DataFile Version 3.0\n");
+    fprintf(fp, "Navier-Stokes Solution t=%.6f\n", j->t);
+    fprintf(fp, "ASCII\n");
+    fprintf(fp, "DATASET STRUCTURED_GRID\n");
+    fprintf(fp, "DIMENSIONS %d %d 1\n", j->nx, j->ny);
+    fprintf(fp, "POINTS %d double\n", points);
+    for (int y = 0; y < j->ny; ++y)
+        for (int x = 0; x < j->nx; ++x) fprintf(fp, "%.9f %.9f 0.0\n", j->x[x], j->y[y]);
+    fprintf(fp, "FIELD FieldData 1\n");
+    fprintf(fp, "TIME 1 1 double\n%.9f\n", j->t);
+    fprintf(fp, "POINT_DATA %d\n", points);
+    fprintf(fp, "VECTORS velocity double\n");
+    for (int i = 0; i < points; ++i) fprintf(fp, "%.9f %.9f 0.0\n", j->u[i], j->v[i]);
+    fprintf(fp, "SCALARS vorticity double 1\n");
+    fprintf(fp, "LOOKUP_TABLE default\n");
+    for (int i = 0; i < points; ++i) fprintf(fp, "%.9f\n", j->w[i]);
+    j->status = (fclose(fp) == 0) ? 0 : -1;
+    return NULL;
+}
+
+static int vtk_finish(vtk_job *j) {
+    if (!j->busy) return 0;
+    pthread_join(j->thread, NULL);
+    j->busy = 0;
+    return j->status;
+}
+
+/* copy u, v, omega of the device state into the job's buffers and start its writer */
+static int vtk_start(vtk_job *j, NSSpectralData *d, const char *dir, long step) {
+    if (vtk_finish(j) != 0) return -1;
+    double t = 0.0, dt = 0.0;
+    if (ns_gpu_download_state(ns_spectral_gpu_handle(d), NULL, NULL, NULL, NULL, NULL, j->u, j->v, j->w, &t, &dt) != 0)
+        return -1;
+    j->t = t;
+    snprintf(j->path, sizeof(j->path), "%s/solution_%06ld.vtk", dir, step);
+    if (pthread_create(&j->thread, NULL, vtk_write, j) != 0) return -1;
+    j->busy = 1;
+    return 0;
+}
 
 static int write_spectrum(NSSpectralData *d, const char *dir, long step) {
     const int nbins = d->nkx < d->nky / 2 ? d->nkx : d->nky / 2;
@@ -104,6 +173,7 @@ int main(int argc, char **argv) {
     const int every = ns_config_get_int(&cfg, "output.every", 100) > 0 ? ns_config_get_int(&cfg, "output.every", 100) : 100;
     const int spec_every = ns_config_get_int(&cfg, "output.spectrum_every", 0);
     const int ck_every = ns_config_get_int(&cfg, "output.checkpoint_every", 0);
+    const int vtk_every = ns_config_get_int(&cfg, "output.vtk_every", 0);
 
     NSSpectralData *d = ns_spectral_allocate_ex(nx, ny, Lx, Ly, Re, fp32 ? NS_PRECISION_FP32 : NS_PRECISION_FP64);
     if (!d) {
@@ -152,6 +222,28 @@ int main(int argc, char **argv) {
         }
     }
 
+    vtk_job vtk[2];
+    memset(vtk, 0, sizeof(vtk));
+    if (vtk_every > 0) {
+        const size_t nr = (size_t)nx * ny * sizeof(double);
+        for (int k = 0; k < 2; ++k) {
+            vtk[k].u = (double *)ns_gpu_host_alloc(nr);
+            vtk[k].v = (double *)ns_gpu_host_alloc(nr);
+            vtk[k].w = (double *)ns_gpu_host_alloc(nr);
+            vtk[k].x = d->x;
+            vtk[k].y = d->y;
+            vtk[k].nx = nx;
+            vtk[k].ny = ny;
+        }
+        if (!vtk[0].u || !vtk[0].v || !vtk[0].w || !vtk[1].u || !vtk[1].v || !vtk[1].w) {
+            fprintf(stderr, "ns_run: host buffers for VTK output\n");
+            ns_spectral_free(d);
+            ns_config_free(&cfg);
+            return 3;
+        }
+    }
+    long nvtk = 0;
+
     long step = 0;
     int status = 0;
     double E = 0.0, Z = 0.0;
@@ -165,12 +257,22 @@ int main(int argc, char **argv) {
         if (d->t + 1.5 * n * d->dt >= t_end) n = 1;
         if (spec_every > 0 && n > spec_every - step % spec_every) n = spec_every - step % spec_every;
         if (ck_every > 0 && n > ck_every - step % ck_every) n = ck_every - step % ck_every;
+        if (vtk_every > 0 && n > vtk_every - step % vtk_every) n = vtk_every - step % vtk_every;
         if (ns_spectral_gpu_advance_n(d, (int)n, cfl > 0.0) != SOLVER_SUCCESS) {
             status = 3;
             break;
         }
         step += n;
-        ns_spectral_gpu_sync_host(d);  /* t, dt and the host arrays */
+        {
+            /* t and dt of the device state (the host arrays stay stale until a file needs them) */
+            double tt = 0.0, dtt = 0.0, e0 = 0.0, z0 = 0.0;
+            if (ns_gpu_diagnostics(ns_spectral_gpu_handle(d), &e0, &z0, &tt, &dtt) != 0) {
+                status = 3;
+                break;
+            }
+            d->t = tt;
+            d->dt = dtt;
+        }
         if (step % every == 0 || d->t >= t_end || (max_steps > 0 && step >= max_steps)) {
             if (ns_spectral_gpu_diagnostics(d, &E, &Z) != SOLVER_SUCCESS || !isfinite(E)) {
                 status = 3;
@@ -184,6 +286,11 @@ int main(int argc, char **argv) {
             status = 3;
             break;
         }
+        if (vtk_every > 0 && step % vtk_every == 0 && vtk_start(&vtk[nvtk++ % 2], d, dir, step) != 0) {
+            fprintf(stderr, "ns_run: VTK output failed\n");
+            status = 3;
+            break;
+        }
         if (ck_every > 0 && step % ck_every == 0) {
             char path[1024];
             snprintf(path, sizeof(path), "%s/checkpoint_%06ld.npz", dir, step);
@@ -193,6 +300,15 @@ int main(int argc, char **argv) {
                 break;
             }
         }
+    }
+    for (int k = 0; k < 2; ++k) {
+        if (vtk_finish(&vtk[k]) != 0 && status == 0) {
+            fprintf(stderr, "ns_run: VTK output failed\n");
+            status = 3;
+        }
+        ns_gpu_host_free(vtk[k].u);
+        ns_gpu_host_free(vtk[k].v);
+        ns_gpu_host_free(vtk[k].w);
     }
     if (status == 0 && ns_config_get_bool(&cfg, "output.solution", 1)) {
         char path[1024];

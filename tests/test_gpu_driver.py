@@ -103,6 +103,45 @@ solution = 0
     assert not (tmp_path / "solution.dat").exists()
 
 
+def test_vtk_snapshots_written_asynchronously(nsgb, tmp_path):
+    """output.vtk_every: legacy VTK files (the reference's structured-grid layout)
+    of the device state, written by a writer thread while the solver continues;
+    the last one holds the same fields as the final solution.dat."""
+    ini = f"""[grid]
+nx = 32
+ny = 16
+[fluid]
+Re = 100.0
+[time]
+dt = 0.01
+t_end = 100.0
+steps = 50
+[output]
+dir = {tmp_path}
+every = 10
+vtk_every = 25
+"""
+    r = _run(tmp_path, ini)
+    assert r.returncode == 0, r.stderr
+    rows = _lines(r.stdout)
+    assert [int(x["step"]) for x in rows][-1] == 50
+    for step in (25, 50):
+        assert (tmp_path / f"solution_{step:06d}.vtk").exists()
+    lines = (tmp_path / "solution_000050.vtk").read_text().splitlines()
+    assert lines[0] == "# vtk DataFile Version 3.0" and lines[3] == "DATASET STRUCTURED_GRID"
+    assert lines[4] == "DIMENSIONS 32 16 1" and lines[5] == "POINTS 512 double"
+    n = 512
+    t_line = lines[6 + n + 2]
+    assert abs(float(t_line) - rows[-1]["t"]) < 1e-9
+    i_vec = lines.index("VECTORS velocity double")
+    uv = np.array([[float(a) for a in ln.split()[:2]] for ln in lines[i_vec + 1:i_vec + 1 + n]])
+    i_sc = lines.index("SCALARS vorticity double 1")
+    w = np.array([float(a) for a in lines[i_sc + 2:i_sc + 2 + n]])
+    sol = np.loadtxt(tmp_path / "solution.dat")  # x y u v omega psi at the end
+    assert np.abs(uv[:, 0] - sol[:, 2]).max() < 1e-8 and np.abs(uv[:, 1] - sol[:, 3]).max() < 1e-8
+    assert np.abs(w - sol[:, 4]).max() < 1e-8
+
+
 def test_configuration_errors(nsgb, tmp_path):
     r = _run(tmp_path, "[grid]\nnx = 32\n")  # grid.ny and fluid.Re are required
     assert r.returncode == 2 and "ny" in r.stderr
