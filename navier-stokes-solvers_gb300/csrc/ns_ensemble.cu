@@ -72,10 +72,14 @@ __device__ __forceinline__ void col_pass(const EnsMember& M, int r, int team) {
 // (its prologue and downloads, or a solo run with the same tiling) take at
 // most 256 threads per row block
 __host__ __device__ constexpr int ens_max_threads(int, int) { return 256; }
+// CTAs per SM the compiler budgets registers for: three for the radix-4 bodies
+// (at most 85 registers a thread; the members' small transforms are latency-bound,
+// so more resident warps pay), one for the radix-16 ones (16 values a thread)
+__host__ __device__ constexpr int ens_min_ctas(int er, int ec) { return (er == 4 && ec == 4) ? 3 : 1; }
 
 // work[w] = 2 * member + shared (1: the member is split over the CTA's cluster)
 template <int ER, int EC>
-__global__ void __launch_bounds__(ens_max_threads(ER, EC)) k_ensemble(const EnsMember* __restrict__ mem, const int* __restrict__ work,
+__global__ void __launch_bounds__(ens_max_threads(ER, EC), ens_min_ctas(ER, EC)) k_ensemble(const EnsMember* __restrict__ mem, const int* __restrict__ work,
                                                   const int* __restrict__ woff, int nsteps, int csize) {
     const int rank = csize > 1 ? (int)cluster_ctarank() : 0;
     for (int w = woff[blockIdx.x]; w < woff[blockIdx.x + 1]; ++w) {
