@@ -139,10 +139,11 @@ __global__ void __launch_bounds__(TP*(COUT / CPT)) k_conv3x3(const float* __rest
 // (B operand) stay in shared memory as [tap][chunk][64 co][8 ci].  One thread
 // issues the MMAs and commits them to an mbarrier.  Two accumulators (128
 // tensor-memory columns) let the MMAs of the next tile run while eight warps
-// drain the current one: warps w and w + 4 read lane quarter w % 4 of the
-// accumulator (pixels), columns 32 (w / 4) .. + 31 (output channels), with
+// drain the current one: warps w, w + 4, w + 8, w + 12 read lane quarter w % 4 of
+// the accumulator (pixels), columns 16 (w / 4) .. + 15 (output channels), with
 // tcgen05.ld, add the bias and stage the tile in shared memory, from where all
-// warps apply GELU and store the tile's outputs as contiguous, coalesced runs.
+// warps apply GELU and store the tile's outputs as contiguous, coalesced runs
+// (sixteen warps: w and w + 4, w + 8, w + 12 share lane quarter w % 4).
 // Every wait is bounded by a clock budget: on expiry the kernel records an
 // error, frees its tensor memory and returns.
 constexpr int TC_W = 128;                                  // pixels per tile
@@ -151,7 +152,7 @@ constexpr int TC_WB_BYTES = 9 * 8 * 64 * 16;               // 73,728
 constexpr int TC_HX_BYTES = 3 * 8 * TC_HP * 16;            // 49,920 per halo buffer
 constexpr int TC_ST = 65;                                  // staged output row pitch (floats)
 constexpr int TC_STG_BYTES = TC_W * TC_ST * 4;             // 33,280
-constexpr int TC_THREADS = 256;                            // eight warps: two per accumulator lane quarter
+constexpr int TC_THREADS = 512;                            // sixteen warps: four per accumulator lane quarter
 constexpr int TC_SMEM = TC_WB_BYTES + 2 * TC_HX_BYTES + TC_STG_BYTES + 64;  // + mbarriers and tmem address
 constexpr long long TC_WAIT_CYCLES = 4000000000LL;         // default wait limit: about 2 s
 
@@ -189,6 +190,20 @@ __device__ __forceinline__ bool mbar_wait(unsigned mbar, unsigned parity, long l
         if (done) return true;
         if (clock64() - t0 > limit) return false;
     }
+}
+
+// 16 consecutive accumulator columns of this thread's row
+__device__ __forceinline__ void tc_ld16(unsigned taddr, float (&v)[16]) {
+    unsigned r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, "
+        "[%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 // 32 consecutive accumulator columns of this thread's row
@@ -302,7 +317,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __nv_bfloat16* 
         if (tile < ntiles) tc_issue(taddr, hxb, wbs, mb0);
         if (tile + gstride < ntiles) tc_issue(taddr + 64u, hxb + TC_HX_BYTES, wbs, mb0 + 8u);
     }
-    const int q = warp & 3, h = warp >> 2;
+    const int q = warp & 3, h = warp >> 2;  // lane quarter q, accumulator columns 16 h .. 16 h + 15
     const bool bf16_only = !pre && !actf && actb;
     for (int it = 0; tile < ntiles; tile += gstride, ++it) {
         const int buf = it & 1;
@@ -319,14 +334,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __nv_bfloat16* 
         // this tile's MMAs are complete: its halo buffer takes the tile two iterations on
         const int t2 = tile + 2 * gstride;
         if (t2 < ntiles) tc_load_halo(in, hx, t2, H, W, ntx, tid);
-        // accumulator rows 32 q .. 32 q + 31 (pixels), columns 32 h .. 32 h + 31 (channels)
+        // accumulator rows 32 q .. 32 q + 31 (pixels), columns 16 h .. 16 h + 15 (channels)
         {
-            float v[32];
-            tc_ld32(taddr + ((unsigned)(32 * q) << 16) + (unsigned)(buf * 64 + h * 32), v);
+            float v[16];
+            tc_ld16(taddr + ((unsigned)(32 * q) << 16) + (unsigned)(buf * 64 + h * 16), v);
             const int prow = 32 * q + lane;
 #pragma unroll
-            for (int k = 0; k < 32; ++k) {
-                const int co = 32 * h + k;
+            for (int k = 0; k < 16; ++k) {
+                const int co = 16 * h + k;
                 stg[prow * TC_ST + co] = v[k] + sbias[co];
             }
         }
@@ -417,8 +432,22 @@ __global__ void __launch_bounds__(256) k_conv_in_tile(const float* __restrict__ 
     __shared__ __align__(16) float sw[9 * 2 * 64];  // [tap][ci][co]
     __shared__ float sb[64];
     __shared__ float2 sx[IN_HALO];
-    for (int i = threadIdx.x; i < 9 * 2 * 64; i += blockDim.x) sw[i] = __bfloat162float(w[i]);
-    if (threadIdx.x < 64) sb[threadIdx.x] = bias ? bias[threadIdx.x] : 0.0f;
+    {
+        // all of this thread's weight loads in flight before the stores (blockDim 256)
+        __nv_bfloat16 wv[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const int i = threadIdx.x + 256 * k;
+            wv[k] = (i < 9 * 2 * 64) ? w[i] : __float2bfloat16_rn(0.0f);
+        }
+        const float bv = (threadIdx.x < 64 && bias) ? bias[threadIdx.x] : 0.0f;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const int i = threadIdx.x + 256 * k;
+            if (i < 9 * 2 * 64) sw[i] = __bfloat162float(wv[k]);
+        }
+        if (threadIdx.x < 64) sb[threadIdx.x] = bv;
+    }
     const int g = threadIdx.x & 7, pl = threadIdx.x >> 3;
     const int ntx = W / IT_W, nty = H / IN_H, ntiles = B * nty * ntx;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {

@@ -171,15 +171,11 @@ static int dalloc(ns_gpu* g, void** p, size_t bytes);
 // sequence at stage 4.
 static int ensure_noise(ns_gpu* g) {
     g->fM = 0;
-    g->fnoise_kernel = 0;
     const StepParams sp = step_params<double>(g);
-    // The FP32 column pass at 2048 / 4096 (k_col_q) fills its columns' entries in
-    // its stage-4 prologue, overlapping the row pass.  The generic column pass
-    // takes a table from k_forcing_noise when a step sums several draws (coarse
-    // steps that receive fine-step forcing); one draw per step costs its stage-4
-    // kernel less than a kernel of its own costs the step.
-    const int colq = g->fast_col && g->prec == NS_GPU_FP32 && nsg_fast_col_q();
-    if (!sp.forcing || (sp.fsub <= 1 && !colq)) return NS_GPU_OK;
+    // one draw per step costs the stage-4 kernel less than a kernel of its own
+    // costs the step; several draws (coarse steps that sum fine-step forcing) go
+    // to the table
+    if (!sp.forcing || sp.fsub <= 1) return NS_GPU_OK;
     const double two_pi = 2.0 * 3.14159265358979323846;
     const int kxr = std::min((int)floor(sp.f_kmax * g->g.Lx / two_pi + 1e-9), g->g.Kx - 1);
     const int kyr = std::min((int)floor(sp.f_kmax * g->g.Ly / two_pi + 1e-9), g->g.Kyh);
@@ -195,7 +191,6 @@ static int ensure_noise(ns_gpu* g) {
     g->fkxr = kxr;
     g->fkyr = kyr;
     g->fM = sp.fsub;
-    g->fnoise_kernel = colq ? 0 : 1;
     return NS_GPU_OK;
 }
 
@@ -217,7 +212,7 @@ template <typename T> static int advance_t(ns_gpu* g, int nsteps) {
     }
     ColArgs<T> a = col_args<T>(g);
     for (int n = 0; n < nsteps; ++n) {
-        if (g->fM > 0 && g->fnoise_kernel) NSG_TRY(launch_noise(g));
+        if (g->fM > 0) NSG_TRY(launch_noise(g));
         NSG_TRY(stage_row<T>(g, 1));
         NSG_TRY((stage_col<T, 1>(g, a)));
         NSG_TRY(stage_row<T>(g, 2));

@@ -49,7 +49,6 @@ struct ns_gpu {
     double2* fnoise;        // this step's forcing draws (k_forcing_noise), [entries][draws]
     size_t fnoise_cap;      // entries x draws allocated
     int fkxr, fkyr, fM;     // table extent (kx index, |ky|) and draws per step; fM = 0: no table
-    int fnoise_kernel;      // the table is filled by k_forcing_noise (else by the k_col_q stage-4 prologue)
     int outside_active;
     int fields_valid;   // F holds the stage-1 fields of the current state
     int psi0_valid;     // PSI0 holds the caller's psi_hat for the next prologue

@@ -757,20 +757,6 @@ template <int NL> __device__ __forceinline__ int cq_mode(int t, int e) {
 // (build: j = TT n1 + t; stage algebra: j = cq_mode<NL>(t, e)).
 // dynamic smem: TW1 [16][TT] | per team: X [XL] (exchange, then WS | ACC), NS [Kyp]
 //               | per team SHV [Kyp] float | KYS [Kyp] float
-// The forcing-noise table entries of kept column i (kx index i <= fkxr): every
-// (ky, draw) pair of the shell box, one team thread each; the team's barriers
-// before the stage-4 post-step make them visible to the threads that add them.
-__device__ __forceinline__ void cq_column_noise(const Geo& g, const ColArgs<float>& a, int i, int t, int TT) {
-    if (i > a.fkxr || !a.sp.forcing) return;
-    const int M = a.sp.fsub, ne = (2 * a.fkyr + 1) * M;
-    double2* tab = const_cast<double2*>(a.fnoise) + (size_t)i * ne;
-    const unsigned long long base = a.ds->step_cur;
-    for (int q = t; q < ne; q += TT) {
-        const int e = q / M, s = q - e * M;
-        tab[q] = forcing_noise_term(i, e - a.fkyr, s, base, a.sp.f_seed, g.Lx, g.Ly, a.sp.f_kmin, a.sp.f_kmax);
-    }
-}
-
 template <int NL, int STAGE, bool IFRK>
 __global__ void __launch_bounds__(CQ<NL>::TT * CQ<NL>::NT, 1) k_col_q(Geo g, ColArgs<float> a) {
     typedef float T;
@@ -799,9 +785,6 @@ __global__ void __launch_bounds__(CQ<NL>::TT * CQ<NL>::NT, 1) k_col_q(Geo g, Col
             cp_async(&NS[jj], &a.W0[base + jj]);
             if (hv) cp_async(&SHV[jj], &a.hvw[base + jj]);
         }
-        // this step's forcing draws of the column's shell modes, while the row
-        // pass still runs: they depend only on the step counter (set at stage 1)
-        if (STAGE == 4 && a.fnoise) cq_column_noise(g, a, i, t, TT);
     }
     wait_previous_kernel();
     if (threadIdx.x == 0) {
@@ -840,7 +823,6 @@ __global__ void __launch_bounds__(CQ<NL>::TT * CQ<NL>::NT, 1) k_col_q(Geo g, Col
                 cp_async(&NS[jj], &a.W0[base + jj]);
                 if (hv) cp_async(&SHV[jj], &a.hvw[base + jj]);
             }
-            if (STAGE == 4 && a.fnoise) cq_column_noise(g, a, i, t, TT);
         }
         const T kx = __ldg(&a.kxv[i]);
         const size_t cbase = (size_t)i * Ky;
