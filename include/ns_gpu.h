@@ -92,6 +92,31 @@ enum { NS_GPU_RK4 = 0, NS_GPU_IFRK4 = 1 };
  * memory than one CTA has (odd nx above about 2700 in FP64).  precision is
  * NS_GPU_FP64 or NS_GPU_FP32. */
 int ns_gpu_create(int nx, int ny, double Lx, double Ly, int precision, ns_gpu **out);
+/* Tiling of an instance's stage kernels (no reference counterpart: the
+ * reference hands its transforms to FFTW plans, spectral_initialization.c:57-69).
+ * Zero fields are chosen by ns_gpu_create's own rule. */
+typedef struct {
+    int row_radix;         /* complex values per thread of a row transform: 4 or 16 */
+    int col_radix;         /* complex values per thread of a column transform: 4 or 16 */
+    int rows_per_cta;      /* rows per row-pass CTA: a power of two dividing ny */
+    int cols_per_cta;      /* kept columns per column-pass CTA: a power of two, at most 64 */
+    int row_field_groups;  /* 1: a thread group per field of a row (the fields' transforms run side
+                            * by side), -1: one group per row, 0: automatic */
+    int col_field_groups;  /* the same for the column pass (four groups per column block) */
+    int register_resident; /* output of ns_gpu_get_tiling: bit 0 (1) the row pass, bit 1 (2) the
+                            * column pass runs the register-resident 2048 / 4096 kernels */
+} ns_gpu_tiling;
+/* ns_gpu_create with a fixed tiling.  Setting row_radix or col_radix selects the
+ * generic stage kernels at every size (also at 2048 and 4096); the radix applies
+ * to power-of-two transform lengths (others run the mixed-radix bodies).
+ * NS_GPU_ERR_INVALID (reason on stderr) when the tiling cannot run: CTAs above
+ * 256 (row) / 512 (column) threads, field groups that are not whole warps,
+ * shared memory above the device's limit. */
+int ns_gpu_create_tiled(int nx, int ny, double Lx, double Ly, int precision, const ns_gpu_tiling *tiling,
+                        ns_gpu **out);
+/* The tiling an instance runs with (every field resolved; radix 0 = mixed radix;
+ * field groups 1 or -1). */
+int ns_gpu_get_tiling(const ns_gpu *g, ns_gpu_tiling *tiling);
 /* Per-instance teardown (spectral_memory.c:71-104 without the global fftw_cleanup). */
 void ns_gpu_destroy(ns_gpu *g);
 const char *ns_gpu_last_error(const ns_gpu *g);
@@ -165,7 +190,9 @@ int ns_gpu_taylor_green(ns_gpu *g, double *u, double *v, double *omega, double *
 int ns_gpu_upload_state(ns_gpu *g, const double *omega_hat, const double *psi_hat, const double *sfd_hat,
                         double t, double dt, uint64_t step0);
 /* Advance nsteps classical RK4 steps on the device (spectral_time_integration.c:34-106,
- * plus the forcing extension), with device-side CFL dt when adaptive. */
+ * plus the forcing extension), with device-side CFL dt when adaptive.  A step's
+ * launches are captured once as a CUDA graph and replayed until ns_gpu_set_params
+ * (or an outside-mode state) changes their arguments. */
 int ns_gpu_advance(ns_gpu *g, int nsteps);
 /* Copy the device state back in reference layouts; any pointer may be NULL.
  * psi_hat/u_hat/v_hat are recomputed from omega_hat as compute_derivatives does;

@@ -46,6 +46,11 @@ __device__ __forceinline__ float gelu_grad(float x) {
     return cdf + x * 0.39894228040143268f * expf(-0.5f * x * x);
 }
 __device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+// any row index onto [0, n) (tile halos that reach past a partial last row band)
+__device__ __forceinline__ int wrapm(int i, int n) {
+    const int r = i % n;
+    return r < 0 ? r + n : r;
+}
 // GELU in the tanh form of Hendrycks and Gimpel (2016),
 // 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))), with the hardware tanh
 // approximation (tanh.approx.f32, relative error about 2^-11): within 1.2e-3 of
@@ -152,7 +157,8 @@ constexpr int TC_WB_BYTES = 9 * 8 * 64 * 16;               // 73,728
 constexpr int TC_HX_BYTES = 3 * 8 * TC_HP * 16;            // 49,920 per halo buffer
 constexpr int TC_ST = 65;                                  // staged output row pitch (floats)
 constexpr int TC_STG_BYTES = TC_W * TC_ST * 4;             // 33,280
-constexpr int TC_THREADS = 512;                            // sixteen warps: four per accumulator lane quarter
+constexpr int TC_THREADS = 512;                            // sixteen epilogue warps: four per accumulator lane quarter
+constexpr int TC_BLOCK = TC_THREADS + 32;                  // + the MMA warp
 constexpr int TC_SMEM = TC_WB_BYTES + 2 * TC_HX_BYTES + TC_STG_BYTES + 64;  // + mbarriers and tmem address
 constexpr long long TC_WAIT_CYCLES = 4000000000LL;         // default wait limit: about 2 s
 
@@ -206,22 +212,6 @@ __device__ __forceinline__ void tc_ld16(unsigned taddr, float (&v)[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// 32 consecutive accumulator columns of this thread's row
-__device__ __forceinline__ void tc_ld32(unsigned taddr, float (&v)[32]) {
-    unsigned r[32];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
-
 // halo of tile `tile` into buffer at shared address hx (cp.async, 16-byte chunks)
 __device__ __forceinline__ void tc_load_halo(const __nv_bfloat16* __restrict__ in, unsigned hx, int tile, int H, int W,
                                              int ntx, int tid) {
@@ -238,298 +228,373 @@ __device__ __forceinline__ void tc_load_halo(const __nv_bfloat16* __restrict__ i
     asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
-// 36 MMAs of one tile from halo buffer hx into the accumulator, committed to mbar (one thread)
+// 36 MMAs of one tile from halo buffer hx into the accumulator, committed to mbar (one
+// thread).  Each descriptor is the buffer's base descriptor plus the operand's byte
+// offset / 16 in its start-address field (shared addresses stay below 2^18 bytes, so
+// the 14-bit field does not carry).
 __device__ __forceinline__ void tc_issue(unsigned taddr, unsigned hx, unsigned wbs, unsigned mb) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll 1
+    const unsigned long long a0 = umma_desc(hx, TC_HP * 16, 128), b0 = umma_desc(wbs, 64 * 16, 128);
+#pragma unroll
     for (int tap = 0; tap < 9; ++tap) {
         const int dy = tap / 3, dx = tap - 3 * dy;
 #pragma unroll
         for (int s = 0; s < 4; ++s) {
-            const unsigned a = hx + (unsigned)(((dy * 8 + 2 * s) * TC_HP + dx) * 16);
-            const unsigned bb = wbs + (unsigned)((tap * 8 + 2 * s) * 64 * 16);
-            tc_mma(taddr, umma_desc(a, TC_HP * 16, 128), umma_desc(bb, 64 * 16, 128), (tap | s) ? 1u : 0u);
+            const unsigned long long a = a0 + (unsigned long long)(((dy * 8 + 2 * s) * TC_HP + dx) * 16 / 16);
+            const unsigned long long bb = b0 + (unsigned long long)((tap * 8 + 2 * s) * 64 * 16 / 16);
+            tc_mma(taddr, a, bb, (tap | s) ? 1u : 0u);
         }
     }
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb) : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(unsigned mbar) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(mbar) : "memory");
+}
+// barrier 1 over the sixteen epilogue warps
+__device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, 512;" ::: "memory"); }
+// barrier 1 over the epilogue warps with the AND of p over their threads
+__device__ __forceinline__ bool epi_and(bool p) {
+    unsigned r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.and.pred q, 1, 512, p;\n\tselp.u32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(r)
+        : "r"((unsigned)p)
+        : "memory");
+    return r != 0;
+}
+
 // in: BF16 activations [B][H][W][64]; w: BF16 weights in the B-operand layout
 // [9 taps][8 ci / 8][64 co][8 ci % 8] (k_round_weights); bias may be null;
 // outputs (each may be null): pre FP32, actf FP32, actb BF16, all
-// [B][H][W][64].  Pipeline per CTA (tiles t = blockIdx.x, + gridDim.x, ...;
-// iteration i uses halo buffer, accumulator and mbarrier i % 2): the MMAs of
-// iteration i + 1 were issued before iteration i's epilogue starts; once
-// iteration i's MMAs are complete its halo buffer takes the halo of iteration
-// i + 2 (cp.async), and after the epilogue has drained accumulator i % 2 the
-// MMAs of iteration i + 2 go into it.
-// wait_cycles bounds each MMA-completion wait (clock64 cycles).  probe != 0 is
-// the self-test of that bound: no MMA is issued, so the first wait (on an
-// mbarrier nothing arrives on) runs out, the kernel records the expiry in err,
-// frees its tensor memory and returns with no tensor-core work in flight.
+// [B][H][W][64].  Warp-specialised pipeline per CTA (tiles t = blockIdx.x,
+// + gridDim.x, ...; iteration i uses accumulator and halo buffer i % 2):
+//  - the MMA warp (warp 16, one thread) issues iteration i's 36 MMAs once
+//    accumulator i % 2 is drained (mbarrier empty, sixteen warp arrivals) and halo
+//    i is in shared memory (mbarrier ready, sixteen warp arrivals), and commits them
+//    to mbarrier full[i % 2];
+//  - the sixteen epilogue warps wait for full[i % 2], start the cp.async of halo
+//    i + 2 into the buffer those MMAs have finished reading, drain the accumulator
+//    (tcgen05.ld, + bias) into the staging tile, release the accumulator, and store
+//    the staged tile (GELU) while the MMAs of iteration i + 1 run; once halo i + 2
+//    has landed they signal ready.
+// Every wait is bounded by wait_cycles (clock64 cycles).  The epilogue warps
+// leave the loop together (a barrier with the AND of their waits' outcomes); the
+// MMA warp leaves on its own expiry, which the epilogue warps then see as their
+// own.  probe != 0 is the self-test of that bound: no MMA is issued, so the first
+// wait (on an mbarrier nothing arrives on) runs out, the kernel records the expiry
+// in err, frees its tensor memory and returns with no tensor-core work in flight.
 template <bool GELU>
-__global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __nv_bfloat16* __restrict__ in,
-                                                           const __nv_bfloat16* __restrict__ w,
-                                                           const float* __restrict__ bias, float* __restrict__ pre,
-                                                           float* __restrict__ actf, __nv_bfloat16* __restrict__ actb,
-                                                           int B, int H, int W, int* __restrict__ err, long long wait_cycles,
-                                                           int probe) {
+__global__ void __launch_bounds__(TC_BLOCK, 1) k_conv_tc(const __nv_bfloat16* __restrict__ in,
+                                                         const __nv_bfloat16* __restrict__ w,
+                                                         const float* __restrict__ bias, float* __restrict__ pre,
+                                                         float* __restrict__ actf, __nv_bfloat16* __restrict__ actb,
+                                                         int B, int H, int W, int* __restrict__ err, long long wait_cycles,
+                                                         int probe) {
     extern __shared__ __align__(128) unsigned char tsm[];
     unsigned char* WB = tsm;                            // [9][8][64][8] bf16
     unsigned char* HXB = tsm + TC_WB_BYTES;             // 2 x [3][8][130][8] bf16
     float* stg = reinterpret_cast<float*>(tsm + TC_WB_BYTES + 2 * TC_HX_BYTES);  // [128][65] fp32
+    // full[2], empty[2], ready[2], then the tensor-memory address
     unsigned long long* mbar = reinterpret_cast<unsigned long long*>(tsm + TC_WB_BYTES + 2 * TC_HX_BYTES + TC_STG_BYTES);
-    unsigned* tslot = reinterpret_cast<unsigned*>(mbar + 2);
+    unsigned* tslot = reinterpret_cast<unsigned*>(mbar + 6);
+    __shared__ float sbias[64];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int ntx = W / TC_W;
     const int ntiles = B * H * ntx;
     const int gstride = gridDim.x;
+    const unsigned hxb = smem_u32(HXB), wbs = smem_u32(WB);
+    const unsigned mfull = smem_u32(mbar), mempty = smem_u32(mbar + 2), mready = smem_u32(mbar + 4);
 
-    // weights, already in the B-operand layout WB[tap][kc][co][j] = w[tap][8 kc + j][co]:
-    // cp.async (all 16-byte chunks in flight at once), completed with the first halos
-    for (int i = tid; i < TC_WB_BYTES / 16; i += TC_THREADS)
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(WB + 16 * i)),
-                     "l"(reinterpret_cast<const uint4*>(w) + i)
-                     : "memory");
-    asm volatile("cp.async.commit_group;" ::: "memory");
-    __shared__ float sbias[64];
     if (tid < 64) sbias[tid] = bias ? bias[tid] : 0.0f;
-    if (warp == 0) {
+    if (warp == 16) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(smem_u32(tslot)));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+        if (lane == 0) {
+            for (int k = 0; k < 2; ++k) {
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mfull + 8u * k));
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], 16;" ::"r"(mempty + 8u * k));
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], 16;" ::"r"(mready + 8u * k));
+            }
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
     }
-    if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar + 1)));
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    const unsigned hxb = smem_u32(HXB), wbs = smem_u32(WB), mb0 = smem_u32(mbar);
-    int tile = blockIdx.x;
-    if (tile < ntiles) tc_load_halo(in, hxb, tile, H, W, ntx, tid);
-    if (tile + gstride < ntiles) tc_load_halo(in, hxb + TC_HX_BYTES, tile + gstride, H, W, ntx, tid);
-    asm volatile("cp.async.wait_all;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic-proxy writes -> tensor-core reads
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
+    __syncthreads();  // barriers initialised, tensor memory allocated, bias staged
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const unsigned taddr = *tslot;
-    if (tid == 0 && !probe) {
-        if (tile < ntiles) tc_issue(taddr, hxb, wbs, mb0);
-        if (tile + gstride < ntiles) tc_issue(taddr + 64u, hxb + TC_HX_BYTES, wbs, mb0 + 8u);
-    }
-    const int q = warp & 3, h = warp >> 2;  // lane quarter q, accumulator columns 16 h .. 16 h + 15
-    const bool bf16_only = !pre && !actf && actb;
-    for (int it = 0; tile < ntiles; tile += gstride, ++it) {
-        const int buf = it & 1;
-        const unsigned mb = mb0 + 8u * (unsigned)buf;
-        const unsigned hx = hxb + (unsigned)(buf * TC_HX_BYTES);
-        // every thread must take the same branch (barriers follow): the tile
-        // succeeds only if every thread saw its MMAs complete in time
-        const bool ok = __syncthreads_and(mbar_wait(mb, (unsigned)((it >> 1) & 1), wait_cycles) ? 1 : 0) != 0;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        if (!ok) {
-            if (tid == 0) atomicExch(err, 1);
-            break;
-        }
-        // this tile's MMAs are complete: its halo buffer takes the tile two iterations on
-        const int t2 = tile + 2 * gstride;
-        if (t2 < ntiles) tc_load_halo(in, hx, t2, H, W, ntx, tid);
-        // accumulator rows 32 q .. 32 q + 31 (pixels), columns 16 h .. 16 h + 15 (channels)
-        {
-            float v[16];
-            tc_ld16(taddr + ((unsigned)(32 * q) << 16) + (unsigned)(buf * 64 + h * 16), v);
-            const int prow = 32 * q + lane;
-#pragma unroll
-            for (int k = 0; k < 16; ++k) {
-                const int co = 16 * h + k;
-                stg[prow * TC_ST + co] = v[k] + sbias[co];
+
+    if (warp == 16) {
+        // ------------------------------------------------------------ MMA warp
+        if (lane == 0 && !probe) {
+            int it = 0;
+            for (int tile = blockIdx.x; tile < ntiles; tile += gstride, ++it) {
+                const int a = it & 1;
+                if (it >= 2 && !mbar_wait(mempty + 8u * a, (unsigned)(((it - 2) >> 1) & 1), wait_cycles)) {
+                    atomicExch(err, 1);
+                    break;
+                }
+                if (!mbar_wait(mready + 8u * a, (unsigned)((it >> 1) & 1), wait_cycles)) {
+                    atomicExch(err, 1);
+                    break;
+                }
+                tc_issue(taddr + (unsigned)(a * 64), hxb + (unsigned)(a * TC_HX_BYTES), wbs, mfull + 8u * a);
             }
         }
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();  // staged; accumulator buf is drained
-        const int b = tile / (H * ntx), r = tile - b * H * ntx;
-        const int y = r / ntx, x0 = (r - y * ntx) * TC_W;
-        const size_t obase = (((size_t)b * H + y) * W + x0) * 64;  // the tile's 128 x 64 outputs are contiguous
-        if (bf16_only) {
-            for (int i = 2 * tid; i < TC_W * 64; i += 2 * TC_THREADS) {
-                const float* sp = stg + (i >> 6) * TC_ST + (i & 63);
-                const float a0 = GELU ? gelu_fast(sp[0]) : sp[0], a1 = GELU ? gelu_fast(sp[1]) : sp[1];
-                *reinterpret_cast<__nv_bfloat162*>(actb + obase + i) = __floats2bfloat162_rn(a0, a1);
-            }
-        } else {
-            for (int i = tid; i < TC_W * 64; i += TC_THREADS) {
-                const float pv = stg[(i >> 6) * TC_ST + (i & 63)];
-                const float av = GELU ? gelu(pv) : pv;
-                if (pre) pre[obase + i] = pv;
-                if (actf) actf[obase + i] = av;
-                if (actb) actb[obase + i] = __float2bfloat16_rn(av);
-            }
-        }
-        // the halo two iterations on must have landed before its MMAs start
+        __syncwarp();
+    } else {
+        // ------------------------------------------------------- epilogue warps
+        // weights (B-operand layout, all 16-byte chunks in flight at once) and the
+        // halos of iterations 0 and 1
+        for (int i = tid; i < TC_WB_BYTES / 16; i += TC_THREADS)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(WB + 16 * i)),
+                         "l"(reinterpret_cast<const uint4*>(w) + i)
+                         : "memory");
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        const int t0 = blockIdx.x;
+        if (t0 < ntiles) tc_load_halo(in, hxb, t0, H, W, ntx, tid);
+        if (t0 + gstride < ntiles) tc_load_halo(in, hxb + TC_HX_BYTES, t0 + gstride, H, W, ntx, tid);
         asm volatile("cp.async.wait_all;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();  // staging read done, that halo visible
-        if (tid == 0 && t2 < ntiles) tc_issue(taddr + (unsigned)(buf * 64), hx, wbs, mb);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic-proxy writes -> tensor-core reads
+        __syncwarp();
+        if (lane == 0) {
+            mbar_arrive(mready);
+            mbar_arrive(mready + 8u);
+        }
+        const int q = warp & 3, h = warp >> 2;  // lane quarter q, accumulator columns 16 h .. 16 h + 15
+        const bool bf16_only = !pre && !actf && actb;
+        int it = 0;
+        for (int tile = t0; tile < ntiles; tile += gstride, ++it) {
+            const int a = it & 1;
+            const unsigned hx = hxb + (unsigned)(a * TC_HX_BYTES);
+            // the epilogue warps leave together: the tile proceeds only if every
+            // thread saw its MMAs complete in time
+            if (!epi_and(mbar_wait(mfull + 8u * a, (unsigned)((it >> 1) & 1), wait_cycles))) {
+                if (tid == 0) atomicExch(err, 1);
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            // iteration it's MMAs are complete: its halo buffer takes the tile two iterations on
+            const int t2 = tile + 2 * gstride;
+            if (t2 < ntiles) tc_load_halo(in, hx, t2, H, W, ntx, tid);
+            // accumulator rows 32 q .. 32 q + 31 (pixels), columns 16 h .. 16 h + 15 (channels)
+            {
+                float v[16];
+                tc_ld16(taddr + ((unsigned)(32 * q) << 16) + (unsigned)(a * 64 + h * 16), v);
+                const int prow = 32 * q + lane;
+#pragma unroll
+                for (int k = 0; k < 16; ++k) {
+                    const int co = 16 * h + k;
+                    stg[prow * TC_ST + co] = v[k] + sbias[co];
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(mempty + 8u * a);  // this warp's part of the accumulator is drained
+            epi_sync();  // staged
+            const int b = tile / (H * ntx), r = tile - b * H * ntx;
+            const int y = r / ntx, x0 = (r - y * ntx) * TC_W;
+            const size_t obase = (((size_t)b * H + y) * W + x0) * 64;  // the tile's 128 x 64 outputs are contiguous
+            if (bf16_only) {
+                for (int i = 2 * tid; i < TC_W * 64; i += 2 * TC_THREADS) {
+                    const float* sp = stg + (i >> 6) * TC_ST + (i & 63);
+                    const float a0 = GELU ? gelu_fast(sp[0]) : sp[0], a1 = GELU ? gelu_fast(sp[1]) : sp[1];
+                    *reinterpret_cast<__nv_bfloat162*>(actb + obase + i) = __floats2bfloat162_rn(a0, a1);
+                }
+            } else {
+                for (int i = tid; i < TC_W * 64; i += TC_THREADS) {
+                    const float pv = stg[(i >> 6) * TC_ST + (i & 63)];
+                    const float av = GELU ? gelu(pv) : pv;
+                    if (pre) pre[obase + i] = pv;
+                    if (actf) actf[obase + i] = av;
+                    if (actb) actb[obase + i] = __float2bfloat16_rn(av);
+                }
+            }
+            if (t2 < ntiles) {  // halo it + 2 in shared memory: the MMA warp may issue it
+                asm volatile("cp.async.wait_all;" ::: "memory");
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(mready + 8u * a);
+            }
+            epi_sync();  // the staging tile is free for the next iteration
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
     }
-    asm volatile("cp.async.wait_all;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 0) {
+    if (warp == 16) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(taddr));
     }
 }
 
-// inference first layer (2 -> 64, GELU) straight to the BF16 activations that the
-// tensor-core layers read: lane l of a warp computes channels 2l and 2l + 1 of one
-// pixel in the arithmetic order of k_conv3x3<2, 64, 32, true> (bias, then taps,
-// then input channels), so each pixel's 64 outputs leave as one 128-byte store and
-// no FP32 activation or separate conversion pass is written
-__global__ void __launch_bounds__(256) k_conv_in_bf16(const float* __restrict__ in, const __nv_bfloat16* __restrict__ w,
-                                                      const float* __restrict__ bias, __nv_bfloat16* __restrict__ out, int B,
-                                                      int H, int W) {
-    __shared__ float sw[9 * 2 * 64];  // [tap][ci][co]
-    for (int i = threadIdx.x; i < 9 * 2 * 64; i += blockDim.x) sw[i] = __bfloat162float(w[i]);
-    __syncthreads();
-    const int co = 2 * (threadIdx.x & 31);
-    const float b0 = bias ? bias[co] : 0.0f, b1 = bias ? bias[co + 1] : 0.0f;
-    const long long npix = (long long)B * H * W, hw = (long long)H * W;
-    for (long long p = blockIdx.x * 8LL + (threadIdx.x >> 5); p < npix; p += gridDim.x * 8LL) {
-        const int b = (int)(p / hw), r = (int)(p - b * hw);
-        const int y = r / W, x = r - y * W;
-        float a0 = b0, a1 = b1;
-#pragma unroll
-        for (int tap = 0; tap < 9; ++tap) {
-            const int dy = tap / 3, dx = tap - 3 * dy;
-            const float* ip = in + (((size_t)b * H + wrapi(y + dy - 1, H)) * W + wrapi(x + dx - 1, W)) * 2;
-#pragma unroll
-            for (int ci = 0; ci < 2; ++ci) {
-                const float xv = ip[ci];
-                a0 = fmaf(xv, sw[(tap * 2 + ci) * 64 + co], a0);
-                a1 = fmaf(xv, sw[(tap * 2 + ci) * 64 + co + 1], a1);
-            }
-        }
-        __nv_bfloat162 o;
-        o.x = __float2bfloat16_rn(gelu_fast(a0));
-        o.y = __float2bfloat16_rn(gelu_fast(a1));
-        *reinterpret_cast<__nv_bfloat162*>(out + p * 64 + co) = o;
-    }
-}
-
 // ---------------------------------------------- tiled inference first / last layers
-// 8 x 32 pixel tiles (W % 32 == 0, H % 8 == 0) with the periodic halo (10 x 34
-// pixels) in shared memory; 256 threads per CTA.
-constexpr int IT_H = 8, IT_W = 32, IT_HALO = (IT_H + 2) * (IT_W + 2);
-constexpr int IN_H = 4, IN_HALO = (IN_H + 2) * (IT_W + 2);  // first layer: 4 x 32 tiles (more CTAs in flight)
+// Tiles of 32 pixels of one row band (W % 32 == 0; rows past H are skipped, so
+// any H works) with the periodic halo in shared memory.
+constexpr int IT_W = 32;
+constexpr int IN_H = 2, IN_HALO = (IN_H + 2) * (IT_W + 2);  // first layer: 2 x 32 tiles
+constexpr int IT_H = 8, IT_HALO = (IT_H + 2) * (IT_W + 2);  // output layer: 8 x 32 tiles
+constexpr int OT_THREADS = 352;                              // >= IT_HALO: one halo pixel per thread
 
-// first layer (2 -> 64, GELU) to the BF16 activations of the tensor-core layers,
-// over 4 x 32 tiles: thread = (pixel column, eight consecutive output channels), eight lanes write
-// one pixel's 128 bytes; the arithmetic order of k_conv_in_bf16 (bias, then taps,
-// then input channels), so the outputs are the same bits
-__global__ void __launch_bounds__(256) k_conv_in_tile(const float* __restrict__ in, const __nv_bfloat16* __restrict__ w,
-                                                      const float* __restrict__ bias, __nv_bfloat16* __restrict__ out,
-                                                      int B, int H, int W) {
-    __shared__ __align__(16) float sw[9 * 2 * 64];  // [tap][ci][co]
-    __shared__ float sb[64];
-    __shared__ float2 sx[IN_HALO];
-    {
-        // all of this thread's weight loads in flight before the stores (blockDim 256)
-        __nv_bfloat16 wv[5];
+// packed FP32 pairs (two lanes of one 64-bit register, element-wise IEEE fma)
+__device__ __forceinline__ unsigned long long pack2(float lo, float hi) {
+    return ((unsigned long long)__float_as_uint(hi) << 32) | __float_as_uint(lo);
+}
+__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b, unsigned long long c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ float lo2(unsigned long long v) { return __uint_as_float((unsigned)v); }
+__device__ __forceinline__ float hi2(unsigned long long v) { return __uint_as_float((unsigned)(v >> 32)); }
+
+// first layer (2 -> 64, GELU) to the BF16 activations of the tensor-core layers.
+// Thread (channel quad cq = tid % 16, pixel lane pl = tid / 16) computes output
+// channels 4 cq .. 4 cq + 3 of pixels pl and pl + 16 of each tile row and keeps
+// its 72 weights in registers as channel pairs; the halo holds each input value
+// twice, (x0, x0, x1, x1) per pixel, so one 16-byte load gives both operands of
+// the packed multiply-adds (fma.rn.f32x2: two IEEE fmas per instruction).  Each
+// output starts from the bias and adds the taps in order, input channel 0 then 1
+// (the order of k_conv3x3<2, 64, 32, true>).  The next tile's halo (one element
+// per thread) is loaded while the current one is computed.  Persistent:
+// grid-stride over tiles, 2 CTAs per SM.  With w0 set, the input pixels are
+// formed from two vorticity fields as k_make_input forms them, (w0 s0, (w1 - w0) s1),
+// instead of read from `in`.
+__global__ void __launch_bounds__(256, 2) k_conv_in_tile(const float* __restrict__ in, const __nv_bfloat16* __restrict__ w,
+                                                         const float* __restrict__ bias, __nv_bfloat16* __restrict__ out,
+                                                         int B, int H, int W, const float* __restrict__ w0,
+                                                         const float* __restrict__ w1, float s0, float s1) {
+    __shared__ __align__(16) ulonglong2 sx[IN_HALO];
+    const int cq = threadIdx.x & 15, pl = threadIdx.x >> 4;
+    unsigned long long wr[9][2][2];  // [tap][ci][channel pair]
 #pragma unroll
-        for (int k = 0; k < 5; ++k) {
-            const int i = threadIdx.x + 256 * k;
-            wv[k] = (i < 9 * 2 * 64) ? w[i] : __float2bfloat16_rn(0.0f);
-        }
-        const float bv = (threadIdx.x < 64 && bias) ? bias[threadIdx.x] : 0.0f;
+    for (int tap = 0; tap < 9; ++tap)
 #pragma unroll
-        for (int k = 0; k < 5; ++k) {
-            const int i = threadIdx.x + 256 * k;
-            if (i < 9 * 2 * 64) sw[i] = __bfloat162float(wv[k]);
+        for (int ci = 0; ci < 2; ++ci) {
+            const uint2 raw = *reinterpret_cast<const uint2*>(w + (tap * 2 + ci) * 64 + 4 * cq);
+            const float2 lo = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&raw.x));
+            const float2 hi = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&raw.y));
+            wr[tap][ci][0] = pack2(lo.x, lo.y);
+            wr[tap][ci][1] = pack2(hi.x, hi.y);
         }
-        if (threadIdx.x < 64) sb[threadIdx.x] = bv;
-    }
-    const int g = threadIdx.x & 7, pl = threadIdx.x >> 3;
-    const int ntx = W / IT_W, nty = H / IN_H, ntiles = B * nty * ntx;
+    unsigned long long bz[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+        bz[k] = bias ? pack2(bias[4 * cq + 2 * k], bias[4 * cq + 2 * k + 1]) : 0ULL;
+    const int ntx = W / IT_W, nty = (H + IN_H - 1) / IN_H, ntiles = B * nty * ntx;
+    auto halo = [&](int tile) -> ulonglong2 {
+        const int b = tile / (nty * ntx), r = tile - b * nty * ntx;
+        const int y0 = (r / ntx) * IN_H, x0 = (r % ntx) * IT_W;
+        const int hy = threadIdx.x / (IT_W + 2), hx = threadIdx.x - hy * (IT_W + 2);
+        const size_t p = ((size_t)b * H + wrapm(y0 + hy - 1, H)) * W + wrapi(x0 + hx - 1, W);
+        float2 v;
+        if (w0) {
+            const float a = w0[p], c = w1[p];
+            v = make_float2(a * s0, (c - a) * s1);
+        } else {
+            v = *reinterpret_cast<const float2*>(in + p * 2);
+        }
+        return make_ulonglong2(pack2(v.x, v.x), pack2(v.y, v.y));
+    };
+    ulonglong2 nxt = make_ulonglong2(0ULL, 0ULL);
+    if (blockIdx.x < ntiles && threadIdx.x < IN_HALO) nxt = halo(blockIdx.x);
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int b = tile / (nty * ntx), r = tile - b * nty * ntx;
         const int y0 = (r / ntx) * IN_H, x0 = (r % ntx) * IT_W;
-        __syncthreads();  // previous tile done with sx (and the weights written)
-        for (int i = threadIdx.x; i < IN_HALO; i += blockDim.x) {
-            const int hy = i / (IT_W + 2), hx = i - hy * (IT_W + 2);
-            sx[i] = *reinterpret_cast<const float2*>(in + (((size_t)b * H + wrapi(y0 + hy - 1, H)) * W + wrapi(x0 + hx - 1, W)) * 2);
-        }
+        __syncthreads();  // the previous tile is done with sx
+        if (threadIdx.x < IN_HALO) sx[threadIdx.x] = nxt;
         __syncthreads();
+        if (tile + gridDim.x < ntiles && threadIdx.x < IN_HALO) nxt = halo(tile + gridDim.x);
 #pragma unroll 1
         for (int py = 0; py < IN_H; ++py) {
-            float a[8];
+            if (y0 + py >= H) break;
+            unsigned long long a0[2] = {bz[0], bz[1]}, a1[2] = {bz[0], bz[1]};
 #pragma unroll
-            for (int k = 0; k < 8; ++k) a[k] = sb[8 * g + k];
-#pragma unroll 1
             for (int tap = 0; tap < 9; ++tap) {
                 const int dy = tap / 3, dx = tap - 3 * dy;
-                const float2 xv = sx[(py + dy) * (IT_W + 2) + pl + dx];
-                const float4* w4 = reinterpret_cast<const float4*>(sw + (tap * 2) * 64 + 8 * g);
-                const float4 wa = w4[0], wb = w4[1], wc = w4[16], wd = w4[17];  // ci 0: k 0-7; ci 1: k 0-7
-                const float w0[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
-                const float w1[8] = {wc.x, wc.y, wc.z, wc.w, wd.x, wd.y, wd.z, wd.w};
+                const ulonglong2 x0v = sx[(py + dy) * (IT_W + 2) + pl + dx];
+                const ulonglong2 x1v = sx[(py + dy) * (IT_W + 2) + pl + 16 + dx];
 #pragma unroll
-                for (int k = 0; k < 8; ++k) a[k] = fmaf(xv.x, w0[k], a[k]);
+                for (int k = 0; k < 2; ++k) {
+                    a0[k] = fma2(x0v.x, wr[tap][0][k], a0[k]);
+                    a1[k] = fma2(x1v.x, wr[tap][0][k], a1[k]);
+                }
 #pragma unroll
-                for (int k = 0; k < 8; ++k) a[k] = fmaf(xv.y, w1[k], a[k]);
+                for (int k = 0; k < 2; ++k) {
+                    a0[k] = fma2(x0v.y, wr[tap][1][k], a0[k]);
+                    a1[k] = fma2(x1v.y, wr[tap][1][k], a1[k]);
+                }
             }
-            uint4 pk;
-            unsigned* pw = reinterpret_cast<unsigned*>(&pk);
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                __nv_bfloat162 h2;
-                h2.x = __float2bfloat16_rn(gelu_fast(a[2 * k]));
-                h2.y = __float2bfloat16_rn(gelu_fast(a[2 * k + 1]));
-                pw[k] = *reinterpret_cast<unsigned*>(&h2);
-            }
-            *reinterpret_cast<uint4*>(out + (((size_t)b * H + y0 + py) * W + x0 + pl) * 64 + 8 * g) = pk;
+            __nv_bfloat16* o = out + (((size_t)b * H + y0 + py) * W + x0 + pl) * 64 + 4 * cq;
+            __nv_bfloat162 p0 = __floats2bfloat162_rn(gelu_fast(lo2(a0[0])), gelu_fast(hi2(a0[0])));
+            __nv_bfloat162 p1 = __floats2bfloat162_rn(gelu_fast(lo2(a0[1])), gelu_fast(hi2(a0[1])));
+            *reinterpret_cast<uint2*>(o) = make_uint2(*reinterpret_cast<unsigned*>(&p0), *reinterpret_cast<unsigned*>(&p1));
+            p0 = __floats2bfloat162_rn(gelu_fast(lo2(a1[0])), gelu_fast(hi2(a1[0])));
+            p1 = __floats2bfloat162_rn(gelu_fast(lo2(a1[1])), gelu_fast(hi2(a1[1])));
+            *reinterpret_cast<uint2*>(o + 16 * 64) =
+                make_uint2(*reinterpret_cast<unsigned*>(&p0), *reinterpret_cast<unsigned*>(&p1));
         }
+    }
+}
+
+__device__ __forceinline__ void act8(const float* p, float (&v)[8]) {
+    const float4 a = reinterpret_cast<const float4*>(p)[0], b = reinterpret_cast<const float4*>(p)[1];
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+__device__ __forceinline__ void act8(const __nv_bfloat16* p, float (&v)[8]) {
+    const uint4 raw = *reinterpret_cast<const uint4*>(p);
+    const unsigned u[4] = {raw.x, raw.y, raw.z, raw.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u[i]));
+        v[2 * i] = f.x;
+        v[2 * i + 1] = f.y;
     }
 }
 
 // output layer (64 -> 1, no activation): every pixel of the tile and its halo is
-// projected once onto the nine taps, P[p][t] = sum_ci act[p][ci] w[t][ci], and
-// out[p] = bias + sum_t P[p + offset(t)][t]; each activation is read once rather
-// than once per tap.  act FP32 [B][H][W][64], w [9][64][1], out [B][H][W].
-__global__ void __launch_bounds__(256) k_conv_out_tile(const float* __restrict__ act, const __nv_bfloat16* __restrict__ w,
-                                                       const float* __restrict__ bias, float* __restrict__ out, int B, int H,
-                                                       int W) {
+// projected once onto the nine taps, P[p][t] = sum_ci act[p][ci] w[t][ci] (one
+// halo pixel per thread), and out[p] = bias + sum_t P[p + offset(t)][t]; each
+// activation is read once rather than once per tap.  act [B][H][W][64] (FP32 or
+// the BF16 activations of the tensor-core path), w [9][64][1], out [B][H][W] times
+// scale (the output normalisation, applied as k_scale applies it).
+template <typename A>
+__global__ void __launch_bounds__(OT_THREADS) k_conv_out_tile(const A* __restrict__ act, const __nv_bfloat16* __restrict__ w,
+                                                              const float* __restrict__ bias, float* __restrict__ out, int B,
+                                                              int H, int W, float scale) {
     __shared__ __align__(16) float sw[9 * 64];  // [tap][ci]
     __shared__ float sp[IT_HALO * 9];
     for (int i = threadIdx.x; i < 9 * 64; i += blockDim.x) sw[i] = __bfloat162float(w[i]);
     const float b0 = bias ? bias[0] : 0.0f;
-    const int ntx = W / IT_W, nty = H / IT_H, ntiles = B * nty * ntx;
+    const int ntx = W / IT_W, nty = (H + IT_H - 1) / IT_H, ntiles = B * nty * ntx;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int b = tile / (nty * ntx), r = tile - b * nty * ntx;
         const int y0 = (r / ntx) * IT_H, x0 = (r % ntx) * IT_W;
         __syncthreads();  // previous tile done with sp (and the weights written)
         for (int i = threadIdx.x; i < IT_HALO; i += blockDim.x) {
             const int hy = i / (IT_W + 2), hx = i - hy * (IT_W + 2);
-            const float4* ap = reinterpret_cast<const float4*>(
-                act + (((size_t)b * H + wrapi(y0 + hy - 1, H)) * W + wrapi(x0 + hx - 1, W)) * 64);
+            const A* ap = act + (((size_t)b * H + wrapm(y0 + hy - 1, H)) * W + wrapi(x0 + hx - 1, W)) * 64;
             float acc[9];
 #pragma unroll
             for (int t = 0; t < 9; ++t) acc[t] = 0.0f;
 #pragma unroll 1
             for (int half = 0; half < 2; ++half) {
-                float4 xv[8];  // 32 of the pixel's activations, all loads in flight before the sums
+                float xv[4][8];  // 32 of the pixel's activations, all loads in flight before the sums
 #pragma unroll
-                for (int c = 0; c < 8; ++c) xv[c] = ap[8 * half + c];
+                for (int c = 0; c < 4; ++c) act8(ap + 32 * half + 8 * c, xv[c]);
 #pragma unroll
-                for (int c = 0; c < 8; ++c) {
-                    const float4 v = xv[c];
-                    const int c4 = 8 * half + c;
+                for (int c = 0; c < 4; ++c) {
 #pragma unroll
-                    for (int t = 0; t < 9; ++t) {
-                        const float4 wv = reinterpret_cast<const float4*>(sw)[t * 16 + c4];
-                        acc[t] = fmaf(v.x, wv.x, acc[t]);
-                        acc[t] = fmaf(v.y, wv.y, acc[t]);
-                        acc[t] = fmaf(v.z, wv.z, acc[t]);
-                        acc[t] = fmaf(v.w, wv.w, acc[t]);
+                    for (int e = 0; e < 2; ++e) {
+                        const int c4 = 8 * half + 2 * c + e;  // float4 index of these four channels
+#pragma unroll
+                        for (int t = 0; t < 9; ++t) {
+                            const float4 wv = reinterpret_cast<const float4*>(sw)[t * 16 + c4];
+                            acc[t] = fmaf(xv[c][4 * e + 0], wv.x, acc[t]);
+                            acc[t] = fmaf(xv[c][4 * e + 1], wv.y, acc[t]);
+                            acc[t] = fmaf(xv[c][4 * e + 2], wv.z, acc[t]);
+                            acc[t] = fmaf(xv[c][4 * e + 3], wv.w, acc[t]);
+                        }
                     }
                 }
             }
@@ -537,14 +602,17 @@ __global__ void __launch_bounds__(256) k_conv_out_tile(const float* __restrict__
             for (int t = 0; t < 9; ++t) sp[i * 9 + t] = acc[t];
         }
         __syncthreads();
-        const int py = threadIdx.x / IT_W, px = threadIdx.x - py * IT_W;
-        float o = b0;
+        for (int i = threadIdx.x; i < IT_H * IT_W; i += blockDim.x) {
+            const int py = i / IT_W, px = i - py * IT_W;
+            if (y0 + py >= H) break;
+            float o = b0;
 #pragma unroll
-        for (int t = 0; t < 9; ++t) {
-            const int dy = t / 3, dx = t - 3 * dy;
-            o += sp[((py + dy) * (IT_W + 2) + px + dx) * 9 + t];
+            for (int t = 0; t < 9; ++t) {
+                const int dy = t / 3, dx = t - 3 * dy;
+                o += sp[((py + dy) * (IT_W + 2) + px + dx) * 9 + t];
+            }
+            out[((size_t)b * H + y0 + py) * W + x0 + px] = (scale == 1.0f) ? o : o * scale;
         }
-        out[((size_t)b * H + y0 + py) * W + x0 + px] = o;
     }
 }
 
@@ -836,7 +904,7 @@ static int conv_tc(ns_cnn* c, cudaStream_t st, const __nv_bfloat16* in, const __
     auto k = k_conv_tc<GELU>;
     CNN_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
     const int tiles = B * c->H * (c->W / TC_W);
-    k<<<grid_of(tiles, 1, c->num_sms), TC_THREADS, TC_SMEM, st>>>(in, w, bias, pre, actf, actb, B, c->H, c->W, c->derr,
+    k<<<grid_of(tiles, 1, c->num_sms), TC_BLOCK, TC_SMEM, st>>>(in, w, bias, pre, actf, actb, B, c->H, c->W, c->derr,
                                                                   c->tc_wait_cycles, 0);
     CNN_LAUNCHED(c);
     return NS_GPU_OK;
@@ -846,23 +914,25 @@ static int conv_tc(ns_cnn* c, cudaStream_t st, const __nv_bfloat16* in, const __
 // With tensor cores the hidden 64 -> 64 layers run on tcgen05 from BF16
 // activations; `training` keeps every layer's FP32 pre-activation and
 // activation for the backward pass, otherwise only what the next layer reads.
-static int forward(ns_cnn* c, cudaStream_t st, int B, bool training = true) {
+static int forward(ns_cnn* c, cudaStream_t st, int B, bool training = true, float out_scale = 1.0f,
+                   const float* in_w0 = nullptr, const float* in_w1 = nullptr) {
     const float* x = c->x0;
-    const bool tiles32 = (c->W % IT_W == 0) && (c->H % IT_H == 0);
+    const bool tiles32 = (c->W % IT_W == 0);
     if (c->tc && !training) {
-        if (tiles32) {
-            const long long tiles = (long long)B * (c->H / IN_H) * (c->W / IT_W);
-            k_conv_in_tile<<<grid_of(tiles, 1, 8 * c->num_sms), 256, 0, st>>>(x, c->wb[0], c->p + c->boff[0], c->ab0, B,
-                                                                             c->H, c->W);
-        } else {
-            const long long npix = (long long)B * c->H * c->W;
-            k_conv_in_bf16<<<grid_of(npix, 8, 8 * c->num_sms), 256, 0, st>>>(x, c->wb[0], c->p + c->boff[0], c->ab0, B,
-                                                                              c->H, c->W);
-        }
+        // inference on tensor cores (W % 128 == 0): every hidden activation in BF16
+        const long long tiles = (long long)B * ((c->H + IN_H - 1) / IN_H) * (c->W / IT_W);
+        k_conv_in_tile<<<grid_of(tiles, 1, 2 * c->num_sms), 256, 0, st>>>(x, c->wb[0], c->p + c->boff[0], c->ab0, B, c->H,
+                                                                         c->W, in_w0, in_w1, c->s0, c->s1);
         CNN_LAUNCHED(c);
     } else {
+        if (in_w0) {
+            const long long n = (long long)B * c->H * c->W;
+            k_make_input<<<grid_of(n, 256, 1024), 256, 0, st>>>(in_w0, in_w1, n, c->s0, c->s1, c->x0);
+            CNN_LAUNCHED(c);
+        }
         CNN_TRY((conv<2, HID, 32, true>(c, st, x, c->wb[0], c->p + c->boff[0], c->pre[0], c->act[0], B)));
     }
+    __nv_bfloat16* alast = nullptr;  // BF16 input of the output layer (tensor-core inference)
     if (c->tc) {
         if (training) {
             const long long n = (long long)B * c->H * c->W * HID;
@@ -872,26 +942,36 @@ static int forward(ns_cnn* c, cudaStream_t st, int B, bool training = true) {
         __nv_bfloat16* ain = c->ab0;
         __nv_bfloat16* aout = c->ab1;
         for (int l = 1; l < NL - 1; ++l) {
-            const bool last = (l == NL - 2);
+            // training keeps FP32 copies for the backward pass; its output layer reads those
             CNN_TRY(conv_tc<true>(c, st, ain, c->wbB[l], c->p + c->boff[l], training ? c->pre[l] : nullptr,
-                                  (training || last) ? c->act[l] : nullptr, last ? nullptr : aout, B));
+                                  training ? c->act[l] : nullptr, (training && l == NL - 2) ? nullptr : aout, B));
             __nv_bfloat16* t = ain;
             ain = aout;
             aout = t;
         }
+        alast = ain;
     } else {
         for (int l = 1; l < NL - 1; ++l)
             CNN_TRY((conv<HID, HID, 32, true>(c, st, c->act[l - 1], c->wb[l], c->p + c->boff[l], c->pre[l], c->act[l], B)));
     }
     if (!training && tiles32) {  // inference: the projected output layer
-        const long long tiles = (long long)B * (c->H / IT_H) * (c->W / IT_W);
-        k_conv_out_tile<<<grid_of(tiles, 1, 8 * c->num_sms), 256, 0, st>>>(c->act[NL - 2], c->wb[NL - 1],
-                                                                          c->p + c->boff[NL - 1], c->pre[NL - 1], B, c->H,
-                                                                          c->W);
+        const long long tiles = (long long)B * ((c->H + IT_H - 1) / IT_H) * (c->W / IT_W);
+        const int grid = grid_of(tiles, 1, 8 * c->num_sms);
+        if (alast)
+            k_conv_out_tile<__nv_bfloat16><<<grid, OT_THREADS, 0, st>>>(alast, c->wb[NL - 1], c->p + c->boff[NL - 1],
+                                                                       c->pre[NL - 1], B, c->H, c->W, out_scale);
+        else
+            k_conv_out_tile<float><<<grid, OT_THREADS, 0, st>>>(c->act[NL - 2], c->wb[NL - 1], c->p + c->boff[NL - 1],
+                                                               c->pre[NL - 1], B, c->H, c->W, out_scale);
         CNN_LAUNCHED(c);
     } else {
         CNN_TRY((conv<HID, 1, 1, false>(c, st, c->act[NL - 2], c->wb[NL - 1], c->p + c->boff[NL - 1], c->pre[NL - 1],
                                         nullptr, B)));
+        if (out_scale != 1.0f) {
+            const long long n = (long long)B * c->H * c->W;
+            k_scale<<<grid_of(n, 256, 1024), 256, 0, st>>>(c->pre[NL - 1], n, out_scale);
+            CNN_LAUNCHED(c);
+        }
     }
     return NS_GPU_OK;
 }
@@ -1165,11 +1245,9 @@ int ns_cnn_forward_host(ns_cnn* c, const float* inputs, int B, float* out) {
         k_gather<<<grid_of((long long)B * hw, 256, 1024), 256, 0, st>>>(din, nullptr, c->didx, B, c->H, c->W, c->s0, c->s1,
                                                                          c->so, c->x0, nullptr);
         c->launches++;
-        s = forward(c, st, B, false);  // the inference path of correct_step
+        s = forward(c, st, B, false, 1.0f / c->so);  // the inference path of correct_step
     }
     if (s == NS_GPU_OK) {
-        k_scale<<<grid_of((long long)B * hw, 256, 1024), 256, 0, st>>>(c->pre[NL - 1], (long long)B * hw, 1.0f / c->so);
-        c->launches++;
         if (cudaMemcpyAsync(out, c->pre[NL - 1], (size_t)B * hw * sizeof(float), cudaMemcpyDeviceToHost, st) != cudaSuccess)
             s = NS_GPU_ERR_CUDA;
     }
@@ -1240,17 +1318,14 @@ int ns_cnn_train(ns_cnn* c, int iterations, int batch, float lr, float weight_de
 int ns_cnn_correct_step(ns_cnn* c, ns_gpu* g, int nsteps) {
     if (!c || !g || nsteps < 0) return NS_GPU_ERR_INVALID;
     if (g->g.nx != c->W || g->g.ny != c->H) CNN_FAIL(c, NS_GPU_ERR_INVALID, "correct_step: grid differs from the network's");
-    const long long hw = (long long)c->H * c->W;
     cudaStream_t st = g->st;
     for (int s = 0; s < nsteps; ++s) {
         CNN_TRY(ns_gpu_vorticity_device(g, c->cw0));
         CNN_TRY(ns_gpu_advance(g, 1));
         CNN_TRY(ns_gpu_vorticity_device(g, c->cw1));
-        k_make_input<<<grid_of(hw, 256, 1024), 256, 0, st>>>(c->cw0, c->cw1, hw, c->s0, c->s1, c->x0);
-        CNN_LAUNCHED(c);
-        CNN_TRY(forward(c, st, 1, false));
-        k_scale<<<grid_of(hw, 256, 1024), 256, 0, st>>>(c->pre[NL - 1], hw, 1.0f / c->so);
-        CNN_LAUNCHED(c);
+        // the network's input is formed from the two fields inside its first layer,
+        // its output leaves scaled by 1 / so
+        CNN_TRY(forward(c, st, 1, false, 1.0f / c->so, c->cw0, c->cw1));
         CNN_TRY(ns_gpu_add_vorticity_device(g, c->pre[NL - 1]));
     }
     CNN_CUDA(c, cudaStreamSynchronize(st));
@@ -1279,7 +1354,7 @@ int ns_cnn_probe_wait_timeout(ns_cnn* c, long long wait_cycles, int* timed_out) 
     auto k = k_conv_tc<true>;
     CNN_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
     const int tiles = c->H * (c->W / TC_W);
-    k<<<grid_of(tiles, 1, c->num_sms), TC_THREADS, TC_SMEM, st>>>(c->ab0, c->wbB[1], nullptr, nullptr, nullptr, nullptr, 1,
+    k<<<grid_of(tiles, 1, c->num_sms), TC_BLOCK, TC_SMEM, st>>>(c->ab0, c->wbB[1], nullptr, nullptr, nullptr, nullptr, 1,
                                                                   c->H, c->W, c->derr, wait_cycles, 1);
     CNN_LAUNCHED(c);
     int e = 0;

@@ -138,6 +138,7 @@ bool member_tiling(int n, const ns_gpu_ensemble_config& c, NsgTiling* t) {
     t->rpc = rpc;
     t->cw = cw;
     t->kxp_align = 64;
+    t->fpr = t->fpc = -1;
     return true;
 }
 
@@ -218,6 +219,7 @@ static int configure(ns_gpu_ensemble* e) {
         g->EC = t.ec;
         g->g.RPC = t.rpc;
         g->g.CW = t.cw;
+        g->g.fpr = g->g.fpc = 0;  // the persistent kernel runs one thread group per row / column block
         EnsMember& d = e->hmem[i];
         memset(&d, 0, sizeof(d));
         nsg_stage_args(g, &d.ra, &d.ca);

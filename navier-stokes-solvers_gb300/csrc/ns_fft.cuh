@@ -51,12 +51,20 @@ __device__ __forceinline__ int spad(int i) { return i + (i >> 4); }
 // padded shared-memory length of one transform of length L
 __host__ __device__ inline int spad_len(int L) { return L + (L >> 4) + 4; }
 
-// barrier between the passes of one transform: a warp barrier when every
-// transform of the CTA is owned by threads of a single warp (ws), else the CTA
-// barrier; ws must be the same for every thread of the CTA
-__device__ __forceinline__ void fft_sync(bool ws) {
-    if (ws) __syncwarp();
-    else __syncthreads();
+// barrier between the passes of one transform, by sync mode sy:
+//   0  the CTA barrier (every thread of the CTA runs the same passes);
+//   1  a warp barrier (every transform of the CTA is owned by threads of a single warp);
+//   (id << 16) | n  named barrier id (1..15) over n threads (a multiple of 32): the
+//      threads of one group of transforms, which run their passes independently of
+//      the CTA's other groups
+__device__ __forceinline__ void fft_sync(int sy) {
+    if (sy == 1) {
+        __syncwarp();
+    } else if (sy == 0) {
+        __syncthreads();
+    } else {
+        asm volatile("bar.sync %0, %1;" ::"r"(sy >> 16), "r"(sy & 0xffff) : "memory");
+    }
 }
 
 // ---------------------------------------------------------------- DFTs
@@ -181,12 +189,12 @@ __device__ __forceinline__ void pass_compute_store(C (&v)[E], C* sb, int L, int 
 template <int LOGE> struct ConstLog;
 
 // In-place FFT of the sequence at sb (padded, natural order in and out).
-// All threads of the CTA must call this (it synchronises); thread t < TT of
-// this transform, TT = L / E.  ws: every transform's threads lie in one warp
-// (the passes synchronise that warp only; the caller synchronises the CTA
-// before other threads read the result).
+// Every thread that the sync mode sy (fft_sync) names must call this; thread
+// t < TT of this transform, TT = L / E.  With sy != 0 the passes synchronise
+// only the warp or the group, and the caller synchronises the CTA before other
+// threads read the result.
 template <int E, bool INV, typename C>
-__device__ void fft_smem(C* sb, int L, int logL, int t, int TT, const C* __restrict__ tw, bool ws = false) {
+__device__ void fft_smem(C* sb, int L, int logL, int t, int TT, const C* __restrict__ tw, int ws = 0) {
     C v[E];
     const int logE = (E == 16) ? 4 : (E == 8) ? 3 : (E == 4) ? 2 : 1;
     int Ns = 1;
@@ -304,11 +312,11 @@ __device__ void mr_pass_direct(const C* src, C* dst, int L, int R, int Ns, int t
     }
 }
 
-// In-place (through sc) FFT of the sequence at sb; all threads of the CTA call
-// it (it synchronises), thread t < TT of this sequence.
+// In-place (through sc) FFT of the sequence at sb; every thread that the sync
+// mode ws names calls it (it synchronises), thread t < TT of this sequence.
 template <bool INV, typename C>
 __device__ void fft_smem_mr(C* sb, C* sc, int L, unsigned long long ra, unsigned long long rb, int np, int t, int TT,
-                            const C* __restrict__ tw, bool ws = false) {
+                            const C* __restrict__ tw, int ws = 0) {
     C* src = sb;
     C* dst = sc;
     int Ns = 1;

@@ -46,10 +46,11 @@ template <typename T> using Cx = typename CT<T>::C;
 template <typename T, int E, int MODE> static int row_launch_e(ns_gpu* g, const RowArgs<T>& a) {
     const int NF = RowNF<MODE>::v;
     const int TT = E ? g->g.H / E : g->g.TTr;
+    const int P = row_groups(g->g.fpr, E, NF);
     // E = 0 (mixed radix): one scratch sequence per row after the NF field buffers
     const size_t smem = (size_t)(NF + (E ? 0 : 1)) * g->g.RPC * spad_len(g->g.H) * sizeof(Cx<T>);
     NSG_TRY(set_smem(g, k_row<T, E, MODE>, smem));
-    k_row<T, E, MODE><<<g->g.ny / g->g.RPC, g->g.RPC * TT, smem, g->st>>>(g->g, a);
+    k_row<T, E, MODE><<<g->g.ny / g->g.RPC, g->g.RPC * P * TT, smem, g->st>>>(g->g, a);
     NSG_LAUNCHED(g);
     return NS_GPU_OK;
 }
@@ -60,9 +61,10 @@ template <typename T, int MODE> static int row_launch(ns_gpu* g, const RowArgs<T
 
 template <typename T, int E, int MODE, int STAGE> static int col_launch_e(ns_gpu* g, const ColArgs<T>& a) {
     const int TC = E ? g->g.ny / E : g->g.TTc;
-    const size_t smem = (size_t)(E ? 1 : 2) * g->g.CW * spad_len(g->g.ny) * sizeof(Cx<T>);
+    const int P = col_groups(g->g.fpc, E, MODE);
+    const size_t smem = (size_t)(E ? P : 2) * g->g.CW * spad_len(g->g.ny) * sizeof(Cx<T>);
     NSG_TRY(set_smem(g, k_col<T, E, MODE, STAGE>, smem));
-    k_col<T, E, MODE, STAGE><<<g->g.Kxp / g->g.CW, g->g.CW * TC, smem, g->st>>>(g->g, a);
+    k_col<T, E, MODE, STAGE><<<g->g.Kxp / g->g.CW, P * g->g.CW * TC, smem, g->st>>>(g->g, a);
     NSG_LAUNCHED(g);
     return NS_GPU_OK;
 }
@@ -203,6 +205,86 @@ static int launch_noise(ns_gpu* g) {
     return NS_GPU_OK;
 }
 
+// the kernels of one RK4 step on the instance stream
+template <typename T> static int one_step(ns_gpu* g, const ColArgs<T>& a) {
+    if (g->fM > 0) NSG_TRY(launch_noise(g));
+    NSG_TRY(stage_row<T>(g, 1));
+    NSG_TRY((stage_col<T, 1>(g, a)));
+    NSG_TRY(stage_row<T>(g, 2));
+    NSG_TRY((stage_col<T, 2>(g, a)));
+    NSG_TRY(stage_row<T>(g, 3));
+    NSG_TRY((stage_col<T, 3>(g, a)));
+    NSG_TRY(stage_row<T>(g, 4));
+    NSG_TRY((stage_col<T, 4>(g, a)));
+    if (g->outside_active) {
+        const long long nn = (long long)g->g.nkx * g->g.nky;
+        k_outside<<<grid_for(nn), 256, 0, g->st>>>(g->g, a.sp, g->hvw_full, g->hv_cutoff, g->hv_inv_bw,
+                                                   g->p.hv_order > 0 ? g->p.hv_order : 1, g->p.sfd_strength, g->ds,
+                                                   g->out, g->outsfd);
+        NSG_LAUNCHED(g);
+    }
+    return NS_GPU_OK;
+}
+
+// every value a step's launches take by value: a captured step stays valid while
+// these bytes are unchanged (the state itself lives in device memory)
+template <typename T> static std::vector<unsigned char> step_key(ns_gpu* g, const ColArgs<T>& a) {
+    const RowArgs<T> r = row_args<T>(g);
+    std::vector<unsigned char> k;
+    auto put = [&k](const void* p, size_t n) {
+        const unsigned char* c = static_cast<const unsigned char*>(p);
+        k.insert(k.end(), c, c + n);
+    };
+    put(&a, sizeof(a));
+    put(&r, sizeof(r));
+    put(&g->g, sizeof(g->g));
+    const int ints[] = {g->prec, g->ER, g->EC, g->fast_row, g->fast_col, g->outside_active, g->fM, g->fkxr, g->fkyr};
+    put(ints, sizeof(ints));
+    const double dbl[] = {g->hv_cutoff, g->hv_inv_bw, g->p.sfd_strength, (double)g->p.hv_order};
+    put(dbl, sizeof(dbl));
+    const void* ptrs[] = {g->fnoise, g->hvw_full, g->out, g->outsfd};
+    put(ptrs, sizeof(ptrs));
+    return k;
+}
+
+static void drop_step_graph(ns_gpu* g) {
+    if (g->step_exec) cudaGraphExecDestroy(g->step_exec);
+    g->step_exec = nullptr;
+    g->step_key.clear();
+}
+
+// Capture one step into g->step_exec (relaxed mode: the launch helpers set
+// kernel attributes); on any failure the instance keeps launching directly.
+template <typename T> static void capture_step(ns_gpu* g, const ColArgs<T>& a, std::vector<unsigned char>&& key) {
+    drop_step_graph(g);
+    if (cudaStreamBeginCapture(g->st, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+        cudaGetLastError();
+        g->step_graph_off = 1;
+        return;
+    }
+    const unsigned long long l0 = g->launches;
+    const int s = one_step<T>(g, a);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(g->st, &graph);
+    g->step_launches = g->launches - l0;
+    g->launches = l0;
+    cudaGraphExec_t exec = nullptr;
+    if (s != NS_GPU_OK || e != cudaSuccess || !graph || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
+        cudaGetLastError();
+        g->step_graph_off = 1;
+        g->err.clear();
+    } else {
+        g->step_exec = exec;
+        g->step_key = std::move(key);
+    }
+    if (graph) cudaGraphDestroy(graph);
+}
+
+// nsteps RK4 steps.  A step's launches are captured once as a CUDA graph and
+// replayed (small grids are launch-bound: a 128^2 step is nine kernels of a few
+// microseconds); the first step with new arguments runs directly, which also
+// sets the kernels' attributes before a capture.  Profiling runs (per-launch
+// events) launch directly.
 template <typename T> static int advance_t(ns_gpu* g, int nsteps) {
     NSG_TRY(ensure_noise(g));
     if (!g->fields_valid) {
@@ -211,24 +293,26 @@ template <typename T> static int advance_t(ns_gpu* g, int nsteps) {
         g->psi0_valid = 0;
     }
     ColArgs<T> a = col_args<T>(g);
-    for (int n = 0; n < nsteps; ++n) {
-        if (g->fM > 0) NSG_TRY(launch_noise(g));
-        NSG_TRY(stage_row<T>(g, 1));
-        NSG_TRY((stage_col<T, 1>(g, a)));
-        NSG_TRY(stage_row<T>(g, 2));
-        NSG_TRY((stage_col<T, 2>(g, a)));
-        NSG_TRY(stage_row<T>(g, 3));
-        NSG_TRY((stage_col<T, 3>(g, a)));
-        NSG_TRY(stage_row<T>(g, 4));
-        NSG_TRY((stage_col<T, 4>(g, a)));
-        if (g->outside_active) {
-            const long long nn = (long long)g->g.nkx * g->g.nky;
-            k_outside<<<grid_for(nn), 256, 0, g->st>>>(g->g, a.sp, g->hvw_full, g->hv_cutoff, g->hv_inv_bw,
-                                                       g->p.hv_order > 0 ? g->p.hv_order : 1, g->p.sfd_strength, g->ds,
-                                                       g->out, g->outsfd);
-            NSG_LAUNCHED(g);
+    if (nsteps > 0 && !g->prof && !g->step_graph_off) {
+        std::vector<unsigned char> key = step_key<T>(g, a);
+        if (!g->step_exec || key != g->step_key) {
+            if (key != g->step_key_seen) {  // new arguments: one direct step first
+                NSG_TRY(one_step<T>(g, a));
+                g->step_key_seen = key;
+                --nsteps;
+                if (nsteps == 0) return NS_GPU_OK;
+            }
+            capture_step<T>(g, a, std::move(key));
+        }
+        if (g->step_exec) {
+            for (int n = 0; n < nsteps; ++n) {
+                NSG_CUDA(g, cudaGraphLaunch(g->step_exec, g->st));
+                g->launches += g->step_launches;
+            }
+            return NS_GPU_OK;
         }
     }
+    for (int n = 0; n < nsteps; ++n) NSG_TRY(one_step<T>(g, a));
     return NS_GPU_OK;
 }
 
@@ -390,6 +474,7 @@ const char* ns_gpu_last_error(const ns_gpu* g) { return g ? g->err.c_str() : "nu
 void ns_gpu_destroy(ns_gpu* g) {
     if (!g) return;
     if (g->st) cudaStreamSynchronize(g->st);
+    drop_step_graph(g);
     void* bufs[] = {g->F[0], g->F[1], g->F[2], g->F[3], g->G, g->W0, g->WS, g->ACC, g->PSI0, g->SFD, g->KS,
                     g->KP, g->hvw, g->sfdw, g->kxv, g->kyv, g->twc, g->twr, g->twh, g->hvw_full, g->ds, g->part,
                     g->dres, g->dflag, g->out, g->outsfd, g->scratch, g->flushbuf};
@@ -454,6 +539,9 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
     g->flushbuf = nullptr;
     g->flush_bytes = 0;
     g->prof = nullptr;
+    g->step_exec = nullptr;
+    g->step_launches = 0;
+    g->step_graph_off = 0;
     g->launches = 0;
     g->outside_active = 0;
     g->fields_valid = 0;
@@ -508,21 +596,30 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
     // column over the group's consecutive rows.
     G.fLB = (g->fast_row || g->fast_col) ? G.logny : 0;
     G.fTG = G.fLB ? 1 : 0;
-    // automatic tiling: 16 values per thread from 512-point transforms up (a
-    // row or column keeps at least 32 threads), 4 values per thread below, so
-    // that small grids still fill warps and spread over the SMs
+    // automatic tiling (timed on GB300 at 128^2 .. 1024^2, FP32 and FP64): rows
+    // with 4 values per thread up to 512-point row transforms (1024^2) and 16 from
+    // 1024 points; columns with 16 values per thread from 512 points, 4 below
     // (E = 0: the mixed-radix bodies, for lengths that are not powers of two)
     const int mr_row = oddx || !is_pow2(G.H), mr_col = !is_pow2(ny);
-    g->ER = mr_row ? 0 : (kc && kc->er) ? kc->er : (G.H >= 512 ? 16 : 4);
+    g->ER = mr_row ? 0 : (kc && kc->er) ? kc->er : (G.H >= 1024 ? 16 : 4);
     g->EC = mr_col ? 0 : (kc && kc->ec) ? kc->ec : (ny >= 512 ? 16 : 4);
     const size_t cs = (precision == NS_GPU_FP64) ? sizeof(double2) : sizeof(float2);
+    // fields in parallel (a thread group per field): automatic when the
+    // transforms are short (TT / TC of one or two warps) and too few to give
+    // the SMs more than a few warps each one after another
+    const int TTp = g->ER ? G.H / g->ER : 0, TCp = g->EC ? ny / g->EC : 0;
+    G.fpr = (kc && kc->fpr) ? (kc->fpr > 0) : (g->ER && TTp % 32 == 0 && TTp <= 64 && (long long)ny * TTp < 64LL * 32 * g->num_sms);
+    G.fpc = (kc && kc->fpc) ? (kc->fpc > 0) : (g->EC && TCp % 32 == 0 && TCp <= 64 && (long long)G.Kx * TCp < 64LL * 32 * g->num_sms);
     // column tile width: up to 16 columns, <= 512 threads, <= ~100 KB shared memory
     {
         const int TC = g->EC ? ny / g->EC : G.TTc;
-        const int nbuf = g->EC ? 1 : 2;
+        const int nbuf = g->EC ? (G.fpc ? 4 : 1) : 2;
+        const int P = G.fpc ? 4 : 1;
         int CW = 1;
-        while (CW < 16 && 2 * CW * TC <= 512 && (size_t)nbuf * 2 * CW * spad_len(ny) * cs <= 100 * 1024 && CW < G.Kx &&
-               G.Kx / (2 * CW) >= g->num_sms)
+        // with a group per field a column block is already four groups: widen it
+        // only while that still leaves two blocks per SM
+        while (CW < 16 && 2 * CW * TC * P <= 512 && (size_t)nbuf * 2 * CW * spad_len(ny) * cs <= 100 * 1024 && CW < G.Kx &&
+               G.Kx / (2 * CW) >= (G.fpc ? 2 : 1) * g->num_sms)
             CW *= 2;
         if (kc && kc->cw) CW = kc->cw;
         G.CW = CW;
@@ -530,16 +627,53 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
         if (kc && kc->kxp_align > al) al = kc->kxp_align;
         G.Kxp = ((G.Kx + al - 1) / al) * al;
     }
-    // rows per CTA: up to 128 threads, <= ~100 KB shared memory for four fields
+    // rows per CTA: up to 256 threads (128 for FP64 rows of one group), <= ~100 KB
+    // shared memory for four fields
     {
         const int TT = g->ER ? G.H / g->ER : G.TTr;
         const int nbuf = g->ER ? 4 : 5;  // four field buffers (+ the mixed-radix scratch)
+        const int P = G.fpr ? 4 : 1;
+        const int budget = (G.fpr || precision == NS_GPU_FP32) ? 256 : 128;
         int RPC = 1;
-        while (2 * RPC * TT <= 128 && 2 * RPC <= ny && ny % (2 * RPC) == 0 &&
-               (size_t)nbuf * 2 * RPC * spad_len(G.H) * cs <= 100 * 1024 && ny / (2 * RPC) >= g->num_sms)
+        while (2 * RPC * TT * P <= budget && 2 * RPC <= ny && ny % (2 * RPC) == 0 &&
+               (size_t)nbuf * 2 * RPC * spad_len(G.H) * cs <= 100 * 1024 && ny / (2 * RPC) >= g->num_sms &&
+               (TT == 32 || !G.fpr || 2 * RPC * P <= 15))
             RPC *= 2;
         if (kc && kc->rpc) RPC = kc->rpc;
         G.RPC = RPC;
+    }
+    // a group per field needs whole warps per group, at most 256 (row) / 512
+    // (column) threads per CTA, and at most 15 named barriers per CTA
+    if (G.fpr && !(g->ER && TTp % 32 == 0 && G.RPC * 4 * TTp <= 256 && (TTp == 32 || G.RPC * 4 <= 15))) {
+        fprintf(stderr, "ns_gpu_create: nx=%d ny=%d: the row pass cannot run a thread group per field with this tiling\n",
+                nx, ny);
+        cudaStreamDestroy(g->st);
+        delete g;
+        return NS_GPU_ERR_INVALID;
+    }
+    if (G.fpc && !(g->EC && (G.CW * TCp) % 32 == 0 && 4 * G.CW * TCp <= 512)) {
+        fprintf(stderr, "ns_gpu_create: nx=%d ny=%d: the column pass cannot run a thread group per field with this tiling\n",
+                nx, ny);
+        cudaStreamDestroy(g->st);
+        delete g;
+        return NS_GPU_ERR_INVALID;
+    }
+    {
+        // the resolved tiling: radix 4 or 16 (or the mixed-radix bodies), row blocks
+        // that cover ny exactly, CTAs within the stage kernels' launch bounds
+        const int TT = g->ER ? G.H / g->ER : G.TTr, TC = g->EC ? ny / g->EC : G.TTc;
+        const int rthr = G.RPC * (G.fpr ? 4 : 1) * TT, cthr = G.CW * (G.fpc ? 4 : 1) * TC;
+        const bool ok = (g->ER == 0 || g->ER == 4 || g->ER == 16) && (g->EC == 0 || g->EC == 4 || g->EC == 16) &&
+                        TT >= 1 && TC >= 1 && G.RPC >= 1 && ny % G.RPC == 0 && G.CW >= 1 && rthr <= 256 && cthr <= 512;
+        if (!ok) {
+            fprintf(stderr,
+                    "ns_gpu_create: nx=%d ny=%d: invalid stage tiling (row radix %d, column radix %d, %d rows and %d "
+                    "columns per CTA)\n",
+                    nx, ny, g->ER, g->EC, G.RPC, G.CW);
+            cudaStreamDestroy(g->st);
+            delete g;
+            return NS_GPU_ERR_INVALID;
+        }
     }
     // the stage kernels' shared memory must fit one CTA (odd nx near the upper
     // bound needs the full length-nx row in five buffers)
@@ -547,7 +681,7 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
         int optin = 0;
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, g->device);
         const size_t row_sm = (size_t)(g->ER ? 4 : 5) * G.RPC * spad_len(G.H) * cs;
-        const size_t col_sm = (size_t)(g->EC ? 1 : 2) * G.CW * spad_len(ny) * cs;
+        const size_t col_sm = (size_t)(g->EC ? (G.fpc ? 4 : 1) : 2) * G.CW * spad_len(ny) * cs;
         if (optin > 0 && (row_sm > (size_t)optin || col_sm > (size_t)optin)) {
             fprintf(stderr,
                     "ns_gpu_create: nx=%d ny=%d: the stage kernels need %zu / %zu bytes of shared memory per CTA, above "
@@ -616,6 +750,38 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
 
 int ns_gpu_create(int nx, int ny, double Lx, double Ly, int precision, ns_gpu** out) {
     return nsg_create(nx, ny, Lx, Ly, precision, nullptr, out);
+}
+
+int ns_gpu_create_tiled(int nx, int ny, double Lx, double Ly, int precision, const ns_gpu_tiling* t, ns_gpu** out) {
+    if (!t) return nsg_create(nx, ny, Lx, Ly, precision, nullptr, out);
+    if (out) *out = nullptr;
+    auto pow2_or_zero = [](int v) { return v == 0 || is_pow2(v); };
+    if (!(t->row_radix == 0 || t->row_radix == 4 || t->row_radix == 16) ||
+        !(t->col_radix == 0 || t->col_radix == 4 || t->col_radix == 16) || !pow2_or_zero(t->rows_per_cta) ||
+        !pow2_or_zero(t->cols_per_cta) || t->rows_per_cta < 0 || t->cols_per_cta < 0 || t->cols_per_cta > 64 ||
+        t->row_field_groups < -1 || t->row_field_groups > 1 || t->col_field_groups < -1 || t->col_field_groups > 1)
+        return NS_GPU_ERR_INVALID;
+    NsgTiling k;
+    memset(&k, 0, sizeof(k));
+    k.er = t->row_radix;
+    k.ec = t->col_radix;
+    k.rpc = t->rows_per_cta;
+    k.cw = t->cols_per_cta;
+    k.fpr = t->row_field_groups;
+    k.fpc = t->col_field_groups;
+    return nsg_create(nx, ny, Lx, Ly, precision, &k, out);
+}
+
+int ns_gpu_get_tiling(const ns_gpu* g, ns_gpu_tiling* t) {
+    if (!g || !t) return NS_GPU_ERR_INVALID;
+    t->row_radix = g->ER;
+    t->col_radix = g->EC;
+    t->rows_per_cta = g->g.RPC;
+    t->cols_per_cta = g->g.CW;
+    t->row_field_groups = g->g.fpr ? 1 : -1;
+    t->col_field_groups = g->g.fpc ? 1 : -1;
+    t->register_resident = (g->fast_row ? 1 : 0) | (g->fast_col ? 2 : 0);
+    return NS_GPU_OK;
 }
 
 int ns_gpu_dims(const ns_gpu* g, int* kx_kept, int* ky_kept) {

@@ -24,6 +24,13 @@ struct ns_gpu {
     int fast_col;       // radix-32 column kernel (ny = 2048)
     cudaStream_t st;
     cudaStream_t st2;              // copies that overlap the instance stream (ns_gpu_step_host)
+    // one RK4 step captured as a CUDA graph (advance): replayed while the kernel
+    // arguments it was captured with (key) still hold
+    cudaGraphExec_t step_exec;
+    std::vector<unsigned char> step_key;      // arguments of the captured step
+    std::vector<unsigned char> step_key_seen; // arguments of the last step launched directly
+    unsigned long long step_launches;         // kernels per captured step
+    int step_graph_off;                       // capture failed once: launch directly
     cudaEvent_t ev_a, ev_b;        // ordering between st and st2
     std::string err;
     unsigned long long launches;
@@ -152,6 +159,7 @@ struct NsgTiling {
     int er, ec;       // complex values per thread in the row / column transforms (4, 8 or 16)
     int rpc, cw;      // rows per row block, kept columns per column block
     int kxp_align;    // the padded kept-column count Kxp is a multiple of this
+    int fpr, fpc;     // fields in parallel in the row / column pass: 1 on, -1 off, 0 automatic
 };
 int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTiling* kc, ns_gpu** out);
 // Run the stage-1 field prologue of an instance if its fields are stale (FP32

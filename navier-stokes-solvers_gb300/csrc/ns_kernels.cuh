@@ -44,18 +44,30 @@ struct Geo {
     // (H = nx) with Hermitian-extended input instead of the half-length packing.
     unsigned long long rxa, rxb, rya, ryb;
     int nrx, nry, TTr, TTc, oddx;
+    // fields in parallel (power-of-two bodies only): the row pass gives each row
+    // one group of transform threads per field (fpr), the column pass gives each
+    // column block four groups, one per inverse-transformed field (fpc), so that
+    // a small grid's transforms run side by side instead of one after another
+    int fpr, fpc;
 };
 
 // one transform of a row or column buffer b: the power-of-two engine for E > 0,
-// the mixed-radix engine (through the scratch sequence sc) for E == 0
-// (the passes synchronise one warp when TT divides the warp size: then every
-// transform of the CTA lies inside a warp)
+// the mixed-radix engine (through the scratch sequence sc) for E == 0; sy is
+// the pass barrier (fft_sync)
 template <int E, bool INV, typename C>
 __device__ __forceinline__ void fft_any(C* b, C* sc, int L, int logL, unsigned long long ra, unsigned long long rb, int np,
-                                        int t, int TT, const C* __restrict__ tw) {
-    const bool ws = TT <= 32 && (32 % TT) == 0;
-    if constexpr (E == 0) fft_smem_mr<INV>(b, sc, L, ra, rb, np, t, TT, tw, ws);
-    else fft_smem<E, INV>(b, L, logL, t, TT, tw, ws);
+                                        int t, int TT, const C* __restrict__ tw, int sy) {
+    if constexpr (E == 0) fft_smem_mr<INV>(b, sc, L, ra, rb, np, t, TT, tw, sy);
+    else fft_smem<E, INV>(b, L, logL, t, TT, tw, sy);
+}
+
+// pass barrier of a transform of TT threads: one warp when TT divides the warp
+// size (every transform of the CTA then lies inside a warp), else named barrier
+// id over the group's n threads when the CTA runs groups independently (id > 0),
+// else the CTA
+__device__ __forceinline__ int sync_mode(int TT, int id, int n) {
+    if (TT <= 32 && (32 % TT) == 0) return 1;
+    return id > 0 ? ((id << 16) | n) : 0;
 }
 
 // element (row y, kept column c) of an F buffer / of the G buffer
@@ -224,6 +236,8 @@ __device__ __forceinline__ double warp_max(double v) {
 
 // =============================================================== row kernel
 enum { ROW_STAGE = 0, ROW_DUMP = 1, ROW_UVW = 2, ROW_INV1 = 3, ROW_FWD1 = 4 };
+// thread groups per row of the row pass (nf = fields inverse-transformed per row)
+__host__ __device__ inline int row_groups(int fpr, int E, int nf) { return (E > 0 && fpr && nf > 1) ? nf : 1; }
 
 template <typename T> struct RowArgs {
     typedef typename CT<T>::C C;
@@ -244,11 +258,15 @@ template <typename T> struct RowArgs {
 
 template <int MODE> struct RowNF { static const int v = (MODE == ROW_STAGE || MODE == ROW_DUMP) ? 4 : (MODE == ROW_UVW ? 3 : 1); };
 
-// grid = ny / RPC, block = RPC * TT with TT = H / E (E > 0) or g.TTr (E = 0),
-// dynamic smem = NF * RPC * spad_len(H) * sizeof(C), plus RPC * spad_len(H) *
-// sizeof(C) of mixed-radix scratch when E = 0
+// grid = ny / RPC, block = RPC * P * TT with TT = H / E (E > 0) or g.TTr (E = 0)
+// and P = row_groups(g.fpr, E, NF) thread groups per row, dynamic smem = NF * RPC *
+// spad_len(H) * sizeof(C), plus RPC * spad_len(H) * sizeof(C) of mixed-radix
+// scratch when E = 0
 // body of the row pass for row block bx (rows bx*RPC .. bx*RPC + RPC - 1); the
-// block must have exactly RPC * TT threads
+// block must have exactly RPC * P * TT threads.  With P > 1 (fields in parallel;
+// TT a multiple of 32, RPC * P <= 15 when TT > 32) group f of a row loads,
+// unpacks and inverse-transforms field f, the row's threads form the products
+// together, and group 0 makes the forward transform.
 template <typename T, int E, int MODE>
 __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, const int bx) {
     typedef typename CT<T>::C C;
@@ -256,7 +274,10 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
     C* sm = reinterpret_cast<C*>(smem_raw);
     constexpr int NF = RowNF<MODE>::v;
     const int H = g.H, TT = (E == 0) ? g.TTr : H / E, LP = spad_len(H);
-    const int r = threadIdx.x / TT, t = threadIdx.x - r * TT;
+    const int P = row_groups(g.fpr, E, NF), TQ = P * TT;
+    const int r = threadIdx.x / TQ, q = threadIdx.x - r * TQ;
+    const int fg = q / TT, t = q - fg * TT;
+    const int sy = sync_mode(TT, P > 1 ? 1 + r * P + fg : 0, TT);
     const int y = bx * g.RPC + r;
     const int nx = g.nx, Kx = g.Kx;
     C* scr = sm + (NF * g.RPC + r) * LP;  // mixed-radix scratch of this row (E = 0 only)
@@ -290,12 +311,13 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
             b[spad(m)] = z;
         }
         __syncthreads();
-        fft_any<E, false>(b, scr, H, g.logH, g.rxa, g.rxb, g.nrx, t, TT, a.twr);
+        fft_any<E, false>(b, scr, H, g.logH, g.rxa, g.rxb, g.nrx, t, TT, a.twr, sy);
     } else {
         // half spectra X_f[k], k < Kx (zero above); odd nx: the full Hermitian
         // spectrum X[k], X[nx - k] = conj X[k], of the length-nx transform
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
+            if (P > 1 && f != fg) continue;
             C* b = sm + (f * g.RPC + r) * LP;
             const C* src = a.F[f];
             for (int k = t; k < H; k += TT) {
@@ -322,6 +344,7 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
         // the imaginary parts of X[0] and the Nyquist bin (zero here) are ignored.
 #pragma unroll
         for (int f = 0; f < NF && !oddx; ++f) {
+            if (P > 1 && f != fg) continue;
             C* b = sm + (f * g.RPC + r) * LP;
             for (int k = t; 2 * k <= H; k += TT) {
                 if (k == 0) {
@@ -346,8 +369,11 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
         }
         if (!oddx) __syncthreads();
 #pragma unroll
-        for (int f = 0; f < NF; ++f)
-            fft_any<E, true>(sm + (f * g.RPC + r) * LP, scr, H, g.logH, g.rxa, g.rxb, g.nrx, t, TT, a.twr);
+        for (int f = 0; f < NF; ++f) {
+            if (P > 1 && f != fg) continue;
+            fft_any<E, true>(sm + (f * g.RPC + r) * LP, scr, H, g.logH, g.rxa, g.rxb, g.nrx, t, TT, a.twr, sy);
+        }
+        if (P > 1) __syncthreads();  // the loops below read every field of the row
 
         if constexpr (MODE == ROW_STAGE || MODE == ROW_DUMP) {
             C* b0 = sm + (0 * g.RPC + r) * LP;
@@ -357,7 +383,7 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
             T vmax2 = (T)0;
             if (oddx) {
                 // one grid point per element (the real parts of the length-nx inverse)
-                for (int m = t; m < H; m += TT) {
+                for (int m = q; m < H; m += TQ) {
                     const T p0 = b0[spad(m)].x, p1 = b1[spad(m)].x, p2 = b2[spad(m)].x, p3 = b3[spad(m)].x;
                     const T jv = p0 * p3 - p1 * p2;
                     if (a.cfl) vmax2 = fmax(vmax2, p0 * p0 + p1 * p1);
@@ -372,7 +398,7 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
                     b0[spad(m)] = cmake<C>(jv, 0.0);
                 }
             }
-            for (int m = oddx ? H : t; m < H; m += TT) {
+            for (int m = oddx ? H : q; m < H; m += TQ) {
                 const C z0 = b0[spad(m)], z1 = b1[spad(m)], z2 = b2[spad(m)], z3 = b3[spad(m)];
                 // z0 = psi_x, z1 = psi_y, z2 = omega_x, z3 = omega_y at points 2m (re) and 2m+1 (im)
                 const T je = z0.x * z3.x - z1.x * z2.x;
@@ -401,11 +427,12 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
                 }
             }
             __syncthreads();
-            fft_any<E, false>(b0, scr, H, g.logH, g.rxa, g.rxb, g.nrx, t, TT, a.twr);
+            if (P > 1 && fg != 0) return;  // group 0 transforms the product and stores it
+            fft_any<E, false>(b0, scr, H, g.logH, g.rxa, g.rxb, g.nrx, t, TT, a.twr, sy);
         } else {
             const C* b0 = sm + (0 * g.RPC + r) * LP;
             if (oddx) {
-                for (int m = t; m < H; m += TT) {
+                for (int m = q; m < H; m += TQ) {
                     const size_t o = (size_t)y * nx + m;
                     const T p0 = b0[spad(m)].x;
                     if constexpr (MODE == ROW_UVW) {
@@ -420,7 +447,7 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
                 }
                 return;
             }
-            for (int m = t; m < H; m += TT) {
+            for (int m = q; m < H; m += TQ) {
                 const size_t o = (size_t)y * nx + 2 * m;
                 const C z0 = b0[spad(m)];
                 if constexpr (MODE == ROW_UVW) {
@@ -470,6 +497,11 @@ __global__ void __launch_bounds__(256) k_row(Geo g, RowArgs<T> a) {
 
 // ============================================================ column kernel
 enum { COL_STAGE = 0, COL_PROLOGUE = 1, COL_INV1 = 2, COL_FWD_EXPORT = 3, COL_NL_EXPORT = 4 };
+// thread groups per column block of the column pass (the modes with several
+// inverse-transformed fields)
+__host__ __device__ inline int col_groups(int fpc, int E, int mode) {
+    return (E > 0 && fpc && (mode == COL_STAGE || mode == COL_PROLOGUE)) ? 4 : 1;
+}
 
 template <typename T> struct ColArgs {
     typedef typename CT<T>::C C;
@@ -671,22 +703,30 @@ __device__ __forceinline__ C post_step_mode(const Geo& g, const ColArgs<T>& a, i
     return wn;
 }
 
-// grid = Kxp / CW, block = CW * TC with TC = ny / E (E > 0) or g.TTc (E = 0),
-// dynamic smem = CW * spad_len(ny) * sizeof(C), twice that when E = 0 (the
+// grid = Kxp / CW, block = P * CW * TC with TC = ny / E (E > 0) or g.TTc (E = 0)
+// and P = col_groups(g.fpc, E, MODE) thread groups, dynamic smem = P * CW *
+// spad_len(ny) * sizeof(C), 2 * CW * spad_len(ny) * sizeof(C) when E = 0 (the
 // mixed-radix scratch)
 // body of the column pass for column block bx (kept columns bx*CW .. bx*CW + CW - 1);
-// the block must have exactly CW * TC threads
+// the block must have exactly P * CW * TC threads.  With P > 1 (fields in
+// parallel; CW * TC a multiple of 32) group 0 makes the forward transforms, the
+// block applies the stage together, and group f inverse-transforms and stores
+// the fields f, f + P, ... in its own buffers, synchronised by named barrier 1 + f.
 template <typename T, int E, int MODE, int STAGE>
 __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, const int bx) {
     typedef typename CT<T>::C C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* sm = reinterpret_cast<C*>(smem_raw);
     const int ny = g.ny, TC = (E == 0) ? g.TTc : ny / E, LP = spad_len(ny), CW = g.CW;
-    const int b = threadIdx.x / TC, t = threadIdx.x - b * TC;
+    const int P = col_groups(g.fpc, E, MODE), GT = CW * TC;
+    const int fg = threadIdx.x / GT, u = threadIdx.x - fg * GT;
+    const int b = u / TC, t = u - b * TC;
+    const int sy = sync_mode(TC, P > 1 ? 1 + fg : 0, GT);
     const int c0 = bx * CW;
     const int Kx = g.Kx, Ky = g.Ky;
     const int nthr = blockDim.x;
-    C* mybuf = sm + b * LP;
+    C* gbuf = sm + fg * CW * LP;  // this group's CW column buffers
+    C* mybuf = gbuf + b * LP;
     C* myscr = sm + (CW + b) * LP;  // mixed-radix scratch (E = 0 only)
     __shared__ double s_dt;
 
@@ -722,7 +762,7 @@ __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, cons
             sm[c * LP + spad(y)] = v;
         }
         __syncthreads();
-        fft_any<E, false>(mybuf, myscr, ny, g.logny, g.rya, g.ryb, g.nry, t, TC, a.twc);
+        if (fg == 0) fft_any<E, false>(mybuf, myscr, ny, g.logny, g.rya, g.ryb, g.nry, t, TC, a.twc, sy);
         __syncthreads();  // the loops below read every column of the block
 
         if constexpr (MODE == COL_FWD_EXPORT || MODE == COL_NL_EXPORT) {
@@ -783,8 +823,8 @@ __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, cons
     // inverse y-transforms of the next-stage fields
     const int nf = (MODE == COL_INV1) ? 1 : (MODE == COL_PROLOGUE ? a.nfields : 4);
     const C* src = (MODE == COL_STAGE) ? ((STAGE == 4) ? a.W0 : a.WS) : a.W0;
-    for (int f = 0; f < nf; ++f) {
-        for (int idx = threadIdx.x; idx < CW * ny; idx += nthr) {
+    for (int f = fg; f < nf; f += P) {
+        for (int idx = u; idx < CW * ny; idx += GT) {
             const int c = idx / ny, j = idx - c * ny, i = c0 + c;
             const int jk = kept_jj(g, j);
             C v = cmake<C>(0.0, 0.0);
@@ -800,18 +840,18 @@ __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, cons
                     v = field_value<T, C>(f, src[s], a.kxv[i], a.kyv[jk]);
                 }
             }
-            sm[c * LP + spad(j)] = v;
+            gbuf[c * LP + spad(j)] = v;
         }
-        __syncthreads();
-        fft_any<E, true>(mybuf, myscr, ny, g.logny, g.rya, g.ryb, g.nry, t, TC, a.twc);
-        __syncthreads();  // the store loop reads every column of the block
+        fft_sync(P > 1 ? ((1 + fg) << 16) | GT : 0);
+        fft_any<E, true>(mybuf, myscr, ny, g.logny, g.rya, g.ryb, g.nry, t, TC, a.twc, sy);
+        fft_sync(P > 1 ? ((1 + fg) << 16) | GT : 0);  // the store loop reads every column of the group
         C* dstF = a.F[f];
-        for (int idx = threadIdx.x; idx < ny * CW; idx += nthr) {
+        for (int idx = u; idx < ny * CW; idx += GT) {
             int y, c;
             if (g.fLB) { c = idx / ny; y = idx - c * ny; } else { y = idx / CW; c = idx - y * CW; }
-            dstF[fidx(g, y, c0 + c)] = sm[c * LP + spad(y)];
+            dstF[fidx(g, y, c0 + c)] = gbuf[c * LP + spad(y)];
         }
-        __syncthreads();
+        fft_sync(P > 1 ? ((1 + fg) << 16) | GT : 0);
     }
 }
 

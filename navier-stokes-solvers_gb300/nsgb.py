@@ -90,6 +90,17 @@ class EnsembleConfig(C.Structure):
         return (self.threads, self.row_radix, self.col_radix, self.cluster)
 
 
+class Tiling(C.Structure):
+    """ns_gpu_tiling (include/ns_gpu.h)."""
+
+    _fields_ = [("row_radix", C.c_int), ("col_radix", C.c_int), ("rows_per_cta", C.c_int),
+                ("cols_per_cta", C.c_int), ("row_field_groups", C.c_int), ("col_field_groups", C.c_int),
+                ("register_resident", C.c_int)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 FP64, FP32 = 0, 1
 _LIB = None
 
@@ -190,6 +201,9 @@ def load(build: bool = True) -> C.CDLL:
     proto("ns_cnn_probe_wait_timeout", C.c_int, vp, C.c_longlong, C.POINTER(C.c_int))
     ecp = C.POINTER(EnsembleConfig)
     proto("ns_gpu_create_for_ensemble", C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, ecp, C.POINTER(vp))
+    proto("ns_gpu_create_tiled", C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.POINTER(Tiling),
+          C.POINTER(vp))
+    proto("ns_gpu_get_tiling", C.c_int, vp, C.POINTER(Tiling))
     proto("ns_gpu_ensemble_create", C.c_int, C.c_int, C.POINTER(C.c_int), C.c_double, ecp, C.POINTER(vp))
     proto("ns_gpu_ensemble_destroy", None, vp)
     proto("ns_gpu_ensemble_member", vp, vp, C.c_int)
@@ -341,12 +355,15 @@ class Gpu:
     """Direct use of the C-ABI (include/ns_gpu.h) with a device-resident state."""
 
     def __init__(self, nx: int, ny: int, Lx: float = 2 * np.pi, Ly: float = 2 * np.pi, precision: int = FP32,
-                 ensemble_config: "EnsembleConfig | None" = None, handle=None):
+                 ensemble_config: "EnsembleConfig | None" = None, handle=None, tiling: "dict | None" = None):
         self.lib = load()
         self.owned = handle is None
         if handle is None:
             h = C.c_void_p()
-            if ensemble_config is None:
+            if tiling is not None:
+                t = Tiling(**tiling)
+                st = self.lib.ns_gpu_create_tiled(nx, ny, Lx, Ly, precision, C.byref(t), C.byref(h))
+            elif ensemble_config is None:
                 st = self.lib.ns_gpu_create(nx, ny, Lx, Ly, precision, C.byref(h))
             else:
                 st = self.lib.ns_gpu_create_for_ensemble(nx, ny, Lx, Ly, precision, C.byref(ensemble_config), C.byref(h))
@@ -447,6 +464,12 @@ class Gpu:
         a, b = C.c_int(), C.c_int()
         self.lib.ns_gpu_dims(self.h, C.byref(a), C.byref(b))
         return a.value, b.value
+
+    def tiling(self) -> dict:
+        """The stage kernels' resolved tiling (ns_gpu_get_tiling)."""
+        t = Tiling()
+        self.check(self.lib.ns_gpu_get_tiling(self.h, C.byref(t)), "get_tiling")
+        return t.as_dict()
 
 
 class Ensemble:

@@ -99,3 +99,25 @@ def test_invalid_sizes_rejected_before_any_device_call(nsgb):
     for nx, ny in [(64, 4), (8192, 64), (0, 64), (74, 64), (64, 37), (64, 246)]:
         assert lib.ns_gpu_create(nx, ny, 1.0, 1.0, 0, C.byref(h)) == 1  # NS_GPU_ERR_INVALID
     assert lib.ns_gpu_create(64, 64, 1.0, 1.0, 7, C.byref(h)) == 1
+
+
+def test_invalid_tilings_rejected_before_any_device_call(nsgb):
+    """ns_gpu_create_tiled checks the tiling's own fields before it looks for a
+    device: radix other than 4 / 16, blocks that are not powers of two, field
+    group switches outside -1..1."""
+    lib = nsgb.load()
+    h = C.c_void_p()
+    bad = [dict(row_radix=8), dict(col_radix=2), dict(rows_per_cta=3), dict(cols_per_cta=128),
+           dict(row_field_groups=2), dict(col_field_groups=-2), dict(rows_per_cta=-4)]
+    for kw in bad:
+        t = nsgb.Tiling(**kw)
+        assert lib.ns_gpu_create_tiled(256, 256, 1.0, 1.0, 1, C.byref(t), C.byref(h)) == 1, kw
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            return
+    except ImportError:
+        pass
+    t = nsgb.Tiling(row_radix=16, col_radix=4, rows_per_cta=1, cols_per_cta=2, row_field_groups=1, col_field_groups=1)
+    assert lib.ns_gpu_create_tiled(256, 256, 1.0, 1.0, 1, C.byref(t), C.byref(h)) == 2  # valid: no device here
