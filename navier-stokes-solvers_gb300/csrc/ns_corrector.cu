@@ -19,6 +19,8 @@
 //   weight grad   k_conv_dw<CIN, COUT>: per-thread 3 x CBI x CBO blocks
 //                 accumulated over the CTA's tiles, one atomic per weight
 //   optimiser     AdamW with bias correction
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -152,13 +154,19 @@ __global__ void __launch_bounds__(TP*(COUT / CPT)) k_conv3x3(const float* __rest
 // Every wait is bounded by a clock budget: on expiry the kernel records an
 // error, frees its tensor memory and returns.
 constexpr int TC_W = 128;                                  // pixels per tile
-constexpr int TC_HP = TC_W + 2;                            // halo pixels per row
+// halo pitch (pixels): slots 8 .. 135 hold the tile's 128 pixels (one TMA box per
+// row and 8-channel chunk, at a 128-byte aligned address), slots 7 and 136 its
+// periodic neighbours x0 - 1 and x0 + 128
+constexpr int TC_HP = 144;
+constexpr int TC_HX0 = 7;                                  // slot of pixel x0 - 1
 constexpr int TC_WB_BYTES = 9 * 8 * 64 * 16;               // 73,728
-constexpr int TC_HX_BYTES = 3 * 8 * TC_HP * 16;            // 49,920 per halo buffer
-constexpr int TC_ST = 65;                                  // staged output row pitch (floats)
+constexpr int TC_HX_BYTES = 3 * 8 * TC_HP * 16;            // 55,296 per halo buffer
+constexpr int TC_ST = 68;  // staged output row pitch (floats): 16-byte aligned rows, so a warp's 16-byte
+                           // stores of one channel quad (32 pixels) fill every bank group evenly
 constexpr int TC_STG_BYTES = TC_W * TC_ST * 4;             // 33,280
 constexpr int TC_THREADS = 512;                            // sixteen epilogue warps: four per accumulator lane quarter
-constexpr int TC_BLOCK = TC_THREADS + 32;                  // + the MMA warp
+constexpr int TC_BLOCK = TC_THREADS + 64;                  // + the MMA warp and the halo warp
+constexpr unsigned TC_BOX_BYTES = 8 * TC_W * 2;            // one TMA box: 8 channels x 128 pixels (BF16)
 constexpr int TC_SMEM = TC_WB_BYTES + 2 * TC_HX_BYTES + TC_STG_BYTES + 64;  // + mbarriers and tmem address
 constexpr long long TC_WAIT_CYCLES = 4000000000LL;         // default wait limit: about 2 s
 
@@ -212,20 +220,44 @@ __device__ __forceinline__ void tc_ld16(unsigned taddr, float (&v)[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// halo of tile `tile` into buffer at shared address hx (cp.async, 16-byte chunks)
-__device__ __forceinline__ void tc_load_halo(const __nv_bfloat16* __restrict__ in, unsigned hx, int tile, int H, int W,
-                                             int ntx, int tid) {
+// halo of tile `tile` into buffer hx by one warp, completing on mbarrier mb
+// (two arrivals and the TMA bytes): lane 0 issues 24 TMA boxes (3 rows x 8
+// channel chunks, 128 pixels each, on the tensor map of `in`: dims {64, W, rows},
+// box {8, 128, 1}) after arming the barrier with their bytes; the periodic
+// neighbours x0 - 1 and x0 + 128 (48 16-byte chunks) come by cp.async from the
+// warp, which fences them for the tensor cores and arrives once they landed.
+__device__ __forceinline__ void tc_halo_load(const CUtensorMap* tm, const __nv_bfloat16* __restrict__ in, unsigned hx,
+                                             int tile, int H, int W, int ntx, unsigned mb, int lane) {
     const int b = tile / (H * ntx), r = tile - b * H * ntx;
     const int y = r / ntx, x0 = (r - y * ntx) * TC_W;
-    for (int i = tid; i < 3 * TC_HP * 8; i += TC_THREADS) {
-        const int row = i / (TC_HP * 8), q = i - row * TC_HP * 8;
-        const int px = q >> 3, kc = q & 7;
-        const int gy = wrapi(y + row - 1, H), gx = wrapi(x0 + px - 1, W);
+    if (lane == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(24u * TC_BOX_BYTES) : "memory");
+#pragma unroll 1
+        for (int row = 0; row < 3; ++row) {
+            const int gy = b * H + wrapi(y + row - 1, H);
+#pragma unroll
+            for (int kc = 0; kc < 8; ++kc) {
+                const unsigned dst = hx + (unsigned)(((row * 8 + kc) * TC_HP + TC_HX0 + 1) * 16);
+                asm volatile(
+                    "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+                    "[%5];" ::"r"(dst),
+                    "l"(reinterpret_cast<unsigned long long>(tm)), "r"(8 * kc), "r"(x0), "r"(gy), "r"(mb)
+                    : "memory");
+            }
+        }
+    }
+    for (int i = lane; i < 48; i += 32) {
+        const int side = i / 24, rk = i - side * 24, row = rk >> 3, kc = rk & 7;
+        const int gx = wrapi(side ? x0 + TC_W : x0 - 1, W), gy = wrapi(y + row - 1, H);
         const __nv_bfloat16* src = in + (((size_t)b * H + gy) * W + gx) * 64 + kc * 8;
-        const unsigned dst = hx + (unsigned)(((row * 8 + kc) * TC_HP + px) * 16);
+        const unsigned dst = hx + (unsigned)(((row * 8 + kc) * TC_HP + (side ? TC_HX0 + 1 + TC_W : TC_HX0)) * 16);
         asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic-proxy writes -> tensor-core reads
+    __syncwarp();
+    if (lane == 0) asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(mb) : "memory");
 }
 
 // 36 MMAs of one tile from halo buffer hx into the accumulator, committed to mbar (one
@@ -240,7 +272,7 @@ __device__ __forceinline__ void tc_issue(unsigned taddr, unsigned hx, unsigned w
         const int dy = tap / 3, dx = tap - 3 * dy;
 #pragma unroll
         for (int s = 0; s < 4; ++s) {
-            const unsigned long long a = a0 + (unsigned long long)(((dy * 8 + 2 * s) * TC_HP + dx) * 16 / 16);
+            const unsigned long long a = a0 + (unsigned long long)(((dy * 8 + 2 * s) * TC_HP + TC_HX0 + dx) * 16 / 16);
             const unsigned long long bb = b0 + (unsigned long long)((tap * 8 + 2 * s) * 64 * 16 / 16);
             tc_mma(taddr, a, bb, (tap | s) ? 1u : 0u);
         }
@@ -264,49 +296,63 @@ __device__ __forceinline__ bool epi_and(bool p) {
     return r != 0;
 }
 
-// in: BF16 activations [B][H][W][64]; w: BF16 weights in the B-operand layout
-// [9 taps][8 ci / 8][64 co][8 ci % 8] (k_round_weights); bias may be null;
-// outputs (each may be null): pre FP32, actf FP32, actb BF16, all
-// [B][H][W][64].  Warp-specialised pipeline per CTA (tiles t = blockIdx.x,
-// + gridDim.x, ...; iteration i uses accumulator and halo buffer i % 2):
-//  - the MMA warp (warp 16, one thread) issues iteration i's 36 MMAs once
-//    accumulator i % 2 is drained (mbarrier empty, sixteen warp arrivals) and halo
-//    i is in shared memory (mbarrier ready, sixteen warp arrivals), and commits them
-//    to mbarrier full[i % 2];
-//  - the sixteen epilogue warps wait for full[i % 2], start the cp.async of halo
-//    i + 2 into the buffer those MMAs have finished reading, drain the accumulator
-//    (tcgen05.ld, + bias) into the staging tile, release the accumulator, and store
-//    the staged tile (GELU) while the MMAs of iteration i + 1 run; once halo i + 2
-//    has landed they signal ready.
+// in: BF16 activations [B][H][W][64] (tmap: its tensor map, dims {64, W, rows},
+// box {8, 128, 1}); w: BF16 weights in the B-operand layout [9 taps][8 ci / 8]
+// [64 co][8 ci % 8] (k_round_weights); bias may be null; outputs (each may be
+// null): pre FP32, actf FP32, actb BF16, all [B][H][W][64].  Warp-specialised
+// pipeline per CTA (tiles t = blockIdx.x, + gridDim.x, ...; iteration i uses
+// accumulator and halo buffer i % 2), synchronised by mbarriers:
+//  - the halo warp (warp 17) copies the weights (one bulk copy, wready) and loads
+//    halo i (TMA boxes and the two periodic neighbour columns) into buffer i % 2
+//    once the MMAs of iteration i - 2 have finished reading it (full), and signals
+//    ready;
+//  - the MMA warp (warp 16, one thread) issues iteration i's 36 MMAs once its
+//    halo is ready and accumulator i % 2 is drained (empty, sixteen warp
+//    arrivals; before the first, the weights), and commits them to full[i % 2];
+//  - the sixteen epilogue warps wait for full[i % 2], drain the accumulator
+//    (tcgen05.ld, + bias) into the staging tile, release the accumulator, and
+//    store the staged tile (GELU) while the MMAs of iteration i + 1 run.
 // Every wait is bounded by wait_cycles (clock64 cycles).  The epilogue warps
-// leave the loop together (a barrier with the AND of their waits' outcomes); the
-// MMA warp leaves on its own expiry, which the epilogue warps then see as their
-// own.  probe != 0 is the self-test of that bound: no MMA is issued, so the first
-// wait (on an mbarrier nothing arrives on) runs out, the kernel records the expiry
-// in err, frees its tensor memory and returns with no tensor-core work in flight.
+// leave the loop together (a barrier with the AND of their waits' outcomes); a
+// producer warp that gives up makes their next wait run out; the halo warp waits
+// (bounded) for its last copies before the CTA exits.  probe != 0 is the
+// self-test of that bound: no halo or MMA is issued, so the first wait (on an
+// mbarrier nothing arrives on) runs out, the kernel records the expiry in err,
+// frees its tensor memory and returns with no copy or tensor-core work in flight.
 template <bool GELU>
-__global__ void __launch_bounds__(TC_BLOCK, 1) k_conv_tc(const __nv_bfloat16* __restrict__ in,
+__global__ void __launch_bounds__(TC_BLOCK, 1) k_conv_tc(const __grid_constant__ CUtensorMap tmap,
+                                                         const __nv_bfloat16* __restrict__ in,
                                                          const __nv_bfloat16* __restrict__ w,
                                                          const float* __restrict__ bias, float* __restrict__ pre,
                                                          float* __restrict__ actf, __nv_bfloat16* __restrict__ actb,
                                                          int B, int H, int W, int* __restrict__ err, long long wait_cycles,
                                                          int probe) {
-    extern __shared__ __align__(128) unsigned char tsm[];
+    extern __shared__ __align__(1024) unsigned char tsm[];
     unsigned char* WB = tsm;                            // [9][8][64][8] bf16
-    unsigned char* HXB = tsm + TC_WB_BYTES;             // 2 x [3][8][130][8] bf16
-    float* stg = reinterpret_cast<float*>(tsm + TC_WB_BYTES + 2 * TC_HX_BYTES);  // [128][65] fp32
-    // full[2], empty[2], ready[2], then the tensor-memory address
+    unsigned char* HXB = tsm + TC_WB_BYTES;             // 2 x [3][8][TC_HP][8] bf16
+    float* stg = reinterpret_cast<float*>(tsm + TC_WB_BYTES + 2 * TC_HX_BYTES);  // [128][TC_ST] fp32
+    // full[2], empty[2], ready[2], wready, then the tensor-memory address
     unsigned long long* mbar = reinterpret_cast<unsigned long long*>(tsm + TC_WB_BYTES + 2 * TC_HX_BYTES + TC_STG_BYTES);
-    unsigned* tslot = reinterpret_cast<unsigned*>(mbar + 6);
-    __shared__ float sbias[64];
+    unsigned* tslot = reinterpret_cast<unsigned*>(mbar + 7);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int ntx = W / TC_W;
     const int ntiles = B * H * ntx;
     const int gstride = gridDim.x;
     const unsigned hxb = smem_u32(HXB), wbs = smem_u32(WB);
-    const unsigned mfull = smem_u32(mbar), mempty = smem_u32(mbar + 2), mready = smem_u32(mbar + 4);
+    const unsigned mfull = smem_u32(mbar), mempty = smem_u32(mbar + 2), mready = smem_u32(mbar + 4),
+                   mwready = smem_u32(mbar + 6);
 
-    if (tid < 64) sbias[tid] = bias ? bias[tid] : 0.0f;
+    // the next kernel of the stream may start its own prologue (programmatic
+    // dependent launch); it waits for this grid before it touches global memory
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    const int q = warp & 3, h = warp >> 2;  // epilogue: lane quarter q, accumulator columns 16 h .. 16 h + 15
+    // TMA boxes land at 128-byte aligned shared addresses: with a misaligned
+    // dynamic shared-memory base the kernel records an error and issues no copy
+    // (the run behaves as a probe)
+    if ((hxb & 127u) != 0) {
+        if (tid == 0) atomicExch(err, 2);
+        probe = 1;
+    }
     if (warp == 16) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(smem_u32(tslot)));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
@@ -314,59 +360,75 @@ __global__ void __launch_bounds__(TC_BLOCK, 1) k_conv_tc(const __nv_bfloat16* __
             for (int k = 0; k < 2; ++k) {
                 asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mfull + 8u * k));
                 asm volatile("mbarrier.init.shared::cta.b64 [%0], 16;" ::"r"(mempty + 8u * k));
-                asm volatile("mbarrier.init.shared::cta.b64 [%0], 16;" ::"r"(mready + 8u * k));
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], 2;" ::"r"(mready + 8u * k));
             }
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mwready));
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();  // barriers initialised, tensor memory allocated, bias staged
+    __syncthreads();  // barriers initialised, tensor memory allocated
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const unsigned taddr = *tslot;
+    // everything above touched only this CTA's own resources: from here on the
+    // previous kernel of the stream (programmatic dependent launch) has completed
+    asm volatile("griddepcontrol.wait;" ::: "memory");
 
-    if (warp == 16) {
+    if (warp == 17) {
+        // ----------------------------------------------------------- halo warp
+        if (!probe) {
+            // the weights (B-operand layout, 73,728 bytes) as one bulk copy
+            if (lane == 0) {
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mwready), "r"((unsigned)TC_WB_BYTES)
+                             : "memory");
+                asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(wbs),
+                             "l"(w), "r"((unsigned)TC_WB_BYTES), "r"(mwready)
+                             : "memory");
+            }
+            int j = 0;
+            for (int tile = blockIdx.x; tile < ntiles; tile += gstride, ++j) {
+                const int buf = j & 1;
+                // the warp leaves together (its lanes then meet at __syncwarp)
+                if (j >= 2 && !__all_sync(0xffffffffu, mbar_wait(mfull + 8u * buf, (unsigned)(((j - 2) >> 1) & 1), wait_cycles))) {
+                    if (lane == 0) atomicExch(err, 1);
+                    break;
+                }
+                tc_halo_load(&tmap, in, hxb + (unsigned)(buf * TC_HX_BYTES), tile, H, W, ntx, mready + 8u * buf, lane);
+            }
+            // the copies of the last halos and of the weights must have landed before the CTA exits
+            for (int k = (j > 2 ? j - 2 : 0); k < j; ++k) mbar_wait(mready + 8u * (k & 1), (unsigned)((k >> 1) & 1), wait_cycles);
+            mbar_wait(mwready, 0u, wait_cycles);
+        }
+        __syncwarp();
+    } else if (warp == 16) {
         // ------------------------------------------------------------ MMA warp
         if (lane == 0 && !probe) {
             int it = 0;
-            for (int tile = blockIdx.x; tile < ntiles; tile += gstride, ++it) {
+            bool ok = mbar_wait(mwready, 0u, wait_cycles);
+            for (int tile = blockIdx.x; ok && tile < ntiles; tile += gstride, ++it) {
                 const int a = it & 1;
                 if (it >= 2 && !mbar_wait(mempty + 8u * a, (unsigned)(((it - 2) >> 1) & 1), wait_cycles)) {
-                    atomicExch(err, 1);
+                    ok = false;
                     break;
                 }
                 if (!mbar_wait(mready + 8u * a, (unsigned)((it >> 1) & 1), wait_cycles)) {
-                    atomicExch(err, 1);
+                    ok = false;
                     break;
                 }
                 tc_issue(taddr + (unsigned)(a * 64), hxb + (unsigned)(a * TC_HX_BYTES), wbs, mfull + 8u * a);
             }
+            if (!ok) atomicExch(err, 1);
         }
         __syncwarp();
     } else {
         // ------------------------------------------------------- epilogue warps
-        // weights (B-operand layout, all 16-byte chunks in flight at once) and the
-        // halos of iterations 0 and 1
-        for (int i = tid; i < TC_WB_BYTES / 16; i += TC_THREADS)
-            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(WB + 16 * i)),
-                         "l"(reinterpret_cast<const uint4*>(w) + i)
-                         : "memory");
-        asm volatile("cp.async.commit_group;" ::: "memory");
-        const int t0 = blockIdx.x;
-        if (t0 < ntiles) tc_load_halo(in, hxb, t0, H, W, ntx, tid);
-        if (t0 + gstride < ntiles) tc_load_halo(in, hxb + TC_HX_BYTES, t0 + gstride, H, W, ntx, tid);
-        asm volatile("cp.async.wait_all;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic-proxy writes -> tensor-core reads
-        __syncwarp();
-        if (lane == 0) {
-            mbar_arrive(mready);
-            mbar_arrive(mready + 8u);
-        }
-        const int q = warp & 3, h = warp >> 2;  // lane quarter q, accumulator columns 16 h .. 16 h + 15
+        float bz[16];  // this thread's sixteen output channels' bias
+#pragma unroll
+        for (int k = 0; k < 16; ++k) bz[k] = bias ? bias[16 * h + k] : 0.0f;
         const bool bf16_only = !pre && !actf && actb;
         int it = 0;
-        for (int tile = t0; tile < ntiles; tile += gstride, ++it) {
+        for (int tile = blockIdx.x; tile < ntiles; tile += gstride, ++it) {
             const int a = it & 1;
-            const unsigned hx = hxb + (unsigned)(a * TC_HX_BYTES);
             // the epilogue warps leave together: the tile proceeds only if every
             // thread saw its MMAs complete in time
             if (!epi_and(mbar_wait(mfull + 8u * a, (unsigned)((it >> 1) & 1), wait_cycles))) {
@@ -374,19 +436,15 @@ __global__ void __launch_bounds__(TC_BLOCK, 1) k_conv_tc(const __nv_bfloat16* __
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            // iteration it's MMAs are complete: its halo buffer takes the tile two iterations on
-            const int t2 = tile + 2 * gstride;
-            if (t2 < ntiles) tc_load_halo(in, hx, t2, H, W, ntx, tid);
             // accumulator rows 32 q .. 32 q + 31 (pixels), columns 16 h .. 16 h + 15 (channels)
             {
                 float v[16];
                 tc_ld16(taddr + ((unsigned)(32 * q) << 16) + (unsigned)(a * 64 + h * 16), v);
-                const int prow = 32 * q + lane;
+                float4* srow = reinterpret_cast<float4*>(stg + (32 * q + lane) * TC_ST + 16 * h);
 #pragma unroll
-                for (int k = 0; k < 16; ++k) {
-                    const int co = 16 * h + k;
-                    stg[prow * TC_ST + co] = v[k] + sbias[co];
-                }
+                for (int k = 0; k < 4; ++k)
+                    srow[k] = make_float4(v[4 * k] + bz[4 * k], v[4 * k + 1] + bz[4 * k + 1], v[4 * k + 2] + bz[4 * k + 2],
+                                          v[4 * k + 3] + bz[4 * k + 3]);
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
@@ -395,30 +453,31 @@ __global__ void __launch_bounds__(TC_BLOCK, 1) k_conv_tc(const __nv_bfloat16* __
             const int b = tile / (H * ntx), r = tile - b * H * ntx;
             const int y = r / ntx, x0 = (r - y * ntx) * TC_W;
             const size_t obase = (((size_t)b * H + y) * W + x0) * 64;  // the tile's 128 x 64 outputs are contiguous
-            if (bf16_only) {
-                for (int i = 2 * tid; i < TC_W * 64; i += 2 * TC_THREADS) {
-                    const float* sp = stg + (i >> 6) * TC_ST + (i & 63);
-                    const float a0 = GELU ? gelu_fast(sp[0]) : sp[0], a1 = GELU ? gelu_fast(sp[1]) : sp[1];
-                    *reinterpret_cast<__nv_bfloat162*>(actb + obase + i) = __floats2bfloat162_rn(a0, a1);
+            // four channels of one pixel per item (pixel i / 16, channels 4 (i % 16) ..): a
+            // warp covers two pixels' 64 channels, contiguous in the output
+            for (int i = tid; i < TC_W * 16; i += TC_THREADS) {
+                const int px = i >> 4, cg = i & 15;
+                const float4 pv = *reinterpret_cast<const float4*>(stg + px * TC_ST + 4 * cg);
+                const size_t o = obase + (size_t)px * 64 + 4 * cg;
+                if (bf16_only) {
+                    const __nv_bfloat162 lo = __floats2bfloat162_rn(GELU ? gelu_fast(pv.x) : pv.x, GELU ? gelu_fast(pv.y) : pv.y);
+                    const __nv_bfloat162 hi = __floats2bfloat162_rn(GELU ? gelu_fast(pv.z) : pv.z, GELU ? gelu_fast(pv.w) : pv.w);
+                    *reinterpret_cast<uint2*>(actb + o) =
+                        make_uint2(*reinterpret_cast<const unsigned*>(&lo), *reinterpret_cast<const unsigned*>(&hi));
+                } else {
+                    const float4 av = GELU ? make_float4(gelu(pv.x), gelu(pv.y), gelu(pv.z), gelu(pv.w)) : pv;
+                    if (pre) *reinterpret_cast<float4*>(pre + o) = pv;
+                    if (actf) *reinterpret_cast<float4*>(actf + o) = av;
+                    if (actb) {
+                        const __nv_bfloat162 lo = __floats2bfloat162_rn(av.x, av.y);
+                        const __nv_bfloat162 hi = __floats2bfloat162_rn(av.z, av.w);
+                        *reinterpret_cast<uint2*>(actb + o) =
+                            make_uint2(*reinterpret_cast<const unsigned*>(&lo), *reinterpret_cast<const unsigned*>(&hi));
+                    }
                 }
-            } else {
-                for (int i = tid; i < TC_W * 64; i += TC_THREADS) {
-                    const float pv = stg[(i >> 6) * TC_ST + (i & 63)];
-                    const float av = GELU ? gelu(pv) : pv;
-                    if (pre) pre[obase + i] = pv;
-                    if (actf) actf[obase + i] = av;
-                    if (actb) actb[obase + i] = __float2bfloat16_rn(av);
-                }
-            }
-            if (t2 < ntiles) {  // halo it + 2 in shared memory: the MMA warp may issue it
-                asm volatile("cp.async.wait_all;" ::: "memory");
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                __syncwarp();
-                if (lane == 0) mbar_arrive(mready + 8u * a);
             }
             epi_sync();  // the staging tile is free for the next iteration
         }
-        asm volatile("cp.async.wait_all;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -840,6 +899,10 @@ struct ns_cnn {
     // have been running when the CTA freed its tensor memory and exited, so the
     // instance refuses further tensor-core launches until it is recreated
     int tc_broken = 0;
+    // TMA tensor maps of the tensor-core layers' inputs (ab0, ab1), by address
+    CUtensorMap tm[2];
+    const void* tm_ptr[2] = {nullptr, nullptr};
+    int tm_next = 0;
     unsigned long long launches = 0;
     std::string err;
 };
@@ -894,6 +957,40 @@ static int conv_dw(ns_cnn* c, cudaStream_t st, const float* in, const float* dpr
         if (_s != NS_GPU_OK) return _s; \
     } while (0)
 
+static int tc_tensor_map(ns_cnn* c, const __nv_bfloat16* in, CUtensorMap* out) {
+    for (int k = 0; k < 2; ++k)
+        if (c->tm_ptr[k] == in) {
+            *out = c->tm[k];
+            return NS_GPU_OK;
+        }
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult qr = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &qr) != cudaSuccess ||
+            qr != cudaDriverEntryPointSuccess || !fn)
+            CNN_FAIL(c, NS_GPU_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    // [rows][W][64] BF16 activations: dims {64 channels, W pixels, maxB H rows},
+    // boxes of 8 channels x 128 pixels x 1 row (16-byte inner extent)
+    const cuuint64_t dims[3] = {64, (cuuint64_t)c->W, (cuuint64_t)c->maxB * c->H};
+    const cuuint64_t strides[2] = {64 * sizeof(__nv_bfloat16), (cuuint64_t)c->W * 64 * sizeof(__nv_bfloat16)};
+    const cuuint32_t box[3] = {8, TC_W, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    CUtensorMap m;
+    const CUresult r = encode(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16*>(in), dims, strides, box, estr,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) CNN_FAIL(c, NS_GPU_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    const int k = c->tm_next;
+    c->tm_next ^= 1;
+    c->tm[k] = m;
+    c->tm_ptr[k] = in;
+    *out = m;
+    return NS_GPU_OK;
+}
+
 template <bool GELU>
 static int conv_tc(ns_cnn* c, cudaStream_t st, const __nv_bfloat16* in, const __nv_bfloat16* w, const float* bias, float* pre,
                    float* actf, __nv_bfloat16* actb, int B) {
@@ -901,11 +998,16 @@ static int conv_tc(ns_cnn* c, cudaStream_t st, const __nv_bfloat16* in, const __
         CNN_FAIL(c, NS_GPU_ERR_CUDA,
                  "tensor-core convolution refused: an earlier launch timed out waiting for its MMAs; destroy and "
                  "recreate the network");
+    if (in != c->ab0 && in != c->ab1) CNN_FAIL(c, NS_GPU_ERR_INVALID, "tensor-core input outside the activation buffers");
+    CUtensorMap tm;
+    CNN_TRY(tc_tensor_map(c, in, &tm));
     auto k = k_conv_tc<GELU>;
     CNN_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
     const int tiles = B * c->H * (c->W / TC_W);
-    k<<<grid_of(tiles, 1, c->num_sms), TC_BLOCK, TC_SMEM, st>>>(in, w, bias, pre, actf, actb, B, c->H, c->W, c->derr,
-                                                                  c->tc_wait_cycles, 0);
+    // programmatic dependent launch: the CTAs start (tensor memory, barriers) while
+    // the previous kernel drains, and wait for it before they read or write
+    CNN_CUDA(c, launch_stage(k, grid_of(tiles, 1, c->num_sms), TC_BLOCK, (size_t)TC_SMEM, st, tm, in, w, bias, pre, actf,
+                             actb, B, c->H, c->W, c->derr, c->tc_wait_cycles, 0));
     CNN_LAUNCHED(c);
     return NS_GPU_OK;
 }
@@ -1351,10 +1453,12 @@ int ns_cnn_probe_wait_timeout(ns_cnn* c, long long wait_cycles, int* timed_out) 
     if (c->tc_broken) CNN_FAIL(c, NS_GPU_ERR_CUDA, "the network must be recreated after a tensor-core timeout");
     cudaStream_t st = c->st;
     CNN_CUDA(c, cudaMemsetAsync(c->derr, 0, sizeof(int), st));
+    CUtensorMap tm;
+    CNN_TRY(tc_tensor_map(c, c->ab0, &tm));
     auto k = k_conv_tc<true>;
     CNN_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
     const int tiles = c->H * (c->W / TC_W);
-    k<<<grid_of(tiles, 1, c->num_sms), TC_BLOCK, TC_SMEM, st>>>(c->ab0, c->wbB[1], nullptr, nullptr, nullptr, nullptr, 1,
+    k<<<grid_of(tiles, 1, c->num_sms), TC_BLOCK, TC_SMEM, st>>>(tm, c->ab0, c->wbB[1], nullptr, nullptr, nullptr, nullptr, 1,
                                                                   c->H, c->W, c->derr, wait_cycles, 1);
     CNN_LAUNCHED(c);
     int e = 0;
