@@ -361,19 +361,25 @@ def corrector_leg(steps: int = 20, batch: int = 32) -> dict:
     t_fine = wall(lambda: (fine.advance(ratio * steps), fine.sync()))
     t_plain = wall(lambda: (plain.advance(steps), plain.sync()))
     t_learned = wall(lambda: (net.correct_step(learned, steps), learned.sync()))
+    ms_inf = net.time_hidden_layer_inference(batch, 10)
     ms_tc = net.time_hidden_layer(batch, 10)
     net.set_tensor_cores(False)
     ms_simt = net.time_hidden_layer(batch, 2)
     net.set_tensor_cores(True)
-    flops = 2.0 * batch * coarse_n * coarse_n * 64 * 576
-    tflops = flops / (ms_tc * 1e-3) / 1e12
+    npx = batch * coarse_n * coarse_n
+    flops = 2.0 * npx * 64 * 576
+    tflops = flops / (ms_inf * 1e-3) / 1e12
+    tflops_train = flops / (ms_tc * 1e-3) / 1e12
+    # training-path layer: BF16 input read, FP32 pre-activation + FP32 activation + BF16 activation written
+    train_bytes = npx * 64 * (2 + 4 + 4 + 2)
     peak = None
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            peak = float(json.load(f)["bf16_tflops"])
+            pk = json.load(f)
+        peak, hbm_peak = float(pk["bf16_tflops"]), float(pk["hbm_gbs"])
         peak_src = "measured"
     except (OSError, KeyError, ValueError):
-        peak, peak_src = 1900.0, "fallback"
+        peak, hbm_peak, peak_src = 1900.0, 6800.0, "fallback"
     for x in (fine, plain, learned):
         x.close()
     net.close()
@@ -383,9 +389,16 @@ def corrector_leg(steps: int = 20, batch: int = 32) -> dict:
                                    "learned_256": t_learned / steps * 1e3},
             "wall_ratio_fine_over_learned": t_fine / t_learned,
             "tensor_roofline": {"kernel": "k_conv_tc (64->64 3x3, tcgen05 BF16 -> FP32 TMEM)", "bound": "tensor",
-                                "batch": batch, "flops_per_launch": flops, "mean_launch_ms": ms_tc,
+                                "path": "inference: BF16 activation in and out (the layer the corrected step runs)",
+                                "batch": batch, "flops_per_launch": flops, "mean_launch_ms": ms_inf,
                                 "achieved": tflops, "peak": peak, "unit": "TFLOP/s", "frac": tflops / peak,
                                 "peak_source": peak_src},
+            "tensor_roofline_training": {"path": "training: FP32 pre-activation and activation plus the BF16 "
+                                                 "activation written (the backward pass reads them)",
+                                         "batch": batch, "mean_launch_ms": ms_tc, "achieved_tflops": tflops_train,
+                                         "frac_tensor": tflops_train / peak, "hbm_bytes_per_launch": train_bytes,
+                                         "achieved_GBps": train_bytes / (ms_tc * 1e-3) / 1e9,
+                                         "frac_hbm": train_bytes / (ms_tc * 1e-3) / 1e9 / hbm_peak},
             "simt_same_layer_ms": ms_simt,
             "accuracy": "not measured in this leg: the trained network's error against the filtered 1024^2 run "
                         "comes from navier-stokes-solvers_gb300/corrector.py on held-out seeds"}

@@ -415,8 +415,11 @@ int ns_cnn_set_tensor_cores(ns_cnn *c, int enable);
  * and recreated. */
 int ns_cnn_probe_wait_timeout(ns_cnn *c, long long wait_cycles, int *timed_out);
 /* Mean CUDA-event time of one 64 -> 64 hidden layer (the network's dominant
- * kernel) on batch samples, over reps launches after one untimed launch. */
+ * kernel) on batch samples, over reps launches after one untimed launch: the
+ * training path (FP32 pre-activation and activation plus the BF16 activation),
+ * and the inference path (BF16 activation only, as the corrected step runs it). */
 int ns_cnn_time_hidden_layer(ns_cnn *c, int batch, int reps, double *ms_per_launch);
+int ns_cnn_time_hidden_layer_inference(ns_cnn *c, int batch, int reps, double *ms_per_launch);
 /* nsteps corrected steps of an instance on the network's grid: plain RK4 step
  * (ns_gpu_advance), then omega += CNN(omega(t), omega(t+dt) - omega(t)) */
 int ns_cnn_correct_step(ns_cnn *c, ns_gpu *g, int nsteps);

@@ -338,9 +338,47 @@ def config5(argv=None):
     return 0
 
 
+def step_timing(argv=None):
+    """Wall time of the learned-corrected coarse step (plain RK4 step + network +
+    correction) against the plain step, on an untrained network (the time does not
+    depend on the weights): `warmup` corrected steps, then `steps` timed ones.  The
+    launch sequence a profiler captures for the corrected step."""
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--ratio", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=2)
+    ap.add_argument("--steps", type=int, default=3)
+    a = ap.parse_args(argv)
+    dt = a.ratio * 7.5e-4
+    g = nsgb.Gpu(a.n, a.n, 2 * np.pi, 2 * np.pi, nsgb.FP32)
+    g.set_params(**params(a.n, dt, forcing_seed=1000, substeps=a.ratio))
+    g.random_spectrum(3, 8.0, 0.5)
+    net = nsgb.Corrector(a.n, a.n, max_batch=1, seed=1)
+    net.set_normalization(1.0, 1.0, 1.0)
+    net.correct_step(g, a.warmup)
+    g.sync()
+    t0 = time.perf_counter()
+    net.correct_step(g, a.steps)
+    g.sync()
+    t1 = time.perf_counter()
+    g.advance(a.steps)
+    g.sync()
+    t2 = time.perf_counter()
+    print(json.dumps({"n": a.n, "steps": a.steps, "learned_ms_per_step": (t1 - t0) / a.steps * 1e3,
+                      "plain_ms_per_step": (t2 - t1) / a.steps * 1e3}))
+    net.close()
+    g.close()
+    return 0
+
+
 if __name__ == "__main__":
     import sys
 
     if len(sys.argv) > 1 and sys.argv[1] == "config5":
         raise SystemExit(config5(sys.argv[2:]))
+    if len(sys.argv) > 1 and sys.argv[1] == "step-timing":
+        raise SystemExit(step_timing(sys.argv[2:]))
     raise SystemExit(main())

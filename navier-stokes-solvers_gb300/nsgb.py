@@ -198,6 +198,7 @@ def load(build: bool = True) -> C.CDLL:
     proto("ns_cnn_correct_step", C.c_int, vp, vp, C.c_int)
     proto("ns_cnn_set_tensor_cores", C.c_int, vp, C.c_int)
     proto("ns_cnn_time_hidden_layer", C.c_int, vp, C.c_int, C.c_int, _DP)
+    proto("ns_cnn_time_hidden_layer_inference", C.c_int, vp, C.c_int, C.c_int, _DP)
     proto("ns_cnn_probe_wait_timeout", C.c_int, vp, C.c_longlong, C.POINTER(C.c_int))
     ecp = C.POINTER(EnsembleConfig)
     proto("ns_gpu_create_for_ensemble", C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, ecp, C.POINTER(vp))
@@ -599,6 +600,13 @@ class Corrector:
     def time_hidden_layer(self, batch: int, reps: int = 10) -> float:
         ms = C.c_double()
         self.check(self.lib.ns_cnn_time_hidden_layer(self.h, batch, reps, C.byref(ms)), "time_hidden_layer")
+        return ms.value
+
+    def time_hidden_layer_inference(self, batch: int, reps: int = 10) -> float:
+        """The same layer on the inference path (BF16 activation out only)."""
+        ms = C.c_double()
+        self.check(self.lib.ns_cnn_time_hidden_layer_inference(self.h, batch, reps, C.byref(ms)),
+                   "time_hidden_layer_inference")
         return ms.value
 
     def probe_wait_timeout(self, wait_cycles: int) -> int:
