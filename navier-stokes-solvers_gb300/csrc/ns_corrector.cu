@@ -28,6 +28,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #define NSG_NO_AUX_KERNELS
@@ -52,6 +53,22 @@ __device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >
 __device__ __forceinline__ int wrapm(int i, int n) {
     const int r = i % n;
     return r < 0 ? r + n : r;
+}
+
+// The BF16 activations of the tensor-core layers are stored periodically padded,
+// [B][H + 2][W + 2][64]: pixel (y, x) at (y + 1, x + 1), and the border rows and
+// columns hold copies of the opposite edge (row 0 = row H - 1, row H + 1 = row 0,
+// likewise for columns), so a 3 x 130 halo is one rectangular box at any tile.
+// pad_put stores v at byte offset off of pixel (b, y, x) and at each of its copies.
+template <typename V>
+__device__ __forceinline__ void pad_put(__nv_bfloat16* P, int b, int y, int x, int H, int W, int off, V v) {
+    unsigned char* base = reinterpret_cast<unsigned char*>(P) + off;
+    const int ys[2] = {y + 1, y == 0 ? H + 1 : 0};
+    const int xs[2] = {x + 1, x == 0 ? W + 1 : 0};
+    const int ny = (y == 0 || y == H - 1) ? 2 : 1, nx = (x == 0 || x == W - 1) ? 2 : 1;
+    for (int i = 0; i < ny; ++i)
+        for (int j = 0; j < nx; ++j)
+            *reinterpret_cast<V*>(base + (((size_t)b * (H + 2) + ys[i]) * (W + 2) + xs[j]) * 128) = v;
 }
 // GELU in the tanh form of Hendrycks and Gimpel (2016),
 // 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))), with the hardware tanh
@@ -138,36 +155,29 @@ __global__ void __launch_bounds__(TP*(COUT / CPT)) k_conv3x3(const float* __rest
 // D[128 pixels][64 co] (FP32, in tensor memory) += A[128 pixels][16 ci] x
 // B[16 ci][64 co] (BF16), 9 taps x 4 K-steps = 36 tcgen05.mma per tile.  A tile
 // is 128 consecutive pixels of one image row (W % 128 == 0).  The periodic halo
-// of the tile (3 rows x 130 pixels x 64 channels, BF16) sits in shared memory
-// as [row][8-channel chunk][130 px][8 ch], which is the canonical K-major,
-// no-swizzle operand layout (core matrix = 8 pixels x 16 bytes, 8-pixel groups
-// 128 B apart, K chunks 2080 B apart); the operand of tap (dy, dx) therefore
-// starts dx x 16 B and dy rows into the halo, with no im2col copy.  The weights
-// (B operand) stay in shared memory as [tap][chunk][64 co][8 ci].  One thread
-// issues the MMAs and commits them to an mbarrier.  Two accumulators (128
-// tensor-memory columns) let the MMAs of the next tile run while eight warps
-// drain the current one: warps w, w + 4, w + 8, w + 12 read lane quarter w % 4 of
-// the accumulator (pixels), columns 16 (w / 4) .. + 15 (output channels), with
-// tcgen05.ld, add the bias and stage the tile in shared memory, from where all
-// warps apply GELU and store the tile's outputs as contiguous, coalesced runs
-// (sixteen warps: w and w + 4, w + 8, w + 12 share lane quarter w % 4).
+// of the tile (3 rows x 130 pixels x 64 channels, BF16) is one TMA box of the
+// periodically padded activations (pad_put: the halo is a rectangle of the
+// padded image) and sits in shared memory as [3 rows][130 px][64 ch] with the
+// 128-byte swizzle (each pixel one 128-byte row, its 16-byte chunks permuted by
+// the row's address bits 7-9), which is the canonical K-major 128B-swizzled
+// operand layout (8-row groups 1024 B apart); the operand of tap (dy, dx) starts
+// at pixel row dy x 130 + dx, and K step s 32 s bytes into the row, with no
+// im2col copy.  The weights (B operand) stay in shared memory as
+// [tap][chunk][64 co][8 ci] (no swizzle).
 // Every wait is bounded by a clock budget: on expiry the kernel records an
 // error, frees its tensor memory and returns.
 constexpr int TC_W = 128;                                  // pixels per tile
-// halo pitch (pixels): slots 8 .. 135 hold the tile's 128 pixels (one TMA box per
-// row and 8-channel chunk, at a 128-byte aligned address), slots 7 and 136 its
-// periodic neighbours x0 - 1 and x0 + 128
-constexpr int TC_HP = 144;
-constexpr int TC_HX0 = 7;                                  // slot of pixel x0 - 1
+constexpr int TC_HP = TC_W + 2;                            // halo pixels per row
 constexpr int TC_WB_BYTES = 9 * 8 * 64 * 16;               // 73,728
-constexpr int TC_HX_BYTES = 3 * 8 * TC_HP * 16;            // 55,296 per halo buffer
+constexpr int TC_HX_BYTES = 50176;                         // halo buffer: 3 x 130 x 128 B = 49,920, to 1024 B
 constexpr int TC_ST = 68;  // staged output row pitch (floats): 16-byte aligned rows, so a warp's 16-byte
                            // stores of one channel quad (32 pixels) fill every bank group evenly
 constexpr int TC_STG_BYTES = TC_W * TC_ST * 4;             // 33,280
 constexpr int TC_THREADS = 512;                            // sixteen epilogue warps: four per accumulator lane quarter
 constexpr int TC_BLOCK = TC_THREADS + 64;                  // + the MMA warp and the halo warp
-constexpr unsigned TC_BOX_BYTES = 8 * TC_W * 2;            // one TMA box: 8 channels x 128 pixels (BF16)
-constexpr int TC_SMEM = TC_WB_BYTES + 2 * TC_HX_BYTES + TC_STG_BYTES + 64;  // + mbarriers and tmem address
+constexpr unsigned TC_BOX_BYTES = 64 * TC_HP * 3 * 2;      // the halo box: 64 channels x 130 pixels x 3 rows (BF16)
+// + up to 1023 B to place the halo buffers on a 1024-byte boundary (128B swizzle), mbarriers, tmem address
+constexpr int TC_SMEM = TC_WB_BYTES + 1024 + 2 * TC_HX_BYTES + TC_STG_BYTES + 64;
 constexpr long long TC_WAIT_CYCLES = 4000000000LL;         // default wait limit: about 2 s
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -180,6 +190,21 @@ __device__ __forceinline__ unsigned long long umma_desc(unsigned addr, unsigned 
     d |= (unsigned long long)((sbo >> 4) & 0x3FFF) << 32;
     d |= 1ULL << 46;  // descriptor version
     return d;         // base offset 0, swizzle none
+}
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle (sm_100 family
+// layout): rows of 128 bytes, 8-row groups 1024 bytes apart (stride offset), the
+// leading offset unused (16 B), base offset 0: the swizzle follows the shared
+// address bits, as the TMA box (1024-byte aligned) was written, so an operand
+// may start at any pixel row
+__device__ __forceinline__ unsigned long long umma_desc_sw128(unsigned addr) {
+    unsigned long long d = 0;
+    d |= (unsigned long long)((addr >> 4) & 0x3FFF);
+    d |= 1ULL << 16;                                    // leading byte offset 16 B (unused)
+    d |= (unsigned long long)(1024 >> 4) << 32;          // stride byte offset
+    d |= 1ULL << 46;                                    // descriptor version
+    d |= 2ULL << 61;                                    // 128-byte swizzle
+    return d;
 }
 
 // instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major, N = 64, M = 128
@@ -220,44 +245,19 @@ __device__ __forceinline__ void tc_ld16(unsigned taddr, float (&v)[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// halo of tile `tile` into buffer hx by one warp, completing on mbarrier mb
-// (two arrivals and the TMA bytes): lane 0 issues 24 TMA boxes (3 rows x 8
-// channel chunks, 128 pixels each, on the tensor map of `in`: dims {64, W, rows},
-// box {8, 128, 1}) after arming the barrier with their bytes; the periodic
-// neighbours x0 - 1 and x0 + 128 (48 16-byte chunks) come by cp.async from the
-// warp, which fences them for the tensor cores and arrives once they landed.
-__device__ __forceinline__ void tc_halo_load(const CUtensorMap* tm, const __nv_bfloat16* __restrict__ in, unsigned hx,
-                                             int tile, int H, int W, int ntx, unsigned mb, int lane) {
+// halo of tile `tile` into buffer hx (1024-byte aligned), completing on mbarrier
+// mb (one arrival and the TMA bytes): one TMA box of the padded activations
+// (tensor map dims {64, W + 2, rows of B (H + 2)}, box {64, 130, 3}, 128-byte
+// swizzle) at padded (0, x0, y), i.e. pixels x0 - 1 .. x0 + 128 of rows
+// y - 1 .. y + 1 with their periodic wrap.  One thread.
+__device__ __forceinline__ void tc_halo_load(const CUtensorMap* tm, unsigned hx, int tile, int H, int ntx, unsigned mb) {
     const int b = tile / (H * ntx), r = tile - b * H * ntx;
     const int y = r / ntx, x0 = (r - y * ntx) * TC_W;
-    if (lane == 0) {
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(24u * TC_BOX_BYTES) : "memory");
-#pragma unroll 1
-        for (int row = 0; row < 3; ++row) {
-            const int gy = b * H + wrapi(y + row - 1, H);
-#pragma unroll
-            for (int kc = 0; kc < 8; ++kc) {
-                const unsigned dst = hx + (unsigned)(((row * 8 + kc) * TC_HP + TC_HX0 + 1) * 16);
-                asm volatile(
-                    "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-                    "[%5];" ::"r"(dst),
-                    "l"(reinterpret_cast<unsigned long long>(tm)), "r"(8 * kc), "r"(x0), "r"(gy), "r"(mb)
-                    : "memory");
-            }
-        }
-    }
-    for (int i = lane; i < 48; i += 32) {
-        const int side = i / 24, rk = i - side * 24, row = rk >> 3, kc = rk & 7;
-        const int gx = wrapi(side ? x0 + TC_W : x0 - 1, W), gy = wrapi(y + row - 1, H);
-        const __nv_bfloat16* src = in + (((size_t)b * H + gy) * W + gx) * 64 + kc * 8;
-        const unsigned dst = hx + (unsigned)(((row * 8 + kc) * TC_HP + (side ? TC_HX0 + 1 + TC_W : TC_HX0)) * 16);
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-    }
-    asm volatile("cp.async.commit_group;" ::: "memory");
-    asm volatile("cp.async.wait_all;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic-proxy writes -> tensor-core reads
-    __syncwarp();
-    if (lane == 0) asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(mb) : "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(TC_BOX_BYTES) : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(hx),
+        "l"(reinterpret_cast<unsigned long long>(tm)), "r"(0), "r"(x0), "r"(b * (H + 2) + y), "r"(mb)
+        : "memory");
 }
 
 // 36 MMAs of one tile from halo buffer hx into the accumulator, committed to mbar (one
@@ -266,13 +266,13 @@ __device__ __forceinline__ void tc_halo_load(const CUtensorMap* tm, const __nv_b
 // the 14-bit field does not carry).
 __device__ __forceinline__ void tc_issue(unsigned taddr, unsigned hx, unsigned wbs, unsigned mb) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const unsigned long long a0 = umma_desc(hx, TC_HP * 16, 128), b0 = umma_desc(wbs, 64 * 16, 128);
+    const unsigned long long b0 = umma_desc(wbs, 64 * 16, 128);
 #pragma unroll
     for (int tap = 0; tap < 9; ++tap) {
         const int dy = tap / 3, dx = tap - 3 * dy;
 #pragma unroll
         for (int s = 0; s < 4; ++s) {
-            const unsigned long long a = a0 + (unsigned long long)(((dy * 8 + 2 * s) * TC_HP + TC_HX0 + dx) * 16 / 16);
+            const unsigned long long a = umma_desc_sw128(hx + (unsigned)((dy * TC_HP + dx) * 128 + 32 * s));
             const unsigned long long bb = b0 + (unsigned long long)((tap * 8 + 2 * s) * 64 * 16 / 16);
             tc_mma(taddr, a, bb, (tap | s) ? 1u : 0u);
         }
@@ -296,16 +296,16 @@ __device__ __forceinline__ bool epi_and(bool p) {
     return r != 0;
 }
 
-// in: BF16 activations [B][H][W][64] (tmap: its tensor map, dims {64, W, rows},
-// box {8, 128, 1}); w: BF16 weights in the B-operand layout [9 taps][8 ci / 8]
+// in: padded BF16 activations [B][H + 2][W + 2][64] (pad_put; tmap: their tensor
+// map, box {64, 130, 3}, 128-byte swizzle); w: BF16 weights in the B-operand layout [9 taps][8 ci / 8]
 // [64 co][8 ci % 8] (k_round_weights); bias may be null; outputs (each may be
-// null): pre FP32, actf FP32, actb BF16, all [B][H][W][64].  Warp-specialised
+// null): pre FP32 and actf FP32 [B][H][W][64], actb BF16 padded.  Warp-specialised
 // pipeline per CTA (tiles t = blockIdx.x, + gridDim.x, ...; iteration i uses
 // accumulator and halo buffer i % 2), synchronised by mbarriers:
 //  - the halo warp (warp 17) copies the weights (one bulk copy, wready) and loads
-//    halo i (TMA boxes and the two periodic neighbour columns) into buffer i % 2
-//    once the MMAs of iteration i - 2 have finished reading it (full), and signals
-//    ready;
+//    halo i (one TMA box of the padded activations) into buffer i % 2 once the
+//    MMAs of iteration i - 2 have finished reading it (full); the box's bytes
+//    complete ready;
 //  - the MMA warp (warp 16, one thread) issues iteration i's 36 MMAs once its
 //    halo is ready and accumulator i % 2 is drained (empty, sixteen warp
 //    arrivals; before the first, the weights), and commits them to full[i % 2];
@@ -331,11 +331,13 @@ __global__ void __launch_bounds__(TC_BLOCK, 1) k_conv_tc(const __grid_constant__
                                                          int B, int H, int W, int* __restrict__ err, long long wait_cycles,
                                                          int probe) {
     extern __shared__ __align__(1024) unsigned char tsm[];
-    unsigned char* WB = tsm;                            // [9][8][64][8] bf16
-    unsigned char* HXB = tsm + TC_WB_BYTES;             // 2 x [3][8][TC_HP][8] bf16
-    float* stg = reinterpret_cast<float*>(tsm + TC_WB_BYTES + 2 * TC_HX_BYTES);  // [128][TC_ST] fp32
+    unsigned char* WB = tsm;  // [9][8][64][8] bf16
+    // 2 x [3][130][64] bf16 (128B swizzle), from the first 1024-byte boundary after the weights
+    const unsigned hx_off = ((smem_u32(tsm) + TC_WB_BYTES + 1023u) & ~1023u) - smem_u32(tsm);
+    unsigned char* HXB = tsm + hx_off;
+    float* stg = reinterpret_cast<float*>(HXB + 2 * TC_HX_BYTES);  // [128][TC_ST] fp32
     // full[2], empty[2], ready[2], wready, then the tensor-memory address
-    unsigned long long* mbar = reinterpret_cast<unsigned long long*>(tsm + TC_WB_BYTES + 2 * TC_HX_BYTES + TC_STG_BYTES);
+    unsigned long long* mbar = reinterpret_cast<unsigned long long*>(HXB + 2 * TC_HX_BYTES + TC_STG_BYTES);
     unsigned* tslot = reinterpret_cast<unsigned*>(mbar + 7);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int ntx = W / TC_W;
@@ -349,10 +351,10 @@ __global__ void __launch_bounds__(TC_BLOCK, 1) k_conv_tc(const __grid_constant__
     // dependent launch); it waits for this grid before it touches global memory
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const int q = warp & 3, h = warp >> 2;  // epilogue: lane quarter q, accumulator columns 16 h .. 16 h + 15
-    // TMA boxes land at 128-byte aligned shared addresses: with a misaligned
-    // dynamic shared-memory base the kernel records an error and issues no copy
-    // (the run behaves as a probe)
-    if ((hxb & 127u) != 0) {
+    // the swizzled TMA box must land at a 1024-byte aligned shared address (placed
+    // so above; checked here): otherwise the kernel records an error and issues
+    // no copy (the run behaves as a probe)
+    if ((hxb & 1023u) != 0) {
         if (tid == 0) atomicExch(err, 2);
         probe = 1;
     }
@@ -363,7 +365,7 @@ __global__ void __launch_bounds__(TC_BLOCK, 1) k_conv_tc(const __grid_constant__
             for (int k = 0; k < 2; ++k) {
                 asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mfull + 8u * k));
                 asm volatile("mbarrier.init.shared::cta.b64 [%0], 16;" ::"r"(mempty + 8u * k));
-                asm volatile("mbarrier.init.shared::cta.b64 [%0], 2;" ::"r"(mready + 8u * k));
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mready + 8u * k));
             }
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mwready));
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -396,7 +398,8 @@ __global__ void __launch_bounds__(TC_BLOCK, 1) k_conv_tc(const __grid_constant__
                     if (lane == 0) atomicExch(err, 1);
                     break;
                 }
-                tc_halo_load(&tmap, in, hxb + (unsigned)(buf * TC_HX_BYTES), tile, H, W, ntx, mready + 8u * buf, lane);
+                if (lane == 0) tc_halo_load(&tmap, hxb + (unsigned)(buf * TC_HX_BYTES), tile, H, ntx, mready + 8u * buf);
+                __syncwarp();
             }
             // the copies of the last halos and of the weights must have landed before the CTA exits
             for (int k = (j > 2 ? j - 2 : 0); k < j; ++k) mbar_wait(mready + 8u * (k & 1), (unsigned)((k >> 1) & 1), wait_cycles);
@@ -465,8 +468,8 @@ __global__ void __launch_bounds__(TC_BLOCK, 1) k_conv_tc(const __grid_constant__
                 if (bf16_only) {
                     const __nv_bfloat162 lo = __floats2bfloat162_rn(GELU ? gelu_fast(pv.x) : pv.x, GELU ? gelu_fast(pv.y) : pv.y);
                     const __nv_bfloat162 hi = __floats2bfloat162_rn(GELU ? gelu_fast(pv.z) : pv.z, GELU ? gelu_fast(pv.w) : pv.w);
-                    *reinterpret_cast<uint2*>(actb + o) =
-                        make_uint2(*reinterpret_cast<const unsigned*>(&lo), *reinterpret_cast<const unsigned*>(&hi));
+                    pad_put(actb, b, y, x0 + px, H, W, 8 * cg,
+                            make_uint2(*reinterpret_cast<const unsigned*>(&lo), *reinterpret_cast<const unsigned*>(&hi)));
                 } else {
                     const float4 av = GELU ? make_float4(gelu(pv.x), gelu(pv.y), gelu(pv.z), gelu(pv.w)) : pv;
                     if (pre) *reinterpret_cast<float4*>(pre + o) = pv;
@@ -474,8 +477,8 @@ __global__ void __launch_bounds__(TC_BLOCK, 1) k_conv_tc(const __grid_constant__
                     if (actb) {
                         const __nv_bfloat162 lo = __floats2bfloat162_rn(av.x, av.y);
                         const __nv_bfloat162 hi = __floats2bfloat162_rn(av.z, av.w);
-                        *reinterpret_cast<uint2*>(actb + o) =
-                            make_uint2(*reinterpret_cast<const unsigned*>(&lo), *reinterpret_cast<const unsigned*>(&hi));
+                        pad_put(actb, b, y, x0 + px, H, W, 8 * cg,
+                                make_uint2(*reinterpret_cast<const unsigned*>(&lo), *reinterpret_cast<const unsigned*>(&hi)));
                     }
                 }
             }
@@ -510,7 +513,8 @@ __device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigne
 __device__ __forceinline__ float lo2(unsigned long long v) { return __uint_as_float((unsigned)v); }
 __device__ __forceinline__ float hi2(unsigned long long v) { return __uint_as_float((unsigned)(v >> 32)); }
 
-// first layer (2 -> 64, GELU) to the BF16 activations of the tensor-core layers.
+// first layer (2 -> 64, GELU) to the BF16 activations of the tensor-core layers
+// (periodically padded layout, pad_put).
 // Thread (channel quad cq = tid % 16, pixel lane pl = tid / 16) computes output
 // channels 4 cq .. 4 cq + 3 of pixels pl and pl + 16 of each tile row and keeps
 // its 72 weights in registers as channel pairs; the halo holds each input value
@@ -587,14 +591,14 @@ __global__ void __launch_bounds__(256, 2) k_conv_in_tile(const float* __restrict
                     a1[k] = fma2(x1v.y, wr[tap][1][k], a1[k]);
                 }
             }
-            __nv_bfloat16* o = out + (((size_t)b * H + y0 + py) * W + x0 + pl) * 64 + 4 * cq;
             __nv_bfloat162 p0 = __floats2bfloat162_rn(gelu_fast(lo2(a0[0])), gelu_fast(hi2(a0[0])));
             __nv_bfloat162 p1 = __floats2bfloat162_rn(gelu_fast(lo2(a0[1])), gelu_fast(hi2(a0[1])));
-            *reinterpret_cast<uint2*>(o) = make_uint2(*reinterpret_cast<unsigned*>(&p0), *reinterpret_cast<unsigned*>(&p1));
+            pad_put(out, b, y0 + py, x0 + pl, H, W, 8 * cq,
+                    make_uint2(*reinterpret_cast<unsigned*>(&p0), *reinterpret_cast<unsigned*>(&p1)));
             p0 = __floats2bfloat162_rn(gelu_fast(lo2(a1[0])), gelu_fast(hi2(a1[0])));
             p1 = __floats2bfloat162_rn(gelu_fast(lo2(a1[1])), gelu_fast(hi2(a1[1])));
-            *reinterpret_cast<uint2*>(o + 16 * 64) =
-                make_uint2(*reinterpret_cast<unsigned*>(&p0), *reinterpret_cast<unsigned*>(&p1));
+            pad_put(out, b, y0 + py, x0 + pl + 16, H, W, 8 * cq,
+                    make_uint2(*reinterpret_cast<unsigned*>(&p0), *reinterpret_cast<unsigned*>(&p1)));
         }
     }
 }
@@ -617,8 +621,8 @@ __device__ __forceinline__ void act8(const __nv_bfloat16* p, float (&v)[8]) {
 // output layer (64 -> 1, no activation): every pixel of the tile and its halo is
 // projected once onto the nine taps, P[p][t] = sum_ci act[p][ci] w[t][ci] (one
 // halo pixel per thread), and out[p] = bias + sum_t P[p + offset(t)][t]; each
-// activation is read once rather than once per tap.  act [B][H][W][64] (FP32 or
-// the BF16 activations of the tensor-core path), w [9][64][1], out [B][H][W] times
+// activation is read once rather than once per tap.  act [B][H][W][64] (FP32) or
+// the padded BF16 activations of the tensor-core path, w [9][64][1], out [B][H][W] times
 // scale (the output normalisation, applied as k_scale applies it).
 template <typename A>
 __global__ void __launch_bounds__(OT_THREADS) k_conv_out_tile(const A* __restrict__ act, const __nv_bfloat16* __restrict__ w,
@@ -635,7 +639,12 @@ __global__ void __launch_bounds__(OT_THREADS) k_conv_out_tile(const A* __restric
         __syncthreads();  // previous tile done with sp (and the weights written)
         for (int i = threadIdx.x; i < IT_HALO; i += blockDim.x) {
             const int hy = i / (IT_W + 2), hx = i - hy * (IT_W + 2);
-            const A* ap = act + (((size_t)b * H + wrapm(y0 + hy - 1, H)) * W + wrapi(x0 + hx - 1, W)) * 64;
+            // FP32 activations are unpadded (wrap the halo); the BF16 ones of the
+            // tensor-core path are periodically padded (pad_put): the halo is a
+            // rectangle of the padded image (rows past a partial band clamped)
+            const A* ap = std::is_same<A, __nv_bfloat16>::value
+                              ? act + (((size_t)b * (H + 2) + min(y0 + hy, H + 1)) * (W + 2) + x0 + hx) * 64
+                              : act + (((size_t)b * H + wrapm(y0 + hy - 1, H)) * W + wrapi(x0 + hx - 1, W)) * 64;
             float acc[9];
 #pragma unroll
             for (int t = 0; t < 9; ++t) acc[t] = 0.0f;
@@ -678,9 +687,22 @@ __global__ void __launch_bounds__(OT_THREADS) k_conv_out_tile(const A* __restric
     }
 }
 
-__global__ void k_to_bf16(const float* __restrict__ a, __nv_bfloat16* __restrict__ b, long long n) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        b[i] = __float2bfloat16_rn(a[i]);
+// FP32 [B][H][W][64] -> the padded BF16 layout (pad_put): one 8-channel chunk per thread
+__global__ void k_to_bf16_pad(const float* __restrict__ a, __nv_bfloat16* __restrict__ out, int B, int H, int W) {
+    const long long n = (long long)B * H * W * 8;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const long long p = i >> 3;
+        const int kc = (int)(i & 7);
+        const int b = (int)(p / ((long long)H * W)), r = (int)(p - (long long)b * H * W);
+        const int y = r / W, x = r - y * W;
+        const float4 u = reinterpret_cast<const float4*>(a + p * 64 + 8 * kc)[0];
+        const float4 v = reinterpret_cast<const float4*>(a + p * 64 + 8 * kc)[1];
+        const __nv_bfloat162 q0 = __floats2bfloat162_rn(u.x, u.y), q1 = __floats2bfloat162_rn(u.z, u.w);
+        const __nv_bfloat162 q2 = __floats2bfloat162_rn(v.x, v.y), q3 = __floats2bfloat162_rn(v.z, v.w);
+        pad_put(out, b, y, x, H, W, 16 * kc,
+                make_uint4(*reinterpret_cast<const unsigned*>(&q0), *reinterpret_cast<const unsigned*>(&q1),
+                           *reinterpret_cast<const unsigned*>(&q2), *reinterpret_cast<const unsigned*>(&q3)));
+    }
 }
 
 __host__ __device__ constexpr int cmin(int a, int b) { return a < b ? a : b; }
@@ -975,15 +997,16 @@ static int tc_tensor_map(ns_cnn* c, const __nv_bfloat16* in, CUtensorMap* out) {
             CNN_FAIL(c, NS_GPU_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
         encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
     }
-    // [rows][W][64] BF16 activations: dims {64 channels, W pixels, maxB H rows},
-    // boxes of 8 channels x 128 pixels x 1 row (16-byte inner extent)
-    const cuuint64_t dims[3] = {64, (cuuint64_t)c->W, (cuuint64_t)c->maxB * c->H};
-    const cuuint64_t strides[2] = {64 * sizeof(__nv_bfloat16), (cuuint64_t)c->W * 64 * sizeof(__nv_bfloat16)};
-    const cuuint32_t box[3] = {8, TC_W, 1};
+    // periodically padded BF16 activations [B][H + 2][W + 2][64]: dims {64 channels,
+    // W + 2 pixels, maxB (H + 2) rows}, boxes of 64 channels x 130 pixels x 3 rows
+    // (one 128-byte row per pixel, 128-byte swizzle: the tensor cores' operand layout)
+    const cuuint64_t dims[3] = {64, (cuuint64_t)c->W + 2, (cuuint64_t)c->maxB * (c->H + 2)};
+    const cuuint64_t strides[2] = {64 * sizeof(__nv_bfloat16), ((cuuint64_t)c->W + 2) * 64 * sizeof(__nv_bfloat16)};
+    const cuuint32_t box[3] = {64, TC_HP, 3};
     const cuuint32_t estr[3] = {1, 1, 1};
     CUtensorMap m;
     const CUresult r = encode(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16*>(in), dims, strides, box, estr,
-                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) CNN_FAIL(c, NS_GPU_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
     const int k = c->tm_next;
@@ -1040,8 +1063,8 @@ static int forward(ns_cnn* c, cudaStream_t st, int B, bool training = true, floa
     __nv_bfloat16* alast = nullptr;  // BF16 input of the output layer (tensor-core inference)
     if (c->tc) {
         if (training) {
-            const long long n = (long long)B * c->H * c->W * HID;
-            k_to_bf16<<<grid_of(n, 256, 8 * c->num_sms), 256, 0, st>>>(c->act[0], c->ab0, n);
+            const long long n = (long long)B * c->H * c->W * 8;
+            k_to_bf16_pad<<<grid_of(n, 256, 8 * c->num_sms), 256, 0, st>>>(c->act[0], c->ab0, B, c->H, c->W);
             CNN_LAUNCHED(c);
         }
         __nv_bfloat16* ain = c->ab0;
@@ -1119,8 +1142,8 @@ static int loss_and_backward(ns_cnn* c, cudaStream_t st, int B, int slot) {
             if (c->tc) {
                 // input gradient on the tensor cores: BF16 output gradient, flipped
                 // and transposed BF16 weights, FP32 result
-                const long long n = npix * HID;
-                k_to_bf16<<<grid_of(n, 256, 8 * c->num_sms), 256, 0, st>>>(dcur, c->ab0, n);
+                const long long n = npix * 8;
+                k_to_bf16_pad<<<grid_of(n, 256, 8 * c->num_sms), 256, 0, st>>>(dcur, c->ab0, B, c->H, c->W);
                 CNN_LAUNCHED(c);
                 CNN_TRY(conv_tc<false>(c, st, c->ab0, c->wbtB[l], nullptr, nullptr, dnext, nullptr, B));
             } else {
@@ -1194,8 +1217,9 @@ int ns_cnn_create(int height, int width, int max_batch, uint64_t seed, ns_cnn** 
     alloc((void**)&c->cw0, (size_t)height * width * sizeof(float));
     c->tc = (width % TC_W == 0) ? 1 : 0;
     if (c->tc) {
-        alloc((void**)&c->ab0, npix * HID * sizeof(__nv_bfloat16));
-        alloc((void**)&c->ab1, npix * HID * sizeof(__nv_bfloat16));
+        const size_t npad = (size_t)max_batch * (height + 2) * (width + 2);  // periodically padded (pad_put)
+        alloc((void**)&c->ab0, npad * HID * sizeof(__nv_bfloat16));
+        alloc((void**)&c->ab1, npad * HID * sizeof(__nv_bfloat16));
     }
     alloc((void**)&c->derr, sizeof(int));
     if (ok && cudaMemset(c->derr, 0, sizeof(int)) != cudaSuccess) ok = false;
@@ -1483,7 +1507,7 @@ static int time_layer(ns_cnn* c, int batch, int reps, bool inference, double* ms
     const long long n = (long long)batch * c->H * c->W * HID;
     CNN_CUDA(c, cudaMemsetAsync(c->act[0], 0, (size_t)n * sizeof(float), st));
     if (c->tc) {
-        k_to_bf16<<<grid_of(n, 256, 8 * c->num_sms), 256, 0, st>>>(c->act[0], c->ab0, n);
+        k_to_bf16_pad<<<grid_of(n / 8, 256, 8 * c->num_sms), 256, 0, st>>>(c->act[0], c->ab0, batch, c->H, c->W);
         CNN_LAUNCHED(c);
     }
     cudaEvent_t a, b;
