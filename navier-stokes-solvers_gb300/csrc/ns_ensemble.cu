@@ -62,7 +62,7 @@ __device__ __forceinline__ void cluster_barrier() {
 template <int EC, int STAGE>
 __device__ __forceinline__ void col_pass(const EnsMember& M, int r, int team) {
     for (int b = r; b < M.ncb; b += team) {
-        col_body<float, EC, COL_STAGE, STAGE>(M.g, M.ca, b);
+        col_body<float, EC, COL_STAGE, STAGE, false>(M.g, M.ca, b);
         __syncthreads();
     }
 }
@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(ens_max_threads(ER, EC), ens_min_ctas(ER, EC))
                 ra.cfl = (stage == 1 && M.adaptive) ? 1 : 0;
                 ra.marker = stage == 1 ? 1 : (stage == 2 ? 2 : 0);
                 for (int b = r; b < M.nrb; b += team) {
-                    row_body<float, ER, ROW_STAGE>(M.g, ra, b);
+                    row_body<float, ER, ROW_STAGE, false>(M.g, ra, b);
                     __syncthreads();
                 }
                 if (shared) cluster_barrier();

@@ -48,7 +48,7 @@ template <typename T, int E, int MODE> static int row_launch_e(ns_gpu* g, const 
     const int TT = E ? g->g.H / E : g->g.TTr;
     const int P = row_groups(g->g.fpr, E, NF);
     // E = 0 (mixed radix): one scratch sequence per row after the NF field buffers
-    const size_t smem = (size_t)(NF + (E ? 0 : 1)) * g->g.RPC * spad_len(g->g.H) * sizeof(Cx<T>);
+    const size_t smem = (size_t)(NF + (E ? 0 : P)) * g->g.RPC * spad_len(g->g.H) * sizeof(Cx<T>);
     NSG_TRY(set_smem(g, k_row<T, E, MODE>, smem));
     k_row<T, E, MODE><<<g->g.ny / g->g.RPC, g->g.RPC * P * TT, smem, g->st>>>(g->g, a);
     NSG_LAUNCHED(g);
@@ -62,7 +62,7 @@ template <typename T, int MODE> static int row_launch(ns_gpu* g, const RowArgs<T
 template <typename T, int E, int MODE, int STAGE> static int col_launch_e(ns_gpu* g, const ColArgs<T>& a) {
     const int TC = E ? g->g.ny / E : g->g.TTc;
     const int P = col_groups(g->g.fpc, E, MODE);
-    const size_t smem = (size_t)(E ? P : 2) * g->g.CW * spad_len(g->g.ny) * sizeof(Cx<T>);
+    const size_t smem = (size_t)(E ? P : 2 * P) * g->g.CW * spad_len(g->g.ny) * sizeof(Cx<T>);
     NSG_TRY(set_smem(g, k_col<T, E, MODE, STAGE>, smem));
     k_col<T, E, MODE, STAGE><<<g->g.Kxp / g->g.CW, P * g->g.CW * TC, smem, g->st>>>(g->g, a);
     NSG_LAUNCHED(g);
@@ -607,14 +607,14 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
     // fields in parallel (a thread group per field): automatic when the
     // transforms are short (TT / TC of one or two warps) and too few to give
     // the SMs more than a few warps each one after another
-    const int TTp = g->ER ? G.H / g->ER : 0, TCp = g->EC ? ny / g->EC : 0;
-    G.fpr = (kc && kc->fpr) ? (kc->fpr > 0) : (g->ER && TTp % 32 == 0 && TTp <= 64 && (long long)ny * TTp < 64LL * 32 * g->num_sms);
-    G.fpc = (kc && kc->fpc) ? (kc->fpc > 0) : (g->EC && TCp % 32 == 0 && TCp <= 64 && (long long)G.Kx * TCp < 64LL * 32 * g->num_sms);
+    const int TTp = g->ER ? G.H / g->ER : G.TTr, TCp = g->EC ? ny / g->EC : G.TTc;
+    G.fpr = (kc && kc->fpr) ? (kc->fpr > 0) : (TTp % 32 == 0 && TTp <= 64 && (long long)ny * TTp < 64LL * 32 * g->num_sms);
+    G.fpc = (kc && kc->fpc) ? (kc->fpc > 0) : (TCp % 32 == 0 && TCp <= 64 && (long long)G.Kx * TCp < 64LL * 32 * g->num_sms);
     // column tile width: up to 16 columns, <= 512 threads, <= ~100 KB shared memory
     {
         const int TC = g->EC ? ny / g->EC : G.TTc;
-        const int nbuf = g->EC ? (G.fpc ? 4 : 1) : 2;
         const int P = G.fpc ? 4 : 1;
+        const int nbuf = g->EC ? P : 2 * P;
         int CW = 1;
         // with a group per field a column block is already four groups: widen it
         // only while that still leaves two blocks per SM
@@ -631,8 +631,8 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
     // shared memory for four fields
     {
         const int TT = g->ER ? G.H / g->ER : G.TTr;
-        const int nbuf = g->ER ? 4 : 5;  // four field buffers (+ the mixed-radix scratch)
         const int P = G.fpr ? 4 : 1;
+        const int nbuf = g->ER ? 4 : 4 + P;  // four field buffers (+ the mixed-radix scratch per group)
         const int budget = (G.fpr || precision == NS_GPU_FP32) ? 256 : 128;
         int RPC = 1;
         while (2 * RPC * TT * P <= budget && 2 * RPC <= ny && ny % (2 * RPC) == 0 &&
@@ -644,14 +644,14 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
     }
     // a group per field needs whole warps per group, at most 256 (row) / 512
     // (column) threads per CTA, and at most 15 named barriers per CTA
-    if (G.fpr && !(g->ER && TTp % 32 == 0 && G.RPC * 4 * TTp <= 256 && (TTp == 32 || G.RPC * 4 <= 15))) {
+    if (G.fpr && !(TTp % 32 == 0 && G.RPC * 4 * TTp <= 256 && (TTp == 32 || G.RPC * 4 <= 15))) {
         fprintf(stderr, "ns_gpu_create: nx=%d ny=%d: the row pass cannot run a thread group per field with this tiling\n",
                 nx, ny);
         cudaStreamDestroy(g->st);
         delete g;
         return NS_GPU_ERR_INVALID;
     }
-    if (G.fpc && !(g->EC && (G.CW * TCp) % 32 == 0 && 4 * G.CW * TCp <= 512)) {
+    if (G.fpc && !((G.CW * TCp) % 32 == 0 && 4 * G.CW * TCp <= 512)) {
         fprintf(stderr, "ns_gpu_create: nx=%d ny=%d: the column pass cannot run a thread group per field with this tiling\n",
                 nx, ny);
         cudaStreamDestroy(g->st);
@@ -680,8 +680,8 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
     {
         int optin = 0;
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, g->device);
-        const size_t row_sm = (size_t)(g->ER ? 4 : 5) * G.RPC * spad_len(G.H) * cs;
-        const size_t col_sm = (size_t)(g->EC ? (G.fpc ? 4 : 1) : 2) * G.CW * spad_len(ny) * cs;
+        const size_t row_sm = (size_t)(g->ER ? 4 : 4 + (G.fpr ? 4 : 1)) * G.RPC * spad_len(G.H) * cs;
+        const size_t col_sm = (size_t)(g->EC ? 1 : 2) * (G.fpc ? 4 : 1) * G.CW * spad_len(ny) * cs;
         if (optin > 0 && (row_sm > (size_t)optin || col_sm > (size_t)optin)) {
             fprintf(stderr,
                     "ns_gpu_create: nx=%d ny=%d: the stage kernels need %zu / %zu bytes of shared memory per CTA, above "

@@ -44,7 +44,7 @@ struct Geo {
     // (H = nx) with Hermitian-extended input instead of the half-length packing.
     unsigned long long rxa, rxb, rya, ryb;
     int nrx, nry, TTr, TTc, oddx;
-    // fields in parallel (power-of-two bodies only): the row pass gives each row
+    // fields in parallel: the row pass gives each row
     // one group of transform threads per field (fpr), the column pass gives each
     // column block four groups, one per inverse-transformed field (fpc), so that
     // a small grid's transforms run side by side instead of one after another
@@ -237,7 +237,7 @@ __device__ __forceinline__ double warp_max(double v) {
 // =============================================================== row kernel
 enum { ROW_STAGE = 0, ROW_DUMP = 1, ROW_UVW = 2, ROW_INV1 = 3, ROW_FWD1 = 4 };
 // thread groups per row of the row pass (nf = fields inverse-transformed per row)
-__host__ __device__ inline int row_groups(int fpr, int E, int nf) { return (E > 0 && fpr && nf > 1) ? nf : 1; }
+__host__ __device__ inline int row_groups(int fpr, int E, int nf) { return (fpr && nf > 1) ? nf : 1; }
 
 template <typename T> struct RowArgs {
     typedef typename CT<T>::C C;
@@ -260,27 +260,29 @@ template <int MODE> struct RowNF { static const int v = (MODE == ROW_STAGE || MO
 
 // grid = ny / RPC, block = RPC * P * TT with TT = H / E (E > 0) or g.TTr (E = 0)
 // and P = row_groups(g.fpr, E, NF) thread groups per row, dynamic smem = NF * RPC *
-// spad_len(H) * sizeof(C), plus RPC * spad_len(H) * sizeof(C) of mixed-radix
-// scratch when E = 0
+// spad_len(H) * sizeof(C), plus P * RPC * spad_len(H) * sizeof(C) of mixed-radix
+// scratch (one sequence per group) when E = 0
 // body of the row pass for row block bx (rows bx*RPC .. bx*RPC + RPC - 1); the
 // block must have exactly RPC * P * TT threads.  With P > 1 (fields in parallel;
 // TT a multiple of 32, RPC * P <= 15 when TT > 32) group f of a row loads,
 // unpacks and inverse-transforms field f, the row's threads form the products
 // together, and group 0 makes the forward transform.
-template <typename T, int E, int MODE>
+// FG = false compiles the field-group logic out (callers that always run one
+// group per row, such as the persistent ensemble kernel)
+template <typename T, int E, int MODE, bool FG = true>
 __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, const int bx) {
     typedef typename CT<T>::C C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* sm = reinterpret_cast<C*>(smem_raw);
     constexpr int NF = RowNF<MODE>::v;
     const int H = g.H, TT = (E == 0) ? g.TTr : H / E, LP = spad_len(H);
-    const int P = row_groups(g.fpr, E, NF), TQ = P * TT;
+    const int P = FG ? row_groups(g.fpr, E, NF) : 1, TQ = P * TT;
     const int r = threadIdx.x / TQ, q = threadIdx.x - r * TQ;
     const int fg = q / TT, t = q - fg * TT;
     const int sy = sync_mode(TT, P > 1 ? 1 + r * P + fg : 0, TT);
     const int y = bx * g.RPC + r;
     const int nx = g.nx, Kx = g.Kx;
-    C* scr = sm + (NF * g.RPC + r) * LP;  // mixed-radix scratch of this row (E = 0 only)
+    C* scr = sm + (NF * g.RPC + r * P + fg) * LP;  // mixed-radix scratch of this row and group (E = 0 only)
     const bool oddx = (E == 0) && g.oddx;
 
     if (MODE == ROW_STAGE && bx == 0 && threadIdx.x == 0) {
@@ -500,7 +502,7 @@ enum { COL_STAGE = 0, COL_PROLOGUE = 1, COL_INV1 = 2, COL_FWD_EXPORT = 3, COL_NL
 // thread groups per column block of the column pass (the modes with several
 // inverse-transformed fields)
 __host__ __device__ inline int col_groups(int fpc, int E, int mode) {
-    return (E > 0 && fpc && (mode == COL_STAGE || mode == COL_PROLOGUE)) ? 4 : 1;
+    return (fpc && (mode == COL_STAGE || mode == COL_PROLOGUE)) ? 4 : 1;
 }
 
 template <typename T> struct ColArgs {
@@ -705,20 +707,19 @@ __device__ __forceinline__ C post_step_mode(const Geo& g, const ColArgs<T>& a, i
 
 // grid = Kxp / CW, block = P * CW * TC with TC = ny / E (E > 0) or g.TTc (E = 0)
 // and P = col_groups(g.fpc, E, MODE) thread groups, dynamic smem = P * CW *
-// spad_len(ny) * sizeof(C), 2 * CW * spad_len(ny) * sizeof(C) when E = 0 (the
-// mixed-radix scratch)
+// spad_len(ny) * sizeof(C), twice that when E = 0 (the mixed-radix scratch)
 // body of the column pass for column block bx (kept columns bx*CW .. bx*CW + CW - 1);
 // the block must have exactly P * CW * TC threads.  With P > 1 (fields in
 // parallel; CW * TC a multiple of 32) group 0 makes the forward transforms, the
 // block applies the stage together, and group f inverse-transforms and stores
 // the fields f, f + P, ... in its own buffers, synchronised by named barrier 1 + f.
-template <typename T, int E, int MODE, int STAGE>
+template <typename T, int E, int MODE, int STAGE, bool FG = true>
 __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, const int bx) {
     typedef typename CT<T>::C C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* sm = reinterpret_cast<C*>(smem_raw);
     const int ny = g.ny, TC = (E == 0) ? g.TTc : ny / E, LP = spad_len(ny), CW = g.CW;
-    const int P = col_groups(g.fpc, E, MODE), GT = CW * TC;
+    const int P = FG ? col_groups(g.fpc, E, MODE) : 1, GT = CW * TC;
     const int fg = threadIdx.x / GT, u = threadIdx.x - fg * GT;
     const int b = u / TC, t = u - b * TC;
     const int sy = sync_mode(TC, P > 1 ? 1 + fg : 0, GT);
@@ -727,7 +728,7 @@ __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, cons
     const int nthr = blockDim.x;
     C* gbuf = sm + fg * CW * LP;  // this group's CW column buffers
     C* mybuf = gbuf + b * LP;
-    C* myscr = sm + (CW + b) * LP;  // mixed-radix scratch (E = 0 only)
+    C* myscr = sm + (P * CW + fg * CW + b) * LP;  // mixed-radix scratch of this group (E = 0 only)
     __shared__ double s_dt;
 
     if (MODE == COL_STAGE) {

@@ -53,3 +53,15 @@ def test_automatic_tiling_reported(nsgb):
     with pytest.raises(RuntimeError):
         # four groups of 64 threads per row at 4 rows per CTA: 1024 threads
         nsgb.Gpu(1024, 1024, precision=1, tiling=dict(row_radix=4, rows_per_cta=4, row_field_groups=1))
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_field_groups_mixed_radix_bit_identical(nsgb, prec):
+    """Lengths that are not powers of two (192 x 96: row transform 96 = 2^5 x 3,
+    column 96): the mixed-radix bodies with a group per field, each group with its
+    own scratch sequence, against one group per row / column block."""
+    a, _ = _run(nsgb, 192, 96, prec, dict(row_field_groups=-1, col_field_groups=-1))
+    b, tb = _run(nsgb, 192, 96, prec, dict(row_field_groups=1, col_field_groups=1))
+    assert tb["row_radix"] == 0 and tb["row_field_groups"] == 1 and tb["col_field_groups"] == 1
+    assert np.isfinite(a).all()
+    assert np.array_equal(a, b)
