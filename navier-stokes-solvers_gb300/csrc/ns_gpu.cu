@@ -607,9 +607,11 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
     // fields in parallel (a thread group per field): automatic when the
     // transforms are short (TT / TC of one or two warps) and too few to give
     // the SMs more than a few warps each one after another
+    // (FP64 only for one-warp transforms: at 768^2 its two-warp groups were slower)
     const int TTp = g->ER ? G.H / g->ER : G.TTr, TCp = g->EC ? ny / g->EC : G.TTc;
-    G.fpr = (kc && kc->fpr) ? (kc->fpr > 0) : (TTp % 32 == 0 && TTp <= 64 && (long long)ny * TTp < 64LL * 32 * g->num_sms);
-    G.fpc = (kc && kc->fpc) ? (kc->fpc > 0) : (TCp % 32 == 0 && TCp <= 64 && (long long)G.Kx * TCp < 64LL * 32 * g->num_sms);
+    const int gmax = precision == NS_GPU_FP32 ? 64 : 32;
+    G.fpr = (kc && kc->fpr) ? (kc->fpr > 0) : (TTp % 32 == 0 && TTp <= gmax && (long long)ny * TTp < 64LL * 32 * g->num_sms);
+    G.fpc = (kc && kc->fpc) ? (kc->fpc > 0) : (TCp % 32 == 0 && TCp <= gmax && (long long)G.Kx * TCp < 64LL * 32 * g->num_sms);
     // column tile width: up to 16 columns, <= 512 threads, <= ~100 KB shared memory
     {
         const int TC = g->EC ? ny / g->EC : G.TTc;
