@@ -190,31 +190,43 @@ static int ensure_noise(ns_gpu* g) {
         NSG_TRY(dalloc(g, (void**)&g->fnoise, need * sizeof(double2)));
         g->fnoise_cap = need;
     }
+    if (!g->stn) {
+        NSG_CUDA(g, cudaStreamCreateWithFlags(&g->stn, cudaStreamNonBlocking));
+        NSG_CUDA(g, cudaEventCreateWithFlags(&g->evn0, cudaEventDisableTiming));
+        NSG_CUDA(g, cudaEventCreateWithFlags(&g->evn1, cudaEventDisableTiming));
+    }
     g->fkxr = kxr;
     g->fkyr = kyr;
     g->fM = sp.fsub;
     return NS_GPU_OK;
 }
 
+// the step's noise table on its own stream, after the stage-1 row pass (which
+// sets step_cur) and joined before the stage-4 column pass: its FP64 draws run
+// beside stages 1-3 instead of ahead of them
 static int launch_noise(ns_gpu* g) {
     const StepParams sp = step_params<double>(g);
     const int n = (g->fkxr + 1) * (2 * g->fkyr + 1) * g->fM;
-    k_forcing_noise<<<(n + 127) / 128, 128, 0, g->st>>>(g->g.ny, g->g.Lx, g->g.Ly, &g->ds->step_next, g->fM, sp.f_seed,
-                                                        sp.f_kmin, sp.f_kmax, g->fkxr, g->fkyr, g->fnoise);
+    NSG_CUDA(g, cudaEventRecord(g->evn0, g->st));
+    NSG_CUDA(g, cudaStreamWaitEvent(g->stn, g->evn0, 0));
+    k_forcing_noise<<<(n + 127) / 128, 128, 0, g->stn>>>(g->g.ny, g->g.Lx, g->g.Ly, &g->ds->step_cur, g->fM, sp.f_seed,
+                                                         sp.f_kmin, sp.f_kmax, g->fkxr, g->fkyr, g->fnoise);
     NSG_LAUNCHED(g);
+    NSG_CUDA(g, cudaEventRecord(g->evn1, g->stn));
     return NS_GPU_OK;
 }
 
 // the kernels of one RK4 step on the instance stream
 template <typename T> static int one_step(ns_gpu* g, const ColArgs<T>& a) {
-    if (g->fM > 0) NSG_TRY(launch_noise(g));
     NSG_TRY(stage_row<T>(g, 1));
+    if (g->fM > 0) NSG_TRY(launch_noise(g));
     NSG_TRY((stage_col<T, 1>(g, a)));
     NSG_TRY(stage_row<T>(g, 2));
     NSG_TRY((stage_col<T, 2>(g, a)));
     NSG_TRY(stage_row<T>(g, 3));
     NSG_TRY((stage_col<T, 3>(g, a)));
     NSG_TRY(stage_row<T>(g, 4));
+    if (g->fM > 0) NSG_CUDA(g, cudaStreamWaitEvent(g->st, g->evn1, 0));
     NSG_TRY((stage_col<T, 4>(g, a)));
     if (g->outside_active) {
         const long long nn = (long long)g->g.nkx * g->g.nky;
@@ -488,6 +500,9 @@ void ns_gpu_destroy(ns_gpu* g) {
     if (g->st2) cudaStreamDestroy(g->st2);
     if (g->ev_a) cudaEventDestroy(g->ev_a);
     if (g->ev_b) cudaEventDestroy(g->ev_b);
+    if (g->stn) cudaStreamDestroy(g->stn);
+    if (g->evn0) cudaEventDestroy(g->evn0);
+    if (g->evn1) cudaEventDestroy(g->evn1);
     if (g->st) cudaStreamDestroy(g->st);
     delete g;
 }
@@ -540,6 +555,8 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
     g->flush_bytes = 0;
     g->prof = nullptr;
     g->step_exec = nullptr;
+    g->stn = nullptr;
+    g->evn0 = g->evn1 = nullptr;
     g->step_launches = 0;
     g->step_graph_off = 0;
     g->launches = 0;

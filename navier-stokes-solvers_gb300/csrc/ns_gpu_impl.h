@@ -32,6 +32,8 @@ struct ns_gpu {
     unsigned long long step_launches;         // kernels per captured step
     int step_graph_off;                       // capture failed once: launch directly
     cudaEvent_t ev_a, ev_b;        // ordering between st and st2
+    cudaStream_t stn;              // the forcing-noise table of a step, beside its stages 1-3
+    cudaEvent_t evn0, evn1;        // fork after the stage-1 row pass, join before the stage-4 column pass
     std::string err;
     unsigned long long launches;
     ns_gpu_params p;

@@ -1084,18 +1084,19 @@ __global__ void k_hv_apply(Geo g, const double* w_full, int visc, int sfd, doubl
 
 // This step's forcing draws, one thread per (mode entry, draw s): entry e is
 // kx index i = e / (2 kyr + 1), ky = e % (2 kyr + 1) - kyr; the draw uses the
-// counter the stage-4 kernel would use, step_next + s (read before the step's
-// first stage advances the counters).  Terms are stored as forcing_xi_sum forms
+// counter the stage-4 kernel uses, *counter + s with counter = the running step's
+// step_cur (set by the step's stage-1 row pass; the kernel runs after it, beside
+// stages 1-3, and is joined before stage 4).  Terms are stored as forcing_xi_sum forms
 // them (the conjugate row of kx = 0, ky < 0 negated), modes outside the shell
 // as zeros.
-__global__ void k_forcing_noise(int ny, double Lx, double Ly, const unsigned long long* step_next, int M,
+__global__ void k_forcing_noise(int ny, double Lx, double Ly, const unsigned long long* counter, int M,
                                 unsigned long long seed, double kmin, double kmax, int kxr, int kyr, double2* out) {
     const int n = (kxr + 1) * (2 * kyr + 1) * M;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const int e = t / M, s = t - e * M;
         const int i = e / (2 * kyr + 1);
         const int ky = e - i * (2 * kyr + 1) - kyr;
-        out[t] = forcing_noise_term(i, ky, s, *step_next, seed, Lx, Ly, kmin, kmax);
+        out[t] = forcing_noise_term(i, ky, s, *counter, seed, Lx, Ly, kmin, kmax);
     }
 }
 
