@@ -531,6 +531,8 @@ __global__ void __launch_bounds__(256, 2) k_conv_in_tile(const float* __restrict
                                                          int B, int H, int W, const float* __restrict__ w0,
                                                          const float* __restrict__ w1, float s0, float s1) {
     __shared__ __align__(16) ulonglong2 sx[IN_HALO];
+    // the next layer (programmatic dependent launch) may set up while this one runs
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const int cq = threadIdx.x & 15, pl = threadIdx.x >> 4;
     unsigned long long wr[9][2][2];  // [tap][ci][channel pair]
 #pragma unroll
@@ -632,6 +634,9 @@ __global__ void __launch_bounds__(OT_THREADS) k_conv_out_tile(const A* __restric
     __shared__ float sp[IT_HALO * 9];
     for (int i = threadIdx.x; i < 9 * 64; i += blockDim.x) sw[i] = __bfloat162float(w[i]);
     const float b0 = bias ? bias[0] : 0.0f;
+    // launched as a programmatic dependent of the last hidden layer: the weights
+    // above are not that layer's output; its activations are read after this
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     const int ntx = W / IT_W, nty = (H + IT_H - 1) / IT_H, ntiles = B * nty * ntx;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int b = tile / (nty * ntx), r = tile - b * nty * ntx;
@@ -1086,8 +1091,9 @@ static int forward(ns_cnn* c, cudaStream_t st, int B, bool training = true, floa
         const long long tiles = (long long)B * ((c->H + IT_H - 1) / IT_H) * (c->W / IT_W);
         const int grid = grid_of(tiles, 1, 8 * c->num_sms);
         if (alast)
-            k_conv_out_tile<__nv_bfloat16><<<grid, OT_THREADS, 0, st>>>(alast, c->wb[NL - 1], c->p + c->boff[NL - 1],
-                                                                       c->pre[NL - 1], B, c->H, c->W, out_scale);
+            CNN_CUDA(c, launch_stage(k_conv_out_tile<__nv_bfloat16>, grid, OT_THREADS, (size_t)0, st,
+                                     (const __nv_bfloat16*)alast, (const __nv_bfloat16*)c->wb[NL - 1],
+                                     (const float*)(c->p + c->boff[NL - 1]), c->pre[NL - 1], B, c->H, c->W, out_scale));
         else
             k_conv_out_tile<float><<<grid, OT_THREADS, 0, st>>>(c->act[NL - 2], c->wb[NL - 1], c->p + c->boff[NL - 1],
                                                                c->pre[NL - 1], B, c->H, c->W, out_scale);

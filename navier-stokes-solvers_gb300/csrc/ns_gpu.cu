@@ -1524,19 +1524,19 @@ int ns_gpu_vorticity_device(ns_gpu* g, float* omega_dev) {
     return g->prec == NS_GPU_FP64 ? vorticity_t<double>(g, omega_dev) : vorticity_t<float>(g, omega_dev);
 }
 
+// W0 += the forward transform of the float field delta (kept modes), and the
+// next step's stage-1 fields from the new W0 in the same column pass (COL_ADD):
+// two kernels, where an exported spectrum, an add and a separate prologue took four
 template <typename T> static int add_vorticity_t(ns_gpu* g, const float* delta) {
     RowArgs<T> a = row_args<T>(g);
     a.in_f32 = delta;  // the row pass reads the float field directly
     NSG_TRY(row_launch<T, ROW_FWD1>(g, a));
-    NSG_CUDA(g, cudaMemsetAsync(g->spec[0], 0, spec_bytes(g), g->st));
     ColArgs<T> c = col_args<T>(g);
-    c.out_spec = g->spec[0];
     c.out_scale = 1.0 / ((double)g->g.nx * (double)g->g.ny);
-    NSG_TRY((col_launch<T, COL_FWD_EXPORT, 0>(g, c)));
-    const long long nk = (long long)g->g.Kx * g->g.Ky;
-    k_add_kept<T><<<grid_for(nk), 256, 0, g->st>>>(g->g, g->spec[0], (Cx<T>*)g->W0);
-    NSG_LAUNCHED(g);
-    g->fields_valid = 0;
+    c.psi_from_w = 1;
+    c.nfields = 4;
+    NSG_TRY((col_launch<T, COL_ADD, 0>(g, c)));
+    g->fields_valid = 1;
     g->psi0_valid = 0;
     return NS_GPU_OK;
 }

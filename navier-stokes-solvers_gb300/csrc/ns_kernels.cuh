@@ -498,11 +498,15 @@ __global__ void __launch_bounds__(256) k_row(Geo g, RowArgs<T> a) {
 }
 
 // ============================================================ column kernel
-enum { COL_STAGE = 0, COL_PROLOGUE = 1, COL_INV1 = 2, COL_FWD_EXPORT = 3, COL_NL_EXPORT = 4 };
+// COL_ADD: forward y-transforms of the G rows (a real field's x-transform),
+// W0 += (scaled) spectrum on the kept modes, then the stage-1 fields of the new
+// W0 (as COL_PROLOGUE with psi from W0): a correction added and the fields ready
+// in one pass
+enum { COL_STAGE = 0, COL_PROLOGUE = 1, COL_INV1 = 2, COL_FWD_EXPORT = 3, COL_NL_EXPORT = 4, COL_ADD = 5 };
 // thread groups per column block of the column pass (the modes with several
 // inverse-transformed fields)
 __host__ __device__ inline int col_groups(int fpc, int E, int mode) {
-    return (fpc && (mode == COL_STAGE || mode == COL_PROLOGUE)) ? 4 : 1;
+    return (fpc && (mode == COL_STAGE || mode == COL_PROLOGUE || mode == COL_ADD)) ? 4 : 1;
 }
 
 template <typename T> struct ColArgs {
@@ -754,7 +758,7 @@ __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, cons
         }
     }
 
-    if (MODE == COL_STAGE || MODE == COL_FWD_EXPORT || MODE == COL_NL_EXPORT) {
+    if (MODE == COL_STAGE || MODE == COL_FWD_EXPORT || MODE == COL_NL_EXPORT || MODE == COL_ADD) {
         for (int idx = threadIdx.x; idx < ny * CW; idx += nthr) {
             int y, c;
             if (g.fTG) { c = idx / ny; y = idx - c * ny; } else { y = idx / CW; c = idx - y * CW; }
@@ -776,6 +780,22 @@ __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, cons
                 a.out_spec[(size_t)j * g.nkx + i] = make_double2((double)(v.x * sc), (double)(v.y * sc));
             }
             return;
+        } else if constexpr (MODE == COL_ADD) {
+            // the scaled value rounded in T, the sum formed in double and rounded once to
+            // T (the roundings of an FP64 export added to the state)
+            const T sc = (T)a.out_scale;
+            for (int idx = threadIdx.x; idx < CW * Ky; idx += nthr) {
+                const int c = idx / Ky, jj = idx - c * Ky, i = c0 + c;
+                if (i >= Kx) continue;
+                const int j = kept_j(g, jj);
+                const C v = sm[c * LP + spad(j)];
+                const size_t s = (size_t)i * Ky + jj;
+                C w = a.W0[s];
+                w.x = (T)((double)w.x + (double)(v.x * sc));
+                w.y = (T)((double)w.y + (double)(v.y * sc));
+                a.W0[s] = w;
+            }
+            __syncthreads();  // the inverse phase reads W0 of every column of the block
         } else {
             const double dt = s_dt;
             const StageCoef<T> q = stage_coef<T>(a.sp, dt);
@@ -822,7 +842,7 @@ __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, cons
     if constexpr (MODE == COL_FWD_EXPORT || MODE == COL_NL_EXPORT) return;
 
     // inverse y-transforms of the next-stage fields
-    const int nf = (MODE == COL_INV1) ? 1 : (MODE == COL_PROLOGUE ? a.nfields : 4);
+    const int nf = (MODE == COL_INV1) ? 1 : (MODE == COL_PROLOGUE ? a.nfields : 4);  // COL_ADD: 4
     const C* src = (MODE == COL_STAGE) ? ((STAGE == 4) ? a.W0 : a.WS) : a.W0;
     for (int f = fg; f < nf; f += P) {
         for (int idx = u; idx < CW * ny; idx += GT) {
@@ -1527,18 +1547,6 @@ __global__ void k_filter(Geo gf, const typename CT<T>::C* Wf, Geo gc, typename C
 }
 
 // W[kept] += spec[j][i] (an FP64 half spectrum in the reference layout)
-template <typename T>
-__global__ void k_add_kept(Geo g, const double2* spec, typename CT<T>::C* W) {
-    const long long n = (long long)g.Kx * g.Ky;
-    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(idx / g.Ky), jj = (int)(idx - (long long)i * g.Ky);
-        const double2 a = spec[(size_t)kept_j(g, jj) * g.nkx + i];
-        typename CT<T>::C w = W[idx];
-        w.x = (T)((double)w.x + a.x);
-        w.y = (T)((double)w.y + a.y);
-        W[idx] = w;
-    }
-}
 
 
 #endif  // NSG_NO_AUX_KERNELS

@@ -308,3 +308,39 @@ def test_host_step_rewrites_what_the_reference_rewrites(nsgb, port):
     for name in ("u", "v", "omega"):
         assert rel_l2(gpu.real(name), ora.real(name)) <= 1e-12, name
     assert gpu.d.t == ora.d.t
+
+
+@pytest.mark.parametrize("prec,tol", [(0, 1e-12), (1, 2e-6)])
+def test_add_vorticity_device_then_advance(nsgb, prec, tol):
+    """ns_gpu_add_vorticity_device adds the masked forward transform of a float
+    field to the state and leaves the next step's fields ready: the spectrum
+    matches numpy's rfft2 on the kept modes, and two steps from there match two
+    steps of an instance that was given the same spectrum by upload."""
+    torch = pytest.importorskip("torch")
+    nx, ny = 64, 48
+    g = nsgb.Gpu(nx, ny, 2 * np.pi, 2 * np.pi, prec)
+    g.set_params(Re=500.0, dt=2e-3, adaptive_dt=0)
+    g.random_spectrum(3, 4.0, 0.5)
+    w0 = g.download(("omega_hat",))["omega_hat"]
+    delta = np.random.default_rng(5).standard_normal((ny, nx)).astype(np.float32)
+    d = torch.from_numpy(delta).cuda()
+    g.check(g.lib.ns_gpu_add_vorticity_device(g.h, C.c_void_p(d.data_ptr())), "add_vorticity_device")
+    w1 = g.download(("omega_hat",))["omega_hat"]
+    kx_kept, ky_kept = g.dims()
+    kyh = (ky_kept - 1) // 2
+    rows = np.r_[0:kyh + 1, ny - kyh:ny]
+    ref = np.fft.rfft2(delta.astype(np.float64)) / (nx * ny)
+    kept = np.zeros(w0.shape, dtype=bool)
+    kept[np.ix_(rows, np.arange(kx_kept))] = True
+    assert rel_l2(w1[kept], (w0 + ref)[kept]) <= tol
+    assert np.array_equal(w1[~kept], w0[~kept])
+    h = nsgb.Gpu(nx, ny, 2 * np.pi, 2 * np.pi, prec)
+    h.set_params(Re=500.0, dt=2e-3, adaptive_dt=0)
+    h.upload(w1, dt=2e-3)  # the upload also sets the step's dt
+    g.advance(2)
+    h.advance(2)
+    a = g.download(("omega_hat",))["omega_hat"]
+    b = h.download(("omega_hat",))["omega_hat"]
+    assert rel_l2(a, b) <= tol
+    g.close()
+    h.close()
