@@ -63,12 +63,15 @@ __device__ __forceinline__ int wrapm(int i, int n) {
 template <typename V>
 __device__ __forceinline__ void pad_put(__nv_bfloat16* P, int b, int y, int x, int H, int W, int off, V v) {
     unsigned char* base = reinterpret_cast<unsigned char*>(P) + off;
-    const int ys[2] = {y + 1, y == 0 ? H + 1 : 0};
-    const int xs[2] = {x + 1, x == 0 ? W + 1 : 0};
-    const int ny = (y == 0 || y == H - 1) ? 2 : 1, nx = (x == 0 || x == W - 1) ? 2 : 1;
-    for (int i = 0; i < ny; ++i)
-        for (int j = 0; j < nx; ++j)
-            *reinterpret_cast<V*>(base + (((size_t)b * (H + 2) + ys[i]) * (W + 2) + xs[j]) * 128) = v;
+    *reinterpret_cast<V*>(base + (((size_t)b * (H + 2) + y + 1) * (W + 2) + x + 1) * 128) = v;
+    if (x == 0 || x == W - 1 || y == 0 || y == H - 1) {  // border pixel: its periodic copies
+        const int ys[2] = {y + 1, y == 0 ? H + 1 : 0};
+        const int xs[2] = {x + 1, x == 0 ? W + 1 : 0};
+        const int ny = (y == 0 || y == H - 1) ? 2 : 1, nx = (x == 0 || x == W - 1) ? 2 : 1;
+        for (int i = 0; i < ny; ++i)
+            for (int j = 0; j < nx; ++j)
+                if (i | j) *reinterpret_cast<V*>(base + (((size_t)b * (H + 2) + ys[i]) * (W + 2) + xs[j]) * 128) = v;
+    }
 }
 // GELU in the tanh form of Hendrycks and Gimpel (2016),
 // 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))), with the hardware tanh
