@@ -115,18 +115,17 @@ def gelu_tanh(x):
 
 def forward(params, inputs, s0=1.0, s1=1.0, so=1.0, bf16_hidden_inputs=False, inference=False):
     """Network output; bf16_hidden_inputs rounds the inputs of the four 64 -> 64
-    layers to bfloat16, as the library's tensor-core training path stores them.
-    inference: the library's tensor-core inference path, which stores every hidden
-    activation (the inputs of layers 1-5) as bfloat16 and applies GELU in its tanh
-    form to all of them."""
+    layers to bfloat16, as the library's tensor-core path stores them.
+    inference: the library's tensor-core inference path, which also applies GELU
+    in its tanh form to the activations it stores as bfloat16 (the outputs of
+    layers 0-3; the last hidden layer keeps the erf form and FP32)."""
     layers = [(bf16(w), b) for w, b in unflatten(np.asarray(params, dtype=np.float64))]
     x = np.stack([inputs[:, 0] * s0, inputs[:, 1] * s1], axis=-1).astype(np.float64)
     bf16_hidden_inputs = bf16_hidden_inputs or inference
-    last_in = len(layers) - 1 if inference else len(layers) - 2
     for l, (w, b) in enumerate(layers):
-        if bf16_hidden_inputs and 1 <= l <= last_in:
+        if bf16_hidden_inputs and 1 <= l <= len(layers) - 2:
             x = bf16(x.astype(np.float32))
         x = conv(x, w, b)
         if l < len(layers) - 1:
-            x = gelu_tanh(x) if inference else gelu(x)
+            x = gelu_tanh(x) if (inference and l <= len(layers) - 3) else gelu(x)
     return x[..., 0] / so

@@ -94,8 +94,9 @@ def test_tensor_core_layers_match_oracle_with_bf16_activations(nsgb, H):
     """W = 128: the four 64 -> 64 layers run on tcgen05 (BF16 operands, FP32
     accumulation in tensor memory); the oracle rounds the same activations to BF16.
     forward() runs the inference path of correct_step (first layer straight to BF16,
-    every hidden activation stored as BF16 after GELU in its tanh form).  H = 24
-    gives the tiled first and output layers several row bands per image."""
+    GELU in its tanh form on the BF16 activations; the last hidden activation FP32
+    with the erf form).  H = 24 gives the tiled first and output layers several row
+    bands per image."""
     W, B = 128, 2
     net = nsgb.Corrector(H, W, max_batch=2, seed=4)
     p = rand_params(21).astype(np.float32)
@@ -104,14 +105,14 @@ def test_tensor_core_layers_match_oracle_with_bf16_activations(nsgb, H):
     x = rng.standard_normal((B, 2, H, W)).astype(np.float32)
     out_tc = net.forward(x)
     ref = CO.forward(p.astype(np.float64), x.astype(np.float64), inference=True)
-    # 5e-3: the hardware tanh approximation (relative error about 2^-11) moves some
-    # activations across a BF16 rounding boundary, one BF16 ulp (2^-8) each, and
-    # the last hidden layer's flips reach the output without a further layer to
-    # average them (measured 2.9e-3 at H = 8)
-    assert np.linalg.norm(out_tc - ref) / np.linalg.norm(ref) <= 5e-3
-    # against the erf form with FP32 output-layer inputs, the tanh form and the
-    # BF16 last hidden activation move the output by about the BF16 rounding of
-    # the activations (the whole BF16 path is held to 2e-2 of the FP32 SIMT path below)
+    # 3e-3: the hardware tanh (relative error about 2^-11) moves a few activations
+    # across a BF16 rounding boundary (one BF16 ulp, 2^-8, each); the resulting
+    # output error is noise of that size, measured 2.0e-3 at H = 24
+    err = np.linalg.norm(out_tc - ref) / np.linalg.norm(ref)
+    assert err <= 3e-3, err
+    # against the erf form the tanh form moves the output by less than the BF16
+    # rounding of the activations does (the whole BF16 path is held to 2e-2 of the
+    # FP32 SIMT path below)
     ref_erf = CO.forward(p.astype(np.float64), x.astype(np.float64), bf16_hidden_inputs=True)
     assert np.linalg.norm(out_tc - ref_erf) / np.linalg.norm(ref_erf) <= 1e-2
     net.set_tensor_cores(False)
