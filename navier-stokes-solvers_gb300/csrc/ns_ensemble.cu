@@ -581,7 +581,7 @@ extern "C" int ns_gpu_ensemble_autotune(ns_gpu_ensemble* e, int steps, const cha
     bool any = false;
     const int threads[] = {64, 128, 256};
     const int radix[] = {4, 16};
-    const int clusters[] = {1, 2, 4};
+    const int clusters[] = {1, 2, 4, 8};
     for (int th : threads)
         for (int er : radix)
             for (int ec : radix)
