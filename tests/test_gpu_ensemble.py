@@ -110,7 +110,7 @@ def test_autotune_picks_a_valid_tiling_and_caches_it(nsgb, tmp_path):
         setup_member(m, n, 3 + i)
     cache = str(tmp_path / "tune.jsonl")
     best, ms = ens.autotune(steps=1, cache_path=cache)
-    assert ms > 0 and best[0] % 32 == 0 and best[1] in (4, 16) and best[2] in (4, 16) and best[3] in (1, 2, 4)
+    assert ms > 0 and best[0] % 32 == 0 and best[1] in (4, 16) and best[2] in (4, 16) and best[3] in (1, 2, 4, 8)
     assert os.path.exists(cache) and "row_radix" in open(cache).read()
     best2, ms2 = ens.autotune(steps=1, cache_path=cache)  # cache hit: same answer, no timing
     assert best2 == best and ms2 == pytest.approx(ms, rel=1e-5)
