@@ -110,8 +110,10 @@ typedef struct {
  * generic stage kernels at every size (also at 2048 and 4096); the radix applies
  * to power-of-two transform lengths (others run the mixed-radix bodies).
  * NS_GPU_ERR_INVALID (reason on stderr) when the tiling cannot run: CTAs above
- * 256 (row) / 512 (column) threads, field groups that are not whole warps,
- * shared memory above the device's limit. */
+ * 256 (row) / 512 (column) threads, row field groups that are neither whole
+ * warps nor a divisor of a warp, column field groups (cols_per_cta times the
+ * transform's threads) that are not whole warps, shared memory above the
+ * device's limit. */
 int ns_gpu_create_tiled(int nx, int ny, double Lx, double Ly, int precision, const ns_gpu_tiling *tiling,
                         ns_gpu **out);
 /* The tiling an instance runs with (every field resolved; radix 0 = mixed radix;

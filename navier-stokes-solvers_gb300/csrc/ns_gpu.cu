@@ -622,19 +622,25 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
     g->EC = mr_col ? 0 : (kc && kc->ec) ? kc->ec : (ny >= 512 ? 16 : 4);
     const size_t cs = (precision == NS_GPU_FP64) ? sizeof(double2) : sizeof(float2);
     // fields in parallel (a thread group per field): automatic when the
-    // transforms are short (TT / TC of one or two warps) and too few to give
-    // the SMs more than a few warps each one after another
-    // (FP64 only for one-warp transforms: at 768^2 its two-warp groups were slower)
+    // transforms are short (row groups of at most two warps, column groups of at
+    // most four) and too few to give the SMs more than a few warps each one after
+    // another: 64 warps per SM in FP32, 8 in FP64 (timed on GB300 from 32^2 to
+    // 1024^2: FP64 768^2 rows, 49152 threads of 64-thread transforms, ran 2 %
+    // slower with groups, 384^2 columns 23 % faster).  Row groups narrower than a
+    // warp share warps (TT divides 32); column groups narrower than a warp take
+    // 32 / TC columns each, so that they are whole warps.
     const int TTp = g->ER ? G.H / g->ER : G.TTr, TCp = g->EC ? ny / g->EC : G.TTc;
-    const int gmax = precision == NS_GPU_FP32 ? 64 : 32;
-    G.fpr = (kc && kc->fpr) ? (kc->fpr > 0) : (TTp % 32 == 0 && TTp <= gmax && (long long)ny * TTp < 64LL * 32 * g->num_sms);
-    G.fpc = (kc && kc->fpc) ? (kc->fpc > 0) : (TCp % 32 == 0 && TCp <= gmax && (long long)G.Kx * TCp < 64LL * 32 * g->num_sms);
+    const long long busy = (precision == NS_GPU_FP32 ? 64LL : 8LL) * 32 * g->num_sms;
+    const bool row_fits = TTp % 32 == 0 || 32 % TTp == 0;
+    const bool col_fits = TCp % 32 == 0 || (32 % TCp == 0 && G.Kx >= 32 / TCp);
+    G.fpr = (kc && kc->fpr) ? (kc->fpr > 0) : (row_fits && TTp <= 64 && (long long)ny * TTp < busy);
+    G.fpc = (kc && kc->fpc) ? (kc->fpc > 0) : (col_fits && TCp <= 128 && (long long)G.Kx * TCp < busy);
     // column tile width: up to 16 columns, <= 512 threads, <= ~100 KB shared memory
     {
         const int TC = g->EC ? ny / g->EC : G.TTc;
         const int P = G.fpc ? 4 : 1;
         const int nbuf = g->EC ? P : 2 * P;
-        int CW = 1;
+        int CW = (G.fpc && TC < 32) ? 32 / TC : 1;
         // with a group per field a column block is already four groups: widen it
         // only while that still leaves two blocks per SM
         while (CW < 16 && 2 * CW * TC * P <= 512 && (size_t)nbuf * 2 * CW * spad_len(ny) * cs <= 100 * 1024 && CW < G.Kx &&
@@ -656,14 +662,15 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
         int RPC = 1;
         while (2 * RPC * TT * P <= budget && 2 * RPC <= ny && ny % (2 * RPC) == 0 &&
                (size_t)nbuf * 2 * RPC * spad_len(G.H) * cs <= 100 * 1024 && ny / (2 * RPC) >= g->num_sms &&
-               (TT == 32 || !G.fpr || 2 * RPC * P <= 15))
+               (TT <= 32 || !G.fpr || 2 * RPC * P <= 15))
             RPC *= 2;
         if (kc && kc->rpc) RPC = kc->rpc;
         G.RPC = RPC;
     }
-    // a group per field needs whole warps per group, at most 256 (row) / 512
-    // (column) threads per CTA, and at most 15 named barriers per CTA
-    if (G.fpr && !(TTp % 32 == 0 && G.RPC * 4 * TTp <= 256 && (TTp == 32 || G.RPC * 4 <= 15))) {
+    // a group per field needs row groups of whole warps or of a divisor of a warp,
+    // column groups of whole warps, at most 256 (row) / 512 (column) threads per
+    // CTA, and at most 15 named barriers per CTA (groups wider than a warp)
+    if (G.fpr && !((TTp % 32 == 0 || 32 % TTp == 0) && G.RPC * 4 * TTp <= 256 && (TTp <= 32 || G.RPC * 4 <= 15))) {
         fprintf(stderr, "ns_gpu_create: nx=%d ny=%d: the row pass cannot run a thread group per field with this tiling\n",
                 nx, ny);
         cudaStreamDestroy(g->st);

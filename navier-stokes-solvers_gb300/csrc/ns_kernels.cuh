@@ -264,9 +264,10 @@ template <int MODE> struct RowNF { static const int v = (MODE == ROW_STAGE || MO
 // scratch (one sequence per group) when E = 0
 // body of the row pass for row block bx (rows bx*RPC .. bx*RPC + RPC - 1); the
 // block must have exactly RPC * P * TT threads.  With P > 1 (fields in parallel;
-// TT a multiple of 32, RPC * P <= 15 when TT > 32) group f of a row loads,
-// unpacks and inverse-transforms field f, the row's threads form the products
-// together, and group 0 makes the forward transform.
+// TT a multiple of 32 or a divisor of 32, RPC * P <= 15 when TT > 32) group f of a
+// row loads, unpacks and inverse-transforms field f, the row's threads form the
+// products together, and group 0 makes the forward transform (every group, on its
+// own copy, when TT < 32).
 // FG = false compiles the field-group logic out (callers that always run one
 // group per row, such as the persistent ensemble kernel)
 template <typename T, int E, int MODE, bool FG = true>
@@ -280,6 +281,9 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
     const int r = threadIdx.x / TQ, q = threadIdx.x - r * TQ;
     const int fg = q / TT, t = q - fg * TT;
     const int sy = sync_mode(TT, P > 1 ? 1 + r * P + fg : 0, TT);
+    // groups narrower than a warp all transform a copy of the product (their warp
+    // barriers stay uniform) and share its stores; wider groups leave both to group 0
+    const bool allfwd = P > 1 && TT < 32;
     const int y = bx * g.RPC + r;
     const int nx = g.nx, Kx = g.Kx;
     C* scr = sm + (NF * g.RPC + r * P + fg) * LP;  // mixed-radix scratch of this row and group (E = 0 only)
@@ -370,18 +374,22 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
             }
         }
         if (!oddx) __syncthreads();
+        if (P > 1) {
+            // one call site for every group: groups that share a warp (TT < 32) meet
+            // the same warp barriers in the same order
+            fft_any<E, true>(sm + (fg * g.RPC + r) * LP, scr, H, g.logH, g.rxa, g.rxb, g.nrx, t, TT, a.twr, sy);
+            __syncthreads();  // the loops below read every field of the row
+        } else {
 #pragma unroll
-        for (int f = 0; f < NF; ++f) {
-            if (P > 1 && f != fg) continue;
-            fft_any<E, true>(sm + (f * g.RPC + r) * LP, scr, H, g.logH, g.rxa, g.rxb, g.nrx, t, TT, a.twr, sy);
+            for (int f = 0; f < NF; ++f)
+                fft_any<E, true>(sm + (f * g.RPC + r) * LP, scr, H, g.logH, g.rxa, g.rxb, g.nrx, t, TT, a.twr, sy);
         }
-        if (P > 1) __syncthreads();  // the loops below read every field of the row
 
         if constexpr (MODE == ROW_STAGE || MODE == ROW_DUMP) {
             C* b0 = sm + (0 * g.RPC + r) * LP;
-            const C* b1 = sm + (1 * g.RPC + r) * LP;
-            const C* b2 = sm + (2 * g.RPC + r) * LP;
-            const C* b3 = sm + (3 * g.RPC + r) * LP;
+            C* b1 = sm + (1 * g.RPC + r) * LP;
+            C* b2 = sm + (2 * g.RPC + r) * LP;
+            C* b3 = sm + (3 * g.RPC + r) * LP;
             T vmax2 = (T)0;
             if (oddx) {
                 // one grid point per element (the real parts of the length-nx inverse)
@@ -397,7 +405,9 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
                         a.out_real[3][o] = p3;
                         a.out_real[4][o] = jv;
                     }
-                    b0[spad(m)] = cmake<C>(jv, 0.0);
+                    const C pj = cmake<C>(jv, 0.0);
+                    b0[spad(m)] = pj;
+                    if (allfwd) { b1[spad(m)] = pj; b2[spad(m)] = pj; b3[spad(m)] = pj; }
                 }
             }
             for (int m = oddx ? H : q; m < H; m += TQ) {
@@ -417,7 +427,9 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
                     a.out_real[3][o] = z3.x; a.out_real[3][o + 1] = z3.y;
                     a.out_real[4][o] = je;   a.out_real[4][o + 1] = jo;
                 }
-                b0[spad(m)] = cmake<C>(je, jo);
+                const C pj = cmake<C>(je, jo);
+                b0[spad(m)] = pj;
+                if (allfwd) { b1[spad(m)] = pj; b2[spad(m)] = pj; b3[spad(m)] = pj; }
             }
             if (a.cfl) {
                 double v = (double)vmax2;
@@ -429,8 +441,8 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
                 }
             }
             __syncthreads();
-            if (P > 1 && fg != 0) return;  // group 0 transforms the product and stores it
-            fft_any<E, false>(b0, scr, H, g.logH, g.rxa, g.rxb, g.nrx, t, TT, a.twr, sy);
+            if (P > 1 && fg != 0 && !allfwd) return;  // group 0 transforms the product and stores it
+            fft_any<E, false>(sm + (fg * g.RPC + r) * LP, scr, H, g.logH, g.rxa, g.rxb, g.nrx, t, TT, a.twr, sy);
         } else {
             const C* b0 = sm + (0 * g.RPC + r) * LP;
             if (oddx) {
@@ -472,14 +484,17 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
     // forward post-processing: X[k] = E[k] + exp(-2 pi i k/nx) O[k],
     // E = (W[k] + conj W[H-k])/2, O = (W[k] - conj W[H-k])/(2i), for the kept k < Kx
     {
-        const C* b0 = sm + r * LP;
+        // this group's transformed row; with allfwd every group holds the same
+        // transform and stores its share k = q, q + P TT, ...
+        const C* b0 = sm + (fg * g.RPC + r) * LP;
+        const int k0 = allfwd ? q : t, ks = allfwd ? TQ : TT;
         C* dst = a.G;
         if (oddx) {  // the length-nx transform of the real row: X[k] directly
-            for (int k = t; k < Kx; k += TT) dst[gidx(g, y, k)] = b0[spad(k)];
+            for (int k = k0; k < Kx; k += ks) dst[gidx(g, y, k)] = b0[spad(k)];
             return;
         }
         const T half = (T)0.5;
-        for (int k = t; k < Kx; k += TT) {
+        for (int k = k0; k < Kx; k += ks) {
             const C wa = b0[spad(k)];
             const C wb = b0[spad(k == 0 ? 0 : H - k)];
             C ev, od;

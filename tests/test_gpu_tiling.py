@@ -8,14 +8,18 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _run(nsgb, n, ny, prec, tiling, steps=6):
+def _run(nsgb, n, ny, prec, tiling, steps=6, physical=False):
     g = nsgb.Gpu(n, ny, 2 * np.pi, 2 * np.pi, prec, tiling=tiling)
     g.set_params(Re=2000.0, cfl_factor=0.4, adaptive_dt=1, hv_enabled=1, hv_coefficient=1e-6, hv_order=4,
                  hv_cutoff_ratio=0.0, forcing_enabled=1, forcing_kmin=2.0, forcing_kmax=4.0, forcing_epsilon=1e-3,
                  forcing_seed=11)
     g.random_spectrum(5, 4.0, 0.5)
     g.advance(steps)
-    out = g.download(("omega_hat",))["omega_hat"]
+    if physical:
+        d = g.download(("omega_hat", "u", "v", "omega"))
+        out = np.concatenate([d["omega_hat"].view(np.float64).ravel()] + [d[k].ravel() for k in ("u", "v", "omega")])
+    else:
+        out = g.download(("omega_hat",))["omega_hat"]
     t = g.tiling()
     g.close()
     return out, t
@@ -28,6 +32,23 @@ def test_field_groups_bit_identical(nsgb, prec, n, ny, er, ec):
     a, ta = _run(nsgb, n, ny, prec, dict(base, row_field_groups=-1, col_field_groups=-1))
     b, tb = _run(nsgb, n, ny, prec, dict(base, row_field_groups=1, col_field_groups=1))
     assert ta["row_field_groups"] == -1 and tb["row_field_groups"] == 1 and tb["col_field_groups"] == 1
+    assert np.isfinite(a).all()
+    assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("n,rpc", [(32, 1), (64, 1), (64, 2), (128, 1), (128, 4)])
+def test_field_groups_narrower_than_a_warp(nsgb, prec, n, rpc):
+    """Row transforms of 4, 8 and 16 threads (radix 4 at 32^2 .. 128^2): the four
+    groups of a row share warps, every group transforms its own copy of the
+    product and stores a quarter of it; column groups of 8 or 16 threads take 4 or
+    2 columns each.  The velocity download runs the three-field row pass (three
+    groups per row)."""
+    base = dict(row_radix=4, col_radix=4, rows_per_cta=rpc)
+    a, _ = _run(nsgb, n, n, prec, dict(base, row_field_groups=-1, col_field_groups=-1), physical=True)
+    b, tb = _run(nsgb, n, n, prec, dict(base, row_field_groups=1, col_field_groups=1), physical=True)
+    assert tb["row_field_groups"] == 1 and tb["col_field_groups"] == 1 and tb["rows_per_cta"] == rpc
+    assert tb["cols_per_cta"] * (n // 4) % 32 == 0
     assert np.isfinite(a).all()
     assert np.array_equal(a, b)
 
