@@ -45,7 +45,48 @@ struct EnsMember {
     int nrb;               // row blocks: ny / RPC
     int ncb;               // column blocks: ceil(Kx / CW)
     int adaptive;          // device-side CFL dt
+    int fold;              // N: the geometry equals fold_geo<N> (bodies with constant sizes), 0: as stored
 };
+
+constexpr int clog2(int n) { return n <= 1 ? 0 : 1 + clog2(n / 2); }
+
+// The geometry of a side-N member (N a power of two) under the 256-thread tiling of
+// radix ER rows and EC columns, with kept columns padded to 64: every field the
+// stage bodies read is a compile-time constant.  Inlined into the generic bodies it
+// turns their loop bounds, divisions and index arithmetic into constants.  The host
+// enables it for a member only when the member's own geometry has exactly these
+// values (fold_matches), so the arithmetic is unchanged.
+template <int N, int ER, int EC>
+__host__ __device__ __forceinline__ void fold_geo(Geo& g) {
+    constexpr int H = N / 2, nkx = N / 2 + 1, Kx = (2 * nkx) / 3 + 1, Kyh = (2 * N) / 6;
+    g.nx = N;
+    g.ny = N;
+    g.nkx = nkx;
+    g.nky = N;
+    g.H = H;
+    g.Kx = Kx;
+    g.Kxp = ((Kx + 63) / 64) * 64;
+    g.Kyh = Kyh;
+    g.Ky = 2 * Kyh + 1;
+    g.logny = clog2(N);
+    g.logH = clog2(H);
+    g.CW = 256 / (N / EC);
+    g.RPC = 256 / (H / ER);
+    g.fLB = 0;
+    g.fTG = 0;
+    g.oddx = 0;
+    g.fpr = 0;
+    g.fpc = 0;
+}
+
+template <int N, int ER, int EC> bool fold_matches(const Geo& g) {
+    Geo f = g;
+    fold_geo<N, ER, EC>(f);
+    return f.nx == g.nx && f.ny == g.ny && f.nkx == g.nkx && f.nky == g.nky && f.H == g.H && f.Kx == g.Kx &&
+           f.Kxp == g.Kxp && f.Kyh == g.Kyh && f.Ky == g.Ky && f.logny == g.logny && f.logH == g.logH &&
+           f.CW == g.CW && f.RPC == g.RPC && f.fLB == g.fLB && f.fTG == g.fTG && f.oddx == g.oddx &&
+           f.fpr == g.fpr && f.fpc == g.fpc;
+}
 
 __device__ __forceinline__ unsigned cluster_ctarank() {
     unsigned r;
@@ -60,10 +101,36 @@ __device__ __forceinline__ void cluster_barrier() {
 }
 
 template <int EC, int STAGE>
-__device__ __forceinline__ void col_pass(const EnsMember& M, int r, int team) {
+__device__ __forceinline__ void col_pass(const Geo& g, const EnsMember& M, int r, int team) {
     for (int b = r; b < M.ncb; b += team) {
-        col_body<float, EC, COL_STAGE, STAGE, false>(M.g, M.ca, b);
+        col_body<float, EC, COL_STAGE, STAGE, false>(g, M.ca, b);
         __syncthreads();
+    }
+}
+
+// nsteps RK4 steps of member M by this CTA (rank r of a team of CTAs that split
+// its row and column blocks); N > 0: the member's geometry folded to constants
+template <int ER, int EC, int N>
+__device__ __forceinline__ void member_steps(const EnsMember& M, int shared, int team, int r, int nsteps) {
+    Geo g = M.g;
+    if constexpr (N > 0) fold_geo<N, ER, EC>(g);
+    for (int s = 0; s < nsteps; ++s) {
+#pragma unroll 1
+        for (int stage = 1; stage <= 4; ++stage) {
+            RowArgs<float> ra = M.ra;
+            ra.cfl = (stage == 1 && M.adaptive) ? 1 : 0;
+            ra.marker = stage == 1 ? 1 : (stage == 2 ? 2 : 0);
+            for (int b = r; b < M.nrb; b += team) {
+                row_body<float, ER, ROW_STAGE, false>(g, ra, b);
+                __syncthreads();
+            }
+            if (shared) cluster_barrier();
+            if (stage == 1) col_pass<EC, 1>(g, M, r, team);
+            else if (stage == 2) col_pass<EC, 2>(g, M, r, team);
+            else if (stage == 3) col_pass<EC, 3>(g, M, r, team);
+            else col_pass<EC, 4>(g, M, r, team);
+            if (shared) cluster_barrier();
+        }
     }
 }
 
@@ -88,24 +155,13 @@ __global__ void __launch_bounds__(ens_max_threads(ER, EC), ens_min_ctas(ER, EC))
         const int shared = code & 1;
         const int team = shared ? csize : 1;
         const int r = shared ? rank : 0;
-        for (int s = 0; s < nsteps; ++s) {
-#pragma unroll 1
-            for (int stage = 1; stage <= 4; ++stage) {
-                RowArgs<float> ra = M.ra;
-                ra.cfl = (stage == 1 && M.adaptive) ? 1 : 0;
-                ra.marker = stage == 1 ? 1 : (stage == 2 ? 2 : 0);
-                for (int b = r; b < M.nrb; b += team) {
-                    row_body<float, ER, ROW_STAGE, false>(M.g, ra, b);
-                    __syncthreads();
-                }
-                if (shared) cluster_barrier();
-                if (stage == 1) col_pass<EC, 1>(M, r, team);
-                else if (stage == 2) col_pass<EC, 2>(M, r, team);
-                else if (stage == 3) col_pass<EC, 3>(M, r, team);
-                else col_pass<EC, 4>(M, r, team);
-                if (shared) cluster_barrier();
-            }
+        // constant-size bodies for the radix-4 tiling's 64^2, 128^2 and 256^2 members
+        if constexpr (ER == 4 && EC == 4) {
+            if (M.fold == 64) { member_steps<ER, EC, 64>(M, shared, team, r, nsteps); continue; }
+            if (M.fold == 128) { member_steps<ER, EC, 128>(M, shared, team, r, nsteps); continue; }
+            if (M.fold == 256) { member_steps<ER, EC, 256>(M, shared, team, r, nsteps); continue; }
         }
+        member_steps<ER, EC, 0>(M, shared, team, r, nsteps);
     }
 }
 
@@ -142,9 +198,11 @@ bool member_tiling(int n, const ns_gpu_ensemble_config& c, NsgTiling* t) {
     return true;
 }
 
-size_t member_smem(int n, const NsgTiling& t) {
+// dynamic shared memory of a member's stage bodies: four row buffers per row of a
+// row block; a column block's buffers plus its next-stage state (cw x Ky modes)
+size_t member_smem(int n, int Ky, const NsgTiling& t) {
     const size_t row = (size_t)4 * t.rpc * spad_len(n / 2) * sizeof(float2);
-    const size_t col = (size_t)t.cw * spad_len(n) * sizeof(float2);
+    const size_t col = ((size_t)t.cw * spad_len(n) + (size_t)t.cw * Ky) * sizeof(float2);
     return row > col ? row : col;
 }
 
@@ -227,7 +285,13 @@ static int configure(ns_gpu_ensemble* e) {
         d.nrb = d.g.ny / t.rpc;
         d.ncb = (d.g.Kx + t.cw - 1) / t.cw;
         d.adaptive = g->p.adaptive_dt;
-        smem = std::max(smem, member_smem(e->n[i], t));
+        d.fold = 0;
+        if (c.threads == 256 && c.row_radix == 4 && c.col_radix == 4) {
+            if (e->n[i] == 64 && fold_matches<64, 4, 4>(d.g)) d.fold = 64;
+            else if (e->n[i] == 128 && fold_matches<128, 4, 4>(d.g)) d.fold = 128;
+            else if (e->n[i] == 256 && fold_matches<256, 4, 4>(d.g)) d.fold = 256;
+        }
+        smem = std::max(smem, member_smem(e->n[i], g->g.Ky, t));
     }
     e->smem = smem;
     if (smem > 48 * 1024) ENS_CUDA(e, cudaFuncSetAttribute(e->kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

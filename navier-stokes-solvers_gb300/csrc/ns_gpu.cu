@@ -62,7 +62,10 @@ template <typename T, int MODE> static int row_launch(ns_gpu* g, const RowArgs<T
 template <typename T, int E, int MODE, int STAGE> static int col_launch_e(ns_gpu* g, const ColArgs<T>& a) {
     const int TC = E ? g->g.ny / E : g->g.TTc;
     const int P = col_groups(g->g.fpc, E, MODE);
-    const size_t smem = (size_t)(E ? P : 2 * P) * g->g.CW * spad_len(g->g.ny) * sizeof(Cx<T>);
+    // the column buffers (and mixed-radix scratch), then the next-stage state of the
+    // block's kept modes for the stage and correction passes
+    const size_t wsm = (MODE == COL_STAGE || MODE == COL_ADD) ? (size_t)g->g.CW * g->g.Ky : 0;
+    const size_t smem = ((size_t)(E ? P : 2 * P) * g->g.CW * spad_len(g->g.ny) + wsm) * sizeof(Cx<T>);
     NSG_TRY(set_smem(g, k_col<T, E, MODE, STAGE>, smem));
     k_col<T, E, MODE, STAGE><<<g->g.Kxp / g->g.CW, P * g->g.CW * TC, smem, g->st>>>(g->g, a);
     NSG_LAUNCHED(g);
@@ -707,7 +710,7 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
         int optin = 0;
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, g->device);
         const size_t row_sm = (size_t)(g->ER ? 4 : 4 + (G.fpr ? 4 : 1)) * G.RPC * spad_len(G.H) * cs;
-        const size_t col_sm = (size_t)(g->EC ? 1 : 2) * (G.fpc ? 4 : 1) * G.CW * spad_len(ny) * cs;
+        const size_t col_sm = ((size_t)(g->EC ? 1 : 2) * (G.fpc ? 4 : 1) * G.CW * spad_len(ny) + (size_t)G.CW * G.Ky) * cs;
         if (optin > 0 && (row_sm > (size_t)optin || col_sm > (size_t)optin)) {
             fprintf(stderr,
                     "ns_gpu_create: nx=%d ny=%d: the stage kernels need %zu / %zu bytes of shared memory per CTA, above "

@@ -326,6 +326,30 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
             if (P > 1 && f != fg) continue;
             C* b = sm + (f * g.RPC + r) * LP;
             const C* src = a.F[f];
+            if constexpr (E > 0) {
+                // exactly E elements a thread (H = E TT): all loads in flight before
+                // the stores (the fields are L2 round trips on small grids)
+                C xv[E];
+#pragma unroll
+                for (int u = 0; u < E; ++u) {
+                    const int k = t + u * TT;
+                    C x = cmake<C>(0.0, 0.0);
+                    if (k < Kx) {
+                        x = src[fidx(g, y, k)];
+                        if (a.dx[f]) {
+                            const T kx = a.kxv[k];
+                            C d;
+                            d.x = -kx * x.y;
+                            d.y = kx * x.x;
+                            x = d;
+                        }
+                    }
+                    xv[u] = x;
+                }
+#pragma unroll
+                for (int u = 0; u < E; ++u) b[spad(t + u * TT)] = xv[u];
+                continue;
+            }
             for (int k = t; k < H; k += TT) {
                 const bool mirror = oddx && k >= g.nkx;
                 const int kk = mirror ? nx - k : k;
@@ -574,9 +598,9 @@ __device__ __forceinline__ C field_value(int f, C w, T kx, T ky) {
 }
 
 // FP64 shell test of mode (i, j): kmin <= |k| <= kmax, |k| > 0 (as the reference's k2)
-__device__ __forceinline__ bool forcing_in_shell(const Geo& g, int i, int j, double kmin, double kmax) {
-    const double kxd = 2.0 * 3.141592653589793 * i / g.Lx;
-    const double kyd = (j <= g.ny / 2) ? 2.0 * 3.141592653589793 * j / g.Ly : 2.0 * 3.141592653589793 * (j - g.ny) / g.Ly;
+__device__ __forceinline__ bool forcing_in_shell(double Lx, double Ly, int ny, int i, int j, double kmin, double kmax) {
+    const double kxd = 2.0 * 3.141592653589793 * i / Lx;
+    const double kyd = (j <= ny / 2) ? 2.0 * 3.141592653589793 * j / Ly : 2.0 * 3.141592653589793 * (j - ny) / Ly;
     const double k2d = kxd * kxd + kyd * kyd;
     const double km = sqrt(k2d);
     return k2d > 1e-12 && km >= kmin && km <= kmax;
@@ -585,13 +609,16 @@ __device__ __forceinline__ bool forcing_in_shell(const Geo& g, int i, int j, dou
 // white-in-time forcing increment of one kept mode: amp times the mode's noise
 // (the sum over this step's draws) when kmin <= |k| <= kmax.  With a noise table
 // the draws were made for the step by k_forcing_noise (in parallel, before the
-// step's first stage); otherwise they are drawn here (forcing_xi_sum).
-static __device__ __noinline__ double2 forcing_increment(const Geo& g, int i, int j, unsigned long long step, int M,
-                                                         unsigned long long seed, double kmin, double kmax, double amp,
-                                                         const double2* fnoise, int fkxr, int fkyr) {
-    if (!forcing_in_shell(g, i, j, kmin, kmax)) return make_double2(0.0, 0.0);
+// step's first stage); otherwise they are drawn here (forcing_xi_sum).  The
+// geometry comes by value (Lx, Ly, ny): a caller's Geo never escapes into this
+// out-of-line call, so its fields stay foldable constants where they are.
+static __device__ __noinline__ double2 forcing_increment(double Lx, double Ly, int ny, int i, int j,
+                                                         unsigned long long step, int M, unsigned long long seed,
+                                                         double kmin, double kmax, double amp, const double2* fnoise,
+                                                         int fkxr, int fkyr) {
+    if (!forcing_in_shell(Lx, Ly, ny, i, j, kmin, kmax)) return make_double2(0.0, 0.0);
     double2 xi;
-    const int ky = (j <= g.ny / 2) ? j : j - g.ny;
+    const int ky = (j <= ny / 2) ? j : j - ny;
     if (fnoise && i <= fkxr && ky >= -fkyr && ky <= fkyr) {
         const double2* t = fnoise + ((size_t)i * (2 * fkyr + 1) + (ky + fkyr)) * M;
         double sx = 0.0, sy = 0.0;
@@ -601,7 +628,7 @@ static __device__ __noinline__ double2 forcing_increment(const Geo& g, int i, in
         }
         xi = make_double2(sx, sy);
     } else {
-        xi = forcing_xi_sum(i, j, g.ny, step, M, seed);
+        xi = forcing_xi_sum(i, j, ny, step, M, seed);
     }
     return make_double2(amp * xi.x, amp * xi.y);
 }
@@ -706,8 +733,8 @@ __device__ __forceinline__ C post_step_mode(const Geo& g, const ColArgs<T>& a, i
     const T k2f = kx * kx + ky * ky;
     if (a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9 && k2f >= (T)(a.sp.f_kmin * a.sp.f_kmin * (1.0 - 1e-3)) &&
         k2f <= (T)(a.sp.f_kmax * a.sp.f_kmax * (1.0 + 1e-3))) {
-        const double2 df = forcing_increment(g, i, j, a.ds->step_cur, a.sp.fsub, a.sp.f_seed, a.sp.f_kmin, a.sp.f_kmax, f_amp,
-                                             a.fnoise, a.fkxr, a.fkyr);
+        const double2 df = forcing_increment(g.Lx, g.Ly, g.ny, i, j, a.ds->step_cur, a.sp.fsub, a.sp.f_seed,
+                                             a.sp.f_kmin, a.sp.f_kmax, f_amp, a.fnoise, a.fkxr, a.fkyr);
         if (df.x != 0.0 || df.y != 0.0) {
             wn.x = (T)((double)wn.x + df.x);
             wn.y = (T)((double)wn.y + df.y);
@@ -744,10 +771,13 @@ __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, cons
     const int sy = sync_mode(TC, P > 1 ? 1 + fg : 0, GT);
     const int c0 = bx * CW;
     const int Kx = g.Kx, Ky = g.Ky;
-    const int nthr = blockDim.x;
+    const int nthr = P * GT;  // the block size
     C* gbuf = sm + fg * CW * LP;  // this group's CW column buffers
     C* mybuf = gbuf + b * LP;
     C* myscr = sm + (P * CW + fg * CW + b) * LP;  // mixed-radix scratch of this group (E = 0 only)
+    // next-stage state of the block's kept modes, CW * Ky values (COL_STAGE, COL_ADD):
+    // the stage loop leaves it here for the inverse transforms of the fields
+    C* wsm = sm + (E == 0 ? 2 : 1) * P * CW * LP;
     __shared__ double s_dt;
 
     if (MODE == COL_STAGE) {
@@ -774,12 +804,25 @@ __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, cons
     }
 
     if (MODE == COL_STAGE || MODE == COL_FWD_EXPORT || MODE == COL_NL_EXPORT || MODE == COL_ADD) {
-        for (int idx = threadIdx.x; idx < ny * CW; idx += nthr) {
-            int y, c;
-            if (g.fTG) { c = idx / ny; y = idx - c * ny; } else { y = idx / CW; c = idx - y * CW; }
-            C v = cmake<C>(0.0, 0.0);
-            if (c0 + c < Kx) v = a.G[gidx(g, y, c0 + c)];
-            sm[c * LP + spad(y)] = v;
+        // four loads of G in flight per thread before their stores (L2 round trips)
+        for (int i0 = threadIdx.x; i0 < ny * CW; i0 += 4 * nthr) {
+            C v[4];
+            int o[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int idx = i0 + q * nthr;
+                v[q] = cmake<C>(0.0, 0.0);
+                o[q] = -1;
+                if (idx < ny * CW) {
+                    int y, c;
+                    if (g.fTG) { c = idx / ny; y = idx - c * ny; } else { y = idx / CW; c = idx - y * CW; }
+                    o[q] = c * LP + spad(y);
+                    if (c0 + c < Kx) v[q] = a.G[gidx(g, y, c0 + c)];
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (o[q] >= 0) sm[o[q]] = v[q];
         }
         __syncthreads();
         if (fg == 0) fft_any<E, false>(mybuf, myscr, ny, g.logny, g.rya, g.ryb, g.nry, t, TC, a.twc, sy);
@@ -809,6 +852,7 @@ __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, cons
                 w.x = (T)((double)w.x + (double)(v.x * sc));
                 w.y = (T)((double)w.y + (double)(v.y * sc));
                 a.W0[s] = w;
+                wsm[idx] = w;
             }
             __syncthreads();  // the inverse phase reads W0 of every column of the block
         } else {
@@ -823,30 +867,49 @@ __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, cons
                     sfd_a = sfd_a > 1.0 ? 1.0 : (sfd_a < 0.0 ? 0.0 : sfd_a);
                 }
             }
-            for (int idx = threadIdx.x; idx < CW * Ky; idx += nthr) {
-                const int c = idx / Ky, jj = idx - c * Ky, i = c0 + c;
-                if (i >= Kx) continue;
-                const int j = kept_j(g, jj);
-                const C gh = sm[c * LP + spad(j)];
-                const size_t s = (size_t)i * Ky + jj;
-                const C w0 = a.W0[s];
-                const C ws = (STAGE == 1) ? w0 : a.WS[s];
-                const C acc0 = (STAGE == 1) ? cmake<C>(0.0, 0.0) : a.ACC[s];
-                const T kx = a.kxv[i], ky = a.kyv[jj];
-                const T hw = a.sp.hv ? a.hvw[s] : (T)0;
-                T sw = (T)0;
-                C fb = cmake<C>(0.0, 0.0);
-                if (a.sp.sfd) {
-                    sw = a.sfdw[s];
-                    fb = a.SFD[s];
+            // two modes a thread per round: both modes' loads in flight before either
+            // mode's arithmetic and stores
+            for (int i0 = threadIdx.x; i0 < CW * Ky; i0 += 2 * nthr) {
+                C w0v[2], wsv[2], accv[2], fbv[2];
+                T hwv[2], swv[2];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int idx = i0 + h * nthr;
+                    const int c = idx / Ky, jj = idx - c * Ky, i = c0 + c;
+                    w0v[h] = wsv[h] = accv[h] = fbv[h] = cmake<C>(0.0, 0.0);
+                    hwv[h] = swv[h] = (T)0;
+                    if (idx >= CW * Ky || i >= Kx) continue;
+                    const size_t s = (size_t)i * Ky + jj;
+                    w0v[h] = a.W0[s];
+                    wsv[h] = (STAGE == 1) ? w0v[h] : a.WS[s];
+                    if (STAGE != 1) accv[h] = a.ACC[s];
+                    if (a.sp.hv) hwv[h] = a.hvw[s];
+                    if (a.sp.sfd) {
+                        swv[h] = a.sfdw[s];
+                        fbv[h] = a.SFD[s];
+                    }
                 }
-                const T k2 = k2sum(kx, ky);
-                C wn = a.sp.ifrk ? rk_stage_mode<T, STAGE, true>(q, gh, w0, ws, acc0, hw, sw, fb, k2, a.ACC, a.WS, s)
-                                 : rk_stage_mode<T, STAGE, false>(q, gh, w0, ws, acc0, hw, sw, fb, k2, a.ACC, a.WS, s);
-                if (STAGE == 4) {
-                    bool forced;
-                    wn = post_step_mode(g, a, i, j, s, wn, kx, ky, f_amp, sfd_a, forced);
-                    a.W0[s] = wn;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int idx = i0 + h * nthr;
+                    const int c = idx / Ky, jj = idx - c * Ky, i = c0 + c;
+                    if (idx >= CW * Ky || i >= Kx) continue;
+                    const int j = kept_j(g, jj);
+                    const C gh = sm[c * LP + spad(j)];
+                    const size_t s = (size_t)i * Ky + jj;
+                    const T kx = a.kxv[i], ky = a.kyv[jj];
+                    const T k2 = k2sum(kx, ky);
+                    C wn = a.sp.ifrk
+                               ? rk_stage_mode<T, STAGE, true>(q, gh, w0v[h], wsv[h], accv[h], hwv[h], swv[h], fbv[h], k2,
+                                                               a.ACC, a.WS, s)
+                               : rk_stage_mode<T, STAGE, false>(q, gh, w0v[h], wsv[h], accv[h], hwv[h], swv[h], fbv[h],
+                                                                k2, a.ACC, a.WS, s);
+                    if (STAGE == 4) {
+                        bool forced;
+                        wn = post_step_mode(g, a, i, j, s, wn, kx, ky, f_amp, sfd_a, forced);
+                        a.W0[s] = wn;
+                    }
+                    wsm[idx] = wn;
                 }
             }
             if (STAGE == 4 && bx == 0 && threadIdx.x == 0) a.ds->t = a.ds->t + dt;
@@ -868,6 +931,8 @@ __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, cons
                 const size_t s = (size_t)i * Ky + jk;
                 if (MODE == COL_INV1) {
                     v = src[s];
+                } else if (MODE == COL_STAGE || MODE == COL_ADD) {
+                    v = field_value<T, C>(f, wsm[c * Ky + jk], a.kxv[i], a.kyv[jk]);
                 } else if (MODE == COL_PROLOGUE && !a.psi_from_w && f < 2) {
                     const C p = a.PSI0[s];
                     v = p;
