@@ -48,7 +48,7 @@ struct EnsMember {
     int fold;              // N: the geometry equals fold_geo<N> (bodies with constant sizes), 0: as stored
 };
 
-constexpr int clog2(int n) { return n <= 1 ? 0 : 1 + clog2(n / 2); }
+__host__ __device__ constexpr int clog2(int n) { return n <= 1 ? 0 : 1 + clog2(n / 2); }
 
 // The geometry of a side-N member (N a power of two) under the 256-thread tiling of
 // radix ER rows and EC columns, with kept columns padded to 64: every field the
@@ -139,10 +139,12 @@ __device__ __forceinline__ void member_steps(const EnsMember& M, int shared, int
 // (its prologue and downloads, or a solo run with the same tiling) take at
 // most 256 threads per row block
 __host__ __device__ constexpr int ens_max_threads(int, int) { return 256; }
-// CTAs per SM the compiler budgets registers for: three for the radix-4 bodies
-// (at most 85 registers a thread; the members' small transforms are latency-bound,
-// so more resident warps pay), one for the radix-16 ones (16 values a thread)
-__host__ __device__ constexpr int ens_min_ctas(int er, int ec) { return (er == 4 && ec == 4) ? 3 : 1; }
+// CTAs per SM the compiler budgets registers for: five for the radix-4 bodies (at
+// most 51 registers a thread, some spilled to L1; the members' small transforms
+// are latency-bound, so more resident warps pay: 3, 4 and 5 CTAs per SM gave 0.658,
+// 0.592 and 0.582 ms per config-3 step on GB300), one for the radix-16 ones (16
+// values a thread)
+__host__ __device__ constexpr int ens_min_ctas(int er, int ec) { return (er == 4 && ec == 4) ? 5 : 1; }
 
 // work[w] = 2 * member + shared (1: the member is split over the CTA's cluster)
 template <int ER, int EC>

@@ -348,24 +348,24 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
                 }
 #pragma unroll
                 for (int u = 0; u < E; ++u) b[spad(t + u * TT)] = xv[u];
-                continue;
-            }
-            for (int k = t; k < H; k += TT) {
-                const bool mirror = oddx && k >= g.nkx;
-                const int kk = mirror ? nx - k : k;
-                C x = cmake<C>(0.0, 0.0);
-                if (kk < Kx) {
-                    x = src[fidx(g, y, kk)];
-                    if (a.dx[f]) {
-                        const T kx = a.kxv[kk];
-                        C d;
-                        d.x = -kx * x.y;
-                        d.y = kx * x.x;
-                        x = d;
+            } else {
+                for (int k = t; k < H; k += TT) {
+                    const bool mirror = oddx && k >= g.nkx;
+                    const int kk = mirror ? nx - k : k;
+                    C x = cmake<C>(0.0, 0.0);
+                    if (kk < Kx) {
+                        x = src[fidx(g, y, kk)];
+                        if (a.dx[f]) {
+                            const T kx = a.kxv[kk];
+                            C d;
+                            d.x = -kx * x.y;
+                            d.y = kx * x.x;
+                            x = d;
+                        }
+                        if (mirror) x.y = -x.y;
                     }
-                    if (mirror) x.y = -x.y;
+                    b[spad(k)] = x;
                 }
-                b[spad(k)] = x;
             }
         }
         __syncthreads();
