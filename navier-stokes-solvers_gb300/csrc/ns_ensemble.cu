@@ -48,8 +48,6 @@ struct EnsMember {
     int fold;              // N: the geometry equals fold_geo<N> (bodies with constant sizes), 0: as stored
 };
 
-__host__ __device__ constexpr int clog2(int n) { return n <= 1 ? 0 : 1 + clog2(n / 2); }
-
 // The geometry of a side-N member (N a power of two) under the 256-thread tiling of
 // radix ER rows and EC columns, with kept columns padded to 64: every field the
 // stage bodies read is a compile-time constant.  Inlined into the generic bodies it
@@ -58,23 +56,10 @@ __host__ __device__ constexpr int clog2(int n) { return n <= 1 ? 0 : 1 + clog2(n
 // values (fold_matches), so the arithmetic is unchanged.
 template <int N, int ER, int EC>
 __host__ __device__ __forceinline__ void fold_geo(Geo& g) {
-    constexpr int H = N / 2, nkx = N / 2 + 1, Kx = (2 * nkx) / 3 + 1, Kyh = (2 * N) / 6;
-    g.nx = N;
-    g.ny = N;
-    g.nkx = nkx;
-    g.nky = N;
-    g.H = H;
-    g.Kx = Kx;
-    g.Kxp = ((Kx + 63) / 64) * 64;
-    g.Kyh = Kyh;
-    g.Ky = 2 * Kyh + 1;
-    g.logny = clog2(N);
-    g.logH = clog2(H);
+    fold_sizes<N>(g);
+    g.Kxp = ((g.Kx + 63) / 64) * 64;
     g.CW = 256 / (N / EC);
-    g.RPC = 256 / (H / ER);
-    g.fLB = 0;
-    g.fTG = 0;
-    g.oddx = 0;
+    g.RPC = 256 / ((N / 2) / ER);
     g.fpr = 0;
     g.fpc = 0;
 }

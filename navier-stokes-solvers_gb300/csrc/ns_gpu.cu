@@ -5,6 +5,7 @@
 // reference's global fftw_cleanup in spectral_memory.c:100-103 has no
 // counterpart).  All work is issued on the instance stream; the host-array
 // entry points synchronise that stream before returning.
+#include <type_traits>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -49,8 +50,18 @@ template <typename T, int E, int MODE> static int row_launch_e(ns_gpu* g, const 
     const int P = row_groups(g->g.fpr, E, NF);
     // E = 0 (mixed radix): one scratch sequence per row after the NF field buffers
     const size_t smem = (size_t)(NF + (E ? 0 : P)) * g->g.RPC * spad_len(g->g.H) * sizeof(Cx<T>);
-    NSG_TRY(set_smem(g, k_row<T, E, MODE>, smem));
-    k_row<T, E, MODE><<<g->g.ny / g->g.RPC, g->g.RPC * P * TT, smem, g->st>>>(g->g, a);
+    void (*kern)(Geo, RowArgs<T>) = k_row<T, E, MODE>;
+    // the step's radix-4 row pass with the grid's size fields as constants
+    // (256^2 in FP32, 128^2 in FP64)
+    if constexpr (E == 4 && MODE == ROW_STAGE) {
+        if constexpr (std::is_same<T, float>::value) {
+            if (g->fold == 256) kern = k_row<T, E, MODE, 256>;
+        } else {
+            if (g->fold == 128) kern = k_row<T, E, MODE, 128>;
+        }
+    }
+    NSG_TRY(set_smem(g, kern, smem));
+    kern<<<g->g.ny / g->g.RPC, g->g.RPC * P * TT, smem, g->st>>>(g->g, a);
     NSG_LAUNCHED(g);
     return NS_GPU_OK;
 }
@@ -66,8 +77,16 @@ template <typename T, int E, int MODE, int STAGE> static int col_launch_e(ns_gpu
     // block's kept modes for the stage and correction passes
     const size_t wsm = (MODE == COL_STAGE || MODE == COL_ADD) ? (size_t)g->g.CW * g->g.Ky : 0;
     const size_t smem = ((size_t)(E ? P : 2 * P) * g->g.CW * spad_len(g->g.ny) + wsm) * sizeof(Cx<T>);
-    NSG_TRY(set_smem(g, k_col<T, E, MODE, STAGE>, smem));
-    k_col<T, E, MODE, STAGE><<<g->g.Kxp / g->g.CW, P * g->g.CW * TC, smem, g->st>>>(g->g, a);
+    void (*kern)(Geo, ColArgs<T>) = k_col<T, E, MODE, STAGE>;
+    if constexpr (E == 4 && MODE == COL_STAGE) {
+        if constexpr (std::is_same<T, float>::value) {
+            if (g->fold == 256) kern = k_col<T, E, MODE, STAGE, 256>;
+        } else {
+            if (g->fold == 128) kern = k_col<T, E, MODE, STAGE, 128>;
+        }
+    }
+    NSG_TRY(set_smem(g, kern, smem));
+    kern<<<g->g.Kxp / g->g.CW, P * g->g.CW * TC, smem, g->st>>>(g->g, a);
     NSG_LAUNCHED(g);
     return NS_GPU_OK;
 }
@@ -704,6 +723,10 @@ int nsg_create(int nx, int ny, double Lx, double Ly, int precision, const NsgTil
             return NS_GPU_ERR_INVALID;
         }
     }
+    // grids whose step kernels have a copy with the size fields as constants
+    g->fold = (precision == NS_GPU_FP32 && fold_sizes_match<256>(G))   ? 256
+              : (precision == NS_GPU_FP64 && fold_sizes_match<128>(G)) ? 128
+                                                                       : 0;
     // the stage kernels' shared memory must fit one CTA (odd nx near the upper
     // bound needs the full length-nx row in five buffers)
     {

@@ -18,6 +18,7 @@ struct ns_gpu {
     Geo g;
     int prec;
     int ER, EC;
+    int fold;  // N: the step's radix-4 stage kernels run with the N x N size fields as constants (fold_sizes)
     int device;
     int num_sms;
     int fast_row;       // radix-32 warp row kernel (nx = 2048)

@@ -51,6 +51,37 @@ struct Geo {
     int fpr, fpc;
 };
 
+__host__ __device__ constexpr int clog2(int n) { return n <= 1 ? 0 : 1 + clog2(n / 2); }
+
+// The size fields of a square N x N grid (N a power of two, generic stage bodies)
+// as compile-time constants; the tiling fields (CW, RPC, Kxp, fpr, fpc) stay as
+// stored.  Inlined into the stage bodies it turns their loop bounds, divisions and
+// index arithmetic into constants.  Used only for a geometry whose stored values
+// equal these (fold_sizes_match), so the arithmetic is unchanged.
+template <int N> __host__ __device__ __forceinline__ void fold_sizes(Geo& g) {
+    constexpr int nkx = N / 2 + 1, Kx = (2 * nkx) / 3 + 1, Kyh = (2 * N) / 6;
+    g.nx = N;
+    g.ny = N;
+    g.nkx = nkx;
+    g.nky = N;
+    g.H = N / 2;
+    g.Kx = Kx;
+    g.Kyh = Kyh;
+    g.Ky = 2 * Kyh + 1;
+    g.logny = clog2(N);
+    g.logH = clog2(N / 2);
+    g.fLB = 0;
+    g.fTG = 0;
+    g.oddx = 0;
+}
+template <int N> inline bool fold_sizes_match(const Geo& g) {
+    Geo f = g;
+    fold_sizes<N>(f);
+    return f.nx == g.nx && f.ny == g.ny && f.nkx == g.nkx && f.nky == g.nky && f.H == g.H && f.Kx == g.Kx &&
+           f.Kyh == g.Kyh && f.Ky == g.Ky && f.logny == g.logny && f.logH == g.logH && f.fLB == g.fLB &&
+           f.fTG == g.fTG && f.oddx == g.oddx;
+}
+
 // one transform of a row or column buffer b: the power-of-two engine for E > 0,
 // the mixed-radix engine (through the scratch sequence sc) for E == 0; sy is
 // the pass barrier (fft_sync)
@@ -531,9 +562,16 @@ __device__ __forceinline__ void row_body(const Geo& g, const RowArgs<T>& a, cons
     }
 }
 
-template <typename T, int E, int MODE>
+// N > 0: the grid's size fields folded to constants (fold_sizes<N>)
+template <typename T, int E, int MODE, int N = 0>
 __global__ void __launch_bounds__(256) k_row(Geo g, RowArgs<T> a) {
-    row_body<T, E, MODE>(g, a, blockIdx.x);
+    if constexpr (N > 0) {
+        Geo f = g;
+        fold_sizes<N>(f);
+        row_body<T, E, MODE>(f, a, blockIdx.x);
+    } else {
+        row_body<T, E, MODE>(g, a, blockIdx.x);
+    }
 }
 
 // ============================================================ column kernel
@@ -956,9 +994,15 @@ __device__ __forceinline__ void col_body(const Geo& g, const ColArgs<T>& a, cons
     }
 }
 
-template <typename T, int E, int MODE, int STAGE>
+template <typename T, int E, int MODE, int STAGE, int N = 0>
 __global__ void __launch_bounds__(512) k_col(Geo g, ColArgs<T> a) {
-    col_body<T, E, MODE, STAGE>(g, a, blockIdx.x);
+    if constexpr (N > 0) {
+        Geo f = g;
+        fold_sizes<N>(f);
+        col_body<T, E, MODE, STAGE>(f, a, blockIdx.x);
+    } else {
+        col_body<T, E, MODE, STAGE>(g, a, blockIdx.x);
+    }
 }
 
 // ======================================================= auxiliary kernels
