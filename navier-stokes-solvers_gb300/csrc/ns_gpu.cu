@@ -146,7 +146,7 @@ template <typename T> static ColArgs<T> col_args(ns_gpu* g) {
     a.ds = g->ds;
     a.sp = step_params<T>(g);
     if (a.sp.forcing && g->fM > 0) {
-        a.fnoise = g->fnoise;
+        a.fsum = g->fsum;
         a.fkxr = g->fkxr;
         a.fkyr = g->fkyr;
     }
@@ -196,10 +196,11 @@ static int dalloc(ns_gpu* g, void** p, size_t bytes);
 static int ensure_noise(ns_gpu* g) {
     g->fM = 0;
     const StepParams sp = step_params<double>(g);
-    // one draw per step costs the stage-4 kernel less than a kernel of its own
-    // costs the step; several draws (coarse steps that sum fine-step forcing) go
-    // to the table
-    if (!sp.forcing || sp.fsub <= 1) return NS_GPU_OK;
+    // the draws (FP64 Philox, logarithm, sine and cosine) and their per-mode sums
+    // run beside stages 1-3 on a second stream; in the stage-4 column pass, where
+    // the forced columns' draws used to run, they cost 7.7 us of a 0.274 ms 2048^2
+    // step with one draw per step
+    if (!sp.forcing || sp.fsub < 1) return NS_GPU_OK;
     const double two_pi = 2.0 * 3.14159265358979323846;
     const int kxr = std::min((int)floor(sp.f_kmax * g->g.Lx / two_pi + 1e-9), g->g.Kx - 1);
     const int kyr = std::min((int)floor(sp.f_kmax * g->g.Ly / two_pi + 1e-9), g->g.Kyh);
@@ -207,10 +208,19 @@ static int ensure_noise(ns_gpu* g) {
     const size_t need = (size_t)(kxr + 1) * (2 * kyr + 1) * sp.fsub;
     if (need > g->fnoise_cap) {
         if (g->fnoise) cudaFree(g->fnoise);
+    if (g->fsum) cudaFree(g->fsum);
         g->fnoise = nullptr;
         g->fnoise_cap = 0;
         NSG_TRY(dalloc(g, (void**)&g->fnoise, need * sizeof(double2)));
         g->fnoise_cap = need;
+    }
+    const size_t modes = (size_t)(kxr + 1) * (2 * kyr + 1);
+    if (modes > g->fsum_cap) {
+        if (g->fsum) cudaFree(g->fsum);
+        g->fsum = nullptr;
+        g->fsum_cap = 0;
+        NSG_TRY(dalloc(g, (void**)&g->fsum, modes * sizeof(double2)));
+        g->fsum_cap = modes;
     }
     if (!g->stn) {
         NSG_CUDA(g, cudaStreamCreateWithFlags(&g->stn, cudaStreamNonBlocking));
@@ -233,6 +243,10 @@ static int launch_noise(ns_gpu* g) {
     NSG_CUDA(g, cudaStreamWaitEvent(g->stn, g->evn0, 0));
     k_forcing_noise<<<(n + 127) / 128, 128, 0, g->stn>>>(g->g.ny, g->g.Lx, g->g.Ly, &g->ds->step_cur, g->fM, sp.f_seed,
                                                          sp.f_kmin, sp.f_kmax, g->fkxr, g->fkyr, g->fnoise);
+    NSG_LAUNCHED(g);
+    const int modes = (g->fkxr + 1) * (2 * g->fkyr + 1);
+    k_forcing_sum<<<(modes + 127) / 128, 128, 0, g->stn>>>(g->g.ny, g->g.Lx, g->g.Ly, g->fM, sp.f_kmin, sp.f_kmax,
+                                                             g->fkxr, g->fkyr, g->fnoise, g->fsum);
     NSG_LAUNCHED(g);
     NSG_CUDA(g, cudaEventRecord(g->evn1, g->stn));
     return NS_GPU_OK;
@@ -276,7 +290,7 @@ template <typename T> static std::vector<unsigned char> step_key(ns_gpu* g, cons
     put(ints, sizeof(ints));
     const double dbl[] = {g->hv_cutoff, g->hv_inv_bw, g->p.sfd_strength, (double)g->p.hv_order};
     put(dbl, sizeof(dbl));
-    const void* ptrs[] = {g->fnoise, g->hvw_full, g->out, g->outsfd};
+    const void* ptrs[] = {g->fnoise, g->fsum, g->hvw_full, g->out, g->outsfd};
     put(ptrs, sizeof(ptrs));
     return k;
 }
@@ -365,7 +379,7 @@ void nsg_stage_args(ns_gpu* g, RowArgs<float>* ra, ColArgs<float>* ca) {
     for (int f = 0; f < 4; ++f) ra->F[f] = (const float2*)g->F[f];
     ra->dx[0] = 1; ra->dx[1] = 0; ra->dx[2] = 1; ra->dx[3] = 0;  // psi_x, psi_y, omega_x, omega_y
     *ca = col_args<float>(g);
-    ca->fnoise = nullptr;  // the ensemble kernel draws its members' forcing itself
+    ca->fsum = nullptr;  // the ensemble kernel draws its members' forcing itself
 }
 
 // ------------------------------------------------------------ allocation
@@ -519,6 +533,7 @@ void ns_gpu_destroy(ns_gpu* g) {
         if (g->real[i]) cudaFree(g->real[i]);
     }
     if (g->fnoise) cudaFree(g->fnoise);
+    if (g->fsum) cudaFree(g->fsum);
     if (g->st2) cudaStreamDestroy(g->st2);
     if (g->ev_a) cudaEventDestroy(g->ev_a);
     if (g->ev_b) cudaEventDestroy(g->ev_b);

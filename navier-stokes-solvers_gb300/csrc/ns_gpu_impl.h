@@ -58,6 +58,8 @@ struct ns_gpu {
     double2 *out, *outsfd;  // masked-out modes of the state (FP64)
     double2* fnoise;        // this step's forcing draws (k_forcing_noise), [entries][draws]
     size_t fnoise_cap;      // entries x draws allocated
+    double2* fsum;          // their per-entry sums, zero outside the shell (k_forcing_sum)
+    size_t fsum_cap;        // entries allocated
     int fkxr, fkyr, fM;     // table extent (kx index, |ky|) and draws per step; fM = 0: no table
     int outside_active;
     int fields_valid;   // F holds the stage-1 fields of the current state

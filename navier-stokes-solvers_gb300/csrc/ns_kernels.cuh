@@ -606,9 +606,10 @@ template <typename T> struct ColArgs {
     double out_scale;           // export scale (1/(nx ny) forward, -1/(nx ny) nonlinear)
     int psi_from_w;             // prologue: Psi = -W0/k^2 instead of PSI0
     int nfields;                // prologue: number of fields (4 for a stage, 3 = Psi,Psi_y,Omega)
-    // this step's forcing noise, one term per (mode, draw) (k_forcing_noise), or null:
-    // entry e = i (2 fkyr + 1) + ky + fkyr for kx index i <= fkxr and |ky| <= fkyr
-    const double2* fnoise;
+    // this step's forcing noise summed per mode (k_forcing_noise, k_forcing_sum), zero
+    // outside the forcing shell, or null: entry e = i (2 fkyr + 1) + ky + fkyr for kx
+    // index i <= fkxr and |ky| <= fkyr
+    const double2* fsum;
     int fkxr, fkyr;
 };
 
@@ -645,27 +646,23 @@ __device__ __forceinline__ bool forcing_in_shell(double Lx, double Ly, int ny, i
 }
 
 // white-in-time forcing increment of one kept mode: amp times the mode's noise
-// (the sum over this step's draws) when kmin <= |k| <= kmax.  With a noise table
-// the draws were made for the step by k_forcing_noise (in parallel, before the
-// step's first stage); otherwise they are drawn here (forcing_xi_sum).  The
-// geometry comes by value (Lx, Ly, ny): a caller's Geo never escapes into this
-// out-of-line call, so its fields stay foldable constants where they are.
+// (the sum over this step's draws) when kmin <= |k| <= kmax.  With a table the
+// draws and their per-mode sums were made for the step by k_forcing_noise and
+// k_forcing_sum (beside the step's first three stages), zero outside the shell;
+// otherwise they are drawn here (forcing_xi_sum).  The geometry comes by value
+// (Lx, Ly, ny): a caller's Geo never escapes into this out-of-line call, so its
+// fields stay foldable constants where they are.
 static __device__ __noinline__ double2 forcing_increment(double Lx, double Ly, int ny, int i, int j,
                                                          unsigned long long step, int M, unsigned long long seed,
-                                                         double kmin, double kmax, double amp, const double2* fnoise,
+                                                         double kmin, double kmax, double amp, const double2* fsum,
                                                          int fkxr, int fkyr) {
-    if (!forcing_in_shell(Lx, Ly, ny, i, j, kmin, kmax)) return make_double2(0.0, 0.0);
     double2 xi;
     const int ky = (j <= ny / 2) ? j : j - ny;
-    if (fnoise && i <= fkxr && ky >= -fkyr && ky <= fkyr) {
-        const double2* t = fnoise + ((size_t)i * (2 * fkyr + 1) + (ky + fkyr)) * M;
-        double sx = 0.0, sy = 0.0;
-        for (int s = 0; s < M; ++s) {
-            sx = __dadd_rn(sx, t[s].x);
-            sy = __dadd_rn(sy, t[s].y);
-        }
-        xi = make_double2(sx, sy);
+    if (fsum && i <= fkxr && ky >= -fkyr && ky <= fkyr) {
+        xi = fsum[(size_t)i * (2 * fkyr + 1) + (ky + fkyr)];
+        if (xi.x == 0.0 && xi.y == 0.0) return make_double2(0.0, 0.0);  // outside the shell
     } else {
+        if (!forcing_in_shell(Lx, Ly, ny, i, j, kmin, kmax)) return make_double2(0.0, 0.0);
         xi = forcing_xi_sum(i, j, ny, step, M, seed);
     }
     return make_double2(amp * xi.x, amp * xi.y);
@@ -771,8 +768,18 @@ __device__ __forceinline__ C post_step_mode(const Geo& g, const ColArgs<T>& a, i
     const T k2f = kx * kx + ky * ky;
     if (a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9 && k2f >= (T)(a.sp.f_kmin * a.sp.f_kmin * (1.0 - 1e-3)) &&
         k2f <= (T)(a.sp.f_kmax * a.sp.f_kmax * (1.0 + 1e-3))) {
-        const double2 df = forcing_increment(g.Lx, g.Ly, g.ny, i, j, a.ds->step_cur, a.sp.fsub, a.sp.f_seed,
-                                             a.sp.f_kmin, a.sp.f_kmax, f_amp, a.fnoise, a.fkxr, a.fkyr);
+        // modes of the step's table read their summed noise inline (no out-of-line
+        // call in the register-heavy stage kernels); the others go through
+        // forcing_increment, which makes the same test and product
+        const int kyi = (j <= g.ny / 2) ? j : j - g.ny;
+        double2 df;
+        if (a.fsum && i <= a.fkxr && kyi >= -a.fkyr && kyi <= a.fkyr) {
+            const double2 xi = a.fsum[(size_t)i * (2 * a.fkyr + 1) + (kyi + a.fkyr)];
+            df = (xi.x == 0.0 && xi.y == 0.0) ? make_double2(0.0, 0.0) : make_double2(f_amp * xi.x, f_amp * xi.y);
+        } else {
+            df = forcing_increment(g.Lx, g.Ly, g.ny, i, j, a.ds->step_cur, a.sp.fsub, a.sp.f_seed, a.sp.f_kmin,
+                                   a.sp.f_kmax, f_amp, a.fsum, a.fkxr, a.fkyr);
+        }
         if (df.x != 0.0 || df.y != 0.0) {
             wn.x = (T)((double)wn.x + df.x);
             wn.y = (T)((double)wn.y + df.y);
@@ -1241,6 +1248,30 @@ __global__ void k_forcing_noise(int ny, double Lx, double Ly, const unsigned lon
         const int i = e / (2 * kyr + 1);
         const int ky = e - i * (2 * kyr + 1) - kyr;
         out[t] = forcing_noise_term(i, ky, s, *counter, seed, Lx, Ly, kmin, kmax);
+    }
+}
+
+// per-mode sums of the step's noise table (k_forcing_noise): the M draws of mode
+// e = i (2 kyr + 1) + ky + kyr summed in order from zero, as forcing_xi_sum sums
+// them, and zero outside the forcing shell (the shell test of forcing_increment)
+__global__ void k_forcing_sum(int ny, double Lx, double Ly, int M, double kmin, double kmax, int kxr, int kyr,
+                              const double2* __restrict__ terms, double2* __restrict__ out) {
+    const int n = (kxr + 1) * (2 * kyr + 1);
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const int i = e / (2 * kyr + 1);
+        const int ky = e - i * (2 * kyr + 1) - kyr;
+        const int j = ky >= 0 ? ky : ny + ky;
+        double2 r = make_double2(0.0, 0.0);
+        if (forcing_in_shell(Lx, Ly, ny, i, j, kmin, kmax)) {
+            const double2* t = terms + (size_t)e * M;
+            double sx = 0.0, sy = 0.0;
+            for (int s = 0; s < M; ++s) {
+                sx = __dadd_rn(sx, t[s].x);
+                sy = __dadd_rn(sy, t[s].y);
+            }
+            r = make_double2(sx, sy);
+        }
+        out[e] = r;
     }
 }
 

@@ -644,14 +644,15 @@ __global__ void __launch_bounds__(64 * cw_teams<T>(), 1) k_col_w(Geo g, ColArgs<
             }
             if (STAGE == 4 && (a.sp.forcing || sfd)) {
                 // forcing increment (few low-|k| modes), then the SFD post-step, on omega_hat^{n+1}
-                const double f_amp = a.sp.forcing ? a.sp.f_sigma * sqrt(dt / a.sp.fsub) : 0.0;
+                // columns beyond the shell only relax the SFD filter (and skip the
+                // FP64 amplitude)
+                const bool force_col = a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9;
+                const double f_amp = force_col ? a.sp.f_sigma * sqrt(dt / a.sp.fsub) : 0.0;
                 double sa = 0.0;
                 if (sfd) {
                     sa = dt / a.sp.sfd_tau;
                     sa = sa > 1.0 ? 1.0 : (sa < 0.0 ? 0.0 : sa);
                 }
-                // columns beyond the shell only relax the SFD filter
-                const bool force_col = a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9;
 #pragma unroll 1
                 for (int k2 = 0; k2 < 32 && (force_col || sfd); ++k2) {
                     const int j = lane + 32 * k2 + 1024 * h;
@@ -902,14 +903,15 @@ __global__ void __launch_bounds__(CQ<NL>::TT * CQ<NL>::NT, 1) k_col_q(Geo g, Col
             }
             if (STAGE == 4 && (a.sp.forcing || sfd)) {
                 // forcing increment (few low-|k| modes), then the SFD post-step, on omega_hat^{n+1}
-                const double f_amp = a.sp.forcing ? a.sp.f_sigma * sqrt(dt / a.sp.fsub) : 0.0;
+                // columns beyond the shell only relax the SFD filter (and skip the
+                // FP64 amplitude)
+                const bool force_col = a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9;
+                const double f_amp = force_col ? a.sp.f_sigma * sqrt(dt / a.sp.fsub) : 0.0;
                 double sa = 0.0;
                 if (sfd) {
                     sa = dt / a.sp.sfd_tau;
                     sa = sa > 1.0 ? 1.0 : (sa < 0.0 ? 0.0 : sa);
                 }
-                // columns beyond the shell only relax the SFD filter
-                const bool force_col = a.sp.forcing && (double)kx <= a.sp.f_kmax + 1e-9;
 #pragma unroll 1
                 for (int e = 0; e < 16 && (force_col || sfd); ++e) {
                     const int j = cq_mode<NL>(t, e);
